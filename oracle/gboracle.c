@@ -1,0 +1,398 @@
+/*
+ * ORACLE — test infrastructure only.  A float64 CPU restatement of the
+ * reference's self-gravity hot path (Khaserdene/real-astronomy-simulation),
+ * used as the checker for the GPU engine and as the timed CPU baseline.
+ * Nothing in the shipped package links or calls this file.
+ *
+ * Pinned against golden fixtures produced by running the reference's own
+ * Python source (tests/golden/gen_golden.py; tests/test_oracle_golden.py).
+ *
+ * Build: gcc -O2 -fopenmp -ffp-contract=off -fPIC -shared (oracle/oracle.py).
+ * -ffp-contract=off keeps every multiply and add separately rounded, matching
+ * the reference's float64 expression order.
+ *
+ * Layouts: positions / velocities / accelerations are (n, 3) row-major
+ * float64, masses (n,) float64, node arrays indexed like the reference
+ * (leaves 0..n-1, internal nodes n..2n-2, root = n).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+int orc_max_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------ direct
+ * core/solvers/gravity.py:13-26 compute_acc_direct: for every i, loop over
+ * ALL j (the i == j term adds exactly zero), d = x_j - x_i,
+ * r2 = d.d + eps2, inv = 1/sqrt(r2), a += (G*m_j*inv*inv*inv) * d. */
+static void direct_one(const double *pos, const double *mass, int64_t n,
+                       double G, double eps2, int64_t i, double *out) {
+    const double px = pos[3 * i], py = pos[3 * i + 1], pz = pos[3 * i + 2];
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    for (int64_t j = 0; j < n; ++j) {
+        const double dx = pos[3 * j] - px;
+        const double dy = pos[3 * j + 1] - py;
+        const double dz = pos[3 * j + 2] - pz;
+        const double r2 = dx * dx + dy * dy + dz * dz + eps2;
+        const double inv = 1.0 / sqrt(r2);
+        const double s = G * mass[j] * inv * inv * inv;
+        ax += s * dx;
+        ay += s * dy;
+        az += s * dz;
+    }
+    out[0] = ax;
+    out[1] = ay;
+    out[2] = az;
+}
+
+void orc_direct_acc(const double *pos, const double *mass, double *acc,
+                    int64_t n, double G, double eps2) {
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < n; ++i) direct_one(pos, mass, n, G, eps2, i, acc + 3 * i);
+}
+
+/* Same sum for a subset of targets (sampled-target FP64 checks). */
+void orc_direct_acc_targets(const double *pos, const double *mass, int64_t n,
+                            const int64_t *targets, int64_t nt, double G,
+                            double eps2, double *acc) {
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t t = 0; t < nt; ++t)
+        direct_one(pos, mass, n, G, eps2, targets[t], acc + 3 * t);
+}
+
+/* Per-target potential sum_{j != i} m_j / sqrt(r2): the inner loop of
+ * core/solvers/gravity.py:49-55. */
+void orc_phi_targets(const double *pos, const double *mass, int64_t n,
+                     const int64_t *targets, int64_t nt, double eps2,
+                     double *phi) {
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t t = 0; t < nt; ++t) {
+        const int64_t i = targets[t];
+        const double px = pos[3 * i], py = pos[3 * i + 1], pz = pos[3 * i + 2];
+        double s = 0.0;
+        for (int64_t j = 0; j < n; ++j) {
+            if (j == i) continue;
+            const double dx = pos[3 * j] - px;
+            const double dy = pos[3 * j + 1] - py;
+            const double dz = pos[3 * j + 2] - pz;
+            const double r2 = dx * dx + dy * dy + dz * dz + eps2;
+            s += mass[j] / sqrt(r2);
+        }
+        phi[t] = s;
+    }
+}
+
+/* core/solvers/gravity.py:29-36 kinetic_energy. */
+double orc_kinetic_energy(const double *vel, const double *mass, int64_t n) {
+    double ke = 0.0;
+#pragma omp parallel for reduction(+ : ke)
+    for (int64_t i = 0; i < n; ++i) {
+        const double *v = vel + 3 * i;
+        ke += 0.5 * mass[i] * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    }
+    return ke;
+}
+
+/* core/solvers/gravity.py:39-57 potential_energy: -1/2 G sum_i m_i
+ * sum_{j != i} m_j / sqrt(r2 + eps2). */
+double orc_potential_energy(const double *pos, const double *mass, int64_t n,
+                            double G, double eps2) {
+    double pe = 0.0;
+#pragma omp parallel for reduction(+ : pe) schedule(dynamic, 64)
+    for (int64_t i = 0; i < n; ++i) {
+        const double px = pos[3 * i], py = pos[3 * i + 1], pz = pos[3 * i + 2];
+        double acc_i = 0.0;
+        for (int64_t j = 0; j < n; ++j) {
+            if (j == i) continue;
+            const double dx = pos[3 * j] - px;
+            const double dy = pos[3 * j + 1] - py;
+            const double dz = pos[3 * j + 2] - pz;
+            const double r2 = dx * dx + dy * dy + dz * dz + eps2;
+            acc_i += mass[j] / sqrt(r2);
+        }
+        pe += -0.5 * G * mass[i] * acc_i;
+    }
+    return pe;
+}
+
+/* core/integrators/leapfrog.py:11-22 in the order of core/engine.py:108-116:
+ * kick(dt/2) -> drift(dt) -> acc -> kick(dt/2); acc holds the previous
+ * step's accelerations on entry (primed by load_state, core/engine.py:81). */
+void orc_kdk_direct(double *pos, double *vel, double *acc, const double *mass,
+                    int64_t n, double G, double eps2, double dt,
+                    int64_t nsteps) {
+    const double half = 0.5 * dt;
+    for (int64_t s = 0; s < nsteps; ++s) {
+        for (int64_t k = 0; k < 3 * n; ++k) vel[k] += acc[k] * half;
+        for (int64_t k = 0; k < 3 * n; ++k) pos[k] += vel[k] * dt;
+        orc_direct_acc(pos, mass, acc, n, G, eps2);
+        for (int64_t k = 0; k < 3 * n; ++k) vel[k] += acc[k] * half;
+    }
+}
+
+/* ------------------------------------------------------------------ Morton
+ * core/solvers/barnes_hut.py:27-46.  lo = per-axis min, span = the largest
+ * per-axis extent (1.0 if not > 0), scale = (2^bits-1)/(span*1.0000001),
+ * q = clip((x-lo)*scale, 0, 2^bits-1) truncated to an integer, key =
+ * interleave(qx, qy, qz) with x in bit 3k, y in 3k+1, z in 3k+2. */
+static uint64_t spread3(uint64_t v, int bits) {
+    uint64_t r = 0;
+    for (int b = 0; b < bits; ++b) r |= ((v >> b) & 1ull) << (3 * b);
+    return r;
+}
+
+void orc_morton(const double *pos, int64_t n, int bits, uint64_t *codes,
+                double *lo_out, double *scale_out) {
+    double lo[3] = {INFINITY, INFINITY, INFINITY};
+    double hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int64_t i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k) {
+            const double v = pos[3 * i + k];
+            if (v < lo[k]) lo[k] = v;
+            if (v > hi[k]) hi[k] = v;
+        }
+    double span = hi[0] - lo[0];
+    for (int k = 1; k < 3; ++k)
+        if (hi[k] - lo[k] > span) span = hi[k] - lo[k];
+    if (!(span > 0)) span = 1.0;
+    const double qmax = (double)((1ull << bits) - 1ull);
+    const double scale = qmax / (span * 1.0000001);
+    for (int64_t i = 0; i < n; ++i) {
+        uint64_t q[3];
+        for (int k = 0; k < 3; ++k) {
+            double t = (pos[3 * i + k] - lo[k]) * scale;
+            if (t < 0.0) t = 0.0;
+            if (t > qmax) t = qmax;
+            q[k] = (uint64_t)t;
+        }
+        codes[i] = spread3(q[0], bits) | (spread3(q[1], bits) << 1) |
+                   (spread3(q[2], bits) << 2);
+    }
+    if (lo_out) memcpy(lo_out, lo, sizeof(lo));
+    if (scale_out) *scale_out = scale;
+}
+
+/* Stable argsort of unsigned 64-bit keys (np.argsort(kind="stable"),
+ * core/solvers/barnes_hut.py:247): LSD radix, 16-bit digits. */
+void orc_stable_argsort_u64(const uint64_t *keys, int64_t n, int32_t *order) {
+    int32_t *tmp = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
+    size_t *cnt = (size_t *)malloc(sizeof(size_t) * 65537);
+    for (int64_t i = 0; i < n; ++i) order[i] = (int32_t)i;
+    uint64_t all_or = 0;
+    for (int64_t i = 0; i < n; ++i) all_or |= keys[i];
+    int32_t *src = order, *dst = tmp;
+    for (int shift = 0; shift < 64; shift += 16) {
+        if (((all_or >> shift) & 0xFFFFull) == 0) continue;
+        memset(cnt, 0, sizeof(size_t) * 65537);
+        for (int64_t i = 0; i < n; ++i) cnt[((keys[src[i]] >> shift) & 0xFFFF) + 1]++;
+        for (int d = 0; d < 65536; ++d) cnt[d + 1] += cnt[d];
+        for (int64_t i = 0; i < n; ++i) dst[cnt[(keys[src[i]] >> shift) & 0xFFFF]++] = src[i];
+        int32_t *t = src; src = dst; dst = t;
+    }
+    if (src != order) memcpy(order, src, sizeof(int32_t) * (size_t)n);
+    free(tmp);
+    free(cnt);
+}
+
+/* ------------------------------------------------------------- Karras build
+ * core/solvers/barnes_hut.py:50-81: common-prefix length over bits 62..0 of
+ * the codes; equal codes fall back to 63 + the prefix of the indices over
+ * bits 30..0; -1 when j is out of range. */
+static int clz63(uint64_t x) {
+    int c = 0;
+    for (uint64_t m = 1ull << 62; m && !(x & m); m >>= 1) ++c;
+    return c;
+}
+
+static int clz31(uint32_t x) {
+    int c = 0;
+    for (uint32_t m = 1u << 30; m && !(x & m); m >>= 1) ++c;
+    return c;
+}
+
+static int delta(int i, int j, int n, const int64_t *code) {
+    if (j < 0 || j >= n) return -1;
+    const uint64_t x = (uint64_t)(code[i] ^ code[j]);
+    if (x == 0) return 63 + clz31((uint32_t)(i ^ j));
+    return clz63(x);
+}
+
+/* core/solvers/barnes_hut.py:84-121 _build_radix (Karras 2012): internal
+ * nodes 0..n-2; children stored as leaf id (< n) or internal id + n;
+ * parent[] must be pre-filled with -1 by the caller (:250). */
+void orc_build_radix(const int64_t *code, int n, int32_t *left, int32_t *right,
+                     int32_t *parent) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n - 1; ++i) {
+        const int d = delta(i, i + 1, n, code) > delta(i, i - 1, n, code) ? 1 : -1;
+        const int d_min = delta(i, i - d, n, code);
+        int l_max = 2;
+        while (delta(i, i + l_max * d, n, code) > d_min) l_max *= 2;
+        int l = 0;
+        for (int t = l_max / 2; t >= 1; t /= 2)
+            if (delta(i, i + (l + t) * d, n, code) > d_min) l += t;
+        const int j = i + l * d;
+        const int d_node = delta(i, j, n, code);
+        int s = 0;
+        int t2 = (l + 1) / 2;
+        while (t2 >= 1) {
+            if (delta(i, i + (s + t2) * d, n, code) > d_node) s += t2;
+            t2 = t2 > 1 ? (t2 + 1) / 2 : 0;
+        }
+        const int gamma = i + s * d + (d < 0 ? d : 0);
+        const int lo = i < j ? i : j;
+        const int hi = i < j ? j : i;
+        const int lc = (lo == gamma) ? gamma : gamma + n;
+        const int rc = (hi == gamma + 1) ? gamma + 1 : gamma + 1 + n;
+        left[i] = lc;
+        right[i] = rc;
+        parent[lc] = i + n;
+        parent[rc] = i + n;
+    }
+}
+
+/* -------------------------------------------------------- node summaries
+ * core/solvers/barnes_hut.py:124-177: leaf com/mass/AABB from the sorted
+ * particle; every leaf adds its mass, mass*position and AABB into each
+ * ancestor (here in leaf order, serially); internal com = moment / mass. */
+void orc_summaries(const int32_t *order, const double *pos, const double *mass,
+                   const int32_t *parent, int n, double *com, double *nmass,
+                   double *nmin, double *nmax) {
+    const int m = 2 * n - 1;
+    double *nmom = (double *)calloc((size_t)(3 * (m > 0 ? m : 1)), sizeof(double));
+    for (int li = 0; li < n; ++li) {
+        const int p = order[li];
+        for (int k = 0; k < 3; ++k) {
+            com[3 * li + k] = pos[3 * p + k];
+            nmin[3 * li + k] = pos[3 * p + k];
+            nmax[3 * li + k] = pos[3 * p + k];
+        }
+        nmass[li] = mass[p];
+    }
+    for (int ii = 0; ii < n - 1; ++ii) {
+        const int node = ii + n;
+        nmass[node] = 0.0;
+        for (int k = 0; k < 3; ++k) {
+            com[3 * node + k] = 0.0;
+            nmin[3 * node + k] = 1e30;
+            nmax[3 * node + k] = -1e30;
+        }
+    }
+    for (int li = 0; li < n; ++li) {
+        const double mm = nmass[li];
+        const double *pp = com + 3 * li;
+        for (int node = parent[li]; node >= 0; node = parent[node]) {
+            nmass[node] += mm;
+            for (int k = 0; k < 3; ++k) {
+                nmom[3 * node + k] += mm * pp[k];
+                if (pp[k] < nmin[3 * node + k]) nmin[3 * node + k] = pp[k];
+                if (pp[k] > nmax[3 * node + k]) nmax[3 * node + k] = pp[k];
+            }
+        }
+    }
+    for (int ii = 0; ii < n - 1; ++ii) {
+        const int node = ii + n;
+        const double mm = nmass[node];
+        if (mm > 0.0)
+            for (int k = 0; k < 3; ++k) com[3 * node + k] = nmom[3 * node + k] / mm;
+    }
+    free(nmom);
+}
+
+/* ---------------------------------------------------------------- traverse
+ * core/solvers/barnes_hut.py:180-217 _traverse for particle p: DFS from the
+ * root with an explicit stack; a leaf adds its monopole unless it is p
+ * itself; an internal node is accepted when size^2 < theta2 * (|d|^2+eps2)
+ * (size = largest AABB extent), else both children are pushed (left, then
+ * right; right is popped first) when sp + 2 <= max_stack, and silently
+ * dropped otherwise.  Returns the number of dropped pushes for p. */
+static int64_t traverse_one(const double *pos, const int32_t *order,
+                            const double *com, const double *nmass,
+                            const double *nmin, const double *nmax,
+                            const int32_t *left, const int32_t *right, int n,
+                            int root, double theta2, double eps2, int max_stack,
+                            double G, int p, int32_t *stack, double *out) {
+    const double px = pos[3 * p], py = pos[3 * p + 1], pz = pos[3 * p + 2];
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    int64_t dropped = 0;
+    int sp = 0;
+    stack[sp++] = root;
+    while (sp > 0) {
+        const int node = stack[--sp];
+        if (node < n) {
+            if (order[node] != p) {
+                const double dx = com[3 * node] - px;
+                const double dy = com[3 * node + 1] - py;
+                const double dz = com[3 * node + 2] - pz;
+                const double r2 = dx * dx + dy * dy + dz * dz + eps2;
+                const double inv = 1.0 / sqrt(r2);
+                const double s = G * nmass[node] * inv * inv * inv;
+                ax += s * dx;
+                ay += s * dy;
+                az += s * dz;
+            }
+        } else {
+            const int ii = node - n;
+            const double dx = com[3 * node] - px;
+            const double dy = com[3 * node + 1] - py;
+            const double dz = com[3 * node + 2] - pz;
+            const double r2 = dx * dx + dy * dy + dz * dz + eps2;
+            double size = nmax[3 * node] - nmin[3 * node];
+            for (int k = 1; k < 3; ++k) {
+                const double e = nmax[3 * node + k] - nmin[3 * node + k];
+                if (e > size) size = e;
+            }
+            if (size * size < theta2 * r2) {
+                const double inv = 1.0 / sqrt(r2);
+                const double s = G * nmass[node] * inv * inv * inv;
+                ax += s * dx;
+                ay += s * dy;
+                az += s * dz;
+            } else if (sp + 2 <= max_stack) {
+                stack[sp++] = left[ii];
+                stack[sp++] = right[ii];
+            } else {
+                ++dropped;
+            }
+        }
+    }
+    out[0] = ax;
+    out[1] = ay;
+    out[2] = az;
+    return dropped;
+}
+
+/* Evaluate the traversal for the given particles (all when targets == NULL).
+ * acc is indexed like targets (or by particle when targets == NULL). */
+int64_t orc_traverse(const double *pos, const int32_t *order, const double *com,
+                     const double *nmass, const double *nmin,
+                     const double *nmax, const int32_t *left,
+                     const int32_t *right, int n, double theta2, double eps2,
+                     int max_stack, double G, const int64_t *targets,
+                     int64_t nt, double *acc) {
+    int64_t dropped = 0;
+    const int64_t count = targets ? nt : n;
+#pragma omp parallel reduction(+ : dropped)
+    {
+        int32_t *stack = (int32_t *)malloc(sizeof(int32_t) * (size_t)(max_stack > 0 ? max_stack : 1));
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t t = 0; t < count; ++t) {
+            const int p = targets ? (int)targets[t] : (int)t;
+            dropped += traverse_one(pos, order, com, nmass, nmin, nmax, left,
+                                    right, n, n, theta2, eps2, max_stack, G, p,
+                                    stack, acc + 3 * t);
+        }
+        free(stack);
+    }
+    return dropped;
+}

@@ -1,0 +1,251 @@
+"""Generate the golden fixtures in this directory by running the REFERENCE's own
+hot-path Python code (Khaserdene/real-astronomy-simulation) on the host.
+
+Taichi is not installable offline, so the reference modules are imported under
+``_taichi_stub`` (kernels run as serial Python over numpy fields).  The only
+source change is ``rewrite_atomics`` applied to ``_accumulate``
+(core/solvers/barnes_hut.py:143-166), turning ``ti.atomic_add/min/max`` on a
+field element into the equivalent in-place update.
+
+Run from the repository root, in a container where the reference is mounted:
+
+    python tests/golden/gen_golden.py /root/reference
+
+Inputs are rounded to float32 first (the GPU engine stores float32), then
+passed to the reference as float64, so the fixtures describe the reference's
+arithmetic on exactly the values the device sees.  Outputs are written as
+compressed ``.npz`` files next to this script; the tests read only those.
+"""
+from __future__ import annotations
+
+import inspect
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _load_reference(ref_root: str):
+    sys.dont_write_bytecode = True
+    sys.path.insert(0, HERE)
+    import _taichi_stub
+    _taichi_stub.install()
+    sys.path.insert(0, ref_root)
+    import core.units as units
+    import core.solvers.gravity as gravity
+    import core.solvers.barnes_hut as bh
+    import core.integrators.leapfrog as leapfrog
+    import core.ic.plummer as plummer
+    import core.ic.disk as disk
+    import core.engine as engine
+    # _accumulate: atomics -> in-place updates (the only source rewrite).
+    src = _taichi_stub.rewrite_atomics(inspect.getsource(bh._accumulate))
+    exec(compile(src, bh.__file__, "exec"), bh.__dict__)
+    return dict(units=units, gravity=gravity, bh=bh, leapfrog=leapfrog,
+                plummer=plummer, disk=disk, engine=engine, stub=_taichi_stub)
+
+
+def _f32(a):
+    return np.asarray(a, np.float64).astype(np.float32).astype(np.float64)
+
+
+def _field_from(stub, arr, dtype="f64"):
+    arr = np.asarray(arr)
+    f = stub._field(dtype, arr.shape)
+    f.from_numpy(arr)
+    return f
+
+
+def gen_plummer_ic(R, out):
+    """make_plummer with G patched to 1 (core/ic/plummer.py:19-66)."""
+    pl = R["plummer"]
+    old = pl.G
+    pl.G = 1.0
+    try:
+        s0 = pl.make_plummer(n=1000, total_mass=1.0, scale_radius=1.0, seed=0)
+        s1 = pl.make_plummer(n=257, total_mass=2.5, scale_radius=0.7, seed=11)
+    finally:
+        pl.G = old
+    out["plummer_ic"] = dict(pos0=s0.pos, vel0=s0.vel, mass0=s0.mass,
+                             pos1=s1.pos, vel1=s1.vel, mass1=s1.mass)
+
+
+def gen_direct(R, out):
+    """compute_acc_direct / kinetic_energy / potential_energy
+    (core/solvers/gravity.py:13-57) on a float32-rounded Plummer sphere."""
+    pl, grav, stub = R["plummer"], R["gravity"], R["stub"]
+    old = pl.G
+    pl.G = 1.0
+    try:
+        s = pl.make_plummer(n=384, total_mass=1.0, scale_radius=1.0, seed=5)
+    finally:
+        pl.G = old
+    pos, vel, mass = _f32(s.pos), _f32(s.vel), _f32(s.mass)
+    n = pos.shape[0]
+    G, eps2 = 1.0, 0.01 ** 2
+    fp = _field_from(stub, pos)
+    fm = _field_from(stub, mass)
+    fv = _field_from(stub, vel)
+    fa = stub._field("f64", (n, 3))
+    grav.compute_acc_direct(fp, fm, fa, n, G, eps2)
+    ke = grav.kinetic_energy(fv, fm, n)
+    pe = grav.potential_energy(fp, fm, n, G, eps2)
+    out["direct"] = dict(pos=pos, vel=vel, mass=mass, G=G, eps2=eps2,
+                         acc=fa.to_numpy(), ke=ke, pe=pe)
+
+
+def gen_engine_direct(R, out):
+    """Engine(softening=0.05) KDK stepping (core/engine.py:108-116) with the
+    reference's own G = 43009.1725 (core/units.py:21)."""
+    pl, eng_mod, units = R["plummer"], R["engine"], R["units"]
+    s = pl.make_plummer(n=48, total_mass=10.0, scale_radius=1.0, seed=42)
+    s.pos, s.vel, s.mass = _f32(s.pos), _f32(s.vel), _f32(s.mass)
+    eng = eng_mod.Engine(softening=0.05)
+    eng.load_state(s)
+    acc0 = eng.acc.to_numpy()
+    e0 = eng.energies()
+    dt, nsteps = 3e-5, 25
+    for _ in range(nsteps):
+        eng.step(dt)
+    st = eng.to_state()
+    out["engine_direct"] = dict(
+        pos0=s.pos, vel0=s.vel, mass=s.mass, acc0=acc0, dt=dt,
+        nsteps=nsteps, softening=0.05, G=units.G, pos=st.pos, vel=st.vel,
+        acc=eng.acc.to_numpy(), e0=np.array(e0), e1=np.array(eng.energies()),
+        time=eng.time, step=eng.step_count)
+
+
+def _disk_positions(R, n, seed):
+    dk = R["disk"]
+    g = dk.make_disk_galaxy(n_disk=n // 2, n_halo=n - n // 2, seed=seed)
+    return _f32(g.pos), _f32(g.mass)
+
+
+def gen_morton(R, out):
+    """morton_codes (core/solvers/barnes_hut.py:27-46) at bits=21 and bits=10,
+    plus the stable argsort of core/solvers/barnes_hut.py:247."""
+    bh = R["bh"]
+    rng = np.random.default_rng(123)
+    cases = {}
+    p, _ = _disk_positions(R, 8192, seed=3)
+    cases["disk"] = p
+    pl = R["plummer"]
+    cases["plummer"] = _f32(pl.make_plummer(n=8192, seed=4).pos)
+    # Heavy duplicates: 600 distinct points each repeated, shuffled.
+    base = _f32(rng.normal(size=(600, 3)))
+    cases["dups"] = base[rng.integers(0, 600, size=4096)]
+    # Degenerate: all points equal (span == 0 -> 1.0 branch, :42).
+    cases["same"] = np.tile(_f32([[1.5, -2.25, 0.125]]), (64, 1))
+    # Planar + tiny extents + negative coordinates.
+    q = _f32(rng.uniform(-1e-3, 1e-3, size=(2048, 3)))
+    q[:, 2] = -7.0
+    cases["plane"] = q
+    # Wide dynamic range.
+    cases["wide"] = _f32(rng.standard_cauchy(size=(4096, 3)) * 50.0)
+    res = {}
+    for name, pos in cases.items():
+        res[f"{name}_pos"] = pos
+        for bits in (21, 10):
+            c = bh.morton_codes(pos, bits=bits)
+            res[f"{name}_code{bits}"] = c
+            res[f"{name}_order{bits}"] = np.argsort(c, kind="stable").astype(np.int32)
+    out["morton"] = res
+
+
+def _bh_pipeline(R, pos, mass, theta, softening, bits, max_stack=64):
+    """The body of BarnesHut.compute (core/solvers/barnes_hut.py:242-259) with
+    the key width as a parameter (the reference hard-codes bits=21 at :246)."""
+    bh, stub = R["bh"], R["stub"]
+    n = pos.shape[0]
+    B = bh.BarnesHut(n, theta=theta, softening=softening, max_stack=max_stack)
+    fp = _field_from(stub, pos)
+    fm = _field_from(stub, mass)
+    fa = stub._field("f64", (n, 3))
+    codes = bh.morton_codes(pos, bits=bits)
+    order = np.argsort(codes, kind="stable").astype(np.int32)
+    B.code.from_numpy(codes[order].astype(np.int64))
+    B.order.from_numpy(order)
+    B.parent.from_numpy(np.full(2 * n - 1, -1, np.int32))
+    bh._build_radix(B.code, B.left, B.right, B.parent, n)
+    bh._leaf_init(B.order, fp, fm, B.com, B.nmass, B.nmom, B.nmin, B.nmax, n)
+    bh._accumulate(B.parent, B.com, B.nmass, B.nmom, B.nmin, B.nmax, n)
+    bh._finalize(B.com, B.nmass, B.nmom, n)
+    bh._traverse(fp, B.order, B.com, B.nmass, B.nmin, B.nmax, B.left, B.right,
+                 fa, B.stack, n, n, B.theta2, B.eps2, B.max_stack)
+    return dict(code=codes, order=order, left=B.left.to_numpy(),
+                right=B.right.to_numpy(), parent=B.parent.to_numpy(),
+                com=B.com.to_numpy(), nmass=B.nmass.to_numpy(),
+                nmin=B.nmin.to_numpy(), nmax=B.nmax.to_numpy(),
+                acc=fa.to_numpy())
+
+
+def gen_bh(R, out):
+    """LBVH Barnes-Hut stages on a disk sample (G = 43009.1725 is compiled
+    into _traverse, core/solvers/barnes_hut.py:202,210)."""
+    bh, stub = R["bh"], R["stub"]
+    pos, mass = _disk_positions(R, 1200, seed=9)
+    res = {"pos": pos, "mass": mass, "theta": 0.5, "softening": 0.05,
+           "G": R["units"].G}
+    for bits in (21, 10):
+        r = _bh_pipeline(R, pos, mass, 0.5, 0.05, bits)
+        for k, v in r.items():
+            res[f"b{bits}_{k}"] = v
+    # BarnesHut.compute itself (bits=21 path), to pin the pipeline above.
+    n = pos.shape[0]
+    B = bh.BarnesHut(n, theta=0.5, softening=0.05)
+    fa = stub._field("f64", (n, 3))
+    B.compute(_field_from(stub, pos), _field_from(stub, mass), fa)
+    res["compute_acc"] = fa.to_numpy()
+    # A tiny stack exercises the silent drop at :212.
+    r = _bh_pipeline(R, pos[:400], mass[:400], 0.5, 0.05, 21, max_stack=6)
+    res["stk6_acc"] = r["acc"]
+    # Duplicate-heavy input: equal codes use the index tie-break (:77-78).
+    rng = np.random.default_rng(77)
+    base = _f32(rng.normal(size=(90, 3)))
+    dpos = base[rng.integers(0, 90, size=500)]
+    dmass = _f32(rng.uniform(0.5, 1.5, size=500) * 1e-3)
+    r = _bh_pipeline(R, dpos, dmass, 0.7, 0.05, 10)
+    res["dup_pos"], res["dup_mass"] = dpos, dmass
+    for k, v in r.items():
+        res[f"dup_{k}"] = v
+    out["bh"] = res
+
+
+def gen_engine_bh(R, out):
+    """Engine(gravity_mode="bh") stepping (core/engine.py:74-80,101-116)."""
+    eng_mod, units = R["engine"], R["units"]
+    dk = R["disk"]
+    g = dk.make_disk_galaxy(n_disk=160, n_halo=140, seed=21)
+    g.pos, g.vel, g.mass = _f32(g.pos), _f32(g.vel), _f32(g.mass)
+    eng = eng_mod.Engine(softening=0.1, gravity_mode="bh", theta=0.6)
+    eng.load_state(g)
+    acc0 = eng.acc.to_numpy()
+    dt, nsteps = 1e-4, 4
+    for _ in range(nsteps):
+        eng.step(dt)
+    out["engine_bh"] = dict(pos0=g.pos, vel0=g.vel, mass=g.mass, acc0=acc0,
+                            dt=dt, nsteps=nsteps, softening=0.1, theta=0.6,
+                            G=units.G, pos=eng.pos.to_numpy(),
+                            vel=eng.vel.to_numpy(), acc=eng.acc.to_numpy())
+
+
+def main(argv):
+    ref_root = argv[1] if len(argv) > 1 else "/root/reference"
+    R = _load_reference(ref_root)
+    out = {}
+    for fn in (gen_plummer_ic, gen_direct, gen_engine_direct, gen_morton,
+               gen_bh, gen_engine_bh):
+        t0 = time.time()
+        fn(R, out)
+        print(f"{fn.__name__}: {time.time() - t0:.1f}s", flush=True)
+    for name, d in out.items():
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **{k: np.asarray(v) for k, v in d.items()})
+        print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KB)")
+
+
+if __name__ == "__main__":
+    main(sys.argv)
