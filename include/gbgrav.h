@@ -1,0 +1,159 @@
+/*
+ * gbgrav.h — C ABI of the GB300 self-gravity engine (sm_103a CUDA).
+ *
+ * Drop-in boundary for the acceleration call of the reference's
+ * Engine(gravity_mode="direct"|"bh") (Khaserdene/real-astronomy-simulation,
+ * core/engine.py:101-106).  Each entry point names the reference function it
+ * replaces.
+ *
+ * Conventions
+ *  - Particle arrays are device pointers to float4 records, passed as float*
+ *    (4 floats per particle, 16-byte aligned):
+ *      xm  = {x, y, z, m}    positions and masses
+ *      vel = {vx, vy, vz, 0} velocities
+ *      acc = {ax, ay, az, 0} accelerations
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).  Every call
+ *    is stream-ordered and asynchronous unless stated otherwise.
+ *  - Every function returns a status code (GB_OK = 0); the message for the
+ *    last failure on the calling thread is gb_last_error_string().
+ *  - Handles are not thread-safe: one thread (or external locking) per
+ *    handle.  The caller owns particle buffers; handles own their scratch.
+ */
+#ifndef GBGRAV_H
+#define GBGRAV_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GB_OK 0
+#define GB_EINVAL 1     /* bad argument (size, pointer, alignment) */
+#define GB_ENOMEM 2     /* device allocation failed */
+#define GB_ESTACK 3     /* traversal stack rule dropped work (see gb_diag_t) */
+#define GB_ETIMEOUT 4   /* a bounded device wait expired */
+#define GB_ECUDA 5      /* CUDA runtime error */
+#define GB_ENOTREADY 6  /* call order violated (e.g. accel before build) */
+
+/* Flags */
+#define GB_ACCUMULATE 0x1  /* acc += result instead of acc = result */
+#define GB_PLAIN_FP32 0x2  /* plain FP32 accumulation (no Kahan compensation) */
+
+/* Device diagnostic counters, read back by gb_*_diag (synchronising). */
+typedef struct gb_diag {
+    uint64_t stack_drops;     /* pushes skipped by the max_stack rule */
+    uint64_t stack_overflow;  /* warp stack capacity reached */
+    uint64_t nonfinite;       /* non-finite positions met while keying */
+    uint64_t bad_tree;        /* inconsistent node met in the bottom-up pass */
+    uint64_t reserved[4];
+} gb_diag_t;
+
+const char *gb_last_error_string(void);
+int gb_version(void);
+
+/* ------------------------------------------------------------ direct N^2 */
+typedef struct gb_direct gb_direct_t;
+
+/* Allocates scratch for systems of up to n_max particles on the current
+ * device.  Replaces the Taichi field allocation in Engine.load_state
+ * (core/engine.py:66-69). */
+int gb_direct_create(gb_direct_t **out, int64_t n_max);
+int gb_direct_destroy(gb_direct_t *h);
+
+/* Tile shape: k targets per lane (2 or 4), warps per CTA (4 or 8), CTAs per
+ * SM (0 = occupancy maximum).  Chosen by the autotuner. */
+int gb_direct_set_tiles(gb_direct_t *h, int k, int warps, int ctas_per_sm);
+
+/* acc_i = G sum_j m_j (x_j - x_i) / (|x_j - x_i|^2 + eps2)^{3/2}, all j
+ * (i == j adds zero).  Replaces compute_acc_direct
+ * (core/solvers/gravity.py:13-26); the GB_ACCUMULATE flag gives the
+ * `acc +=` form of grav_self_direct (core/living_galaxy_engine.py:102-114). */
+int gb_direct_acc(gb_direct_t *h, const float *xm, float *acc, int64_t n,
+                  float G, float eps2, int flags, void *stream);
+
+/* nsteps kick-drift-kick leapfrog steps with direct forces, in place.
+ * acc must hold the accelerations of the current positions on entry.
+ * Replaces Engine.step (core/engine.py:108-116) with kick/drift
+ * (core/integrators/leapfrog.py:11-22) fused into the force pass. */
+int gb_direct_kdk(gb_direct_t *h, float *xm, float *vel, float *acc, int64_t n,
+                  float G, float eps2, float dt, int64_t nsteps, int flags,
+                  void *stream);
+
+/* phi_i = sum_{j != i} m_j / sqrt(|x_j - x_i|^2 + eps2) (FP32, Kahan): the
+ * inner sum of potential_energy (core/solvers/gravity.py:47-55). */
+int gb_direct_phi(gb_direct_t *h, const float *xm, float *phi, int64_t n,
+                  float eps2, int flags, void *stream);
+
+/* FP64 energies into out3 (device, 3 doubles): kinetic, potential, total.
+ * KE = 1/2 sum m v^2 (core/solvers/gravity.py:29-36); PE = -1/2 G sum m_i
+ * phi_i (core/solvers/gravity.py:39-57) with phi from gb_direct_phi; the
+ * reductions run in FP64 in a fixed order. */
+int gb_energy(gb_direct_t *h, const float *xm, const float *vel, int64_t n,
+              float G, float eps2, double *out3, void *stream);
+
+/* FP64 oracle on the device for sampled targets: acc_out (nt x 3 doubles)
+ * = compute_acc_direct (core/solvers/gravity.py:13-26) in float64 for the
+ * particles listed in targets. */
+int gb_direct_acc_fp64(const float *xm, int64_t n, const int64_t *targets,
+                       int64_t nt, double G, double eps2, double *acc_out,
+                       void *stream);
+
+int gb_direct_diag(gb_direct_t *h, gb_diag_t *out, int reset);
+
+/* ----------------------------------------------------- LBVH Barnes-Hut */
+typedef struct gb_bh gb_bh_t;
+
+/* Allocates tree scratch for up to n_max particles with key_bits bits per
+ * axis (21: the reference's 63-bit keys, core/solvers/barnes_hut.py:38; 10:
+ * 30-bit keys).  Replaces BarnesHut.__init__ (core/solvers/barnes_hut.py:
+ * 223-240). */
+int gb_bh_create(gb_bh_t **out, int64_t n_max, int key_bits);
+int gb_bh_destroy(gb_bh_t *h);
+
+/* Device build: bounding box, Morton keys (bit-identical to morton_codes,
+ * core/solvers/barnes_hut.py:27-46), stable radix sort (the permutation of
+ * np.argsort(kind="stable"), :247), Karras tree (_build_radix, :84-121),
+ * node summaries (_leaf_init/_accumulate/_finalize, :124-177). */
+int gb_bh_build(gb_bh_t *h, const float *xm, int64_t n, void *stream);
+
+/* Accelerations from the last build: _traverse (core/solvers/barnes_hut.py:
+ * 180-217) with the same acceptance test and max_stack rule; pushes that the
+ * rule skips are counted in gb_diag_t.stack_drops. */
+int gb_bh_accel(gb_bh_t *h, float *acc, float theta, float eps2, float G,
+                int max_stack, int flags, void *stream);
+
+/* build + accel: BarnesHut.compute (core/solvers/barnes_hut.py:242-259). */
+int gb_bh_compute(gb_bh_t *h, const float *xm, float *acc, int64_t n,
+                  float theta, float eps2, float G, int max_stack, int flags,
+                  void *stream);
+
+/* nsteps KDK steps with tree forces, in place (Engine.step with the BH
+ * solver, core/engine.py:101-116); kick and drift are fused into the first
+ * tree stage and the closing kick into the traversal. */
+int gb_bh_kdk(gb_bh_t *h, float *xm, float *vel, float *acc, int64_t n,
+              float theta, float eps2, float G, float dt, int64_t nsteps,
+              int max_stack, void *stream);
+
+/* Copies one array of the last build, in the reference's layout, to device
+ * memory dst: 0 codes (uint64[n], key order), 1 order (int32[n]), 2 left,
+ * 3 right (int32[n-1]), 4 parent (int32[2n-1]), 5 mass (double[2n-1]),
+ * 6 com, 7 min, 8 max (double[2n-1][3]); nodes are leaves 0..n-1 then
+ * internal nodes n..2n-2 as in core/solvers/barnes_hut.py:229-240. */
+int gb_bh_export(gb_bh_t *h, int what, void *dst, void *stream);
+
+int gb_bh_diag(gb_bh_t *h, gb_diag_t *out, int reset);
+
+/* ------------------------------------------------------------ calibration */
+/* Launches an FP32 FMA-throughput kernel (packed = 1: .f32x2 form) on
+ * `stream`; *flops receives the FLOP count of the launch, which the caller
+ * times.  Measures the FP32 CUDA-core peak used as the direct-sum roofline.
+ * No reference counterpart (measurement support). */
+int gb_calib_fp32(float *scratch, int iters, int packed, double *flops, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBGRAV_H */

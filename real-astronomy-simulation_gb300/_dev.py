@@ -1,0 +1,88 @@
+"""Device-buffer plumbing between torch tensors and the C ABI.
+
+Particle records are float32 float4 rows: xm = {x, y, z, m}, vel = {vx, vy,
+vz, 0}, acc = {ax, ay, az, 0}.  torch only provides the memory and the
+stream; all arithmetic runs in the CUDA library.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+
+def require_cuda(device=None) -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError("the GB300 gravity engine needs a CUDA device; none is visible")
+    dev = torch.device(device if device is not None else "cuda")
+    if dev.type != "cuda":
+        raise ValueError(f"device must be a CUDA device, got {dev}")
+    if dev.index is None:
+        dev = torch.device("cuda", torch.cuda.current_device())
+    return dev
+
+
+def stream_handle(device=None) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def ptr(t: torch.Tensor, name: str = "tensor", dtype=torch.float32, rows4: bool = True) -> int:
+    """Raw device pointer of a contiguous CUDA tensor (checked)."""
+    if not isinstance(t, torch.Tensor):
+        raise TypeError(f"{name} must be a torch tensor")
+    if not t.is_cuda:
+        raise ValueError(f"{name} must live on a CUDA device")
+    if t.dtype != dtype:
+        raise TypeError(f"{name} must be {dtype}, got {t.dtype}")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+    if rows4 and (t.dim() != 2 or t.shape[1] != 4):
+        raise ValueError(f"{name} must have shape (n, 4), got {tuple(t.shape)}")
+    return t.data_ptr()
+
+
+def pack_xm(pos, mass, device) -> torch.Tensor:
+    pos = np.asarray(pos, dtype=np.float64).reshape(-1, 3)
+    mass = np.asarray(mass, dtype=np.float64).reshape(-1)
+    host = np.empty((pos.shape[0], 4), np.float32)
+    host[:, :3] = pos
+    host[:, 3] = mass
+    return torch.from_numpy(host).to(device)
+
+
+def pack_vec(v, device) -> torch.Tensor:
+    v = np.asarray(v, dtype=np.float64).reshape(-1, 3)
+    host = np.zeros((v.shape[0], 4), np.float32)
+    host[:, :3] = v
+    return torch.from_numpy(host).to(device)
+
+
+def empty4(n: int, device) -> torch.Tensor:
+    return torch.zeros((n, 4), dtype=torch.float32, device=device)
+
+
+class FieldView:
+    """Reference-style field access (``to_numpy`` / ``from_numpy``) over a
+    column slice of a float4 device buffer."""
+
+    def __init__(self, buf: torch.Tensor, cols):
+        self._buf = buf
+        self._cols = cols
+
+    @property
+    def tensor(self) -> torch.Tensor:
+        return self._buf[:, self._cols]
+
+    @property
+    def shape(self):
+        return tuple(self.tensor.shape)
+
+    def to_numpy(self) -> np.ndarray:
+        return self.tensor.detach().to("cpu", torch.float64).numpy()
+
+    def from_numpy(self, arr) -> None:
+        src = torch.as_tensor(np.asarray(arr, dtype=np.float32)).reshape(self.shape)
+        self._buf[:, self._cols] = src.to(self._buf.device)
+
+    def __array__(self, dtype=None, copy=None):
+        a = self.to_numpy()
+        return a.astype(dtype) if dtype is not None else a

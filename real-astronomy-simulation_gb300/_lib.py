@@ -1,0 +1,110 @@
+"""ctypes binding of the C ABI in include/gbgrav.h (libgbgrav.so).
+
+The library must have been built (``_buildlib.build()`` / ``build()`` in
+``__graft_entry__``).  There is no fallback: if it is missing, every entry
+point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import _buildlib
+
+P = ctypes.c_void_p
+I32 = ctypes.c_int
+I64 = ctypes.c_int64
+F32 = ctypes.c_float
+F64 = ctypes.c_double
+
+GB_OK = 0
+GB_EINVAL = 1
+GB_ENOMEM = 2
+GB_ESTACK = 3
+GB_ETIMEOUT = 4
+GB_ECUDA = 5
+GB_ENOTREADY = 6
+
+GB_ACCUMULATE = 0x1
+GB_PLAIN_FP32 = 0x2
+
+_STATUS = {GB_EINVAL: "GB_EINVAL", GB_ENOMEM: "GB_ENOMEM", GB_ESTACK: "GB_ESTACK",
+           GB_ETIMEOUT: "GB_ETIMEOUT", GB_ECUDA: "GB_ECUDA",
+           GB_ENOTREADY: "GB_ENOTREADY"}
+
+
+class GravityError(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+    def __init__(self, status: int, func: str, msg: str):
+        self.status = status
+        super().__init__(f"{func}: {_STATUS.get(status, status)}: {msg}")
+
+
+class Diag(ctypes.Structure):
+    _fields_ = [("stack_drops", ctypes.c_uint64), ("stack_overflow", ctypes.c_uint64),
+                ("nonfinite", ctypes.c_uint64), ("bad_tree", ctypes.c_uint64),
+                ("reserved", ctypes.c_uint64 * 4)]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "reserved"}
+
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "gb_last_error_string": (ctypes.c_char_p, []),
+    "gb_version": (I32, []),
+    "gb_direct_create": (I32, [ctypes.POINTER(P), I64]),
+    "gb_direct_destroy": (I32, [P]),
+    "gb_direct_set_tiles": (I32, [P, I32, I32, I32]),
+    "gb_direct_acc": (I32, [P, P, P, I64, F32, F32, I32, P]),
+    "gb_direct_kdk": (I32, [P, P, P, P, I64, F32, F32, F32, I64, I32, P]),
+    "gb_direct_phi": (I32, [P, P, P, I64, F32, I32, P]),
+    "gb_energy": (I32, [P, P, P, I64, F32, F32, P, P]),
+    "gb_direct_acc_fp64": (I32, [P, I64, P, I64, F64, F64, P, P]),
+    "gb_direct_diag": (I32, [P, ctypes.POINTER(Diag), I32]),
+    "gb_calib_fp32": (I32, [P, I32, I32, ctypes.POINTER(F64), P]),
+    "gb_bh_create": (I32, [ctypes.POINTER(P), I64, I32]),
+    "gb_bh_destroy": (I32, [P]),
+    "gb_bh_build": (I32, [P, P, I64, P]),
+    "gb_bh_accel": (I32, [P, P, F32, F32, F32, I32, I32, P]),
+    "gb_bh_compute": (I32, [P, P, P, I64, F32, F32, F32, I32, I32, P]),
+    "gb_bh_kdk": (I32, [P, P, P, P, I64, F32, F32, F32, F32, I64, I32, P]),
+    "gb_bh_export": (I32, [P, I32, P, P]),
+    "gb_bh_diag": (I32, [P, ctypes.POINTER(Diag), I32]),
+}
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _buildlib.LIB
+
+
+def load():
+    """Load libgbgrav.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        raise ImportError(
+            f"{path} is missing: build the CUDA engine first "
+            "(python -c 'import __graft_entry__ as g; g.build()')")
+    L = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def call(name: str, *args) -> int:
+    """Call an int-returning entry point; raise GravityError on failure."""
+    L = load()
+    st = getattr(L, name)(*args)
+    if st != GB_OK:
+        msg = L.gb_last_error_string()
+        raise GravityError(st, name, msg.decode() if msg else "")
+    return st

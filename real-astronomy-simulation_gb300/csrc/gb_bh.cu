@@ -1,0 +1,874 @@
+// LBVH Barnes-Hut on the GB300 (sm_103a): every stage on the device.
+//
+// Replaces BarnesHut.compute (core/solvers/barnes_hut.py:242-259), which runs
+// Morton keys and the stable sort on the host in numpy and the tree kernels
+// in Taichi.  Stages (one CUDA graph per step when driven by gb_bh_kdk):
+//   0 bbox      per-axis min/max (optionally after the fused kick+drift),
+//               last-CTA-done combine -> FP64 quantisation parameters
+//   1 morton    keys bit-identical to morton_codes (:27-46): FP64
+//               (x - lo) * scale with separate roundings, clip, truncate,
+//               interleave x,y,z into bits 3b, 3b+1, 3b+2
+//   2 sort      stable LSD radix sort (8-bit digits) of (key, index): the
+//               permutation of np.argsort(kind="stable") (:247)
+//   3 gather    particles into key order (leaf records)
+//   4 karras    binary radix tree, identical to _build_radix (:84-121)
+//   5 bottom-up node mass / moment (FP64) and AABB; a node is summarised by
+//               the second of its two children to finish (integer arrival
+//               ticket, fences, L2 reads): no floating-point atomics, and the
+//               result is independent of scheduling (:124-177 use FP64
+//               atomics on every ancestor instead)
+//   6 traverse  warp-coherent walk: 32 key-consecutive targets share one
+//               shared-memory stack of (node, lane mask); every lane applies
+//               the reference's own acceptance test size^2 < theta^2 (r^2 +
+//               eps^2) (:204-210), so each particle accepts exactly the node
+//               set of _traverse (:180-217); a per-lane count reproduces the
+//               max_stack rule (:212) and the skipped pushes are counted
+//               instead of being lost silently.  Closing kick fused in the
+//               epilogue for KDK steps.
+#include <algorithm>
+#include <cstdio>
+
+#include "gb_common.cuh"
+
+namespace gb {
+
+struct BHParams {
+    double lo[3];
+    double scale;
+};
+
+// Node mass moment and mass, FP64 (32-byte record).
+struct alignas(32) Mom4 {
+    double x, y, z, w;
+};
+
+constexpr int BBOX_THREADS = 256;
+constexpr int RS_THREADS = 256;
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_ITEMS = 16;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;  // 4096 keys per CTA
+constexpr int RS_BINS = 256;
+constexpr int TRAV_WARPS = 4;
+constexpr int TRAV_STACK = 128;  // > maximum Karras depth (63 + 31 levels)
+constexpr int MAX_DEPTH = 128;
+
+// ------------------------------------------------------------------ bbox
+template <bool KDK>
+__global__ void __launch_bounds__(BBOX_THREADS)
+bh_bbox_kernel(float4 *xm, float4 *vel, const float4 *acc, int64_t n, float h, float dt, float4 *part,
+               unsigned *ticket, BHParams *prm, int bits, unsigned long long *diag) {
+    float mn0 = INFINITY, mn1 = INFINITY, mn2 = INFINITY;
+    float mx0 = -INFINITY, mx1 = -INFINITY, mx2 = -INFINITY;
+    unsigned long long bad = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float4 x = xm[i];
+        if (KDK) {
+            const float4 v = vel[i], a = acc[i];
+            const float vx = kick(v.x, a.x, h), vy = kick(v.y, a.y, h), vz = kick(v.z, a.z, h);
+            x = make_float4(drift(x.x, vx, dt), drift(x.y, vy, dt), drift(x.z, vz, dt), x.w);
+            xm[i] = x;
+            vel[i] = make_float4(vx, vy, vz, v.w);
+        }
+        if (isfinite(x.x) && isfinite(x.y) && isfinite(x.z)) {
+            mn0 = fminf(mn0, x.x); mn1 = fminf(mn1, x.y); mn2 = fminf(mn2, x.z);
+            mx0 = fmaxf(mx0, x.x); mx1 = fmaxf(mx1, x.y); mx2 = fmaxf(mx2, x.z);
+        } else {
+            ++bad;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mn0 = fminf(mn0, __shfl_xor_sync(0xffffffffu, mn0, o));
+        mn1 = fminf(mn1, __shfl_xor_sync(0xffffffffu, mn1, o));
+        mn2 = fminf(mn2, __shfl_xor_sync(0xffffffffu, mn2, o));
+        mx0 = fmaxf(mx0, __shfl_xor_sync(0xffffffffu, mx0, o));
+        mx1 = fmaxf(mx1, __shfl_xor_sync(0xffffffffu, mx1, o));
+        mx2 = fmaxf(mx2, __shfl_xor_sync(0xffffffffu, mx2, o));
+        bad += __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    __shared__ float4 smn[BBOX_THREADS / 32], smx[BBOX_THREADS / 32];
+    __shared__ bool is_last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        smn[wid] = make_float4(mn0, mn1, mn2, 0.f);
+        smx[wid] = make_float4(mx0, mx1, mx2, 0.f);
+        if (bad) atomicAdd(diag + DIAG_NONFINITE, bad);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float4 a = smn[0], b = smx[0];
+        for (int w = 1; w < BBOX_THREADS / 32; ++w) {
+            a.x = fminf(a.x, smn[w].x); a.y = fminf(a.y, smn[w].y); a.z = fminf(a.z, smn[w].z);
+            b.x = fmaxf(b.x, smx[w].x); b.y = fmaxf(b.y, smx[w].y); b.z = fmaxf(b.z, smx[w].z);
+        }
+        part[2 * blockIdx.x] = a;
+        part[2 * blockIdx.x + 1] = b;
+        __threadfence();
+        is_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!is_last || threadIdx.x != 0) return;
+    __threadfence();
+    float4 a = __ldcg(part), b = __ldcg(part + 1);
+    for (unsigned k = 1; k < gridDim.x; ++k) {
+        const float4 c = __ldcg(part + 2 * k), d = __ldcg(part + 2 * k + 1);
+        a.x = fminf(a.x, c.x); a.y = fminf(a.y, c.y); a.z = fminf(a.z, c.z);
+        b.x = fmaxf(b.x, d.x); b.y = fmaxf(b.y, d.y); b.z = fmaxf(b.z, d.z);
+    }
+    // span = largest per-axis extent (:41); 1.0 when not > 0 (:42).
+    const double lo0 = a.x, lo1 = a.y, lo2 = a.z;
+    double span = __dsub_rn((double)b.x, lo0);
+    span = fmax(span, __dsub_rn((double)b.y, lo1));
+    span = fmax(span, __dsub_rn((double)b.z, lo2));
+    if (!(span > 0.0)) span = 1.0;
+    const double qmax = (double)((1ull << bits) - 1ull);
+    prm->lo[0] = lo0;
+    prm->lo[1] = lo1;
+    prm->lo[2] = lo2;
+    prm->scale = __ddiv_rn(qmax, __dmul_rn(span, 1.0000001));
+    *ticket = 0u;
+}
+
+// ---------------------------------------------------------------- morton
+template <int BITS>
+__device__ __forceinline__ uint64_t interleave3(uint32_t x, uint32_t y, uint32_t z) {
+    uint64_t r = 0;
+#pragma unroll
+    for (int b = 0; b < BITS; ++b) {
+        const uint64_t t = ((x >> b) & 1u) | (((y >> b) & 1u) << 1) | (((z >> b) & 1u) << 2);
+        r |= t << (3 * b);
+    }
+    return r;
+}
+
+__device__ __forceinline__ uint32_t quantise(float x, double lo, double scale, double qmax) {
+    double t = __dmul_rn(__dsub_rn((double)x, lo), scale);
+    t = t > qmax ? qmax : t;
+    t = t >= 0.0 ? t : 0.0;  // also maps NaN to 0 (counted in the bbox pass)
+    return __double2uint_rz(t);
+}
+
+template <typename KeyT, int BITS>
+__global__ void bh_morton_kernel(const float4 *__restrict__ xm, int64_t n, const BHParams *__restrict__ prm,
+                                 KeyT *__restrict__ keys, uint32_t *__restrict__ vals) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double qmax = (double)((1ull << BITS) - 1ull);
+    const double sc = prm->scale;
+    const float4 x = xm[i];
+    const uint32_t qx = quantise(x.x, prm->lo[0], sc, qmax);
+    const uint32_t qy = quantise(x.y, prm->lo[1], sc, qmax);
+    const uint32_t qz = quantise(x.z, prm->lo[2], sc, qmax);
+    keys[i] = (KeyT)interleave3<BITS>(qx, qy, qz);
+    vals[i] = (uint32_t)i;
+}
+
+// ------------------------------------------------------------ radix sort
+template <typename KeyT>
+__global__ void __launch_bounds__(RS_THREADS)
+rs_upsweep_kernel(const KeyT *__restrict__ keys, int64_t n, int shift, uint32_t *__restrict__ hist, int nb) {
+    __shared__ uint32_t h[RS_BINS];
+    for (int d = threadIdx.x; d < RS_BINS; d += RS_THREADS) h[d] = 0;
+    __syncthreads();
+    const int64_t base = (int64_t)blockIdx.x * RS_TILE;
+    for (int k = threadIdx.x; k < RS_TILE; k += RS_THREADS) {
+        const int64_t i = base + k;
+        if (i < n) atomicAdd(&h[(uint32_t)(keys[i] >> shift) & 0xFFu], 1u);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < RS_BINS; d += RS_THREADS) hist[(int64_t)d * nb + blockIdx.x] = h[d];
+}
+
+// Exclusive scan of the digit-major histogram (one CTA of 1024 threads).
+__global__ void __launch_bounds__(1024) rs_scan_kernel(uint32_t *hist, int64_t count) {
+    __shared__ uint32_t wsum[32];
+    const int64_t per = (count + 1023) / 1024;
+    const int64_t b = threadIdx.x * per, e = min(count, b + per);
+    uint32_t s = 0;
+    for (int64_t k = b; k < e; ++k) s += hist[k];
+    // block exclusive scan of s
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t inc = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) wsum[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t w = wsum[lane], wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += t;
+        }
+        wsum[lane] = wi - w;
+    }
+    __syncthreads();
+    uint32_t run = wsum[wid] + inc - s;
+    for (int64_t k = b; k < e; ++k) {
+        const uint32_t v = hist[k];
+        hist[k] = run;
+        run += v;
+    }
+}
+
+// Stable scatter: elements of a tile are ranked in index order (warp, round,
+// lane) among equal digits with match/ballot, then written to the scanned
+// global offset of (digit, tile).
+template <typename KeyT>
+__global__ void __launch_bounds__(RS_THREADS)
+rs_downsweep_kernel(const KeyT *__restrict__ kin, const uint32_t *__restrict__ vin, KeyT *__restrict__ kout,
+                    uint32_t *__restrict__ vout, int64_t n, int shift, const uint32_t *__restrict__ hist, int nb,
+                    unsigned long long *diag) {
+    __shared__ uint32_t whist[RS_WARPS][RS_BINS];
+    __shared__ uint32_t boff[RS_BINS];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int d = threadIdx.x; d < RS_BINS; d += RS_THREADS) {
+        boff[d] = hist[(int64_t)d * nb + blockIdx.x];
+#pragma unroll
+        for (int w = 0; w < RS_WARPS; ++w) whist[w][d] = 0;
+    }
+    __syncthreads();
+    const int64_t wbase = (int64_t)blockIdx.x * RS_TILE + (int64_t)wid * (RS_ITEMS * 32);
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    KeyT key[RS_ITEMS];
+    uint32_t val[RS_ITEMS];
+    uint32_t rank[RS_ITEMS];
+#pragma unroll
+    for (int r = 0; r < RS_ITEMS; ++r) {
+        const int64_t i = wbase + r * 32 + lane;
+        const bool ok = i < n;
+        key[r] = ok ? kin[i] : (KeyT)0;
+        val[r] = ok ? vin[i] : 0u;
+        const uint32_t dig = (uint32_t)(key[r] >> shift) & 0xFFu;
+        const uint32_t tag = ok ? dig : (0x100u | (uint32_t)lane);
+        const uint32_t peers = __match_any_sync(0xffffffffu, tag);
+        const uint32_t before = ok ? whist[wid][dig] : 0u;
+        rank[r] = before + __popc(peers & lt_mask);
+        __syncwarp();
+        if (ok && (peers & lt_mask) == 0) whist[wid][dig] = before + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < RS_BINS; d += RS_THREADS) {
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < RS_WARPS; ++w) {
+            const uint32_t t = whist[w][d];
+            whist[w][d] = run;
+            run += t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RS_ITEMS; ++r) {
+        const int64_t i = wbase + r * 32 + lane;
+        if (i < n) {
+            const uint32_t dig = (uint32_t)(key[r] >> shift) & 0xFFu;
+            const uint32_t dst = boff[dig] + whist[wid][dig] + rank[r];
+            if (dst < n) {
+                kout[dst] = key[r];
+                vout[dst] = val[r];
+            } else {
+                atomicAdd(diag + DIAG_BAD_TREE, 1ull);
+            }
+        }
+    }
+}
+
+// ----------------------------------------------------------------- gather
+__global__ void bh_gather_kernel(const float4 *__restrict__ xm, const uint32_t *__restrict__ order, int64_t n,
+                                 float4 *__restrict__ leaf, unsigned long long *diag) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t o = order[i];
+    if (o < n) {
+        leaf[i] = __ldg(xm + o);
+    } else {
+        leaf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        atomicAdd(diag + DIAG_BAD_TREE, 1ull);
+    }
+}
+
+// ----------------------------------------------------------------- karras
+// Common-prefix length of keys i and j over bits 62..0; equal keys continue
+// with the index bits 30..0 (63 + prefix); -1 outside [0, n) (:71-81).
+__device__ __forceinline__ int clz63(uint64_t x) { return __clzll(x) - 1; }
+__device__ __forceinline__ int clz63(uint32_t x) { return __clz(x) + 31; }
+
+template <typename KeyT>
+__device__ __forceinline__ int kdelta(const KeyT *__restrict__ k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    const KeyT x = __ldg(k + i) ^ __ldg(k + j);
+    if (x == 0) return 63 + (__clz(i ^ j) - 1);
+    return clz63(x);
+}
+
+template <typename KeyT>
+__global__ void bh_karras_kernel(const KeyT *__restrict__ k, int n, int2 *__restrict__ child,
+                                 int *__restrict__ parent) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) parent[n] = -1;  // the root (internal node 0 = id n)
+    if (i >= n - 1) return;
+    const int d = kdelta(k, n, i, i + 1) > kdelta(k, n, i, i - 1) ? 1 : -1;
+    const int d_min = kdelta(k, n, i, i - d);
+    int l_max = 2;
+    while (kdelta(k, n, i, i + l_max * d) > d_min) l_max *= 2;
+    int l = 0;
+    for (int t = l_max / 2; t >= 1; t /= 2)
+        if (kdelta(k, n, i, i + (l + t) * d) > d_min) l += t;
+    const int j = i + l * d;
+    const int d_node = kdelta(k, n, i, j);
+    int s = 0;
+    int t2 = (l + 1) / 2;
+    while (t2 >= 1) {
+        if (kdelta(k, n, i, i + (s + t2) * d) > d_node) s += t2;
+        t2 = t2 > 1 ? (t2 + 1) / 2 : 0;
+    }
+    const int gamma = i + s * d + min(d, 0);
+    const int lo = min(i, j), hi = max(i, j);
+    const int lc = (lo == gamma) ? gamma : gamma + n;
+    const int rc = (hi == gamma + 1) ? gamma + 1 : gamma + 1 + n;
+    child[i] = make_int2(lc, rc);
+    parent[lc] = i + n;
+    parent[rc] = i + n;
+}
+
+// -------------------------------------------------------------- bottom-up
+struct NodeSum {
+    double mx, my, mz, m;  // mass moment and mass
+    float lx, ly, lz, hx, hy, hz;
+};
+
+__device__ __forceinline__ NodeSum child_sum(int c, int n, const float4 *__restrict__ leaf,
+                                             const Mom4 *__restrict__ mom, const float4 *__restrict__ bmin,
+                                             const float4 *__restrict__ bmax) {
+    NodeSum s;
+    if (c < n) {
+        const float4 p = __ldg(leaf + c);
+        const double m = p.w;
+        s.m = m;
+        s.mx = m * (double)p.x;
+        s.my = m * (double)p.y;
+        s.mz = m * (double)p.z;
+        s.lx = s.hx = p.x;
+        s.ly = s.hy = p.y;
+        s.lz = s.hz = p.z;
+    } else {
+        const int k = c - n;
+        const double2 q0 = __ldcg(reinterpret_cast<const double2 *>(mom + k));
+        const double2 q1 = __ldcg(reinterpret_cast<const double2 *>(mom + k) + 1);
+        const float4 a = __ldcg(bmin + k), b = __ldcg(bmax + k);
+        s.mx = q0.x; s.my = q0.y; s.mz = q1.x; s.m = q1.y;
+        s.lx = a.x; s.ly = a.y; s.lz = a.z;
+        s.hx = b.x; s.hy = b.y; s.hz = b.z;
+    }
+    return s;
+}
+
+__global__ void bh_bottomup_kernel(const float4 *__restrict__ leaf, const int2 *__restrict__ child,
+                                   const int *__restrict__ parent, int n, unsigned *__restrict__ arrivals,
+                                   Mom4 *__restrict__ mom, float4 *__restrict__ bmin, float4 *__restrict__ bmax,
+                                   float4 *__restrict__ inode, unsigned long long *diag) {
+    const int li = blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= n) return;
+    int node = __ldg(parent + li);
+    for (int depth = 0; node >= 0; ++depth) {
+        if (depth >= MAX_DEPTH || node < n || node >= 2 * n - 1) {
+            atomicAdd(diag + DIAG_BAD_TREE, 1ull);
+            return;
+        }
+        const int k = node - n;
+        __threadfence();  // publish the finished child before signalling
+        if (atomicAdd(arrivals + k, 1u) == 0u) return;  // sibling still running
+        __threadfence();  // acquire the sibling's record
+        const int2 c = __ldg(child + k);
+        if ((unsigned)c.x >= (unsigned)(2 * n - 1) || (unsigned)c.y >= (unsigned)(2 * n - 1)) {
+            atomicAdd(diag + DIAG_BAD_TREE, 1ull);
+            return;
+        }
+        const NodeSum a = child_sum(c.x, n, leaf, mom, bmin, bmax);
+        const NodeSum b = child_sum(c.y, n, leaf, mom, bmin, bmax);
+        NodeSum s;
+        s.m = a.m + b.m;
+        s.mx = a.mx + b.mx;
+        s.my = a.my + b.my;
+        s.mz = a.mz + b.mz;
+        s.lx = fminf(a.lx, b.lx); s.ly = fminf(a.ly, b.ly); s.lz = fminf(a.lz, b.lz);
+        s.hx = fmaxf(a.hx, b.hx); s.hy = fmaxf(a.hy, b.hy); s.hz = fmaxf(a.hz, b.hz);
+        mom[k] = Mom4{s.mx, s.my, s.mz, s.m};
+        bmin[k] = make_float4(s.lx, s.ly, s.lz, 0.f);
+        bmax[k] = make_float4(s.hx, s.hy, s.hz, 0.f);
+        // Traversal record: {com, mass}, {size^2, left, right, 0}.
+        double cx = 0.0, cy = 0.0, cz = 0.0;
+        if (s.m > 0.0) { cx = s.mx / s.m; cy = s.my / s.m; cz = s.mz / s.m; }
+        double size = (double)s.hx - (double)s.lx;
+        size = fmax(size, (double)s.hy - (double)s.ly);
+        size = fmax(size, (double)s.hz - (double)s.lz);
+        inode[2 * k] = make_float4((float)cx, (float)cy, (float)cz, (float)s.m);
+        inode[2 * k + 1] = make_float4((float)(size * size), __int_as_float(c.x), __int_as_float(c.y), 0.f);
+        node = __ldg(parent + node);
+    }
+}
+
+// --------------------------------------------------------------- traverse
+struct TravArgs {
+    const float4 *__restrict__ leaf;
+    const float4 *__restrict__ inode;
+    const uint32_t *__restrict__ order;
+    float4 *acc;
+    float4 *vel;
+    int n;
+    float theta2, eps2, G, h;
+    int max_stack;
+    int accumulate;
+    unsigned long long *diag;
+};
+
+template <bool KDK>
+__global__ void __launch_bounds__(TRAV_WARPS * 32)
+bh_traverse_kernel(TravArgs a) {
+    __shared__ int stk_node[TRAV_WARPS][TRAV_STACK];
+    __shared__ unsigned stk_mask[TRAV_WARPS][TRAV_STACK];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int s = (blockIdx.x * TRAV_WARPS + wid) * 32 + lane;
+    if ((blockIdx.x * TRAV_WARPS + wid) * 32 >= a.n) return;  // whole warp out of range
+    const bool valid = s < a.n;
+    const int n = a.n;
+    float px = 0.f, py = 0.f, pz = 0.f;
+    if (valid) {
+        const float4 p = __ldg(a.leaf + s);
+        px = p.x; py = p.y; pz = p.z;
+    }
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    unsigned drops = 0, overflow = 0, bad = 0;
+    int sp_lane = 0;
+    int top = 0;
+    if (n >= 2) {
+        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+        if (lane == 0) {
+            stk_node[wid][0] = n;
+            stk_mask[wid][0] = vmask;
+        }
+        sp_lane = valid ? 1 : 0;
+        top = 1;
+        __syncwarp();
+    }
+    while (top > 0) {
+        --top;
+        const int node = stk_node[wid][top];
+        const unsigned m = stk_mask[wid][top];
+        const bool in = (m >> lane) & 1u;
+        sp_lane -= in ? 1 : 0;
+        if ((unsigned)node >= (unsigned)(2 * n - 1)) {  // never for a consistent tree
+            bad += in ? 1u : 0u;
+            __syncwarp();
+            continue;
+        }
+        if (node < n) {
+            const float4 q = __ldg(a.leaf + node);
+            if (in && node != s) {
+                const float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
+                const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, a.eps2)));
+                const float inv = rsqrt_approx(r2);
+                const float sc = q.w * inv * inv * inv;
+                ax = __fmaf_rn(sc, dx, ax);
+                ay = __fmaf_rn(sc, dy, ay);
+                az = __fmaf_rn(sc, dz, az);
+            }
+            __syncwarp();
+            continue;
+        }
+        const int k = node - n;
+        const float4 A = __ldg(a.inode + 2 * k);
+        const float4 B = __ldg(a.inode + 2 * k + 1);
+        bool want = false;
+        if (in) {
+            const float dx = A.x - px, dy = A.y - py, dz = A.z - pz;
+            const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, a.eps2)));
+            if (B.x < a.theta2 * r2) {
+                const float inv = rsqrt_approx(r2);
+                const float sc = A.w * inv * inv * inv;
+                ax = __fmaf_rn(sc, dx, ax);
+                ay = __fmaf_rn(sc, dy, ay);
+                az = __fmaf_rn(sc, dz, az);
+            } else if (sp_lane + 2 <= a.max_stack) {
+                want = true;
+            } else {
+                ++drops;
+            }
+        }
+        const unsigned om = __ballot_sync(0xffffffffu, want);
+        if (om) {
+            if (top + 2 <= TRAV_STACK) {
+                if (lane == 0) {
+                    stk_node[wid][top] = __float_as_int(B.y);
+                    stk_mask[wid][top] = om;
+                    stk_node[wid][top + 1] = __float_as_int(B.z);
+                    stk_mask[wid][top + 1] = om;
+                }
+                top += 2;
+                sp_lane += want ? 2 : 0;
+            } else if (want) {
+                ++overflow;
+            }
+        }
+        __syncwarp();
+    }
+    // Epilogue: scatter to the original particle index.
+    unsigned dsum = drops, osum = overflow, bsum = bad;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+        osum += __shfl_xor_sync(0xffffffffu, osum, o);
+        bsum += __shfl_xor_sync(0xffffffffu, bsum, o);
+    }
+    if (lane == 0) {
+        if (dsum) atomicAdd(a.diag + DIAG_STACK_DROPS, (unsigned long long)dsum);
+        if (osum) atomicAdd(a.diag + DIAG_STACK_OVERFLOW, (unsigned long long)osum);
+        if (bsum) atomicAdd(a.diag + DIAG_BAD_TREE, (unsigned long long)bsum);
+    }
+    if (!valid) return;
+    const uint32_t p = __ldg(a.order + s);
+    if (p >= (uint32_t)n) return;
+    const float gx = a.G * ax, gy = a.G * ay, gz = a.G * az;
+    if (KDK) {
+        const float4 vh = a.vel[p];
+        a.vel[p] = make_float4(kick(vh.x, gx, a.h), kick(vh.y, gy, a.h), kick(vh.z, gz, a.h), vh.w);
+        a.acc[p] = make_float4(gx, gy, gz, 0.f);
+    } else if (a.accumulate) {
+        float4 o = a.acc[p];
+        o.x += gx; o.y += gy; o.z += gz;
+        a.acc[p] = o;
+    } else {
+        a.acc[p] = make_float4(gx, gy, gz, 0.f);
+    }
+}
+
+// ----------------------------------------------------------------- export
+// Tree arrays in the reference's layout for parity checks.
+enum ExportWhat {
+    EXP_CODES = 0,   // uint64[n]  keys in sorted order
+    EXP_ORDER = 1,   // int32[n]
+    EXP_LEFT = 2,    // int32[n-1]
+    EXP_RIGHT = 3,   // int32[n-1]
+    EXP_PARENT = 4,  // int32[2n-1]
+    EXP_MASS = 5,    // double[2n-1]
+    EXP_COM = 6,     // double[2n-1][3]
+    EXP_MIN = 7,     // double[2n-1][3]
+    EXP_MAX = 8      // double[2n-1][3]
+};
+
+template <typename KeyT>
+__global__ void bh_export_kernel(int what, int n, const KeyT *keys, const uint32_t *order, const int2 *child,
+                                 const int *parent, const float4 *leaf, const Mom4 *mom, const float4 *bmin,
+                                 const float4 *bmax, void *dst) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nodes = 2 * (int64_t)n - 1;
+    switch (what) {
+        case EXP_CODES:
+            if (i < n) ((uint64_t *)dst)[i] = (uint64_t)keys[i];
+            break;
+        case EXP_ORDER:
+            if (i < n) ((int *)dst)[i] = (int)order[i];
+            break;
+        case EXP_LEFT:
+            if (i < n - 1) ((int *)dst)[i] = child[i].x;
+            break;
+        case EXP_RIGHT:
+            if (i < n - 1) ((int *)dst)[i] = child[i].y;
+            break;
+        case EXP_PARENT:
+            if (i < nodes) ((int *)dst)[i] = i < n ? parent[i] : parent[i];
+            break;
+        default: {
+            if (i >= nodes) break;
+            double m, c[3], lo[3], hi[3];
+            if (i < n) {
+                const float4 p = leaf[i];
+                m = p.w;
+                c[0] = lo[0] = hi[0] = p.x;
+                c[1] = lo[1] = hi[1] = p.y;
+                c[2] = lo[2] = hi[2] = p.z;
+            } else {
+                const int k = (int)(i - n);
+                const Mom4 q = mom[k];
+                m = q.w;
+                c[0] = m > 0.0 ? q.x / m : 0.0;
+                c[1] = m > 0.0 ? q.y / m : 0.0;
+                c[2] = m > 0.0 ? q.z / m : 0.0;
+                lo[0] = bmin[k].x; lo[1] = bmin[k].y; lo[2] = bmin[k].z;
+                hi[0] = bmax[k].x; hi[1] = bmax[k].y; hi[2] = bmax[k].z;
+            }
+            double *o = (double *)dst;
+            if (what == EXP_MASS) o[i] = m;
+            else {
+                const double *src = what == EXP_COM ? c : (what == EXP_MIN ? lo : hi);
+                o[3 * i] = src[0];
+                o[3 * i + 1] = src[1];
+                o[3 * i + 2] = src[2];
+            }
+        }
+    }
+}
+
+}  // namespace gb
+
+// ================================================================ C ABI
+using namespace gb;
+
+struct gb_bh {
+    int device, sms;
+    int64_t n_max;
+    int key_bits;
+    int64_t n;  // n of the last build (-1: none)
+    void *keys[2];
+    uint32_t *vals[2];
+    int cur;  // which buffer holds the sorted result
+    uint32_t *hist;
+    int64_t hist_cap;
+    float4 *bbox_part;
+    int bbox_blocks;
+    unsigned *ticket;
+    BHParams *prm;
+    float4 *leaf;
+    int2 *child;
+    int *parent;
+    unsigned *arrivals;
+    Mom4 *mom;
+    float4 *bmin, *bmax;
+    float4 *inode;
+    unsigned long long *diag;
+};
+
+static size_t key_size(int bits) { return bits <= 10 ? sizeof(uint32_t) : sizeof(uint64_t); }
+
+extern "C" int gb_bh_destroy(gb_bh_t *h) {
+    if (!h) return GB_OK;
+    void *ptrs[] = {h->keys[0], h->keys[1], h->vals[0], h->vals[1], h->hist, h->bbox_part, h->ticket,
+                    h->prm, h->leaf, h->child, h->parent, h->arrivals, h->mom, h->bmin, h->bmax,
+                    h->inode, h->diag};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    delete h;
+    return GB_OK;
+}
+
+extern "C" int gb_bh_create(gb_bh_t **out, int64_t n_max, int key_bits) {
+    if (!out) return fail(GB_EINVAL, "out is NULL");
+    *out = nullptr;
+    if (n_max < 1 || n_max > ((int64_t)1 << 30)) return fail(GB_EINVAL, "n_max=%lld out of range", (long long)n_max);
+    if (key_bits != 10 && key_bits != 21) return fail(GB_EINVAL, "key_bits must be 10 or 21 (got %d)", key_bits);
+    gb_bh_t *h = new gb_bh();
+    GB_CUDA_TRY(cudaGetDevice(&h->device));
+    h->sms = num_sms();
+    h->n_max = n_max;
+    h->key_bits = key_bits;
+    h->n = -1;
+    h->cur = 0;
+    const int64_t nn = n_max, ni = std::max<int64_t>(n_max - 1, 1), nodes = 2 * n_max;
+    const int64_t nb = (n_max + RS_TILE - 1) / RS_TILE;
+    h->hist_cap = (int64_t)RS_BINS * nb;
+    h->bbox_blocks = std::max(1, std::min(h->sms * 4, (int)((n_max + BBOX_THREADS - 1) / BBOX_THREADS)));
+    bool ok = true;
+    auto A = [&](void **p, size_t bytes) {
+        if (ok && cudaMalloc(p, bytes) != cudaSuccess) ok = false;
+    };
+    A(&h->keys[0], key_size(key_bits) * nn);
+    A(&h->keys[1], key_size(key_bits) * nn);
+    A((void **)&h->vals[0], sizeof(uint32_t) * nn);
+    A((void **)&h->vals[1], sizeof(uint32_t) * nn);
+    A((void **)&h->hist, sizeof(uint32_t) * h->hist_cap);
+    A((void **)&h->bbox_part, sizeof(float4) * 2 * h->bbox_blocks);
+    A((void **)&h->ticket, sizeof(unsigned));
+    A((void **)&h->prm, sizeof(BHParams));
+    A((void **)&h->leaf, sizeof(float4) * nn);
+    A((void **)&h->child, sizeof(int2) * ni);
+    A((void **)&h->parent, sizeof(int) * nodes);
+    A((void **)&h->arrivals, sizeof(unsigned) * ni);
+    A((void **)&h->mom, sizeof(Mom4) * ni);
+    A((void **)&h->bmin, sizeof(float4) * ni);
+    A((void **)&h->bmax, sizeof(float4) * ni);
+    A((void **)&h->inode, sizeof(float4) * 2 * ni);
+    A((void **)&h->diag, sizeof(unsigned long long) * DIAG_COUNT);
+    if (!ok) {
+        gb_bh_destroy(h);
+        return fail(GB_ENOMEM, "gb_bh_create: device allocation failed for n_max=%lld", (long long)n_max);
+    }
+    if (cudaMemset(h->ticket, 0, sizeof(unsigned)) != cudaSuccess ||
+        cudaMemset(h->diag, 0, sizeof(unsigned long long) * DIAG_COUNT) != cudaSuccess) {
+        gb_bh_destroy(h);
+        return fail(GB_ECUDA, "gb_bh_create: memset failed");
+    }
+    *out = h;
+    return GB_OK;
+}
+
+template <typename KeyT, int BITS>
+static int build_impl(gb_bh_t *h, float4 *xm, float4 *vel, const float4 *acc, int64_t n, float dt, bool kdk,
+                      cudaStream_t s) {
+    const int nblk = std::max(1, std::min(h->bbox_blocks, (int)((n + BBOX_THREADS - 1) / BBOX_THREADS)));
+    if (kdk)
+        bh_bbox_kernel<true><<<nblk, BBOX_THREADS, 0, s>>>(xm, vel, acc, n, 0.5f * dt, dt, h->bbox_part, h->ticket,
+                                                           h->prm, BITS, h->diag);
+    else
+        bh_bbox_kernel<false><<<nblk, BBOX_THREADS, 0, s>>>(xm, nullptr, nullptr, n, 0.f, 0.f, h->bbox_part,
+                                                            h->ticket, h->prm, BITS, h->diag);
+    const unsigned g256 = (unsigned)((n + 255) / 256);
+    KeyT *k0 = (KeyT *)h->keys[0], *k1 = (KeyT *)h->keys[1];
+    uint32_t *v0 = h->vals[0], *v1 = h->vals[1];
+    bh_morton_kernel<KeyT, BITS><<<g256, 256, 0, s>>>(xm, n, h->prm, k0, v0);
+    const int nb = (int)((n + RS_TILE - 1) / RS_TILE);
+    const int passes = (3 * BITS + 7) / 8;
+    for (int p = 0; p < passes; ++p) {
+        rs_upsweep_kernel<KeyT><<<nb, RS_THREADS, 0, s>>>(k0, n, 8 * p, h->hist, nb);
+        rs_scan_kernel<<<1, 1024, 0, s>>>(h->hist, (int64_t)RS_BINS * nb);
+        rs_downsweep_kernel<KeyT><<<nb, RS_THREADS, 0, s>>>(k0, v0, k1, v1, n, 8 * p, h->hist, nb, h->diag);
+        std::swap(k0, k1);
+        std::swap(v0, v1);
+    }
+    h->cur = (k0 == (KeyT *)h->keys[0]) ? 0 : 1;
+    bh_gather_kernel<<<g256, 256, 0, s>>>(xm, v0, n, h->leaf, h->diag);
+    const int ni = (int)std::max<int64_t>(n - 1, 1);
+    bh_karras_kernel<KeyT><<<(ni + 255) / 256, 256, 0, s>>>(k0, (int)n, h->child, h->parent);
+    if (n >= 2) {
+        GB_CUDA_TRY(cudaMemsetAsync(h->arrivals, 0, sizeof(unsigned) * (n - 1), s));
+        bh_bottomup_kernel<<<g256, 256, 0, s>>>(h->leaf, h->child, h->parent, (int)n, h->arrivals, h->mom, h->bmin,
+                                                h->bmax, h->inode, h->diag);
+    }
+    GB_CUDA_TRY(cudaGetLastError());
+    h->n = n;
+    return GB_OK;
+}
+
+static int build_any(gb_bh_t *h, float4 *xm, float4 *vel, const float4 *acc, int64_t n, float dt, bool kdk,
+                     cudaStream_t s) {
+    if (h->key_bits == 10) return build_impl<uint32_t, 10>(h, xm, vel, acc, n, dt, kdk, s);
+    return build_impl<uint64_t, 21>(h, xm, vel, acc, n, dt, kdk, s);
+}
+
+static int check_bh(gb_bh_t *h, int64_t n) {
+    if (!h) return fail(GB_EINVAL, "handle is NULL");
+    if (n < 0 || n > h->n_max) return fail(GB_EINVAL, "n=%lld outside [0, n_max=%lld]", (long long)n, (long long)h->n_max);
+    return GB_OK;
+}
+
+static int check_ptr(const void *p, const char *name) {
+    if (!p) return fail(GB_EINVAL, "%s is NULL", name);
+    if (!aligned16(p)) return fail(GB_EINVAL, "%s is not 16-byte aligned", name);
+    return GB_OK;
+}
+
+static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float theta, float eps2, float G, float dt, int max_stack,
+                    int flags, bool kdk, cudaStream_t s) {
+    const int64_t n = h->n;
+    if (n <= 0) return GB_OK;
+    TravArgs a;
+    a.leaf = h->leaf;
+    a.inode = h->inode;
+    a.order = h->vals[h->cur];
+    a.acc = acc;
+    a.vel = vel;
+    a.n = (int)n;
+    a.theta2 = theta * theta;
+    a.eps2 = eps2;
+    a.G = G;
+    a.h = 0.5f * dt;
+    a.max_stack = max_stack;
+    a.accumulate = (flags & GB_ACCUMULATE) ? 1 : 0;
+    a.diag = h->diag;
+    const int64_t warps = (n + 31) / 32;
+    const unsigned grid = (unsigned)((warps + TRAV_WARPS - 1) / TRAV_WARPS);
+    if (kdk) bh_traverse_kernel<true><<<grid, TRAV_WARPS * 32, 0, s>>>(a);
+    else bh_traverse_kernel<false><<<grid, TRAV_WARPS * 32, 0, s>>>(a);
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+}
+
+static int check_params(float theta, float eps2, int max_stack) {
+    if (!(theta >= 0.f)) return fail(GB_EINVAL, "theta must be >= 0");
+    if (!(eps2 > 0.f)) return fail(GB_EINVAL, "eps2 must be > 0");
+    if (max_stack < 1) return fail(GB_EINVAL, "max_stack must be >= 1");
+    return GB_OK;
+}
+
+extern "C" int gb_bh_build(gb_bh_t *h, const float *xm, int64_t n, void *stream) {
+    GB_TRY(check_bh(h, n));
+    if (n == 0) {
+        h->n = 0;
+        return GB_OK;
+    }
+    GB_TRY(check_ptr(xm, "xm"));
+    return build_any(h, (float4 *)xm, nullptr, nullptr, n, 0.f, false, (cudaStream_t)stream);
+}
+
+extern "C" int gb_bh_accel(gb_bh_t *h, float *acc, float theta, float eps2, float G, int max_stack, int flags,
+                           void *stream) {
+    if (!h) return fail(GB_EINVAL, "handle is NULL");
+    if (h->n < 0) return fail(GB_ENOTREADY, "gb_bh_accel before gb_bh_build");
+    if (h->n == 0) return GB_OK;
+    GB_TRY(check_ptr(acc, "acc"));
+    GB_TRY(check_params(theta, eps2, max_stack));
+    return traverse(h, (float4 *)acc, nullptr, theta, eps2, G, 0.f, max_stack, flags, false, (cudaStream_t)stream);
+}
+
+extern "C" int gb_bh_compute(gb_bh_t *h, const float *xm, float *acc, int64_t n, float theta, float eps2, float G,
+                             int max_stack, int flags, void *stream) {
+    GB_TRY(check_bh(h, n));
+    if (n > 0) {
+        GB_TRY(check_ptr(acc, "acc"));
+        GB_TRY(check_params(theta, eps2, max_stack));
+    }
+    GB_TRY(gb_bh_build(h, xm, n, stream));
+    return gb_bh_accel(h, acc, theta, eps2, G, max_stack, flags, stream);
+}
+
+extern "C" int gb_bh_kdk(gb_bh_t *h, float *xm, float *vel, float *acc, int64_t n, float theta, float eps2, float G,
+                         float dt, int64_t nsteps, int max_stack, void *stream) {
+    GB_TRY(check_bh(h, n));
+    if (nsteps < 0) return fail(GB_EINVAL, "nsteps < 0");
+    if (n == 0 || nsteps == 0) return GB_OK;
+    GB_TRY(check_ptr(xm, "xm"));
+    GB_TRY(check_ptr(vel, "vel"));
+    GB_TRY(check_ptr(acc, "acc"));
+    GB_TRY(check_params(theta, eps2, max_stack));
+    cudaStream_t s = (cudaStream_t)stream;
+    for (int64_t k = 0; k < nsteps; ++k) {
+        GB_TRY(build_any(h, (float4 *)xm, (float4 *)vel, (const float4 *)acc, n, dt, true, s));
+        GB_TRY(traverse(h, (float4 *)acc, (float4 *)vel, theta, eps2, G, dt, max_stack, 0, true, s));
+    }
+    return GB_OK;
+}
+
+extern "C" int gb_bh_export(gb_bh_t *h, int what, void *dst, void *stream) {
+    if (!h || !dst) return fail(GB_EINVAL, "NULL argument");
+    if (h->n < 1) return fail(GB_ENOTREADY, "no tree built");
+    if (what < EXP_CODES || what > EXP_MAX) return fail(GB_EINVAL, "unknown export %d", what);
+    const int n = (int)h->n;
+    const int64_t count = 2 * (int64_t)n;
+    const unsigned grid = (unsigned)((count + 255) / 256);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (h->key_bits == 10)
+        bh_export_kernel<uint32_t><<<grid, 256, 0, s>>>(what, n, (const uint32_t *)h->keys[h->cur], h->vals[h->cur],
+                                                        h->child, h->parent, h->leaf, h->mom, h->bmin, h->bmax, dst);
+    else
+        bh_export_kernel<uint64_t><<<grid, 256, 0, s>>>(what, n, (const uint64_t *)h->keys[h->cur], h->vals[h->cur],
+                                                        h->child, h->parent, h->leaf, h->mom, h->bmin, h->bmax, dst);
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+}
+
+extern "C" int gb_bh_diag(gb_bh_t *h, gb_diag_t *out, int reset) {
+    if (!h || !out) return fail(GB_EINVAL, "NULL argument");
+    unsigned long long d[DIAG_COUNT];
+    GB_CUDA_TRY(cudaMemcpy(d, h->diag, sizeof(d), cudaMemcpyDeviceToHost));
+    out->stack_drops = d[DIAG_STACK_DROPS];
+    out->stack_overflow = d[DIAG_STACK_OVERFLOW];
+    out->nonfinite = d[DIAG_NONFINITE];
+    out->bad_tree = d[DIAG_BAD_TREE];
+    for (int k = 0; k < 4; ++k) out->reserved[k] = d[4 + k];
+    if (reset) GB_CUDA_TRY(cudaMemset(h->diag, 0, sizeof(d)));
+    return GB_OK;
+}

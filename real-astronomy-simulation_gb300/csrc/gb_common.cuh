@@ -1,0 +1,118 @@
+// Shared device/host helpers for the GB300 self-gravity engine (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/gbgrav.h"
+
+namespace gb {
+
+// ---------------------------------------------------------------- status
+// Per-thread last error text, returned by gb_last_error_string().
+void set_error(const char *fmt, ...);
+int fail(int code, const char *fmt, ...);
+
+#define GB_CUDA_TRY(expr)                                                    \
+    do {                                                                     \
+        cudaError_t e_ = (expr);                                             \
+        if (e_ != cudaSuccess)                                               \
+            return ::gb::fail(GB_ECUDA, "%s failed: %s (%s:%d)", #expr,      \
+                              cudaGetErrorString(e_), __FILE__, __LINE__);   \
+    } while (0)
+
+#define GB_TRY(expr)                                                         \
+    do {                                                                     \
+        int s_ = (expr);                                                     \
+        if (s_ != GB_OK) return s_;                                          \
+    } while (0)
+
+inline bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// Device-side diagnostic counters (one block per context, zeroed at create).
+// Index meaning is fixed by the C-ABI (gb_diag_t field order).
+enum DiagIndex {
+    DIAG_STACK_DROPS = 0,     // pushes skipped by the max_stack rule
+    DIAG_STACK_OVERFLOW = 1,  // warp stack capacity hit (never expected)
+    DIAG_NONFINITE = 2,       // non-finite key-quantisation inputs
+    DIAG_BAD_TREE = 3,        // bottom-up pass found an inconsistent node
+    DIAG_COUNT = 8
+};
+
+int num_sms();
+
+// ------------------------------------------------------- packed FP32 pairs
+// Blackwell executes two FP32 operations per lane per instruction with the
+// .f32x2 forms; a pair lives in one 64-bit register.
+typedef unsigned long long f2;
+
+__device__ __forceinline__ f2 pack2(float lo, float hi) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void unpack2(f2 v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+    f2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+    f2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+    f2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+// Hardware reciprocal square root (MUFU), flush-to-zero: the argument is
+// always >= eps^2 > 0 on the gravity paths.
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ f2 rsqrt2(f2 v) {
+    float a, b;
+    unpack2(v, a, b);
+    return pack2(rsqrt_approx(a), rsqrt_approx(b));
+}
+
+// Kahan-compensated add of x into (s, c); s - c is the running estimate.
+__device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
+    const float y = __fsub_rn(x, c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+}
+__device__ __forceinline__ void kahan_add2(f2 &s, f2 &c, f2 x) {
+    const f2 y = sub2(x, c);
+    const f2 t = add2(s, y);
+    c = sub2(sub2(t, s), y);
+    s = t;
+}
+
+// Leapfrog predictor used identically for targets and sources so that a
+// particle's own source copy sits exactly on its target position:
+// v_half = v + a*dt/2 (kick), x' = x + v_half*dt (drift).
+__device__ __forceinline__ float kick(float v, float a, float h) { return __fmaf_rn(a, h, v); }
+__device__ __forceinline__ float drift(float x, float vh, float dt) { return __fmaf_rn(vh, dt, x); }
+
+__device__ __forceinline__ float4 predict_xm(float4 xm, float4 v, float4 a, float h, float dt) {
+    return make_float4(drift(xm.x, kick(v.x, a.x, h), dt), drift(xm.y, kick(v.y, a.y, h), dt),
+                       drift(xm.z, kick(v.z, a.z, h), dt), xm.w);
+}
+
+__device__ __forceinline__ float4 ldg4(const float4 *p) { return __ldg(p); }
+
+}  // namespace gb

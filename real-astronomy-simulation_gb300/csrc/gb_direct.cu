@@ -1,0 +1,681 @@
+// Direct N^2 self-gravity on the FP32 CUDA cores (sm_103a).
+//
+// Replaces compute_acc_direct / potential_energy / kinetic_energy
+// (core/solvers/gravity.py:13-57) and the KDK kernels
+// (core/integrators/leapfrog.py:11-22) of the reference.
+//
+// Work decomposition ("stream-K"): the (targets x sources) plane is cut into
+// units of one target supertile (WARPS*32*K targets, K per lane) by one
+// source chunk (WARPS*32 sources).  A persistent grid of P CTAs takes equal
+// contiguous runs of units in supertile-major order, so every SM gets the
+// same number of interactions at any N.  A CTA stages each source chunk in
+// shared memory as duplicated pairs {(x,x),(y,y)},{(z,z),(m,m)} so the inner
+// loop runs on packed .f32x2 instructions (two targets per instruction);
+// per-unit partial sums are Kahan-added into the running sum.  When a run
+// leaves a supertile the CTA writes its compensated partial (hi, lo) to
+// scratch; the fix-up kernel merges the partials of every target in a fixed
+// CTA order (deterministic for a given grid) and applies the epilogue
+// (store / accumulate / closing kick).
+//
+// KDK fusion: in KDK mode the source loader and the target loader both
+// predict x' = x + (v + a dt/2) dt on the fly from the stored state, and the
+// fix-up applies v' = v + a dt/2 + a' dt/2, writing x', v', a' in place.
+#include <algorithm>
+#include <cstdio>
+
+#include "gb_common.cuh"
+
+namespace gb {
+
+enum DirectMode { MODE_ACC = 0, MODE_KDK = 1, MODE_PHI = 2 };
+
+struct DirectArgs {
+    const float4 *__restrict__ xm;
+    const float4 *__restrict__ vel;
+    const float4 *__restrict__ acc;
+    float4 *__restrict__ part;
+    int64_t n, num_ju, U;
+    int64_t P;
+    int smax;
+    float eps2, h, dt;
+};
+
+__device__ __forceinline__ int64_t unit_begin(int64_t U, int64_t P, int64_t c) { return U * c / P; }
+// CTA whose unit run contains unit u: the largest c with U*c/P <= u.
+__device__ __forceinline__ int64_t unit_owner(int64_t U, int64_t P, int64_t u) {
+    return ((u + 1) * P - 1) / U;
+}
+
+template <int MODE>
+__device__ __forceinline__ float4 load_particle(const DirectArgs &a, int64_t i) {
+    if (i >= a.n) return make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 x = ldg4(a.xm + i);
+    if (MODE == MODE_KDK) x = predict_xm(x, ldg4(a.vel + i), ldg4(a.acc + i), a.h, a.dt);
+    return x;
+}
+
+// Force kernel for MODE_ACC / MODE_KDK.  NP packed target pairs per lane.
+template <int NP, int WARPS, int MODE, bool KAHAN>
+__global__ void __launch_bounds__(WARPS * 32)
+direct_force_kernel(DirectArgs a) {
+    constexpr int K = 2 * NP;
+    constexpr int TILE = 32 * K;
+    constexpr int ST = WARPS * TILE;
+    constexpr int JU = WARPS * 32;
+    __shared__ ulonglong2 src[2 * JU];
+
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int64_t c = blockIdx.x;
+    const int64_t u_begin = unit_begin(a.U, a.P, c);
+    const int64_t u_end = unit_begin(a.U, a.P, c + 1);
+    if (u_begin >= u_end) return;  // whole CTA idle (tiny n)
+    const int64_t st0 = u_begin / a.num_ju;
+    const f2 E2 = pack2(a.eps2, a.eps2);
+
+    int64_t u = u_begin;
+    while (u < u_end) {
+        const int64_t st = u / a.num_ju;
+        const int64_t run_end = min(u_end, (st + 1) * a.num_ju);
+        const int64_t tbase = st * ST + wib * TILE + lane;
+
+        f2 X[NP], Y[NP], Z[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            const float4 t0 = load_particle<MODE>(a, tbase + (2 * p) * 32);
+            const float4 t1 = load_particle<MODE>(a, tbase + (2 * p + 1) * 32);
+            X[p] = pack2(t0.x, t1.x);
+            Y[p] = pack2(t0.y, t1.y);
+            Z[p] = pack2(t0.z, t1.z);
+        }
+        f2 SX[NP], SY[NP], SZ[NP], CX[NP], CY[NP], CZ[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) SX[p] = SY[p] = SZ[p] = CX[p] = CY[p] = CZ[p] = 0ull;
+
+        for (; u < run_end; ++u) {
+            const int64_t ju = u - st * a.num_ju;
+            const float4 s4 = load_particle<MODE>(a, ju * JU + threadIdx.x);
+            __syncthreads();  // previous chunk fully consumed
+            src[2 * threadIdx.x] = make_ulonglong2(pack2(s4.x, s4.x), pack2(s4.y, s4.y));
+            src[2 * threadIdx.x + 1] = make_ulonglong2(pack2(s4.z, s4.z), pack2(s4.w, s4.w));
+            __syncthreads();
+
+            f2 AX[NP], AY[NP], AZ[NP];
+#pragma unroll
+            for (int p = 0; p < NP; ++p) AX[p] = AY[p] = AZ[p] = 0ull;
+#pragma unroll 4
+            for (int jj = 0; jj < JU; ++jj) {
+                const ulonglong2 A = src[2 * jj];
+                const ulonglong2 B = src[2 * jj + 1];
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    const f2 dx = sub2(A.x, X[p]);
+                    const f2 dy = sub2(A.y, Y[p]);
+                    const f2 dz = sub2(B.x, Z[p]);
+                    f2 r2 = fma2(dx, dx, E2);
+                    r2 = fma2(dy, dy, r2);
+                    r2 = fma2(dz, dz, r2);
+                    const f2 inv = rsqrt2(r2);
+                    const f2 inv2 = mul2(inv, inv);
+                    const f2 s = mul2(mul2(B.y, inv), inv2);
+                    AX[p] = fma2(s, dx, AX[p]);
+                    AY[p] = fma2(s, dy, AY[p]);
+                    AZ[p] = fma2(s, dz, AZ[p]);
+                }
+            }
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                if (KAHAN) {
+                    kahan_add2(SX[p], CX[p], AX[p]);
+                    kahan_add2(SY[p], CY[p], AY[p]);
+                    kahan_add2(SZ[p], CZ[p], AZ[p]);
+                } else {
+                    SX[p] = add2(SX[p], AX[p]);
+                    SY[p] = add2(SY[p], AY[p]);
+                    SZ[p] = add2(SZ[p], AZ[p]);
+                }
+            }
+        }
+        // Flush the compensated partial: estimate = hi + lo with lo = -c.
+        const int64_t slot = (c * a.smax + (st - st0)) * ST + wib * TILE + lane;
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            float hx0, hx1, hy0, hy1, hz0, hz1, cx0, cx1, cy0, cy1, cz0, cz1;
+            unpack2(SX[p], hx0, hx1);
+            unpack2(SY[p], hy0, hy1);
+            unpack2(SZ[p], hz0, hz1);
+            unpack2(CX[p], cx0, cx1);
+            unpack2(CY[p], cy0, cy1);
+            unpack2(CZ[p], cz0, cz1);
+            const int64_t s0 = slot + (2 * p) * 32, s1 = s0 + 32;
+            a.part[2 * s0] = make_float4(hx0, hy0, hz0, 0.f);
+            a.part[2 * s0 + 1] = make_float4(-cx0, -cy0, -cz0, 0.f);
+            a.part[2 * s1] = make_float4(hx1, hy1, hz1, 0.f);
+            a.part[2 * s1 + 1] = make_float4(-cx1, -cy1, -cz1, 0.f);
+        }
+    }
+}
+
+// Potential kernel: phi_i = sum_{j != i} m_j / sqrt(r^2 + eps2), scalar FP32
+// with the same stream-K layout (K = 2 targets per lane, partial in .x).
+template <int WARPS, bool KAHAN>
+__global__ void __launch_bounds__(WARPS * 32)
+direct_phi_kernel(DirectArgs a) {
+    constexpr int K = 2;
+    constexpr int TILE = 32 * K;
+    constexpr int ST = WARPS * TILE;
+    constexpr int JU = WARPS * 32;
+    __shared__ float4 src[JU];
+
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int64_t c = blockIdx.x;
+    const int64_t u_begin = unit_begin(a.U, a.P, c);
+    const int64_t u_end = unit_begin(a.U, a.P, c + 1);
+    if (u_begin >= u_end) return;
+    const int64_t st0 = u_begin / a.num_ju;
+
+    int64_t u = u_begin;
+    while (u < u_end) {
+        const int64_t st = u / a.num_ju;
+        const int64_t run_end = min(u_end, (st + 1) * a.num_ju);
+        const int64_t tbase = st * ST + wib * TILE + lane;
+        float tx[K], ty[K], tz[K], S[K], C[K];
+        int64_t ti[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            ti[k] = tbase + k * 32;
+            const float4 t = load_particle<MODE_ACC>(a, ti[k]);
+            tx[k] = t.x; ty[k] = t.y; tz[k] = t.z;
+            S[k] = C[k] = 0.f;
+        }
+        for (; u < run_end; ++u) {
+            const int64_t ju = u - st * a.num_ju;
+            const int64_t j0 = ju * JU;
+            const float4 s4 = load_particle<MODE_ACC>(a, j0 + threadIdx.x);
+            __syncthreads();
+            src[threadIdx.x] = s4;
+            __syncthreads();
+            float A[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) A[k] = 0.f;
+#pragma unroll 4
+            for (int jj = 0; jj < JU; ++jj) {
+                const float4 s = src[jj];
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    const float dx = s.x - tx[k], dy = s.y - ty[k], dz = s.z - tz[k];
+                    const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, a.eps2)));
+                    const float t = s.w * rsqrt_approx(r2);
+                    A[k] += (j0 + jj != ti[k]) ? t : 0.f;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                if (KAHAN) kahan_add(S[k], C[k], A[k]);
+                else S[k] += A[k];
+            }
+        }
+        const int64_t slot = (c * a.smax + (st - st0)) * ST + wib * TILE + lane;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int64_t s = slot + k * 32;
+            a.part[2 * s] = make_float4(S[k], 0.f, 0.f, 0.f);
+            a.part[2 * s + 1] = make_float4(-C[k], 0.f, 0.f, 0.f);
+        }
+    }
+}
+
+struct FixArgs {
+    const float4 *__restrict__ part;
+    float4 *xm;   // KDK: in/out positions
+    float4 *vel;  // KDK: in/out velocities
+    float4 *acc;  // ACC/KDK: output accelerations (KDK: in = previous)
+    float *phi;   // PHI: output
+    int64_t n, num_ju, U, P, st_size;
+    int smax;
+    float G, h, dt;
+    int accumulate;
+};
+
+template <int MODE>
+__global__ void direct_fixup_kernel(FixArgs f) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= f.n) return;
+    const int64_t st = i / f.st_size;
+    const int64_t off = i - st * f.st_size;
+    const int64_t c_lo = unit_owner(f.U, f.P, st * f.num_ju);
+    const int64_t c_hi = unit_owner(f.U, f.P, (st + 1) * f.num_ju - 1);
+    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+    for (int64_t c = c_lo; c <= c_hi; ++c) {
+        const int64_t st0c = unit_begin(f.U, f.P, c) / f.num_ju;
+        const int64_t slot = (c * f.smax + (st - st0c)) * f.st_size + off;
+        const float4 hi = f.part[2 * slot];
+        const float4 lo = f.part[2 * slot + 1];
+        kahan_add(sx, cx, hi.x);
+        kahan_add(sx, cx, lo.x);
+        if (MODE != MODE_PHI) {
+            kahan_add(sy, cy, hi.y);
+            kahan_add(sy, cy, lo.y);
+            kahan_add(sz, cz, hi.z);
+            kahan_add(sz, cz, lo.z);
+        }
+    }
+    const float tx = sx - cx, ty = sy - cy, tz = sz - cz;
+    if (MODE == MODE_PHI) {
+        f.phi[i] = tx;
+        return;
+    }
+    const float4 an = make_float4(f.G * tx, f.G * ty, f.G * tz, 0.f);
+    if (MODE == MODE_ACC) {
+        if (f.accumulate) {
+            float4 o = f.acc[i];
+            o.x += an.x; o.y += an.y; o.z += an.z;
+            f.acc[i] = o;
+        } else {
+            f.acc[i] = an;
+        }
+        return;
+    }
+    // MODE_KDK: closing kick and state write-back (in place).
+    const float4 x = f.xm[i], v = f.vel[i], a0 = f.acc[i];
+    const float vhx = kick(v.x, a0.x, f.h), vhy = kick(v.y, a0.y, f.h), vhz = kick(v.z, a0.z, f.h);
+    f.xm[i] = make_float4(drift(x.x, vhx, f.dt), drift(x.y, vhy, f.dt), drift(x.z, vhz, f.dt), x.w);
+    f.vel[i] = make_float4(kick(vhx, an.x, f.h), kick(vhy, an.y, f.h), kick(vhz, an.z, f.h), v.w);
+    f.acc[i] = an;
+}
+
+// ------------------------------------------------------------- energies
+// Per-block FP64 partial sums of KE = 1/2 m v.v and W = m phi, then a single
+// block combines them in block order (deterministic).
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__global__ void energy_partial_kernel(const float4 *__restrict__ xm, const float4 *__restrict__ vel,
+                                      const float *__restrict__ phi, int64_t n, double2 *out) {
+    double ke = 0.0, w = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 x = xm[i], v = vel[i];
+        const double m = x.w;
+        const double vv = (double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z;
+        ke += 0.5 * m * vv;
+        w += m * (double)phi[i];
+    }
+    __shared__ double sk[32], sw[32];
+    ke = warp_sum_d(ke);
+    w = warp_sum_d(w);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { sk[wid] = ke; sw[wid] = w; }
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        ke = lane < nw ? sk[lane] : 0.0;
+        w = lane < nw ? sw[lane] : 0.0;
+        ke = warp_sum_d(ke);
+        w = warp_sum_d(w);
+        if (lane == 0) out[blockIdx.x] = make_double2(ke, w);
+    }
+}
+
+__global__ void energy_final_kernel(const double2 *__restrict__ part, int nb, double G, double *out3) {
+    double ke = 0.0, w = 0.0;
+    for (int b = threadIdx.x; b < nb; b += 32) { ke += part[b].x; w += part[b].y; }
+    ke = warp_sum_d(ke);
+    w = warp_sum_d(w);
+    if (threadIdx.x == 0) {
+        const double pe = -0.5 * G * w;
+        out3[0] = ke;
+        out3[1] = pe;
+        out3[2] = ke + pe;
+    }
+}
+
+// ------------------------------------------------- FP64 sampled oracle
+// One CTA per sampled target; threads stride the sources; FP64 arithmetic in
+// the order of core/solvers/gravity.py:22-25; fixed-order block reduction.
+__global__ void direct_fp64_kernel(const float4 *__restrict__ xm, int64_t n,
+                                   const int64_t *__restrict__ targets, double G, double eps2,
+                                   double *__restrict__ out) {
+    const int64_t i = targets[blockIdx.x];
+    const float4 t = xm[i];
+    const double px = t.x, py = t.y, pz = t.z;
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
+        const float4 s = xm[j];
+        const double dx = __dsub_rn((double)s.x, px);
+        const double dy = __dsub_rn((double)s.y, py);
+        const double dz = __dsub_rn((double)s.z, pz);
+        const double r2 = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
+                                              __dmul_rn(dz, dz)), eps2);
+        const double inv = 1.0 / sqrt(r2);
+        const double sc = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(G, (double)s.w), inv), inv), inv);
+        ax = __dadd_rn(ax, __dmul_rn(sc, dx));
+        ay = __dadd_rn(ay, __dmul_rn(sc, dy));
+        az = __dadd_rn(az, __dmul_rn(sc, dz));
+    }
+    __shared__ double sx[32], sy[32], sz[32];
+    ax = warp_sum_d(ax);
+    ay = warp_sum_d(ay);
+    az = warp_sum_d(az);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { sx[wid] = ax; sy[wid] = ay; sz[wid] = az; }
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        ax = lane < nw ? sx[lane] : 0.0;
+        ay = lane < nw ? sy[lane] : 0.0;
+        az = lane < nw ? sz[lane] : 0.0;
+        ax = warp_sum_d(ax);
+        ay = warp_sum_d(ay);
+        az = warp_sum_d(az);
+        if (lane == 0) {
+            out[3 * blockIdx.x] = ax;
+            out[3 * blockIdx.x + 1] = ay;
+            out[3 * blockIdx.x + 2] = az;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ host
+struct DirectPlan {
+    int np, warps;
+    int64_t n, st_size, num_st, num_ju, U, P;
+    int smax;
+};
+
+static void make_plan(int64_t n, int np, int warps, int64_t P, DirectPlan *p) {
+    p->np = np;
+    p->warps = warps;
+    p->n = n;
+    p->st_size = (int64_t)warps * 32 * 2 * np;
+    p->num_st = (n + p->st_size - 1) / p->st_size;
+    const int64_t ju = (int64_t)warps * 32;
+    p->num_ju = (n + ju - 1) / ju;
+    p->U = p->num_st * p->num_ju;
+    p->P = std::max<int64_t>(1, std::min<int64_t>(P, p->U));
+    const int64_t per = (p->U + p->P - 1) / p->P;
+    p->smax = (int)((per + p->num_ju - 1) / p->num_ju + 1);
+}
+
+// Scratch (float4 elements) a plan needs for its partials.
+static int64_t plan_partials(const DirectPlan &p) { return 2 * p.P * p.smax * p.st_size; }
+
+template <int NP, int WARPS>
+static cudaError_t launch_force(int mode, bool kahan, const DirectPlan &pl, const DirectArgs &a,
+                                cudaStream_t s) {
+    const dim3 grid((unsigned)pl.P), block(WARPS * 32);
+    if (mode == MODE_ACC) {
+        if (kahan) direct_force_kernel<NP, WARPS, MODE_ACC, true><<<grid, block, 0, s>>>(a);
+        else direct_force_kernel<NP, WARPS, MODE_ACC, false><<<grid, block, 0, s>>>(a);
+    } else {
+        if (kahan) direct_force_kernel<NP, WARPS, MODE_KDK, true><<<grid, block, 0, s>>>(a);
+        else direct_force_kernel<NP, WARPS, MODE_KDK, false><<<grid, block, 0, s>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+typedef const void *KernelPtr;
+
+static KernelPtr force_kernel_ptr(int np, int warps) {
+    if (np == 1 && warps == 4) return (KernelPtr)direct_force_kernel<1, 4, MODE_KDK, true>;
+    if (np == 1 && warps == 8) return (KernelPtr)direct_force_kernel<1, 8, MODE_KDK, true>;
+    if (np == 2 && warps == 4) return (KernelPtr)direct_force_kernel<2, 4, MODE_KDK, true>;
+    return (KernelPtr)direct_force_kernel<2, 8, MODE_KDK, true>;
+}
+
+}  // namespace gb
+
+// ================================================================ C ABI
+using namespace gb;
+
+struct gb_direct {
+    int device;
+    int sms;
+    int64_t n_max;
+    int np, warps, ctas_per_sm;  // tile shape (ctas_per_sm 0 = occupancy max)
+    float4 *part;
+    int64_t part_cap;            // float4 elements
+    float *phi;                  // n_max floats (energy scratch)
+    double2 *epart;              // energy block partials
+    int epart_cap;
+    unsigned long long *diag;
+};
+
+static int64_t grid_ctas(gb_direct_t *h, int np, int warps) {
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, force_kernel_ptr(np, warps), warps * 32, 0);
+    if (occ < 1) occ = 1;
+    const int per_sm = h->ctas_per_sm > 0 ? std::min(h->ctas_per_sm, occ) : occ;
+    return (int64_t)h->sms * per_sm;
+}
+
+static int ensure_partials(gb_direct_t *h, int64_t need) {
+    if (need <= h->part_cap) return GB_OK;
+    if (h->part) cudaFree(h->part);
+    h->part = nullptr;
+    h->part_cap = 0;
+    if (cudaMalloc(&h->part, sizeof(float4) * need) != cudaSuccess)
+        return fail(GB_ENOMEM, "partials: cannot allocate %lld bytes", (long long)(sizeof(float4) * need));
+    h->part_cap = need;
+    return GB_OK;
+}
+
+// Scratch for every supported tile shape at n_max, so a call never allocates.
+static int64_t max_partials(gb_direct_t *h, int64_t n) {
+    int64_t need = 0;
+    const int shapes[4][2] = {{1, 4}, {1, 8}, {2, 4}, {2, 8}};
+    for (auto &s : shapes) {
+        DirectPlan pl;
+        make_plan(n, s[0], s[1], grid_ctas(h, s[0], s[1]), &pl);
+        need = std::max(need, plan_partials(pl));
+        make_plan(n, 1, s[1], grid_ctas(h, s[0], s[1]), &pl);  // phi layout (K=2)
+        need = std::max(need, plan_partials(pl));
+    }
+    return need;
+}
+
+static int check_xm(const void *p, const char *name) {
+    if (!p) return fail(GB_EINVAL, "%s is NULL", name);
+    if (!aligned16(p)) return fail(GB_EINVAL, "%s is not 16-byte aligned", name);
+    return GB_OK;
+}
+
+extern "C" int gb_direct_create(gb_direct_t **out, int64_t n_max) {
+    if (!out) return fail(GB_EINVAL, "out is NULL");
+    *out = nullptr;
+    if (n_max < 1 || n_max > (int64_t)1 << 31) return fail(GB_EINVAL, "n_max=%lld out of range", (long long)n_max);
+    gb_direct_t *h = new gb_direct();
+    GB_CUDA_TRY(cudaGetDevice(&h->device));
+    h->sms = num_sms();
+    h->n_max = n_max;
+    h->np = 2;
+    h->warps = 8;
+    h->ctas_per_sm = 0;
+    int st = ensure_partials(h, max_partials(h, n_max));
+    if (st == GB_OK && cudaMalloc(&h->phi, sizeof(float) * n_max) != cudaSuccess)
+        st = fail(GB_ENOMEM, "phi scratch");
+    h->epart_cap = 4 * h->sms;
+    if (st == GB_OK && cudaMalloc(&h->epart, sizeof(double2) * h->epart_cap) != cudaSuccess)
+        st = fail(GB_ENOMEM, "energy scratch");
+    if (st == GB_OK && cudaMalloc(&h->diag, sizeof(unsigned long long) * DIAG_COUNT) != cudaSuccess)
+        st = fail(GB_ENOMEM, "diag");
+    if (st == GB_OK && cudaMemset(h->diag, 0, sizeof(unsigned long long) * DIAG_COUNT) != cudaSuccess)
+        st = fail(GB_ECUDA, "diag memset");
+    if (st != GB_OK) {
+        gb_direct_destroy(h);
+        return st;
+    }
+    *out = h;
+    return GB_OK;
+}
+
+extern "C" int gb_direct_destroy(gb_direct_t *h) {
+    if (!h) return GB_OK;
+    cudaFree(h->part);
+    cudaFree(h->phi);
+    cudaFree(h->epart);
+    cudaFree(h->diag);
+    delete h;
+    return GB_OK;
+}
+
+extern "C" int gb_direct_set_tiles(gb_direct_t *h, int k, int warps, int ctas_per_sm) {
+    if (!h) return fail(GB_EINVAL, "handle is NULL");
+    if (k != 2 && k != 4) return fail(GB_EINVAL, "k must be 2 or 4 (got %d)", k);
+    if (warps != 4 && warps != 8) return fail(GB_EINVAL, "warps must be 4 or 8 (got %d)", warps);
+    if (ctas_per_sm < 0 || ctas_per_sm > 32) return fail(GB_EINVAL, "ctas_per_sm=%d", ctas_per_sm);
+    h->np = k / 2;
+    h->warps = warps;
+    h->ctas_per_sm = ctas_per_sm;
+    return GB_OK;
+}
+
+static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, float4 *acc, float *phi,
+                      int64_t n, float G, float eps2, float dt, int flags, cudaStream_t s) {
+    DirectPlan pl;
+    const int np = mode == MODE_PHI ? 1 : h->np;
+    make_plan(n, np, h->warps, grid_ctas(h, h->np, h->warps), &pl);
+    if (plan_partials(pl) > h->part_cap) return fail(GB_EINVAL, "scratch too small for n=%lld", (long long)n);
+    DirectArgs a;
+    a.xm = xm;
+    a.vel = vel;
+    a.acc = acc;
+    a.part = h->part;
+    a.n = n;
+    a.num_ju = pl.num_ju;
+    a.U = pl.U;
+    a.P = pl.P;
+    a.smax = pl.smax;
+    a.eps2 = eps2;
+    a.h = 0.5f * dt;
+    a.dt = dt;
+    const bool kahan = !(flags & GB_PLAIN_FP32);
+    cudaError_t e;
+    if (mode == MODE_PHI) {
+        const dim3 grid((unsigned)pl.P), block(h->warps * 32);
+        if (h->warps == 4) {
+            if (kahan) direct_phi_kernel<4, true><<<grid, block, 0, s>>>(a);
+            else direct_phi_kernel<4, false><<<grid, block, 0, s>>>(a);
+        } else {
+            if (kahan) direct_phi_kernel<8, true><<<grid, block, 0, s>>>(a);
+            else direct_phi_kernel<8, false><<<grid, block, 0, s>>>(a);
+        }
+        e = cudaGetLastError();
+    } else if (pl.np == 1) {
+        e = pl.warps == 4 ? launch_force<1, 4>(mode, kahan, pl, a, s) : launch_force<1, 8>(mode, kahan, pl, a, s);
+    } else {
+        e = pl.warps == 4 ? launch_force<2, 4>(mode, kahan, pl, a, s) : launch_force<2, 8>(mode, kahan, pl, a, s);
+    }
+    if (e != cudaSuccess) return fail(GB_ECUDA, "force launch: %s", cudaGetErrorString(e));
+    FixArgs f;
+    f.part = h->part;
+    f.xm = const_cast<float4 *>(xm);
+    f.vel = vel;
+    f.acc = acc;
+    f.phi = phi;
+    f.n = n;
+    f.num_ju = pl.num_ju;
+    f.U = pl.U;
+    f.P = pl.P;
+    f.st_size = pl.st_size;
+    f.smax = pl.smax;
+    f.G = G;
+    f.h = 0.5f * dt;
+    f.dt = dt;
+    f.accumulate = (flags & GB_ACCUMULATE) ? 1 : 0;
+    const unsigned fb = 256, fg = (unsigned)((n + fb - 1) / fb);
+    if (mode == MODE_ACC) direct_fixup_kernel<MODE_ACC><<<fg, fb, 0, s>>>(f);
+    else if (mode == MODE_KDK) direct_fixup_kernel<MODE_KDK><<<fg, fb, 0, s>>>(f);
+    else direct_fixup_kernel<MODE_PHI><<<fg, fb, 0, s>>>(f);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(GB_ECUDA, "fix-up launch: %s", cudaGetErrorString(e));
+    return GB_OK;
+}
+
+static int check_n(gb_direct_t *h, int64_t n) {
+    if (!h) return fail(GB_EINVAL, "handle is NULL");
+    if (n < 0 || n > h->n_max) return fail(GB_EINVAL, "n=%lld outside [0, n_max=%lld]", (long long)n, (long long)h->n_max);
+    return GB_OK;
+}
+
+extern "C" int gb_direct_acc(gb_direct_t *h, const float *xm, float *acc, int64_t n, float G, float eps2,
+                             int flags, void *stream) {
+    GB_TRY(check_n(h, n));
+    if (n == 0) return GB_OK;
+    GB_TRY(check_xm(xm, "xm"));
+    GB_TRY(check_xm(acc, "acc"));
+    if (!(eps2 > 0.f)) return fail(GB_EINVAL, "eps2 must be > 0");
+    return run_direct(h, MODE_ACC, (const float4 *)xm, nullptr, (float4 *)acc, nullptr, n, G, eps2, 0.f,
+                      flags, (cudaStream_t)stream);
+}
+
+extern "C" int gb_direct_kdk(gb_direct_t *h, float *xm, float *vel, float *acc, int64_t n, float G, float eps2,
+                             float dt, int64_t nsteps, int flags, void *stream) {
+    GB_TRY(check_n(h, n));
+    if (n == 0 || nsteps == 0) return GB_OK;
+    if (nsteps < 0) return fail(GB_EINVAL, "nsteps < 0");
+    GB_TRY(check_xm(xm, "xm"));
+    GB_TRY(check_xm(vel, "vel"));
+    GB_TRY(check_xm(acc, "acc"));
+    if (!(eps2 > 0.f)) return fail(GB_EINVAL, "eps2 must be > 0");
+    for (int64_t s = 0; s < nsteps; ++s)
+        GB_TRY(run_direct(h, MODE_KDK, (const float4 *)xm, (float4 *)vel, (float4 *)acc, nullptr, n, G, eps2,
+                          dt, flags & GB_PLAIN_FP32, (cudaStream_t)stream));
+    return GB_OK;
+}
+
+extern "C" int gb_direct_phi(gb_direct_t *h, const float *xm, float *phi, int64_t n, float eps2, int flags,
+                             void *stream) {
+    GB_TRY(check_n(h, n));
+    if (n == 0) return GB_OK;
+    GB_TRY(check_xm(xm, "xm"));
+    if (!phi) return fail(GB_EINVAL, "phi is NULL");
+    if (!(eps2 > 0.f)) return fail(GB_EINVAL, "eps2 must be > 0");
+    return run_direct(h, MODE_PHI, (const float4 *)xm, nullptr, nullptr, phi, n, 1.f, eps2, 0.f, flags,
+                      (cudaStream_t)stream);
+}
+
+extern "C" int gb_energy(gb_direct_t *h, const float *xm, const float *vel, int64_t n, float G, float eps2,
+                         double *out3, void *stream) {
+    GB_TRY(check_n(h, n));
+    GB_TRY(check_xm(xm, "xm"));
+    GB_TRY(check_xm(vel, "vel"));
+    if (!out3) return fail(GB_EINVAL, "out3 is NULL");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (n > 0) GB_TRY(gb_direct_phi(h, xm, h->phi, n, eps2, 0, stream));
+    const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(h->epart_cap, (n + 255) / 256));
+    energy_partial_kernel<<<nb, 256, 0, s>>>((const float4 *)xm, (const float4 *)vel, h->phi, n, h->epart);
+    energy_final_kernel<<<1, 32, 0, s>>>(h->epart, nb, (double)G, out3);
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+}
+
+extern "C" int gb_direct_acc_fp64(const float *xm, int64_t n, const int64_t *targets, int64_t nt, double G,
+                                  double eps2, double *acc_out, void *stream) {
+    if (n < 0 || nt < 0) return fail(GB_EINVAL, "negative size");
+    if (nt == 0) return GB_OK;
+    GB_TRY(check_xm(xm, "xm"));
+    if (!targets || !acc_out) return fail(GB_EINVAL, "targets/acc_out is NULL");
+    if (nt > INT32_MAX) return fail(GB_EINVAL, "too many targets");
+    direct_fp64_kernel<<<(unsigned)nt, 256, 0, (cudaStream_t)stream>>>((const float4 *)xm, n, targets, G, eps2,
+                                                                       acc_out);
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+}
+
+extern "C" int gb_direct_diag(gb_direct_t *h, gb_diag_t *out, int reset) {
+    if (!h || !out) return fail(GB_EINVAL, "NULL argument");
+    unsigned long long d[DIAG_COUNT];
+    GB_CUDA_TRY(cudaMemcpy(d, h->diag, sizeof(d), cudaMemcpyDeviceToHost));
+    out->stack_drops = d[DIAG_STACK_DROPS];
+    out->stack_overflow = d[DIAG_STACK_OVERFLOW];
+    out->nonfinite = d[DIAG_NONFINITE];
+    out->bad_tree = d[DIAG_BAD_TREE];
+    for (int k = 0; k < 4; ++k) out->reserved[k] = d[4 + k];
+    if (reset) GB_CUDA_TRY(cudaMemset(h->diag, 0, sizeof(d)));
+    return GB_OK;
+}

@@ -1,0 +1,161 @@
+"""Drop-in ``Engine`` for the reference's core/engine.py:32-124.
+
+Same constructor (softening, gravity_mode, theta), same methods (load_state,
+to_state, step, energies, _compute_acc) and attributes (n, time, step_count,
+seed, meta, pos/vel/acc/mass), with the state resident on the GPU as float32
+float4 records and every force evaluation running in the sm_103a CUDA
+library.  Extra keyword arguments: ``G`` (default core/units.py:21),
+``key_bits`` (Morton key width of the tree path; the reference uses 21),
+``max_stack`` (traversal stack rule, reference default 64), ``plain_fp32``
+(disable Kahan accumulation), ``device``.
+
+As in the reference (core/engine.py:75-80), gravity_mode="bh" uses the tree
+only for n >= 256; smaller systems use the direct sum.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import units
+from ._dev import FieldView, empty4, pack_vec, pack_xm, require_cuda
+from .solvers.gravity import DirectGravity
+from .state import State
+
+BH_MIN_N = 256
+
+
+def init_taichi(arch: str = "cuda") -> None:
+    """Accepted for call-site compatibility with core/engine.py:21-29; the
+    engine always runs on the CUDA device."""
+    require_cuda()
+
+
+class Engine:
+    def __init__(self, softening: float = 0.05, gravity_mode: str = "direct",
+                 theta: float = 0.6, *, G: float = units.G, key_bits: int = 21,
+                 max_stack: int = 64, plain_fp32: bool = False, device=None):
+        if gravity_mode not in ("direct", "bh"):
+            raise ValueError(f"gravity_mode must be 'direct' or 'bh', got {gravity_mode!r}")
+        self.softening = float(softening)
+        self.gravity_mode = gravity_mode
+        self.theta = float(theta)
+        self.G = float(G)
+        self.key_bits = int(key_bits)
+        self.max_stack = int(max_stack)
+        self.plain_fp32 = bool(plain_fp32)
+        self.device = require_cuda(device)
+        self._bh = None
+        self._direct = None
+        self.n = 0
+        self.time = 0.0
+        self.step_count = 0
+        self.seed = 0
+        self.meta: dict = {}
+        self.xm = self.v4 = self.a4 = None
+        self._ptype = self._ids = None
+        self._age = self._temperature = self._metallicity = None
+
+    # ---------------------------------------------------------------- fields
+    @property
+    def pos(self):
+        return None if self.xm is None else FieldView(self.xm, slice(0, 3))
+
+    @property
+    def mass(self):
+        return None if self.xm is None else FieldView(self.xm, 3)
+
+    @property
+    def vel(self):
+        return None if self.v4 is None else FieldView(self.v4, slice(0, 3))
+
+    @property
+    def acc(self):
+        return None if self.a4 is None else FieldView(self.a4, slice(0, 3))
+
+    @property
+    def eps2(self) -> float:
+        return self.softening ** 2
+
+    # ----------------------------------------------------------------- setup
+    def load_state(self, state: State) -> None:
+        """Upload a State and prime the accelerations (core/engine.py:53-81)."""
+        self.n = state.n
+        self.time = state.time
+        self.step_count = state.step
+        self.seed = state.seed
+        self.meta = dict(state.meta)
+        self._ptype = state.ptype.copy()
+        self._ids = state.ids.copy()
+        self._age = state.age
+        self._temperature = state.temperature
+        self._metallicity = state.metallicity
+        with torch.cuda.device(self.device):
+            self.xm = pack_xm(state.pos, state.mass, self.device)
+            self.v4 = pack_vec(state.vel, self.device)
+            self.a4 = empty4(self.n, self.device)
+            if self._direct is None or self._direct.n_max < max(self.n, 1):
+                self._direct = DirectGravity(max(self.n, 1), self.device)
+            if self.gravity_mode == "bh" and self.n >= BH_MIN_N:
+                from .solvers.barnes_hut import BarnesHut
+                self._bh = BarnesHut(self.n, theta=self.theta, softening=self.softening,
+                                     max_stack=self.max_stack, key_bits=self.key_bits,
+                                     G=self.G, device=self.device)
+            else:
+                self._bh = None
+            self._compute_acc()
+
+    def to_state(self) -> State:
+        """Download the state into a host State (core/engine.py:83-98)."""
+        xm = self.xm.detach().cpu().numpy().astype(np.float64)
+        vel = self.v4.detach().cpu().numpy().astype(np.float64)
+        return State(pos=xm[:, :3], vel=vel[:, :3], mass=xm[:, 3], ptype=self._ptype,
+                     ids=self._ids, time=self.time, step=self.step_count, seed=self.seed,
+                     age=self._age, temperature=self._temperature,
+                     metallicity=self._metallicity, meta=dict(self.meta))
+
+    # -------------------------------------------------------------- stepping
+    def _compute_acc(self) -> None:
+        """core/engine.py:101-106."""
+        if self.n == 0:
+            return
+        with torch.cuda.device(self.device):
+            if self._bh is not None:
+                self._bh.compute(self.xm, self.a4)
+            else:
+                self._direct.acc(self.xm, self.a4, self.G, self.eps2, plain=self.plain_fp32)
+
+    def step(self, dt: float) -> None:
+        """One KDK step (core/engine.py:108-116); kick and drift are fused
+        into the force pass."""
+        self.run(dt, 1)
+
+    def run(self, dt: float, nsteps: int) -> None:
+        """nsteps KDK steps without returning to Python in between."""
+        if nsteps <= 0:
+            return
+        if self.n > 0:
+            with torch.cuda.device(self.device):
+                if self._bh is not None:
+                    self._bh.kdk(self.xm, self.v4, self.a4, dt, nsteps)
+                else:
+                    self._direct.kdk(self.xm, self.v4, self.a4, self.G, self.eps2, dt, nsteps,
+                                     plain=self.plain_fp32)
+        self.time += dt * nsteps
+        self.step_count += nsteps
+
+    # ----------------------------------------------------------- diagnostics
+    def energies(self) -> tuple[float, float, float]:
+        """(kinetic, potential, total) in code units (core/engine.py:119-124);
+        FP64 reductions over FP32-Kahan pair sums."""
+        if self.n == 0:
+            return 0.0, 0.0, 0.0
+        with torch.cuda.device(self.device):
+            return self._direct.energies(self.xm, self.v4, self.G, self.eps2)
+
+    def diag(self) -> dict:
+        d = self._direct.diag() if self._direct is not None else {}
+        if self._bh is not None:
+            for k, v in self._bh.diag().items():
+                d[k] = d.get(k, 0) + v
+        return d

@@ -1,0 +1,108 @@
+"""LBVH Barnes-Hut on the GB300 (host side of gb_bh_*).
+
+Mirrors ``BarnesHut(n, theta, softening, max_stack).compute(pos, mass, acc)``
+(core/solvers/barnes_hut.py:220-259).  Every stage (Morton keys, stable
+sort, Karras build, node summaries, traversal) runs on the device; keys,
+order and topology are bit-identical to the reference's and each particle
+accepts the same node set.  Extra keyword arguments: ``key_bits`` (21 = the
+reference's 63-bit keys, 10 = 30-bit keys) and ``G`` (the reference compiles
+core/units.py:21 into its traversal).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from .. import _lib, units
+from .._dev import ptr, require_cuda, stream_handle
+
+EXPORTS = {"code": (0, np.uint64, 1, 0), "order": (1, np.int32, 1, 0),
+           "left": (2, np.int32, 1, -1), "right": (3, np.int32, 1, -1),
+           "parent": (4, np.int32, 2, -1), "nmass": (5, np.float64, 2, -1),
+           "com": (6, np.float64, 2, -1), "nmin": (7, np.float64, 2, -1),
+           "nmax": (8, np.float64, 2, -1)}
+_TORCH = {np.uint64: torch.int64, np.int32: torch.int32, np.float64: torch.float64}
+
+
+class BarnesHut:
+    def __init__(self, n: int, theta: float = 0.6, softening: float = 0.1,
+                 max_stack: int = 64, *, key_bits: int = 21, G: float = units.G,
+                 device=None):
+        self.device = require_cuda(device)
+        self.n = int(n)
+        self.theta = float(theta)
+        self.theta2 = self.theta ** 2
+        self.softening = float(softening)
+        self.eps2 = self.softening ** 2
+        self.max_stack = int(max_stack)
+        self.key_bits = int(key_bits)
+        self.G = float(G)
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.call("gb_bh_create", ctypes.byref(h), max(self.n, 1), self.key_bits)
+        self._h = h
+        self._last_n = 0
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.load().gb_bh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _n(self, xm) -> int:
+        n = xm.shape[0]
+        if n > self.n:
+            raise ValueError(f"BarnesHut was sized for n={self.n}, got {n}")
+        return n
+
+    def build(self, xm: torch.Tensor) -> None:
+        self._last_n = self._n(xm)
+        _lib.call("gb_bh_build", self._h, ptr(xm, "xm"), self._last_n, stream_handle(self.device))
+
+    def accel(self, acc: torch.Tensor, accumulate: bool = False) -> torch.Tensor:
+        _lib.call("gb_bh_accel", self._h, ptr(acc, "acc"), self.theta, self.eps2, self.G,
+                  self.max_stack, _lib.GB_ACCUMULATE if accumulate else 0,
+                  stream_handle(self.device))
+        return acc
+
+    def compute(self, xm: torch.Tensor, acc: torch.Tensor, accumulate: bool = False) -> torch.Tensor:
+        """acc <- tree accelerations of the particles in xm
+        (core/solvers/barnes_hut.py:242-259)."""
+        self._last_n = self._n(xm)
+        _lib.call("gb_bh_compute", self._h, ptr(xm, "xm"), ptr(acc, "acc"), self._last_n,
+                  self.theta, self.eps2, self.G, self.max_stack,
+                  _lib.GB_ACCUMULATE if accumulate else 0, stream_handle(self.device))
+        return acc
+
+    def kdk(self, xm, vel, acc, dt: float, nsteps: int = 1) -> None:
+        """nsteps KDK leapfrog steps with tree forces, in place."""
+        self._last_n = self._n(xm)
+        _lib.call("gb_bh_kdk", self._h, ptr(xm, "xm"), ptr(vel, "vel"), ptr(acc, "acc"),
+                  self._n(xm), self.theta, self.eps2, self.G, float(dt), int(nsteps),
+                  self.max_stack, stream_handle(self.device))
+
+    def export(self, name: str) -> np.ndarray:
+        """One array of the last build in the reference's layout."""
+        what, dt, mult, off = EXPORTS[name]
+        n = self._last_n
+        count = mult * n + off
+        shape = (count, 3) if name in ("com", "nmin", "nmax") else (count,)
+        out = torch.empty(shape, dtype=_TORCH[dt], device=self.device)
+        _lib.call("gb_bh_export", self._h, what, out.data_ptr(), stream_handle(self.device))
+        a = out.cpu().numpy()
+        return a.view(np.uint64) if dt is np.uint64 else a
+
+    def tree_arrays(self) -> dict:
+        return {k: self.export(k) for k in EXPORTS}
+
+    def diag(self, reset: bool = False) -> dict:
+        d = _lib.Diag()
+        _lib.call("gb_bh_diag", self._h, ctypes.byref(d), 1 if reset else 0)
+        return d.as_dict()

@@ -1,0 +1,137 @@
+"""Direct N^2 gravity on the GB300 (host side of gb_direct_*).
+
+Mirrors core/solvers/gravity.py:13-57 of the reference:
+
+* ``compute_acc_direct(xm, acc, n, grav, eps2)``  (gravity.py:13-26)
+* ``kinetic_energy(vel, xm, n)``                  (gravity.py:29-36)
+* ``potential_energy(xm, n, grav, eps2)``          (gravity.py:39-57)
+
+Positions and masses travel together as one (n, 4) float32 ``xm`` tensor;
+accelerations and velocities are (n, 4) float32 tensors.  The arithmetic is
+FP32 with Kahan-compensated accumulation (FP64 for the energy reductions).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from .. import _lib
+from .._dev import ptr, require_cuda, stream_handle
+
+
+class DirectGravity:
+    """Owns a gb_direct handle (scratch for up to ``n_max`` particles)."""
+
+    def __init__(self, n_max: int, device=None, tiles=None):
+        self.device = require_cuda(device)
+        self.n_max = int(n_max)
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.call("gb_direct_create", ctypes.byref(h), self.n_max)
+        self._h = h
+        self._out3 = torch.zeros(3, dtype=torch.float64, device=self.device)
+        if tiles is not None:
+            self.set_tiles(*tiles)
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.load().gb_direct_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_tiles(self, k: int, warps: int, ctas_per_sm: int = 0):
+        _lib.call("gb_direct_set_tiles", self._h, int(k), int(warps), int(ctas_per_sm))
+
+    # -- compute
+    def acc(self, xm, acc, G, eps2, accumulate=False, plain=False):
+        flags = (_lib.GB_ACCUMULATE if accumulate else 0) | (_lib.GB_PLAIN_FP32 if plain else 0)
+        n = xm.shape[0]
+        _lib.call("gb_direct_acc", self._h, ptr(xm, "xm"), ptr(acc, "acc"), n,
+                  float(G), float(eps2), flags, stream_handle(self.device))
+        return acc
+
+    def kdk(self, xm, vel, acc, G, eps2, dt, nsteps=1, plain=False):
+        n = xm.shape[0]
+        _lib.call("gb_direct_kdk", self._h, ptr(xm, "xm"), ptr(vel, "vel"), ptr(acc, "acc"),
+                  n, float(G), float(eps2), float(dt), int(nsteps),
+                  _lib.GB_PLAIN_FP32 if plain else 0, stream_handle(self.device))
+
+    def phi(self, xm, eps2, out=None, plain=False):
+        n = xm.shape[0]
+        if out is None:
+            out = torch.empty(n, dtype=torch.float32, device=xm.device)
+        _lib.call("gb_direct_phi", self._h, ptr(xm, "xm"), ptr(out, "phi", rows4=False), n,
+                  float(eps2), _lib.GB_PLAIN_FP32 if plain else 0, stream_handle(self.device))
+        return out
+
+    def energies_async(self, xm, vel, G, eps2) -> torch.Tensor:
+        """(KE, PE, KE+PE) as a float64 device tensor (no host sync)."""
+        _lib.call("gb_energy", self._h, ptr(xm, "xm"), ptr(vel, "vel"), xm.shape[0],
+                  float(G), float(eps2), ptr(self._out3, "out3", torch.float64, rows4=False),
+                  stream_handle(self.device))
+        return self._out3
+
+    def energies(self, xm, vel, G, eps2):
+        e = self.energies_async(xm, vel, G, eps2).cpu().numpy()
+        return float(e[0]), float(e[1]), float(e[2])
+
+    def diag(self, reset=False) -> dict:
+        d = _lib.Diag()
+        _lib.call("gb_direct_diag", self._h, ctypes.byref(d), 1 if reset else 0)
+        return d.as_dict()
+
+
+def acc_fp64_targets(xm: torch.Tensor, targets, G: float, eps2: float) -> np.ndarray:
+    """FP64 accelerations of the listed particles, computed on the device
+    (gb_direct_acc_fp64); returns a (len(targets), 3) float64 array."""
+    t = torch.as_tensor(np.asarray(targets, dtype=np.int64), device=xm.device)
+    out = torch.empty((t.numel(), 3), dtype=torch.float64, device=xm.device)
+    if t.numel():
+        _lib.call("gb_direct_acc_fp64", ptr(xm, "xm"), xm.shape[0],
+                  ptr(t, "targets", torch.int64, rows4=False), t.numel(), float(G), float(eps2),
+                  ptr(out, "acc_out", torch.float64, rows4=False), stream_handle(xm.device))
+    return out.cpu().numpy()
+
+
+_CACHE: dict = {}
+
+
+def _solver_for(xm: torch.Tensor) -> DirectGravity:
+    key = xm.device.index
+    s = _CACHE.get(key)
+    if s is None or s.n_max < xm.shape[0]:
+        s = DirectGravity(max(xm.shape[0], 1), xm.device)
+        _CACHE[key] = s
+    return s
+
+
+def compute_acc_direct(xm, acc, n, grav, eps2):
+    """acc[:n] = G sum_j m_j d_ij / (|d_ij|^2 + eps2)^{3/2} (core/solvers/gravity.py:13-26)."""
+    xm_n = xm[:n] if n != xm.shape[0] else xm
+    acc_n = acc[:n] if n != acc.shape[0] else acc
+    _solver_for(xm).acc(xm_n, acc_n, grav, eps2)
+
+
+def kinetic_energy(vel, xm, n, grav=1.0, eps2=1.0):
+    """1/2 sum m |v|^2 in FP64 (core/solvers/gravity.py:29-36)."""
+    return _solver_for(xm).energies(xm[:n], vel[:n], grav, eps2)[0]
+
+
+def potential_energy(xm, n, grav, eps2, vel=None):
+    """-1/2 G sum_i m_i sum_{j != i} m_j / sqrt(r^2 + eps2)
+    (core/solvers/gravity.py:39-57); FP32 pair sums, FP64 reduction."""
+    if vel is None:
+        vel = torch.zeros_like(xm)
+    return _solver_for(xm).energies(xm[:n], vel[:n], grav, eps2)[1]

@@ -1,0 +1,218 @@
+"""LBVH Barnes-Hut CUDA path against the reference fixtures and the oracle.
+
+Bit-exact: Morton keys, sort permutation, Karras topology (left, right,
+parent), node AABBs.  FP64 node masses / centres: relative 1e-12 (summation
+order differs from the reference's atomics).  Accelerations: the device
+traversal is FP32, so per-particle relative differences from the FP64
+traversal are ~1e-6; a node whose acceptance test sits on the FP32/FP64
+rounding boundary can flip, which moves that particle by about one node's
+multipole error.  Hence: median <= 1e-5, 99th percentile <= 1e-4, max <=
+1e-2 against the FP64 traversal, and the BH error against direct N^2 must
+match the FP64 traversal's own error within 1e-4.
+"""
+import importlib
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import PKG_NAME, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _mods():
+    pkg = importlib.import_module(PKG_NAME)
+    bh = importlib.import_module(PKG_NAME + ".solvers.barnes_hut")
+    ic = importlib.import_module(PKG_NAME + ".ic")
+    grav = importlib.import_module(PKG_NAME + ".solvers.gravity")
+    return pkg, bh, ic, grav
+
+
+def _f32(a):
+    return np.asarray(a, np.float64).astype(np.float32).astype(np.float64)
+
+
+def _xm(pos, mass, dev):
+    return torch.tensor(np.column_stack((pos, mass)), dtype=torch.float32, device=dev)
+
+
+def _rel(a, ref):
+    return np.linalg.norm(a - ref, axis=1) / np.maximum(np.linalg.norm(ref, axis=1), 1e-300)
+
+
+def _check_acc(a, ref):
+    rel = _rel(a, ref)
+    assert np.median(rel) < 1e-5, np.median(rel)
+    assert np.percentile(rel, 99) < 1e-4, np.percentile(rel, 99)
+    assert rel.max() < 1e-2, rel.max()
+
+
+def _run(bhmod, pos, mass, dev, theta=0.5, soft=0.05, bits=21, G=None, max_stack=64):
+    kw = {} if G is None else {"G": G}
+    n = pos.shape[0]
+    b = bhmod.BarnesHut(n, theta=theta, softening=soft, max_stack=max_stack, key_bits=bits,
+                        device=dev, **kw)
+    xm = _xm(pos, mass, dev)
+    acc = torch.zeros_like(xm)
+    b.compute(xm, acc)
+    torch.cuda.synchronize()
+    return b, acc[:, :3].double().cpu().numpy()
+
+
+@pytest.mark.parametrize("bits", [21, 10])
+def test_golden_tree_bit_exact(cuda_dev, bits):
+    _, bhmod, _, _ = _mods()
+    g = load_golden("bh")
+    pre = f"b{bits}_"
+    b, a = _run(bhmod, g["pos"], g["mass"], cuda_dev, bits=bits, G=float(g["G"]))
+    t = b.tree_arrays()
+    ref_sorted = g[pre + "code"][g[pre + "order"]]
+    np.testing.assert_array_equal(t["code"], ref_sorted)
+    np.testing.assert_array_equal(t["order"], g[pre + "order"])
+    np.testing.assert_array_equal(t["left"], g[pre + "left"])
+    np.testing.assert_array_equal(t["right"], g[pre + "right"])
+    np.testing.assert_array_equal(t["parent"], g[pre + "parent"])
+    np.testing.assert_array_equal(t["nmin"], g[pre + "nmin"])
+    np.testing.assert_array_equal(t["nmax"], g[pre + "nmax"])
+    np.testing.assert_allclose(t["nmass"], g[pre + "nmass"], rtol=1e-12)
+    np.testing.assert_allclose(t["com"], g[pre + "com"], rtol=1e-12, atol=1e-12)
+    _check_acc(a, g[pre + "acc"])
+    assert b.diag()["stack_drops"] == 0
+
+
+def test_golden_compute_and_duplicates(cuda_dev):
+    _, bhmod, _, _ = _mods()
+    g = load_golden("bh")
+    _, a = _run(bhmod, g["pos"], g["mass"], cuda_dev, bits=21, G=float(g["G"]))
+    _check_acc(a, g["compute_acc"])
+    b, a = _run(bhmod, g["dup_pos"], g["dup_mass"], cuda_dev, theta=0.7, bits=10, G=float(g["G"]))
+    t = b.tree_arrays()
+    np.testing.assert_array_equal(t["order"], g["dup_order"])
+    np.testing.assert_array_equal(t["left"], g["dup_left"])
+    np.testing.assert_array_equal(t["right"], g["dup_right"])
+    np.testing.assert_array_equal(t["parent"], g["dup_parent"])
+    _check_acc(a, g["dup_acc"])
+
+
+def test_stack_rule_matches_reference(cuda_dev, orc):
+    """max_stack=6 silently drops subtrees in the reference (:212); the
+    device applies the same rule per lane and counts the drops."""
+    _, bhmod, _, _ = _mods()
+    g = load_golden("bh")
+    pos, mass = g["pos"][:400], g["mass"][:400]
+    b, a = _run(bhmod, pos, mass, cuda_dev, bits=21, G=float(g["G"]), max_stack=6)
+    _check_acc(a, g["stk6_acc"])
+    _, _, dropped = orc.bh_compute(pos, mass, 0.5, 0.05, float(g["G"]), max_stack=6)
+    d = b.diag()["stack_drops"]
+    assert dropped > 0 and abs(d - dropped) <= max(2, dropped // 100), (d, dropped)
+
+
+def test_engine_bh_golden(cuda_dev):
+    pkg, _, _, _ = _mods()
+    g = load_golden("engine_bh")
+    eng = pkg.Engine(softening=float(g["softening"]), gravity_mode="bh",
+                     theta=float(g["theta"]), device=cuda_dev)
+    eng.load_state(pkg.State.from_arrays(g["pos0"], g["vel0"], g["mass"]))
+    assert eng._bh is not None
+    _check_acc(eng.acc.to_numpy(), g["acc0"])
+    for _ in range(int(g["nsteps"])):
+        eng.step(float(g["dt"]))
+    st = eng.to_state()
+    assert np.abs(st.pos - g["pos"]).max() < 1e-5 * np.abs(g["pos"]).max()
+    assert np.abs(st.vel - g["vel"]).max() < 1e-4 * np.abs(g["vel"]).max()
+
+
+@pytest.mark.parametrize("n", [2, 3, 33, 256, 1000])
+def test_small_sizes(cuda_dev, orc, n):
+    _, bhmod, ic, _ = _mods()
+    pos, _, mass = ic.exponential_disk(n, seed=n)
+    pos, mass = _f32(pos), _f32(mass)
+    b, a = _run(bhmod, pos, mass, cuda_dev)
+    ref, tree, _ = orc.bh_compute(pos, mass, 0.5, 0.05, b.G)
+    t = b.tree_arrays()
+    np.testing.assert_array_equal(t["order"], tree["order"])
+    np.testing.assert_array_equal(t["parent"], tree["parent"])
+    _check_acc(a, ref)
+
+
+@pytest.mark.parametrize("bits", [10, 21])
+def test_config2_disk_1m(cuda_dev, orc, bits):
+    """N = 1,000,000 exponential disk (M = 5, Rd = 3, z0 = 0.3, galactic G),
+    theta = 0.5, eps = 0.05: keys, order, topology bit-exact at full size;
+    forces on 4,096 seeded targets against FP64 direct and FP64 BH."""
+    _, bhmod, ic, grav = _mods()
+    n = 1_000_000
+    pos, _, mass = ic.exponential_disk(n, seed=0)
+    pos, mass = _f32(pos), _f32(mass)
+    b, a = _run(bhmod, pos, mass, cuda_dev, bits=bits)
+    t = b.tree_arrays()
+    codes = orc.morton_codes(pos, bits)
+    order = orc.stable_argsort(codes)
+    np.testing.assert_array_equal(t["code"], codes[order])
+    np.testing.assert_array_equal(t["order"], order)
+    left, right, parent = orc.build_radix(codes[order])
+    np.testing.assert_array_equal(t["left"], left)
+    np.testing.assert_array_equal(t["right"], right)
+    np.testing.assert_array_equal(t["parent"], parent)
+    targets = np.random.default_rng(0).choice(n, 4096, replace=False)
+    com, nmass, nmin, nmax = orc.summaries(order, pos, mass, parent)
+    np.testing.assert_array_equal(t["nmin"], nmin)
+    np.testing.assert_array_equal(t["nmax"], nmax)
+    np.testing.assert_allclose(t["nmass"], nmass, rtol=1e-12)
+    ref_bh, _ = orc.traverse(pos, order, com, nmass, nmin, nmax, left, right, 0.5, 0.0025, b.G,
+                             targets=targets)
+    _check_acc(a[targets], ref_bh)
+    xm = _xm(pos, mass, cuda_dev)
+    direct = grav.acc_fp64_targets(xm, targets, b.G, 0.0025)
+    err_gpu = _rel(a[targets], direct)
+    err_ref = _rel(ref_bh, direct)
+    assert abs(err_gpu.mean() - err_ref.mean()) < 1e-4
+    assert err_gpu.mean() < 0.02  # the theta = 0.5 monopole budget
+
+
+def test_deterministic(cuda_dev):
+    _, bhmod, ic, _ = _mods()
+    pos, _, mass = ic.exponential_disk(50000, seed=5)
+    b, a1 = _run(bhmod, pos, mass, cuda_dev)
+    xm = _xm(pos, mass, cuda_dev)
+    acc = torch.zeros_like(xm)
+    b.compute(xm, acc)
+    assert np.array_equal(a1, acc[:, :3].double().cpu().numpy())
+
+
+def test_bh_kdk_matches_oracle(cuda_dev, orc):
+    _, bhmod, ic, _ = _mods()
+    n = 3000
+    pos, vel, mass = ic.exponential_disk(n, seed=7)
+    pos, vel, mass = _f32(pos), _f32(vel), _f32(mass)
+    b = bhmod.BarnesHut(n, theta=0.5, softening=0.05, device=cuda_dev)
+    xm = _xm(pos, mass, cuda_dev)
+    v4 = torch.zeros_like(xm)
+    v4[:, :3] = torch.tensor(vel, dtype=torch.float32)
+    acc = torch.zeros_like(xm)
+    b.compute(xm, acc)
+    dt = 1e-4
+    b.kdk(xm, v4, acc, dt, 3)
+    p, v = pos.copy(), vel.copy()
+    a, _, _ = orc.bh_compute(p, mass, 0.5, 0.05, b.G)
+    for _ in range(3):
+        v = v + a * (0.5 * dt)
+        p = p + v * dt
+        a, _, _ = orc.bh_compute(p, mass, 0.5, 0.05, b.G)
+        v = v + a * (0.5 * dt)
+    gp = xm[:, :3].double().cpu().numpy()
+    gv = v4[:, :3].double().cpu().numpy()
+    assert np.abs(gp - p).max() < 1e-5 * np.abs(p).max()
+    assert np.abs(gv - v).max() < 1e-3 * np.abs(v).max()
+
+
+def test_bad_arguments(cuda_dev):
+    pkg, bhmod, _, _ = _mods()
+    b = bhmod.BarnesHut(100, device=cuda_dev)
+    with pytest.raises(pkg.GravityError, match="before"):
+        b.accel(torch.zeros((100, 4), device=cuda_dev))
+    with pytest.raises(ValueError):
+        b.compute(torch.zeros((200, 4), device=cuda_dev), torch.zeros((200, 4), device=cuda_dev))
+    with pytest.raises(pkg.GravityError, match="key_bits"):
+        bhmod.BarnesHut(100, key_bits=16, device=cuda_dev)

@@ -1,0 +1,195 @@
+"""Direct N^2 CUDA path against the reference fixtures and the FP64 oracle.
+
+Tolerance (FP32 pair arithmetic, Kahan accumulation, per-particle relative
+error |a - a_ref| / |a_ref|): RMS <= 1e-5 everywhere and max <= 1e-4 (a few
+particles near the centre of a sphere have nearly cancelling sums).
+"""
+import importlib
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import PKG_NAME, load_golden
+
+pytestmark = pytest.mark.gpu
+
+RMS_TOL = 1e-5
+MAX_TOL = 1e-4
+
+
+def _mods():
+    pkg = importlib.import_module(PKG_NAME)
+    grav = importlib.import_module(PKG_NAME + ".solvers.gravity")
+    ic = importlib.import_module(PKG_NAME + ".ic")
+    return pkg, grav, ic
+
+
+def _xm(pos, mass, dev):
+    return torch.tensor(np.column_stack((pos, mass)), dtype=torch.float32, device=dev)
+
+
+def _f32(a):
+    return np.asarray(a, np.float64).astype(np.float32).astype(np.float64)
+
+
+def _rel(a, ref):
+    return np.linalg.norm(a - ref, axis=1) / np.maximum(np.linalg.norm(ref, axis=1), 1e-300)
+
+
+def _acc(grav, xm, G, eps2, **kw):
+    solver = grav.DirectGravity(xm.shape[0], xm.device, tiles=kw.pop("tiles", None))
+    acc = torch.zeros_like(xm)
+    solver.acc(xm, acc, G, eps2, **kw)
+    torch.cuda.synchronize()
+    return acc[:, :3].double().cpu().numpy(), solver
+
+
+def test_golden_direct_acc(cuda_dev):
+    _, grav, _ = _mods()
+    g = load_golden("direct")
+    xm = _xm(g["pos"], g["mass"], cuda_dev)
+    a, _ = _acc(grav, xm, float(g["G"]), float(g["eps2"]))
+    rel = _rel(a, g["acc"])
+    assert np.sqrt((rel ** 2).mean()) < RMS_TOL and rel.max() < MAX_TOL
+
+
+@pytest.mark.parametrize("k,warps", [(2, 4), (2, 8), (4, 4), (4, 8)])
+@pytest.mark.parametrize("plain", [False, True])
+def test_config1_plummer_20k_all_tiles(cuda_dev, orc, k, warps, plain):
+    """N = 20,000 Plummer sphere, G = 1, eps = 0.01 (the direct workload)."""
+    _, grav, ic = _mods()
+    pos, _, mass = ic.plummer(20000, seed=0)
+    pos, mass = _f32(pos), _f32(mass)
+    xm = _xm(pos, mass, cuda_dev)
+    a, _ = _acc(grav, xm, 1.0, 1e-4, tiles=(k, warps), plain=plain)
+    targets = np.random.default_rng(1).choice(20000, 2048, replace=False)
+    ref = orc.direct_acc(pos, mass, 1.0, 1e-4, targets)
+    rel = _rel(a[targets], ref)
+    assert np.sqrt((rel ** 2).mean()) < RMS_TOL, np.sqrt((rel ** 2).mean())
+    assert rel.max() < MAX_TOL, rel.max()
+
+
+def test_deterministic_repeat(cuda_dev):
+    _, grav, ic = _mods()
+    pos, _, mass = ic.plummer(7777, seed=2)
+    xm = _xm(pos, mass, cuda_dev)
+    a1, s = _acc(grav, xm, 1.0, 1e-4)
+    acc = torch.zeros_like(xm)
+    s.acc(xm, acc, 1.0, 1e-4)
+    a2 = acc[:, :3].double().cpu().numpy()
+    assert np.array_equal(a1, a2)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 31, 32, 33, 255, 257, 1000, 4099])
+def test_ragged_sizes(cuda_dev, orc, n):
+    _, grav, ic = _mods()
+    pos, _, mass = ic.plummer(max(n, 2), seed=n)
+    pos, mass = _f32(pos[:n]), _f32(mass[:n])
+    xm = _xm(pos, mass, cuda_dev)
+    a, _ = _acc(grav, xm, 2.5, 0.05 ** 2)
+    ref = orc.direct_acc(pos, mass, 2.5, 0.05 ** 2)
+    if n == 1:
+        assert np.all(a == 0.0)
+        return
+    rel = _rel(a, ref)
+    assert rel.max() < MAX_TOL
+
+
+def test_accumulate_flag(cuda_dev, orc):
+    _, grav, ic = _mods()
+    pos, _, mass = ic.plummer(3000, seed=4)
+    pos, mass = _f32(pos), _f32(mass)
+    xm = _xm(pos, mass, cuda_dev)
+    s = grav.DirectGravity(3000, cuda_dev)
+    acc = torch.zeros_like(xm)
+    acc[:, 0] = 1.0
+    s.acc(xm, acc, 1.0, 1e-4, accumulate=True)
+    a = acc[:, :3].double().cpu().numpy()
+    ref = orc.direct_acc(pos, mass, 1.0, 1e-4)
+    ref[:, 0] += 1.0
+    rel = _rel(a, ref)
+    assert rel.max() < MAX_TOL
+
+
+def test_engine_kdk_golden(cuda_dev):
+    """Engine stepping against the reference Engine's own 25-step run."""
+    pkg, _, _ = _mods()
+    g = load_golden("engine_direct")
+    eng = pkg.Engine(softening=float(g["softening"]), device=cuda_dev)
+    eng.load_state(pkg.State.from_arrays(g["pos0"], g["vel0"], g["mass"]))
+    a0 = eng.acc.to_numpy()
+    assert _rel(a0, g["acc0"]).max() < MAX_TOL
+    for _ in range(int(g["nsteps"])):
+        eng.step(float(g["dt"]))
+    st = eng.to_state()
+    assert eng.step_count == int(g["step"]) and eng.time == pytest.approx(float(g["time"]))
+    scale = np.abs(g["pos"]).max()
+    assert np.abs(st.pos - g["pos"]).max() < 1e-5 * scale
+    vscale = np.abs(g["vel"]).max()
+    assert np.abs(st.vel - g["vel"]).max() < 1e-4 * vscale
+    ke, pe, tot = eng.energies()
+    np.testing.assert_allclose([ke, pe, tot], g["e1"], rtol=1e-4)
+
+
+def test_engine_run_matches_oracle_kdk(cuda_dev, orc):
+    pkg, _, ic = _mods()
+    pos, vel, mass = ic.plummer(2048, seed=6)
+    pos, vel, mass = _f32(pos), _f32(vel), _f32(mass)
+    eng = pkg.Engine(softening=0.01, G=1.0, device=cuda_dev)
+    eng.load_state(pkg.State.from_arrays(pos, vel, mass))
+    eng.run(1e-3, 10)
+    a0 = orc.direct_acc(pos, mass, 1.0, 1e-4)
+    p, v, a = orc.kdk_direct(pos, vel, a0, mass, 1.0, 1e-4, 1e-3, 10)
+    st = eng.to_state()
+    assert np.abs(st.pos - p).max() < 2e-5 * np.abs(p).max()
+    assert np.abs(st.vel - v).max() < 1e-4 * np.abs(v).max()
+
+
+def test_energies_golden(cuda_dev):
+    _, grav, _ = _mods()
+    g = load_golden("direct")
+    xm = _xm(g["pos"], g["mass"], cuda_dev)
+    vel = torch.zeros_like(xm)
+    vel[:, :3] = torch.tensor(g["vel"], dtype=torch.float32)
+    s = grav.DirectGravity(xm.shape[0], cuda_dev)
+    ke, pe, tot = s.energies(xm, vel, float(g["G"]), float(g["eps2"]))
+    assert ke == pytest.approx(float(g["ke"]), rel=1e-6)
+    assert pe == pytest.approx(float(g["pe"]), rel=1e-5)
+    assert tot == pytest.approx(ke + pe, rel=1e-12)
+
+
+def test_phi_matches_oracle(cuda_dev, orc):
+    _, grav, ic = _mods()
+    pos, _, mass = ic.plummer(5000, seed=8)
+    pos, mass = _f32(pos), _f32(mass)
+    xm = _xm(pos, mass, cuda_dev)
+    s = grav.DirectGravity(5000, cuda_dev)
+    phi = s.phi(xm, 1e-4).double().cpu().numpy()
+    t = np.arange(0, 5000, 7)
+    ref = orc.phi_targets(pos, mass, 1e-4, t)
+    assert np.abs(phi[t] - ref).max() / np.abs(ref).max() < 1e-5
+
+
+def test_fp64_targets_match_oracle(cuda_dev, orc):
+    _, grav, ic = _mods()
+    pos, _, mass = ic.plummer(3000, seed=9)
+    pos, mass = _f32(pos), _f32(mass)
+    xm = _xm(pos, mass, cuda_dev)
+    t = np.array([0, 1, 17, 2999, 1500])
+    a = grav.acc_fp64_targets(xm, t, 1.0, 1e-4)
+    ref = orc.direct_acc(pos, mass, 1.0, 1e-4, t)
+    np.testing.assert_allclose(a, ref, rtol=1e-12, atol=1e-12)
+
+
+def test_bad_arguments_raise(cuda_dev):
+    pkg, grav, _ = _mods()
+    s = grav.DirectGravity(100, cuda_dev)
+    xm = torch.zeros((200, 4), dtype=torch.float32, device=cuda_dev)
+    acc = torch.zeros_like(xm)
+    with pytest.raises(pkg.GravityError, match="n_max"):
+        s.acc(xm, acc, 1.0, 1e-4)
+    with pytest.raises(pkg.GravityError, match="eps2"):
+        s.acc(xm[:10], acc[:10], 1.0, 0.0)
+    with pytest.raises(pkg.GravityError):
+        s.set_tiles(3, 8)
