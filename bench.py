@@ -1,0 +1,509 @@
+"""Benchmark of the GB300 self-gravity engine.
+
+Headline workload (one JSON line on rank 0): LBVH Barnes-Hut KDK steps on a
+1,000,000-particle exponential stellar disk (M = 5e10 Msun, Rd = 3 kpc,
+sech^2 z0 = 0.3 kpc, 10% dispersion, seed 0, galactic units), theta = 0.5,
+eps = 0.05 kpc, 30-bit Morton keys, dt = 1e-4.  A step is one full KDK step:
+fused kick+drift, bounding box, keys, radix sort, Karras build, bottom-up
+summaries, traversal with the closing kick.  Metric: particle-steps/s.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb|reference]
+
+Timing: W untimed steps, then K steps; each step is bracketed by CUDA events
+on the launching stream, and a 512 MiB memset between steps (outside the
+events) flushes the 129 MB L2.  Under torchrun every rank runs an
+independent replica (the tree build is global: replicas only) and the
+slowest rank's time sets the aggregate.  Secondary results (direct N^2
+Plummer, FP32/Kahan/FP64 precision on a two-Plummer merger, batching,
+adjoint) run on rank 0 at N = 1 and are reported under "secondary".
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import importlib
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+import torch
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+PKG = "real-astronomy-simulation_gb300"
+
+BH_N = 1_000_000
+BH_THETA = 0.5
+BH_EPS = 0.05
+BH_BITS = 10
+BH_DT = 1e-4
+FLUSH_BYTES = 512 << 20
+METRIC = "BH particle-steps/s (LBVH theta=0.5, 1M exponential disk, KDK step)"
+
+
+# ---------------------------------------------------------------- helpers
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                    power.append(float(parts[3]))
+                except ValueError:
+                    continue
+                for nm, val in zip(names, parts[5:9]):
+                    if val.lower().startswith("active"):
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)),
+                "power_w_max": float(max(power)), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def _events(k):
+    return ([torch.cuda.Event(enable_timing=True) for _ in range(k)],
+            [torch.cuda.Event(enable_timing=True) for _ in range(k)])
+
+
+def _f32(a):
+    return np.asarray(a, np.float64).astype(np.float32).astype(np.float64)
+
+
+def _xm(pos, mass, dev):
+    return torch.tensor(np.column_stack((pos, mass)), dtype=torch.float32, device=dev)
+
+
+def _v4(vel, dev):
+    v = torch.zeros((vel.shape[0], 4), dtype=torch.float32, device=dev)
+    v[:, :3] = torch.tensor(vel, dtype=torch.float32)
+    return v
+
+
+def _rel_stats(a, ref):
+    rel = np.linalg.norm(a - ref, axis=1) / np.maximum(np.linalg.norm(ref, axis=1), 1e-300)
+    return {"rms": float(np.sqrt((rel ** 2).mean())), "max": float(rel.max()),
+            "median": float(np.median(rel))}
+
+
+def fp32_peak_tflops(lib_mod, dev):
+    """Measured FP32 CUDA-core peak (best of scalar FFMA and packed FFMA2)."""
+    buf = torch.zeros(1 << 16, device=dev)
+    fl = ctypes.c_double()
+    s = torch.cuda.current_stream().cuda_stream
+    best = 0.0
+    for packed in (0, 1):
+        for _ in range(2):
+            lib_mod.call("gb_calib_fp32", buf.data_ptr(), 2000, packed, ctypes.byref(fl), s)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            lib_mod.call("gb_calib_fp32", buf.data_ptr(), 2000, packed, ctypes.byref(fl), s)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, fl.value * 5 / (e0.elapsed_time(e1) / 1e3) / 1e12)
+    return best
+
+
+# --------------------------------------------------------------- headline
+def bench_bh(args, dev, rank, world, dist):
+    ic = importlib.import_module(PKG + ".ic")
+    bhmod = importlib.import_module(PKG + ".solvers.barnes_hut")
+    units = importlib.import_module(PKG + ".units")
+    pos, vel, mass = ic.exponential_disk(BH_N, seed=rank)
+    xm, v4 = _xm(pos, mass, dev), _v4(vel, dev)
+    a4 = torch.zeros_like(xm)
+    bh = bhmod.BarnesHut(BH_N, theta=BH_THETA, softening=BH_EPS, key_bits=BH_BITS,
+                         G=units.G, device=dev)
+    bh.compute(xm, a4)
+    for _ in range(args.warmup):
+        bh.kdk(xm, v4, a4, BH_DT, 1)
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    starts, ends = _events(args.steps)
+    torch.cuda.synchronize()
+    bh.diag(reset=True)
+    bh.timing(True)
+    bh.stage_times()
+    launches0 = bh.launch_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev.index).start()
+    for k in range(args.steps):
+        flush.zero_()
+        starts[k].record()
+        bh.kdk(xm, v4, a4, BH_DT, 1)
+        ends[k].record()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    launches = bh.launch_count() - launches0
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    stages, nst = bh.stage_times()
+    bh.timing(False)
+    diag = bh.diag(reset=True)
+    total_ms = float(sum(step_ms))
+    if dist:
+        t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * BH_N * args.steps / (total_ms / 1e3)
+    res = {"value": value, "ms_per_step": total_ms / args.steps, "clocks": clk,
+           "gpu_launches": int(launches), "diag": diag,
+           "stages_ms_per_step": {k: v / max(nst, 1) for k, v in stages.items()}}
+
+    # Work of one traversal, counted by an extra untimed evaluation with the
+    # counting kernel variant on the final state of the timed steps.
+    tmp = torch.zeros_like(a4)
+    bh.compute(xm, tmp, count_work=True)
+    per_step = {k: v for k, v in bh.diag(reset=True).items()
+                if k in ("warp_node_reads", "warp_root_reads", "lane_interactions", "lane_tests")}
+    del tmp
+    # Roofline of the dominant kernel (traversal): algorithmic bytes per launch
+    # = node records read per warp (48 B two-children record per expansion,
+    # 32 B root record) + per particle: own leaf 16 B, order 4 B, velocity
+    # 16 B read + 16 B write, acceleration 16 B write.
+    trav_ms = res["stages_ms_per_step"]["traverse"]
+    bytes_launch = (48 * per_step["warp_node_reads"] + 32 * per_step["warp_root_reads"]
+                    + BH_N * (16 + 4 + 16 + 16 + 16))
+    hbm, src = _peaks()
+    achieved = bytes_launch / (trav_ms / 1e3) / 1e9
+    res["roofline"] = {"kernel": "bh_traverse_kernel", "bound": "hbm", "achieved": achieved,
+                       "peak": hbm, "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)"
+                       if src == "measured" else "fallback 6800 GB/s",
+                       "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                       "algorithmic_bytes_per_launch": bytes_launch,
+                       "launch_ms": trav_ms}
+    # The same launch seen as FP32 work: 20 flop per monopole term, 10 per
+    # acceptance test.
+    flops = 20 * per_step["lane_interactions"] + 10 * per_step["lane_tests"]
+    res["work_per_step"] = per_step
+    res["traverse_fp32_tflops"] = flops / (trav_ms / 1e3) / 1e12
+
+    # e2e: the same step through the C ABI with host buffers; pinned host
+    # state is copied in before and read back after every step.
+    hx = xm.detach().cpu().pin_memory()
+    hv = v4.detach().cpu().pin_memory()
+    ha = a4.detach().cpu().pin_memory()
+    e_s, e_e = _events(args.steps)
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        flush.zero_()
+        e_s[k].record()
+        xm.copy_(hx, non_blocking=True)
+        v4.copy_(hv, non_blocking=True)
+        a4.copy_(ha, non_blocking=True)
+        bh.kdk(xm, v4, a4, BH_DT, 1)
+        hx.copy_(xm, non_blocking=True)
+        hv.copy_(v4, non_blocking=True)
+        ha.copy_(a4, non_blocking=True)
+        e_e[k].record()
+    torch.cuda.synchronize()
+    e2e_ms = float(sum(s.elapsed_time(e) for s, e in zip(e_s, e_e)))
+    if dist:
+        t = torch.tensor([e2e_ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    nbytes = 3 * BH_N * 16
+    res["e2e"] = {"value": world * BH_N * args.steps / (e2e_ms / 1e3),
+                  "unit": "particle-steps/s", "h2d_bytes_per_step": nbytes,
+                  "d2h_bytes_per_step": nbytes,
+                  "path": "gb_bh_kdk via the C ABI, pinned host state copied in/out each step"}
+    bh.close()
+    return res
+
+
+# ------------------------------------------------------------ CPU oracle
+def cpu_bh_step(budget_s: float = 20.0):
+    """One KDK step of the same workload with the float64 oracle (OpenMP, all
+    host threads): tree build over all particles, traversal of a seeded
+    target sample sized to the budget, scaled to the full particle count."""
+    from oracle import oracle
+
+    ic = importlib.import_module(PKG + ".ic")
+    units = importlib.import_module(PKG + ".units")
+    pos, vel, mass = ic.exponential_disk(BH_N, seed=0)
+    pos, vel, mass = _f32(pos), _f32(vel), _f32(mass)
+    acc = np.zeros_like(pos)
+    oracle.build()
+    rng = np.random.default_rng(0)
+    probe = rng.choice(BH_N, 20000, replace=False)
+    t0 = time.perf_counter()
+    tree = oracle.bh_tree(pos, mass, bits=BH_BITS)
+    t_build = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    oracle.traverse(pos, tree["order"], tree["com"], tree["nmass"], tree["nmin"], tree["nmax"],
+                    tree["left"], tree["right"], BH_THETA, BH_EPS ** 2, units.G, targets=probe)
+    per_target = (time.perf_counter() - t0) / probe.size
+    sample = int(min(BH_N, max(20000, (budget_s - t_build) / max(per_target, 1e-9))))
+    targets = np.sort(rng.choice(BH_N, sample, replace=False)) if sample < BH_N else None
+    t0 = time.perf_counter()
+    vh = vel + acc * (0.5 * BH_DT)
+    p1 = pos + vh * BH_DT
+    t_kick = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    tree = oracle.bh_tree(p1, mass, bits=BH_BITS)
+    t_build = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    a1, _ = oracle.traverse(p1, tree["order"], tree["com"], tree["nmass"], tree["nmin"],
+                            tree["nmax"], tree["left"], tree["right"], BH_THETA, BH_EPS ** 2,
+                            units.G, targets=targets)
+    t_trav = time.perf_counter() - t0
+    nt = BH_N if targets is None else targets.size
+    t_step = 2 * t_kick + t_build + t_trav * BH_N / nt
+    return {"value": BH_N / t_step, "unit": "particle-steps/s", "cores": oracle.max_threads(),
+            "kind": "port",
+            "sample": (f"one KDK step: kick/drift and tree build over all {BH_N} particles, "
+                       f"traversal of {nt} seeded targets scaled to {BH_N}"),
+            "seconds": {"build": t_build, "traverse": t_trav, "kick": t_kick}}
+
+
+# ------------------------------------------------------------- secondary
+def bench_direct(dev, lib_mod, peak_tflops):
+    """Direct N^2 Plummer, N = 20,000, G = 1, eps = 0.01, dt = 1e-3, 100 KDK
+    steps; plus the force kernel's own FP32 fraction at N = 20k and 262k."""
+    pkg = importlib.import_module(PKG)
+    ic = importlib.import_module(PKG + ".ic")
+    grav = importlib.import_module(PKG + ".solvers.gravity")
+    n, steps = 20000, 100
+    pos, vel, mass = ic.plummer(n, seed=0)
+    pos, vel, mass = _f32(pos), _f32(vel), _f32(mass)
+    eng = pkg.Engine(softening=0.01, G=1.0, device=dev)
+    eng.load_state(pkg.State.from_arrays(pos, vel, mass))
+    targets = np.random.default_rng(0).choice(n, 2048, replace=False)
+    ref = grav.acc_fp64_targets(eng.xm, targets, 1.0, 1e-4)
+    err = _rel_stats(eng.acc.to_numpy()[targets], ref)
+    e0 = eng.energies()
+    eng.run(1e-3, 3)
+    eng.load_state(pkg.State.from_arrays(pos, vel, mass))
+    e0 = eng.energies()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    eng.run(1e-3, steps)
+    e.record()
+    torch.cuda.synchronize()
+    t = s.elapsed_time(e) / 1e3
+    e1 = eng.energies()
+    out = {"workload": "direct N^2 Plummer N=20000, G=1, eps=0.01, dt=1e-3, 100 KDK steps",
+           "gint_per_s": n * n * steps / t / 1e9, "ms_per_step": t / steps * 1e3,
+           "energy_drift": abs((e1[2] - e0[2]) / e0[2]), "acc_err_vs_fp64_2048_targets": err}
+    kern = {}
+    for nk in (20000, 262144):
+        p2, _, m2 = ic.plummer(nk, seed=1)
+        xm = _xm(p2, m2, dev)
+        acc = torch.zeros_like(xm)
+        g = grav.DirectGravity(nk, dev)
+        for _ in range(3):
+            g.acc(xm, acc, 1.0, 1e-4)
+        reps = max(3, int(3e11 / nk / nk))
+        s.record()
+        for _ in range(reps):
+            g.acc(xm, acc, 1.0, 1e-4)
+        e.record()
+        torch.cuda.synchronize()
+        tk = s.elapsed_time(e) / reps / 1e3
+        tf = 20.0 * nk * nk / tk / 1e12
+        kern[str(nk)] = {"ms": tk * 1e3, "gint_per_s": nk * nk / tk / 1e9, "tflops_20flop": tf,
+                         "frac_of_fp32_peak": tf / peak_tflops}
+        g.close()
+    out["force_kernel"] = kern
+    return out
+
+
+def bench_merger(dev, drift_steps=1000):
+    """Precision: two Plummer spheres (2 x 131,072, G = 1, a = 1, M = 1) 10
+    apart on a parabolic orbit, eps = 0.01.  FP32+Kahan vs plain FP32 vs FP64
+    on 8,192 targets; FP64 energy drift over KDK steps at dt = 5e-4."""
+    pkg = importlib.import_module(PKG)
+    ic = importlib.import_module(PKG + ".ic")
+    grav = importlib.import_module(PKG + ".solvers.gravity")
+    pos, vel, mass = ic.plummer_pair(131072)
+    pos, vel, mass = _f32(pos), _f32(vel), _f32(mass)
+    n = pos.shape[0]
+    xm = _xm(pos, mass, dev)
+    targets = np.random.default_rng(0).choice(n, 8192, replace=False)
+    ref = grav.acc_fp64_targets(xm, targets, 1.0, 1e-4)
+    g = grav.DirectGravity(n, dev)
+    acc = torch.zeros_like(xm)
+    g.acc(xm, acc, 1.0, 1e-4)
+    kahan = _rel_stats(acc[:, :3].double().cpu().numpy()[targets], ref)
+    g.acc(xm, acc, 1.0, 1e-4, plain=True)
+    plain = _rel_stats(acc[:, :3].double().cpu().numpy()[targets], ref)
+    g.close()
+    eng = pkg.Engine(softening=0.01, G=1.0, device=dev)
+    eng.load_state(pkg.State.from_arrays(pos, vel, mass))
+    e0 = eng.energies()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    eng.run(5e-4, drift_steps)
+    e.record()
+    torch.cuda.synchronize()
+    t = s.elapsed_time(e) / 1e3
+    e1 = eng.energies()
+    return {"workload": f"two-Plummer merger 2x131072, eps=0.01, dt=5e-4, {drift_steps} KDK steps",
+            "impact_parameter": 2.0, "kahan_vs_fp64": kahan, "plain_fp32_vs_fp64": plain,
+            "energy_drift": abs((e1[2] - e0[2]) / e0[2]), "E0": e0, "E1": e1,
+            "gint_per_s": n * n * drift_steps / t / 1e9}
+
+
+# ------------------------------------------------------------------- main
+def run_reference(args):
+    """Reference arm: the float64 CPU restatement of the reference's BH path
+    (oracle, OpenMP over all host threads) on the same workload."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    steps = []
+    info = None
+    for k in range(args.warmup + args.steps):
+        r = cpu_bh_step(budget_s=8.0)
+        if k >= args.warmup:
+            steps.append(BH_N / r["value"])
+            info = r
+    t = float(sum(steps))
+    value = BH_N * args.steps / t
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": _config(),
+            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": info["cores"],
+                             "kind": "port", "sample": info["sample"]},
+            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _config():
+    return {"workload": "LBVH Barnes-Hut KDK step, exponential disk N=1,000,000 (M=5, Rd=3, "
+                        "sech2 z0=0.3, G=43009.1725), theta=0.5, eps=0.05, 30-bit Morton keys, "
+                        "dt=1e-4",
+            "n": BH_N, "theta": BH_THETA, "eps": BH_EPS, "key_bits": 3 * BH_BITS, "dt": BH_DT,
+            "l2": "flushed: 512 MiB memset between timed steps, outside the step events"}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("gb", "reference"), default="gb")
+    ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--drift-steps", type=int, default=1000)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
+    ap.add_argument("--only", choices=("direct", "merger"),
+                    help="run one secondary workload alone (profiling runs)")
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    pkg = importlib.import_module(PKG)
+    pkg.load_library()
+    lib_mod = importlib.import_module(PKG + "._lib")
+    if args.only:
+        peak = fp32_peak_tflops(lib_mod, dev)
+        fn = {"direct": lambda: bench_direct(dev, lib_mod, peak),
+              "merger": lambda: bench_merger(dev, args.drift_steps)}[args.only]
+        print(json.dumps({"only": args.only, "fp32_peak_tflops_measured": peak,
+                          "result": fn()}), flush=True)
+        return 0
+
+    res = bench_bh(args, dev, rank, world, dist)
+    line = {"metric": METRIC, "value": res["value"], "unit": "particle-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (FP64 key quantisation)",
+            "data": "synthetic (seeded exponential disk; one replica per rank)",
+            "config": _config(), "roofline": res["roofline"], "e2e": res["e2e"],
+            "gpu_launches": res["gpu_launches"], "clocks": res["clocks"],
+            "stages_ms_per_step": res["stages_ms_per_step"],
+            "traverse_work_per_step": res["work_per_step"],
+            "traverse_fp32_tflops": res["traverse_fp32_tflops"],
+            "diag": {k: res["diag"][k] for k in ("stack_drops", "stack_overflow", "nonfinite",
+                                                  "bad_tree")}}
+    if rank == 0 and world == 1:
+        if not args.no_cpu:
+            line["cpu_baseline"] = cpu_bh_step()
+        if not args.no_secondary:
+            peak = fp32_peak_tflops(lib_mod, dev)
+            sec = {"fp32_peak_tflops_measured": peak}
+            sec["direct"] = bench_direct(dev, lib_mod, peak)
+            sec["merger"] = bench_merger(dev, args.drift_steps)
+            line["secondary"] = sec
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -40,14 +40,19 @@ extern "C" {
 /* Flags */
 #define GB_ACCUMULATE 0x1  /* acc += result instead of acc = result */
 #define GB_PLAIN_FP32 0x2  /* plain FP32 accumulation (no Kahan compensation) */
+#define GB_COUNT_WORK 0x4  /* tree traversal also counts its work (gb_diag_t) */
 
 /* Device diagnostic counters, read back by gb_*_diag (synchronising). */
 typedef struct gb_diag {
     uint64_t stack_drops;     /* pushes skipped by the max_stack rule */
     uint64_t stack_overflow;  /* warp stack capacity reached */
     uint64_t nonfinite;       /* non-finite positions met while keying */
-    uint64_t bad_tree;        /* inconsistent node met in the bottom-up pass */
-    uint64_t reserved[4];
+    uint64_t bad_tree;        /* inconsistent index met (never for a valid tree) */
+    /* Traversal work, counted only by calls with GB_COUNT_WORK: */
+    uint64_t warp_node_reads;   /* 48-byte two-children node records read (per warp) */
+    uint64_t warp_root_reads;   /* 32-byte root records read (per warp) */
+    uint64_t lane_interactions; /* monopole terms summed (per particle) */
+    uint64_t lane_tests;        /* acceptance tests evaluated (per particle) */
 } gb_diag_t;
 
 const char *gb_last_error_string(void);
@@ -102,6 +107,10 @@ int gb_direct_acc_fp64(const float *xm, int64_t n, const int64_t *targets,
 
 int gb_direct_diag(gb_direct_t *h, gb_diag_t *out, int reset);
 
+/* Kernels launched through this handle so far (host-side count; measurement
+ * support, no reference counterpart). */
+uint64_t gb_direct_launch_count(gb_direct_t *h);
+
 /* ----------------------------------------------------- LBVH Barnes-Hut */
 typedef struct gb_bh gb_bh_t;
 
@@ -144,6 +153,19 @@ int gb_bh_kdk(gb_bh_t *h, float *xm, float *vel, float *acc, int64_t n,
 int gb_bh_export(gb_bh_t *h, int what, void *dst, void *stream);
 
 int gb_bh_diag(gb_bh_t *h, gb_diag_t *out, int reset);
+
+/* Stage timing for measurement: with timing enabled, every build/step records
+ * CUDA events on its stream at the boundaries of the GB_BH_STAGES stages
+ * (0 bbox+keys, 1 sort, 2 gather+Karras, 3 summaries, 4 traversal).
+ * gb_bh_stage_times synchronises, returns the summed milliseconds per stage
+ * over the (at most GB_BH_TIMING_STEPS) steps since the last call, and the
+ * step count.  gb_bh_launch_count returns the kernels this handle launched.
+ * No reference counterpart (measurement support). */
+#define GB_BH_STAGES 5
+#define GB_BH_TIMING_STEPS 64
+int gb_bh_timing(gb_bh_t *h, int enable);
+int gb_bh_stage_times(gb_bh_t *h, float *ms, int *steps);
+uint64_t gb_bh_launch_count(gb_bh_t *h);
 
 /* ------------------------------------------------------------ calibration */
 /* Launches an FP32 FMA-throughput kernel (packed = 1: .f32x2 form) on

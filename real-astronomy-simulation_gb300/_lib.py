@@ -27,6 +27,7 @@ GB_ENOTREADY = 6
 
 GB_ACCUMULATE = 0x1
 GB_PLAIN_FP32 = 0x2
+GB_COUNT_WORK = 0x4
 
 _STATUS = {GB_EINVAL: "GB_EINVAL", GB_ENOMEM: "GB_ENOMEM", GB_ESTACK: "GB_ESTACK",
            GB_ETIMEOUT: "GB_ETIMEOUT", GB_ECUDA: "GB_ECUDA",
@@ -44,10 +45,11 @@ class GravityError(RuntimeError):
 class Diag(ctypes.Structure):
     _fields_ = [("stack_drops", ctypes.c_uint64), ("stack_overflow", ctypes.c_uint64),
                 ("nonfinite", ctypes.c_uint64), ("bad_tree", ctypes.c_uint64),
-                ("reserved", ctypes.c_uint64 * 4)]
+                ("warp_node_reads", ctypes.c_uint64), ("warp_root_reads", ctypes.c_uint64),
+                ("lane_interactions", ctypes.c_uint64), ("lane_tests", ctypes.c_uint64)]
 
     def as_dict(self):
-        return {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "reserved"}
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
 
 
 # name -> (restype, argtypes)
@@ -63,6 +65,7 @@ SIGNATURES = {
     "gb_energy": (I32, [P, P, P, I64, F32, F32, P, P]),
     "gb_direct_acc_fp64": (I32, [P, I64, P, I64, F64, F64, P, P]),
     "gb_direct_diag": (I32, [P, ctypes.POINTER(Diag), I32]),
+    "gb_direct_launch_count": (ctypes.c_uint64, [P]),
     "gb_calib_fp32": (I32, [P, I32, I32, ctypes.POINTER(F64), P]),
     "gb_bh_create": (I32, [ctypes.POINTER(P), I64, I32]),
     "gb_bh_destroy": (I32, [P]),
@@ -72,6 +75,9 @@ SIGNATURES = {
     "gb_bh_kdk": (I32, [P, P, P, P, I64, F32, F32, F32, F32, I64, I32, P]),
     "gb_bh_export": (I32, [P, I32, P, P]),
     "gb_bh_diag": (I32, [P, ctypes.POINTER(Diag), I32]),
+    "gb_bh_timing": (I32, [P, I32]),
+    "gb_bh_stage_times": (I32, [P, ctypes.POINTER(F32), ctypes.POINTER(I32)]),
+    "gb_bh_launch_count": (ctypes.c_uint64, [P]),
 }
 
 _lib = None

@@ -12,11 +12,12 @@
 //               permutation of np.argsort(kind="stable") (:247)
 //   3 gather    particles into key order (leaf records)
 //   4 karras    binary radix tree, identical to _build_radix (:84-121)
-//   5 bottom-up node mass / moment (FP64) and AABB; a node is summarised by
-//               the second of its two children to finish (integer arrival
-//               ticket, fences, L2 reads): no floating-point atomics, and the
-//               result is independent of scheduling (:124-177 use FP64
-//               atomics on every ancestor instead)
+//   5 bottom-up node mass, first moment and AABB (FP32); a node is
+//               summarised by the second of its two children to finish
+//               (integer arrival ticket with acquire-release ordering, L2
+//               reads): no floating-point atomics, and the result is
+//               independent of scheduling (:124-177 use FP64 atomics on
+//               every ancestor instead)
 //   6 traverse  warp-coherent walk: 32 key-consecutive targets share one
 //               shared-memory stack of (node, lane mask); every lane applies
 //               the reference's own acceptance test size^2 < theta^2 (r^2 +
@@ -37,10 +38,7 @@ struct BHParams {
     double scale;
 };
 
-// Node mass moment and mass, FP64 (32-byte record).
-struct alignas(32) Mom4 {
-    double x, y, z, w;
-};
+
 
 constexpr int BBOX_THREADS = 256;
 constexpr int RS_THREADS = 256;
@@ -179,16 +177,10 @@ rs_upsweep_kernel(const KeyT *__restrict__ keys, int64_t n, int shift, uint32_t 
     for (int d = threadIdx.x; d < RS_BINS; d += RS_THREADS) hist[(int64_t)d * nb + blockIdx.x] = h[d];
 }
 
-// Exclusive scan of the digit-major histogram (one CTA of 1024 threads).
-__global__ void __launch_bounds__(1024) rs_scan_kernel(uint32_t *hist, int64_t count) {
-    __shared__ uint32_t wsum[32];
-    const int64_t per = (count + 1023) / 1024;
-    const int64_t b = threadIdx.x * per, e = min(count, b + per);
-    uint32_t s = 0;
-    for (int64_t k = b; k < e; ++k) s += hist[k];
-    // block exclusive scan of s
+// Exclusive scan of 256 values held one per thread of a 256-thread CTA.
+__device__ __forceinline__ uint32_t cta256_exclusive_scan(uint32_t v, uint32_t *wsum) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    uint32_t inc = s;
+    uint32_t inc = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
@@ -197,21 +189,36 @@ __global__ void __launch_bounds__(1024) rs_scan_kernel(uint32_t *hist, int64_t c
     if (lane == 31) wsum[wid] = inc;
     __syncthreads();
     if (wid == 0) {
-        uint32_t w = wsum[lane], wi = w;
+        const uint32_t w = lane < RS_WARPS ? wsum[lane] : 0u;
+        uint32_t wi = w;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
             if (lane >= o) wi += t;
         }
-        wsum[lane] = wi - w;
+        if (lane < RS_WARPS) wsum[lane] = wi - w;
     }
     __syncthreads();
-    uint32_t run = wsum[wid] + inc - s;
-    for (int64_t k = b; k < e; ++k) {
-        const uint32_t v = hist[k];
-        hist[k] = run;
-        run += v;
+    return wsum[wid] + inc - v;
+}
+
+// Row scan: CTA d turns row d of the digit-major histogram (one count per
+// tile) into exclusive offsets within the digit and stores the digit total.
+__global__ void __launch_bounds__(RS_THREADS) rs_rowscan_kernel(uint32_t *hist, int nb, uint32_t *totals) {
+    __shared__ uint32_t wsum[RS_WARPS];
+    uint32_t *row = hist + (int64_t)blockIdx.x * nb;
+    const int per = (nb + RS_THREADS - 1) / RS_THREADS;
+    const int b0 = min(nb, (int)threadIdx.x * per), b1 = min(nb, b0 + per);
+    uint32_t v = 0;
+    for (int b = b0; b < b1; ++b) v += row[b];
+    const uint32_t excl = cta256_exclusive_scan(v, wsum);
+    uint32_t run = excl;
+    for (int b = b0; b < b1; ++b) {
+        const uint32_t t = row[b];
+        row[b] = run;
+        run += t;
     }
+    if (threadIdx.x == RS_THREADS - 1) totals[blockIdx.x] = excl + v;
 }
 
 // Stable scatter: elements of a tile are ranked in index order (warp, round,
@@ -221,12 +228,16 @@ template <typename KeyT>
 __global__ void __launch_bounds__(RS_THREADS)
 rs_downsweep_kernel(const KeyT *__restrict__ kin, const uint32_t *__restrict__ vin, KeyT *__restrict__ kout,
                     uint32_t *__restrict__ vout, int64_t n, int shift, const uint32_t *__restrict__ hist, int nb,
-                    unsigned long long *diag) {
+                    const uint32_t *__restrict__ totals, unsigned long long *diag) {
+    static_assert(RS_THREADS == RS_BINS, "one thread per digit");
     __shared__ uint32_t whist[RS_WARPS][RS_BINS];
     __shared__ uint32_t boff[RS_BINS];
+    __shared__ uint32_t wsum[RS_WARPS];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int d = threadIdx.x; d < RS_BINS; d += RS_THREADS) {
-        boff[d] = hist[(int64_t)d * nb + blockIdx.x];
+    {
+        const int d = threadIdx.x;
+        const uint32_t base = cta256_exclusive_scan(totals[d], wsum);
+        boff[d] = base + hist[(int64_t)d * nb + blockIdx.x];
 #pragma unroll
         for (int w = 0; w < RS_WARPS; ++w) whist[w][d] = 0;
     }
@@ -337,41 +348,66 @@ __global__ void bh_karras_kernel(const KeyT *__restrict__ k, int n, int2 *__rest
 }
 
 // -------------------------------------------------------------- bottom-up
+// Node summary in FP32: mass, first moment about the node's AABB minimum
+// corner, and the AABB.  Moments about the corner keep the centre of mass
+// accurate to rounding of the node size (a cluster of coincident particles
+// gets its exact position); the reference keeps FP64 moments about the
+// origin (core/solvers/barnes_hut.py:143-177).
 struct NodeSum {
-    double mx, my, mz, m;  // mass moment and mass
+    float m, sx, sy, sz;    // mass, moment about (lx, ly, lz)
     float lx, ly, lz, hx, hy, hz;
 };
 
 __device__ __forceinline__ NodeSum child_sum(int c, int n, const float4 *__restrict__ leaf,
-                                             const Mom4 *__restrict__ mom, const float4 *__restrict__ bmin,
+                                             const float4 *__restrict__ sums, const float4 *__restrict__ bmin,
                                              const float4 *__restrict__ bmax) {
     NodeSum s;
     if (c < n) {
         const float4 p = __ldg(leaf + c);
-        const double m = p.w;
-        s.m = m;
-        s.mx = m * (double)p.x;
-        s.my = m * (double)p.y;
-        s.mz = m * (double)p.z;
+        s.m = p.w;
+        s.sx = s.sy = s.sz = 0.f;
         s.lx = s.hx = p.x;
         s.ly = s.hy = p.y;
         s.lz = s.hz = p.z;
     } else {
         const int k = c - n;
-        const double2 q0 = __ldcg(reinterpret_cast<const double2 *>(mom + k));
-        const double2 q1 = __ldcg(reinterpret_cast<const double2 *>(mom + k) + 1);
-        const float4 a = __ldcg(bmin + k), b = __ldcg(bmax + k);
-        s.mx = q0.x; s.my = q0.y; s.mz = q1.x; s.m = q1.y;
+        const float4 q = __ldcg(sums + k), a = __ldcg(bmin + k), b = __ldcg(bmax + k);
+        s.m = q.x; s.sx = q.y; s.sy = q.z; s.sz = q.w;
         s.lx = a.x; s.ly = a.y; s.lz = a.z;
         s.hx = b.x; s.hy = b.y; s.hz = b.z;
     }
     return s;
 }
 
+// Centre of mass and mass; a node without mass keeps a zero centre, like the
+// freshly allocated com field of the reference.
+__device__ __forceinline__ float4 trav_com(const NodeSum &s) {
+    if (!(s.m > 0.f)) return make_float4(0.f, 0.f, 0.f, 0.f);
+    return make_float4(s.lx + __fdiv_rn(s.sx, s.m), s.ly + __fdiv_rn(s.sy, s.m), s.lz + __fdiv_rn(s.sz, s.m), s.m);
+}
+
+// Squared largest AABB extent (:207).
+__device__ __forceinline__ float size2_of(const NodeSum &s) {
+    const float e = fmaxf(fmaxf(s.hx - s.lx, s.hy - s.ly), s.hz - s.lz);
+    return e * e;
+}
+
+// Arrival ticket with acquire-release ordering at GPU scope: the first child
+// to finish publishes its summary; the second observes it.
+__device__ __forceinline__ unsigned arrive(unsigned *p) {
+    unsigned old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+    return old;
+}
+
+// Summarises every internal node k once both children are done and writes
+// the traversal record of its two children:
+//   inode[3k] = left {com, m}, inode[3k+1] = right {com, m},
+//   inode[3k+2] = {size2 left, size2 right, left id, right id} (ids as bits).
 __global__ void bh_bottomup_kernel(const float4 *__restrict__ leaf, const int2 *__restrict__ child,
                                    const int *__restrict__ parent, int n, unsigned *__restrict__ arrivals,
-                                   Mom4 *__restrict__ mom, float4 *__restrict__ bmin, float4 *__restrict__ bmax,
-                                   float4 *__restrict__ inode, unsigned long long *diag) {
+                                   float4 *__restrict__ sums, float4 *__restrict__ bmin, float4 *__restrict__ bmax,
+                                   float4 *__restrict__ inode, float4 *__restrict__ root, unsigned long long *diag) {
     const int li = blockIdx.x * blockDim.x + threadIdx.x;
     if (li >= n) return;
     int node = __ldg(parent + li);
@@ -381,35 +417,33 @@ __global__ void bh_bottomup_kernel(const float4 *__restrict__ leaf, const int2 *
             return;
         }
         const int k = node - n;
-        __threadfence();  // publish the finished child before signalling
-        if (atomicAdd(arrivals + k, 1u) == 0u) return;  // sibling still running
-        __threadfence();  // acquire the sibling's record
+        if (arrive(arrivals + k) == 0u) return;  // the sibling subtree is still running
         const int2 c = __ldg(child + k);
         if ((unsigned)c.x >= (unsigned)(2 * n - 1) || (unsigned)c.y >= (unsigned)(2 * n - 1)) {
             atomicAdd(diag + DIAG_BAD_TREE, 1ull);
             return;
         }
-        const NodeSum a = child_sum(c.x, n, leaf, mom, bmin, bmax);
-        const NodeSum b = child_sum(c.y, n, leaf, mom, bmin, bmax);
+        const NodeSum a = child_sum(c.x, n, leaf, sums, bmin, bmax);
+        const NodeSum b = child_sum(c.y, n, leaf, sums, bmin, bmax);
         NodeSum s;
-        s.m = a.m + b.m;
-        s.mx = a.mx + b.mx;
-        s.my = a.my + b.my;
-        s.mz = a.mz + b.mz;
         s.lx = fminf(a.lx, b.lx); s.ly = fminf(a.ly, b.ly); s.lz = fminf(a.lz, b.lz);
         s.hx = fmaxf(a.hx, b.hx); s.hy = fmaxf(a.hy, b.hy); s.hz = fmaxf(a.hz, b.hz);
-        mom[k] = Mom4{s.mx, s.my, s.mz, s.m};
+        s.m = a.m + b.m;
+        s.sx = __fmaf_rn(b.m, b.lx - s.lx, __fmaf_rn(a.m, a.lx - s.lx, a.sx + b.sx));
+        s.sy = __fmaf_rn(b.m, b.ly - s.ly, __fmaf_rn(a.m, a.ly - s.ly, a.sy + b.sy));
+        s.sz = __fmaf_rn(b.m, b.lz - s.lz, __fmaf_rn(a.m, a.lz - s.lz, a.sz + b.sz));
+        sums[k] = make_float4(s.m, s.sx, s.sy, s.sz);
         bmin[k] = make_float4(s.lx, s.ly, s.lz, 0.f);
         bmax[k] = make_float4(s.hx, s.hy, s.hz, 0.f);
-        // Traversal record: {com, mass}, {size^2, left, right, 0}.
-        double cx = 0.0, cy = 0.0, cz = 0.0;
-        if (s.m > 0.0) { cx = s.mx / s.m; cy = s.my / s.m; cz = s.mz / s.m; }
-        double size = (double)s.hx - (double)s.lx;
-        size = fmax(size, (double)s.hy - (double)s.ly);
-        size = fmax(size, (double)s.hz - (double)s.lz);
-        inode[2 * k] = make_float4((float)cx, (float)cy, (float)cz, (float)s.m);
-        inode[2 * k + 1] = make_float4((float)(size * size), __int_as_float(c.x), __int_as_float(c.y), 0.f);
-        node = __ldg(parent + node);
+        inode[3 * k] = trav_com(a);
+        inode[3 * k + 1] = trav_com(b);
+        inode[3 * k + 2] = make_float4(size2_of(a), size2_of(b), __int_as_float(c.x), __int_as_float(c.y));
+        const int up = __ldg(parent + node);
+        if (up < 0) {
+            root[0] = trav_com(s);
+            root[1] = make_float4(size2_of(s), 0.f, 0.f, 0.f);
+        }
+        node = up;
     }
 }
 
@@ -417,6 +451,7 @@ __global__ void bh_bottomup_kernel(const float4 *__restrict__ leaf, const int2 *
 struct TravArgs {
     const float4 *__restrict__ leaf;
     const float4 *__restrict__ inode;
+    const float4 *__restrict__ root;
     const uint32_t *__restrict__ order;
     float4 *acc;
     float4 *vel;
@@ -427,113 +462,147 @@ struct TravArgs {
     unsigned long long *diag;
 };
 
-template <bool KDK>
+struct Lane {
+    float px, py, pz, ax, ay, az;
+    unsigned n_int, n_test, drops;
+};
+
+// One child for one lane of the expanding mask (branch-free): a leaf adds
+// its monopole unless it is the lane's own particle; an internal node adds
+// its monopole when size^2 < theta^2 (|d|^2 + eps^2), else it is opened if
+// the reference's stack (depth sp once the child is popped) has room for two
+// pushes, else the push is dropped and counted.  Returns "open".
+template <bool COUNT>
+__device__ __forceinline__ bool visit_child(Lane &L, const TravArgs &a, float4 q, float size2, int id, int s,
+                                            int sp, bool in) {
+    const float dx = q.x - L.px, dy = q.y - L.py, dz = q.z - L.pz;
+    const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, a.eps2)));
+    const bool is_leaf = id < a.n;
+    const bool accept = is_leaf ? (id != s) : (size2 < a.theta2 * r2);
+    const bool add = in && accept;
+    const float inv = rsqrt_approx(r2);
+    const float sc = add ? q.w * inv * inv * inv : 0.f;
+    L.ax = __fmaf_rn(sc, dx, L.ax);
+    L.ay = __fmaf_rn(sc, dy, L.ay);
+    L.az = __fmaf_rn(sc, dz, L.az);
+    const bool open = in && !is_leaf && !accept;
+    const bool room = sp + 2 <= a.max_stack;
+    if (COUNT) {
+        L.n_int += add ? 1u : 0u;
+        L.n_test += (in && !is_leaf) ? 1u : 0u;
+    }
+    L.drops += (open && !room) ? 1u : 0u;
+    return open && room;
+}
+
+// Warp-coherent traversal: 32 key-consecutive targets per warp walk the tree
+// together.  The warp expands one internal node per iteration: it loads the
+// node's two-children record (48 B) and every lane of the node's mask visits
+// both children (right first, as the reference pops it first).  The right
+// child, if any lane opened it, is expanded next straight from registers; an
+// opened left child waits on a shared-memory stack of {node, mask, sp}.  sp,
+// the depth of the reference's per-particle stack when a node is popped,
+// depends only on the node's path (one pending left sibling per right turn),
+// so it travels with the node.
+template <bool KDK, bool COUNT>
 __global__ void __launch_bounds__(TRAV_WARPS * 32)
 bh_traverse_kernel(TravArgs a) {
-    __shared__ int stk_node[TRAV_WARPS][TRAV_STACK];
-    __shared__ unsigned stk_mask[TRAV_WARPS][TRAV_STACK];
+    __shared__ int4 stk[TRAV_WARPS][TRAV_STACK];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int s = (blockIdx.x * TRAV_WARPS + wid) * 32 + lane;
-    if ((blockIdx.x * TRAV_WARPS + wid) * 32 >= a.n) return;  // whole warp out of range
+    const int wbase = (blockIdx.x * TRAV_WARPS + wid) * 32;
+    if (wbase >= a.n) return;  // whole warp out of range
+    const int s = wbase + lane;
     const bool valid = s < a.n;
     const int n = a.n;
-    float px = 0.f, py = 0.f, pz = 0.f;
+    Lane L;
+    L.px = L.py = L.pz = 0.f;
     if (valid) {
         const float4 p = __ldg(a.leaf + s);
-        px = p.x; py = p.y; pz = p.z;
+        L.px = p.x; L.py = p.y; L.pz = p.z;
     }
-    float ax = 0.f, ay = 0.f, az = 0.f;
-    unsigned drops = 0, overflow = 0, bad = 0;
-    int sp_lane = 0;
+    L.ax = L.ay = L.az = 0.f;
+    L.n_int = L.n_test = L.drops = 0;
+    unsigned overflow = 0, bad = 0, iters = 0;
     int top = 0;
+    int k = 0, sp = 0;
+    unsigned m = 0;
     if (n >= 2) {
-        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-        if (lane == 0) {
-            stk_node[wid][0] = n;
-            stk_mask[wid][0] = vmask;
-        }
-        sp_lane = valid ? 1 : 0;
-        top = 1;
-        __syncwarp();
+        // The root is popped first, with an empty stack (sp = 0).
+        const float4 R0 = __ldg(a.root), R1 = __ldg(a.root + 1);
+        const bool want = visit_child<COUNT>(L, a, R0, R1.x, n, s, 0, valid);
+        m = __ballot_sync(0xffffffffu, want);
     }
-    while (top > 0) {
-        --top;
-        const int node = stk_node[wid][top];
-        const unsigned m = stk_mask[wid][top];
+    while (m) {
         const bool in = (m >> lane) & 1u;
-        sp_lane -= in ? 1 : 0;
-        if ((unsigned)node >= (unsigned)(2 * n - 1)) {  // never for a consistent tree
+        if ((unsigned)k >= (unsigned)(n - 1)) {  // never for a consistent tree
             bad += in ? 1u : 0u;
-            __syncwarp();
-            continue;
-        }
-        if (node < n) {
-            const float4 q = __ldg(a.leaf + node);
-            if (in && node != s) {
-                const float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
-                const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, a.eps2)));
-                const float inv = rsqrt_approx(r2);
-                const float sc = q.w * inv * inv * inv;
-                ax = __fmaf_rn(sc, dx, ax);
-                ay = __fmaf_rn(sc, dy, ay);
-                az = __fmaf_rn(sc, dz, az);
-            }
-            __syncwarp();
-            continue;
-        }
-        const int k = node - n;
-        const float4 A = __ldg(a.inode + 2 * k);
-        const float4 B = __ldg(a.inode + 2 * k + 1);
-        bool want = false;
-        if (in) {
-            const float dx = A.x - px, dy = A.y - py, dz = A.z - pz;
-            const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, a.eps2)));
-            if (B.x < a.theta2 * r2) {
-                const float inv = rsqrt_approx(r2);
-                const float sc = A.w * inv * inv * inv;
-                ax = __fmaf_rn(sc, dx, ax);
-                ay = __fmaf_rn(sc, dy, ay);
-                az = __fmaf_rn(sc, dz, az);
-            } else if (sp_lane + 2 <= a.max_stack) {
-                want = true;
-            } else {
-                ++drops;
-            }
-        }
-        const unsigned om = __ballot_sync(0xffffffffu, want);
-        if (om) {
-            if (top + 2 <= TRAV_STACK) {
-                if (lane == 0) {
-                    stk_node[wid][top] = __float_as_int(B.y);
-                    stk_mask[wid][top] = om;
-                    stk_node[wid][top + 1] = __float_as_int(B.z);
-                    stk_mask[wid][top + 1] = om;
+            m = 0;
+        } else {
+            const float4 QL = __ldg(a.inode + 3 * k);
+            const float4 QR = __ldg(a.inode + 3 * k + 1);
+            const float4 C = __ldg(a.inode + 3 * k + 2);
+            if (COUNT) ++iters;
+            const bool wantR = visit_child<COUNT>(L, a, QR, C.y, __float_as_int(C.w), s, sp + 1, in);
+            const bool wantL = visit_child<COUNT>(L, a, QL, C.x, __float_as_int(C.z), s, sp, in);
+            const unsigned omL = __ballot_sync(0xffffffffu, wantL);
+            const unsigned omR = __ballot_sync(0xffffffffu, wantR);
+            if (omL) {
+                if (top < TRAV_STACK) {
+                    if (lane == 0) stk[wid][top] = make_int4(__float_as_int(C.z) - n, (int)omL, sp, 0);
+                    ++top;
+                } else {
+                    overflow += wantL ? 1u : 0u;
                 }
-                top += 2;
-                sp_lane += want ? 2 : 0;
-            } else if (want) {
-                ++overflow;
             }
+            if (omR) {  // expand the right child next
+                k = __float_as_int(C.w) - n;
+                m = omR;
+                sp = sp + 1;
+                continue;
+            }
+            m = 0;
         }
-        __syncwarp();
+        if (top > 0) {
+            __syncwarp();
+            const int4 e = stk[wid][--top];
+            k = e.x;
+            m = (unsigned)e.y;
+            sp = e.z;
+            __syncwarp();
+        }
     }
-    // Epilogue: scatter to the original particle index.
-    unsigned dsum = drops, osum = overflow, bsum = bad;
+    // Counters: one atomic per warp and counter.
+    unsigned dsum = L.drops, osum = overflow, bsum = bad;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
         osum += __shfl_xor_sync(0xffffffffu, osum, o);
         bsum += __shfl_xor_sync(0xffffffffu, bsum, o);
     }
+    if (COUNT) {
+        unsigned isum = L.n_int, tsum = L.n_test;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            isum += __shfl_xor_sync(0xffffffffu, isum, o);
+            tsum += __shfl_xor_sync(0xffffffffu, tsum, o);
+        }
+        if (lane == 0) {
+            atomicAdd(a.diag + DIAG_NODE_READS, (unsigned long long)iters);
+            atomicAdd(a.diag + DIAG_ROOT_READS, 1ull);
+            atomicAdd(a.diag + DIAG_INTERACTIONS, (unsigned long long)isum);
+            atomicAdd(a.diag + DIAG_TESTS, (unsigned long long)tsum);
+        }
+    }
     if (lane == 0) {
         if (dsum) atomicAdd(a.diag + DIAG_STACK_DROPS, (unsigned long long)dsum);
         if (osum) atomicAdd(a.diag + DIAG_STACK_OVERFLOW, (unsigned long long)osum);
         if (bsum) atomicAdd(a.diag + DIAG_BAD_TREE, (unsigned long long)bsum);
     }
+    // Epilogue: scatter to the original particle index.
     if (!valid) return;
     const uint32_t p = __ldg(a.order + s);
     if (p >= (uint32_t)n) return;
-    const float gx = a.G * ax, gy = a.G * ay, gz = a.G * az;
+    const float gx = a.G * L.ax, gy = a.G * L.ay, gz = a.G * L.az;
     if (KDK) {
         const float4 vh = a.vel[p];
         a.vel[p] = make_float4(kick(vh.x, gx, a.h), kick(vh.y, gy, a.h), kick(vh.z, gz, a.h), vh.w);
@@ -563,7 +632,7 @@ enum ExportWhat {
 
 template <typename KeyT>
 __global__ void bh_export_kernel(int what, int n, const KeyT *keys, const uint32_t *order, const int2 *child,
-                                 const int *parent, const float4 *leaf, const Mom4 *mom, const float4 *bmin,
+                                 const int *parent, const float4 *leaf, const float4 *sums, const float4 *bmin,
                                  const float4 *bmax, void *dst) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t nodes = 2 * (int64_t)n - 1;
@@ -594,12 +663,12 @@ __global__ void bh_export_kernel(int what, int n, const KeyT *keys, const uint32
                 c[2] = lo[2] = hi[2] = p.z;
             } else {
                 const int k = (int)(i - n);
-                const Mom4 q = mom[k];
-                m = q.w;
-                c[0] = m > 0.0 ? q.x / m : 0.0;
-                c[1] = m > 0.0 ? q.y / m : 0.0;
-                c[2] = m > 0.0 ? q.z / m : 0.0;
+                const float4 q = sums[k];
+                m = q.x;
                 lo[0] = bmin[k].x; lo[1] = bmin[k].y; lo[2] = bmin[k].z;
+                c[0] = m > 0.0 ? lo[0] + q.y / m : 0.0;
+                c[1] = m > 0.0 ? lo[1] + q.z / m : 0.0;
+                c[2] = m > 0.0 ? lo[2] + q.w / m : 0.0;
                 hi[0] = bmax[k].x; hi[1] = bmax[k].y; hi[2] = bmax[k].z;
             }
             double *o = (double *)dst;
@@ -637,21 +706,37 @@ struct gb_bh {
     int2 *child;
     int *parent;
     unsigned *arrivals;
-    Mom4 *mom;
+    float4 *sums;
     float4 *bmin, *bmax;
     float4 *inode;
+    float4 *root;
+    uint32_t *totals;
     unsigned long long *diag;
+    // Stage timing (gb_bh_timing): events recorded on the launch stream at
+    // stage boundaries, GB_BH_STAGES + 1 per step, reused cyclically.
+    int timing;
+    int ev_used;
+    cudaEvent_t ev[GB_BH_TIMING_STEPS * (GB_BH_STAGES + 1)];
+    uint64_t launches;  // kernels launched by this handle (host count)
+    int pending_slot;   // timing slot of the last gb_bh_build
 };
+
+static void mark(gb_bh_t *h, int step_slot, int stage, cudaStream_t s) {
+    if (!h->timing) return;
+    cudaEventRecord(h->ev[step_slot * (GB_BH_STAGES + 1) + stage], s);
+}
 
 static size_t key_size(int bits) { return bits <= 10 ? sizeof(uint32_t) : sizeof(uint64_t); }
 
 extern "C" int gb_bh_destroy(gb_bh_t *h) {
     if (!h) return GB_OK;
     void *ptrs[] = {h->keys[0], h->keys[1], h->vals[0], h->vals[1], h->hist, h->bbox_part, h->ticket,
-                    h->prm, h->leaf, h->child, h->parent, h->arrivals, h->mom, h->bmin, h->bmax,
-                    h->inode, h->diag};
+                    h->prm, h->leaf, h->child, h->parent, h->arrivals, h->sums, h->bmin, h->bmax,
+                    h->inode, h->root, h->totals, h->diag};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    for (auto &e : h->ev)
+        if (e) cudaEventDestroy(e);
     delete h;
     return GB_OK;
 }
@@ -688,10 +773,12 @@ extern "C" int gb_bh_create(gb_bh_t **out, int64_t n_max, int key_bits) {
     A((void **)&h->child, sizeof(int2) * ni);
     A((void **)&h->parent, sizeof(int) * nodes);
     A((void **)&h->arrivals, sizeof(unsigned) * ni);
-    A((void **)&h->mom, sizeof(Mom4) * ni);
+    A((void **)&h->sums, sizeof(float4) * ni);
     A((void **)&h->bmin, sizeof(float4) * ni);
     A((void **)&h->bmax, sizeof(float4) * ni);
-    A((void **)&h->inode, sizeof(float4) * 2 * ni);
+    A((void **)&h->inode, sizeof(float4) * 3 * ni);
+    A((void **)&h->root, sizeof(float4) * 2);
+    A((void **)&h->totals, sizeof(uint32_t) * RS_BINS);
     A((void **)&h->diag, sizeof(unsigned long long) * DIAG_COUNT);
     if (!ok) {
         gb_bh_destroy(h);
@@ -708,7 +795,8 @@ extern "C" int gb_bh_create(gb_bh_t **out, int64_t n_max, int key_bits) {
 
 template <typename KeyT, int BITS>
 static int build_impl(gb_bh_t *h, float4 *xm, float4 *vel, const float4 *acc, int64_t n, float dt, bool kdk,
-                      cudaStream_t s) {
+                      cudaStream_t s, int slot) {
+    mark(h, slot, 0, s);
     const int nblk = std::max(1, std::min(h->bbox_blocks, (int)((n + BBOX_THREADS - 1) / BBOX_THREADS)));
     if (kdk)
         bh_bbox_kernel<true><<<nblk, BBOX_THREADS, 0, s>>>(xm, vel, acc, n, 0.5f * dt, dt, h->bbox_part, h->ticket,
@@ -720,33 +808,46 @@ static int build_impl(gb_bh_t *h, float4 *xm, float4 *vel, const float4 *acc, in
     KeyT *k0 = (KeyT *)h->keys[0], *k1 = (KeyT *)h->keys[1];
     uint32_t *v0 = h->vals[0], *v1 = h->vals[1];
     bh_morton_kernel<KeyT, BITS><<<g256, 256, 0, s>>>(xm, n, h->prm, k0, v0);
+    mark(h, slot, 1, s);
     const int nb = (int)((n + RS_TILE - 1) / RS_TILE);
     const int passes = (3 * BITS + 7) / 8;
     for (int p = 0; p < passes; ++p) {
         rs_upsweep_kernel<KeyT><<<nb, RS_THREADS, 0, s>>>(k0, n, 8 * p, h->hist, nb);
-        rs_scan_kernel<<<1, 1024, 0, s>>>(h->hist, (int64_t)RS_BINS * nb);
-        rs_downsweep_kernel<KeyT><<<nb, RS_THREADS, 0, s>>>(k0, v0, k1, v1, n, 8 * p, h->hist, nb, h->diag);
+        rs_rowscan_kernel<<<RS_BINS, RS_THREADS, 0, s>>>(h->hist, nb, h->totals);
+        rs_downsweep_kernel<KeyT><<<nb, RS_THREADS, 0, s>>>(k0, v0, k1, v1, n, 8 * p, h->hist, nb, h->totals,
+                                                            h->diag);
         std::swap(k0, k1);
         std::swap(v0, v1);
     }
     h->cur = (k0 == (KeyT *)h->keys[0]) ? 0 : 1;
+    mark(h, slot, 2, s);
     bh_gather_kernel<<<g256, 256, 0, s>>>(xm, v0, n, h->leaf, h->diag);
     const int ni = (int)std::max<int64_t>(n - 1, 1);
     bh_karras_kernel<KeyT><<<(ni + 255) / 256, 256, 0, s>>>(k0, (int)n, h->child, h->parent);
+    mark(h, slot, 3, s);
     if (n >= 2) {
         GB_CUDA_TRY(cudaMemsetAsync(h->arrivals, 0, sizeof(unsigned) * (n - 1), s));
-        bh_bottomup_kernel<<<g256, 256, 0, s>>>(h->leaf, h->child, h->parent, (int)n, h->arrivals, h->mom, h->bmin,
-                                                h->bmax, h->inode, h->diag);
+        bh_bottomup_kernel<<<g256, 256, 0, s>>>(h->leaf, h->child, h->parent, (int)n, h->arrivals, h->sums, h->bmin,
+                                                h->bmax, h->inode, h->root, h->diag);
     }
     GB_CUDA_TRY(cudaGetLastError());
+    mark(h, slot, 4, s);
+    h->launches += 6 + 3 * passes - (n >= 2 ? 0 : 1);
     h->n = n;
     return GB_OK;
 }
 
+static int next_slot(gb_bh_t *h) {
+    if (!h->timing) return 0;
+    const int slot = h->ev_used % GB_BH_TIMING_STEPS;
+    ++h->ev_used;
+    return slot;
+}
+
 static int build_any(gb_bh_t *h, float4 *xm, float4 *vel, const float4 *acc, int64_t n, float dt, bool kdk,
-                     cudaStream_t s) {
-    if (h->key_bits == 10) return build_impl<uint32_t, 10>(h, xm, vel, acc, n, dt, kdk, s);
-    return build_impl<uint64_t, 21>(h, xm, vel, acc, n, dt, kdk, s);
+                     cudaStream_t s, int slot) {
+    if (h->key_bits == 10) return build_impl<uint32_t, 10>(h, xm, vel, acc, n, dt, kdk, s, slot);
+    return build_impl<uint64_t, 21>(h, xm, vel, acc, n, dt, kdk, s, slot);
 }
 
 static int check_bh(gb_bh_t *h, int64_t n) {
@@ -762,12 +863,13 @@ static int check_ptr(const void *p, const char *name) {
 }
 
 static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float theta, float eps2, float G, float dt, int max_stack,
-                    int flags, bool kdk, cudaStream_t s) {
+                    int flags, bool kdk, cudaStream_t s, int slot) {
     const int64_t n = h->n;
     if (n <= 0) return GB_OK;
     TravArgs a;
     a.leaf = h->leaf;
     a.inode = h->inode;
+    a.root = h->root;
     a.order = h->vals[h->cur];
     a.acc = acc;
     a.vel = vel;
@@ -781,9 +883,17 @@ static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float theta, float eps
     a.diag = h->diag;
     const int64_t warps = (n + 31) / 32;
     const unsigned grid = (unsigned)((warps + TRAV_WARPS - 1) / TRAV_WARPS);
-    if (kdk) bh_traverse_kernel<true><<<grid, TRAV_WARPS * 32, 0, s>>>(a);
-    else bh_traverse_kernel<false><<<grid, TRAV_WARPS * 32, 0, s>>>(a);
+    const bool count = (flags & GB_COUNT_WORK) != 0;
+    if (kdk) {
+        if (count) bh_traverse_kernel<true, true><<<grid, TRAV_WARPS * 32, 0, s>>>(a);
+        else bh_traverse_kernel<true, false><<<grid, TRAV_WARPS * 32, 0, s>>>(a);
+    } else {
+        if (count) bh_traverse_kernel<false, true><<<grid, TRAV_WARPS * 32, 0, s>>>(a);
+        else bh_traverse_kernel<false, false><<<grid, TRAV_WARPS * 32, 0, s>>>(a);
+    }
     GB_CUDA_TRY(cudaGetLastError());
+    mark(h, slot, 5, s);
+    h->launches += 1;
     return GB_OK;
 }
 
@@ -801,7 +911,8 @@ extern "C" int gb_bh_build(gb_bh_t *h, const float *xm, int64_t n, void *stream)
         return GB_OK;
     }
     GB_TRY(check_ptr(xm, "xm"));
-    return build_any(h, (float4 *)xm, nullptr, nullptr, n, 0.f, false, (cudaStream_t)stream);
+    h->pending_slot = next_slot(h);
+    return build_any(h, (float4 *)xm, nullptr, nullptr, n, 0.f, false, (cudaStream_t)stream, h->pending_slot);
 }
 
 extern "C" int gb_bh_accel(gb_bh_t *h, float *acc, float theta, float eps2, float G, int max_stack, int flags,
@@ -811,7 +922,8 @@ extern "C" int gb_bh_accel(gb_bh_t *h, float *acc, float theta, float eps2, floa
     if (h->n == 0) return GB_OK;
     GB_TRY(check_ptr(acc, "acc"));
     GB_TRY(check_params(theta, eps2, max_stack));
-    return traverse(h, (float4 *)acc, nullptr, theta, eps2, G, 0.f, max_stack, flags, false, (cudaStream_t)stream);
+    return traverse(h, (float4 *)acc, nullptr, theta, eps2, G, 0.f, max_stack, flags, false, (cudaStream_t)stream,
+                    h->pending_slot);
 }
 
 extern "C" int gb_bh_compute(gb_bh_t *h, const float *xm, float *acc, int64_t n, float theta, float eps2, float G,
@@ -836,8 +948,9 @@ extern "C" int gb_bh_kdk(gb_bh_t *h, float *xm, float *vel, float *acc, int64_t 
     GB_TRY(check_params(theta, eps2, max_stack));
     cudaStream_t s = (cudaStream_t)stream;
     for (int64_t k = 0; k < nsteps; ++k) {
-        GB_TRY(build_any(h, (float4 *)xm, (float4 *)vel, (const float4 *)acc, n, dt, true, s));
-        GB_TRY(traverse(h, (float4 *)acc, (float4 *)vel, theta, eps2, G, dt, max_stack, 0, true, s));
+        const int slot = next_slot(h);
+        GB_TRY(build_any(h, (float4 *)xm, (float4 *)vel, (const float4 *)acc, n, dt, true, s, slot));
+        GB_TRY(traverse(h, (float4 *)acc, (float4 *)vel, theta, eps2, G, dt, max_stack, 0, true, s, slot));
     }
     return GB_OK;
 }
@@ -852,23 +965,44 @@ extern "C" int gb_bh_export(gb_bh_t *h, int what, void *dst, void *stream) {
     cudaStream_t s = (cudaStream_t)stream;
     if (h->key_bits == 10)
         bh_export_kernel<uint32_t><<<grid, 256, 0, s>>>(what, n, (const uint32_t *)h->keys[h->cur], h->vals[h->cur],
-                                                        h->child, h->parent, h->leaf, h->mom, h->bmin, h->bmax, dst);
+                                                        h->child, h->parent, h->leaf, h->sums, h->bmin, h->bmax, dst);
     else
         bh_export_kernel<uint64_t><<<grid, 256, 0, s>>>(what, n, (const uint64_t *)h->keys[h->cur], h->vals[h->cur],
-                                                        h->child, h->parent, h->leaf, h->mom, h->bmin, h->bmax, dst);
+                                                        h->child, h->parent, h->leaf, h->sums, h->bmin, h->bmax, dst);
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
 }
 
 extern "C" int gb_bh_diag(gb_bh_t *h, gb_diag_t *out, int reset) {
     if (!h || !out) return fail(GB_EINVAL, "NULL argument");
-    unsigned long long d[DIAG_COUNT];
-    GB_CUDA_TRY(cudaMemcpy(d, h->diag, sizeof(d), cudaMemcpyDeviceToHost));
-    out->stack_drops = d[DIAG_STACK_DROPS];
-    out->stack_overflow = d[DIAG_STACK_OVERFLOW];
-    out->nonfinite = d[DIAG_NONFINITE];
-    out->bad_tree = d[DIAG_BAD_TREE];
-    for (int k = 0; k < 4; ++k) out->reserved[k] = d[4 + k];
-    if (reset) GB_CUDA_TRY(cudaMemset(h->diag, 0, sizeof(d)));
+    return read_diag(h->diag, out, reset);
+}
+
+extern "C" int gb_bh_timing(gb_bh_t *h, int enable) {
+    if (!h) return fail(GB_EINVAL, "handle is NULL");
+    if (enable && !h->ev[0]) {
+        for (auto &e : h->ev) GB_CUDA_TRY(cudaEventCreate(&e));
+    }
+    h->timing = enable ? 1 : 0;
+    h->ev_used = 0;
     return GB_OK;
 }
+
+extern "C" int gb_bh_stage_times(gb_bh_t *h, float *ms, int *steps) {
+    if (!h || !ms || !steps) return fail(GB_EINVAL, "NULL argument");
+    for (int k = 0; k < GB_BH_STAGES; ++k) ms[k] = 0.f;
+    const int used = std::min(h->ev_used, GB_BH_TIMING_STEPS);
+    GB_CUDA_TRY(cudaDeviceSynchronize());
+    for (int st = 0; st < used; ++st)
+        for (int k = 0; k < GB_BH_STAGES; ++k) {
+            float t = 0.f;
+            GB_CUDA_TRY(cudaEventElapsedTime(&t, h->ev[st * (GB_BH_STAGES + 1) + k],
+                                             h->ev[st * (GB_BH_STAGES + 1) + k + 1]));
+            ms[k] += t;
+        }
+    *steps = used;
+    h->ev_used = 0;
+    return GB_OK;
+}
+
+extern "C" uint64_t gb_bh_launch_count(gb_bh_t *h) { return h ? h->launches : 0; }

@@ -35,11 +35,18 @@ enum DiagIndex {
     DIAG_STACK_DROPS = 0,     // pushes skipped by the max_stack rule
     DIAG_STACK_OVERFLOW = 1,  // warp stack capacity hit (never expected)
     DIAG_NONFINITE = 2,       // non-finite key-quantisation inputs
-    DIAG_BAD_TREE = 3,        // bottom-up pass found an inconsistent node
+    DIAG_BAD_TREE = 3,        // inconsistent index met (never for a valid tree)
+    DIAG_NODE_READS = 4,      // traversal work counters (see gb_diag_t)
+    DIAG_ROOT_READS = 5,
+    DIAG_INTERACTIONS = 6,
+    DIAG_TESTS = 7,
     DIAG_COUNT = 8
 };
 
 int num_sms();
+
+// Copies the device counters into the C-ABI struct (synchronising).
+int read_diag(unsigned long long *dev, gb_diag_t *out, int reset);
 
 // ------------------------------------------------------- packed FP32 pairs
 // Blackwell executes two FP32 operations per lane per instruction with the

@@ -55,8 +55,9 @@ __device__ __forceinline__ float4 load_particle(const DirectArgs &a, int64_t i) 
 }
 
 // Force kernel for MODE_ACC / MODE_KDK.  NP packed target pairs per lane.
+// One packed pair per lane (NP = 1) fits 64 registers: 32 resident warps/SM.
 template <int NP, int WARPS, int MODE, bool KAHAN>
-__global__ void __launch_bounds__(WARPS * 32)
+__global__ void __launch_bounds__(WARPS * 32, NP == 1 ? 1024 / (WARPS * 32) : 1)
 direct_force_kernel(DirectArgs a) {
     constexpr int K = 2 * NP;
     constexpr int TILE = 32 * K;
@@ -443,6 +444,7 @@ struct gb_direct {
     double2 *epart;              // energy block partials
     int epart_cap;
     unsigned long long *diag;
+    uint64_t launches;  // kernels launched by this handle (host count)
 };
 
 static int64_t grid_ctas(gb_direct_t *h, int np, int warps) {
@@ -593,6 +595,7 @@ static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, f
     else direct_fixup_kernel<MODE_PHI><<<fg, fb, 0, s>>>(f);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(GB_ECUDA, "fix-up launch: %s", cudaGetErrorString(e));
+    h->launches += 2;
     return GB_OK;
 }
 
@@ -651,6 +654,7 @@ extern "C" int gb_energy(gb_direct_t *h, const float *xm, const float *vel, int6
     energy_partial_kernel<<<nb, 256, 0, s>>>((const float4 *)xm, (const float4 *)vel, h->phi, n, h->epart);
     energy_final_kernel<<<1, 32, 0, s>>>(h->epart, nb, (double)G, out3);
     GB_CUDA_TRY(cudaGetLastError());
+    h->launches += 2;
     return GB_OK;
 }
 
@@ -669,13 +673,7 @@ extern "C" int gb_direct_acc_fp64(const float *xm, int64_t n, const int64_t *tar
 
 extern "C" int gb_direct_diag(gb_direct_t *h, gb_diag_t *out, int reset) {
     if (!h || !out) return fail(GB_EINVAL, "NULL argument");
-    unsigned long long d[DIAG_COUNT];
-    GB_CUDA_TRY(cudaMemcpy(d, h->diag, sizeof(d), cudaMemcpyDeviceToHost));
-    out->stack_drops = d[DIAG_STACK_DROPS];
-    out->stack_overflow = d[DIAG_STACK_OVERFLOW];
-    out->nonfinite = d[DIAG_NONFINITE];
-    out->bad_tree = d[DIAG_BAD_TREE];
-    for (int k = 0; k < 4; ++k) out->reserved[k] = d[4 + k];
-    if (reset) GB_CUDA_TRY(cudaMemset(h->diag, 0, sizeof(d)));
-    return GB_OK;
+    return read_diag(h->diag, out, reset);
 }
+
+extern "C" uint64_t gb_direct_launch_count(gb_direct_t *h) { return h ? h->launches : 0; }

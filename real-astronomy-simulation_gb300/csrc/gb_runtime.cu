@@ -30,6 +30,21 @@ int num_sms() {
     return sms > 0 ? sms : 1;
 }
 
+int read_diag(unsigned long long *dev, gb_diag_t *out, int reset) {
+    unsigned long long d[DIAG_COUNT];
+    GB_CUDA_TRY(cudaMemcpy(d, dev, sizeof(d), cudaMemcpyDeviceToHost));
+    out->stack_drops = d[DIAG_STACK_DROPS];
+    out->stack_overflow = d[DIAG_STACK_OVERFLOW];
+    out->nonfinite = d[DIAG_NONFINITE];
+    out->bad_tree = d[DIAG_BAD_TREE];
+    out->warp_node_reads = d[DIAG_NODE_READS];
+    out->warp_root_reads = d[DIAG_ROOT_READS];
+    out->lane_interactions = d[DIAG_INTERACTIONS];
+    out->lane_tests = d[DIAG_TESTS];
+    if (reset) GB_CUDA_TRY(cudaMemset(dev, 0, sizeof(d)));
+    return GB_OK;
+}
+
 }  // namespace gb
 
 extern "C" const char *gb_last_error_string(void) { return gb::g_err; }

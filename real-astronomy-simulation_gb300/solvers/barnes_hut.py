@@ -72,13 +72,15 @@ class BarnesHut:
                   stream_handle(self.device))
         return acc
 
-    def compute(self, xm: torch.Tensor, acc: torch.Tensor, accumulate: bool = False) -> torch.Tensor:
+    def compute(self, xm: torch.Tensor, acc: torch.Tensor, accumulate: bool = False,
+                count_work: bool = False) -> torch.Tensor:
         """acc <- tree accelerations of the particles in xm
-        (core/solvers/barnes_hut.py:242-259)."""
+        (core/solvers/barnes_hut.py:242-259).  count_work adds the traversal
+        work counters to diag() (a slightly slower kernel variant)."""
         self._last_n = self._n(xm)
+        flags = (_lib.GB_ACCUMULATE if accumulate else 0) | (_lib.GB_COUNT_WORK if count_work else 0)
         _lib.call("gb_bh_compute", self._h, ptr(xm, "xm"), ptr(acc, "acc"), self._last_n,
-                  self.theta, self.eps2, self.G, self.max_stack,
-                  _lib.GB_ACCUMULATE if accumulate else 0, stream_handle(self.device))
+                  self.theta, self.eps2, self.G, self.max_stack, flags, stream_handle(self.device))
         return acc
 
     def kdk(self, xm, vel, acc, dt: float, nsteps: int = 1) -> None:
@@ -101,6 +103,23 @@ class BarnesHut:
 
     def tree_arrays(self) -> dict:
         return {k: self.export(k) for k in EXPORTS}
+
+    # -- measurement hooks
+    STAGES = ("keys", "sort", "build", "summaries", "traverse")
+
+    def timing(self, enable: bool = True) -> None:
+        """Record CUDA events at stage boundaries of every build/step."""
+        _lib.call("gb_bh_timing", self._h, 1 if enable else 0)
+
+    def stage_times(self) -> tuple[dict, int]:
+        """(summed ms per stage, steps) since the last call (synchronises)."""
+        ms = (ctypes.c_float * len(self.STAGES))()
+        steps = ctypes.c_int()
+        _lib.call("gb_bh_stage_times", self._h, ms, ctypes.byref(steps))
+        return {k: float(ms[i]) for i, k in enumerate(self.STAGES)}, int(steps.value)
+
+    def launch_count(self) -> int:
+        return int(_lib.load().gb_bh_launch_count(self._h))
 
     def diag(self, reset: bool = False) -> dict:
         d = _lib.Diag()

@@ -87,6 +87,9 @@ class DirectGravity:
         e = self.energies_async(xm, vel, G, eps2).cpu().numpy()
         return float(e[0]), float(e[1]), float(e[2])
 
+    def launch_count(self) -> int:
+        return int(_lib.load().gb_direct_launch_count(self._h))
+
     def diag(self, reset=False) -> dict:
         d = _lib.Diag()
         _lib.call("gb_direct_diag", self._h, ctypes.byref(d), 1 if reset else 0)

@@ -1,8 +1,9 @@
 """LBVH Barnes-Hut CUDA path against the reference fixtures and the oracle.
 
 Bit-exact: Morton keys, sort permutation, Karras topology (left, right,
-parent), node AABBs.  FP64 node masses / centres: relative 1e-12 (summation
-order differs from the reference's atomics).  Accelerations: the device
+parent), node AABBs.  Node masses and centres of mass are FP32 on the device
+(the reference sums in FP64): masses within 5e-6 relative, centres within
+1e-5 of the system size.  Accelerations: the device
 traversal is FP32, so per-particle relative differences from the FP64
 traversal are ~1e-6; a node whose acceptance test sits on the FP32/FP64
 rounding boundary can flip, which moves that particle by about one node's
@@ -75,8 +76,9 @@ def test_golden_tree_bit_exact(cuda_dev, bits):
     np.testing.assert_array_equal(t["parent"], g[pre + "parent"])
     np.testing.assert_array_equal(t["nmin"], g[pre + "nmin"])
     np.testing.assert_array_equal(t["nmax"], g[pre + "nmax"])
-    np.testing.assert_allclose(t["nmass"], g[pre + "nmass"], rtol=1e-12)
-    np.testing.assert_allclose(t["com"], g[pre + "com"], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(t["nmass"], g[pre + "nmass"], rtol=5e-6)
+    scale = np.abs(g["pos"]).max()
+    np.testing.assert_allclose(t["com"], g[pre + "com"], rtol=0, atol=1e-5 * scale)
     _check_acc(a, g[pre + "acc"])
     assert b.diag()["stack_drops"] == 0
 
@@ -159,7 +161,8 @@ def test_config2_disk_1m(cuda_dev, orc, bits):
     com, nmass, nmin, nmax = orc.summaries(order, pos, mass, parent)
     np.testing.assert_array_equal(t["nmin"], nmin)
     np.testing.assert_array_equal(t["nmax"], nmax)
-    np.testing.assert_allclose(t["nmass"], nmass, rtol=1e-12)
+    np.testing.assert_allclose(t["nmass"], nmass, rtol=5e-6)
+    np.testing.assert_allclose(t["com"], com, rtol=0, atol=1e-5 * np.abs(pos).max())
     ref_bh, _ = orc.traverse(pos, order, com, nmass, nmin, nmax, left, right, 0.5, 0.0025, b.G,
                              targets=targets)
     _check_acc(a[targets], ref_bh)
