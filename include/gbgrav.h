@@ -71,6 +71,10 @@ int gb_direct_destroy(gb_direct_t *h);
  * SM (0 = occupancy maximum).  Chosen by the autotuner. */
 int gb_direct_set_tiles(gb_direct_t *h, int k, int warps, int ctas_per_sm);
 
+/* Inner-loop form: 0 = scalar FP32 (default), 1 = packed .f32x2 FP32.  Same
+ * results up to FP32 rounding order; chosen by the autotuner. */
+int gb_direct_set_variant(gb_direct_t *h, int packed);
+
 /* acc_i = G sum_j m_j (x_j - x_i) / (|x_j - x_i|^2 + eps2)^{3/2}, all j
  * (i == j adds zero).  Replaces compute_acc_direct
  * (core/solvers/gravity.py:13-26); the GB_ACCUMULATE flag gives the

@@ -403,7 +403,8 @@ __device__ __forceinline__ unsigned arrive(unsigned *p) {
 // Summarises every internal node k once both children are done and writes
 // the traversal record of its two children:
 //   inode[3k] = left {com, m}, inode[3k+1] = right {com, m},
-//   inode[3k+2] = {size2 left, size2 right, left id, right id} (ids as bits).
+//   inode[3k+2] = {size2 left, size2 right, left id, right id} (ids as bits;
+//   size2 = -1 marks a leaf child).
 __global__ void bh_bottomup_kernel(const float4 *__restrict__ leaf, const int2 *__restrict__ child,
                                    const int *__restrict__ parent, int n, unsigned *__restrict__ arrivals,
                                    float4 *__restrict__ sums, float4 *__restrict__ bmin, float4 *__restrict__ bmax,
@@ -437,7 +438,8 @@ __global__ void bh_bottomup_kernel(const float4 *__restrict__ leaf, const int2 *
         bmax[k] = make_float4(s.hx, s.hy, s.hz, 0.f);
         inode[3 * k] = trav_com(a);
         inode[3 * k + 1] = trav_com(b);
-        inode[3 * k + 2] = make_float4(size2_of(a), size2_of(b), __int_as_float(c.x), __int_as_float(c.y));
+        inode[3 * k + 2] = make_float4(c.x < n ? -1.f : size2_of(a), c.y < n ? -1.f : size2_of(b),
+                                       __int_as_float(c.x), __int_as_float(c.y));
         const int up = __ldg(parent + node);
         if (up < 0) {
             root[0] = trav_com(s);
@@ -467,32 +469,38 @@ struct Lane {
     unsigned n_int, n_test, drops;
 };
 
-// One child for one lane of the expanding mask (branch-free): a leaf adds
-// its monopole unless it is the lane's own particle; an internal node adds
-// its monopole when size^2 < theta^2 (|d|^2 + eps^2), else it is opened if
-// the reference's stack (depth sp once the child is popped) has room for two
-// pushes, else the push is dropped and counted.  Returns "open".
+// One child for one lane of the expanding mask (branch-free).  Leaves carry
+// size2 = -1 in the record, so the one comparison size2 < theta^2 (|d|^2 +
+// eps^2) accepts every leaf and applies the reference's test (:208) to
+// internal nodes; the self test id != s is true for every internal id (ids
+// >= n > s).  An accepted child adds its monopole unless it is the lane's own
+// particle; a rejected (internal) child is opened.  Returns "open".
 template <bool COUNT>
 __device__ __forceinline__ bool visit_child(Lane &L, const TravArgs &a, float4 q, float size2, int id, int s,
-                                            int sp, bool in) {
+                                            bool in) {
     const float dx = q.x - L.px, dy = q.y - L.py, dz = q.z - L.pz;
     const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, a.eps2)));
-    const bool is_leaf = id < a.n;
-    const bool accept = is_leaf ? (id != s) : (size2 < a.theta2 * r2);
-    const bool add = in && accept;
+    const bool accept = size2 < a.theta2 * r2;
+    const bool add = in && accept && id != s;
     const float inv = rsqrt_approx(r2);
     const float sc = add ? q.w * inv * inv * inv : 0.f;
     L.ax = __fmaf_rn(sc, dx, L.ax);
     L.ay = __fmaf_rn(sc, dy, L.ay);
     L.az = __fmaf_rn(sc, dz, L.az);
-    const bool open = in && !is_leaf && !accept;
-    const bool room = sp + 2 <= a.max_stack;
     if (COUNT) {
         L.n_int += add ? 1u : 0u;
-        L.n_test += (in && !is_leaf) ? 1u : 0u;
+        L.n_test += (in && size2 >= 0.f) ? 1u : 0u;
     }
-    L.drops += (open && !room) ? 1u : 0u;
-    return open && room;
+    return in && !accept;
+}
+
+// The reference's push rule (:212): a lane that opens a node popped at stack
+// depth sp pushes its children only if sp + 2 <= max_stack.  sp is uniform
+// over the warp, so the (rare) drop path is a uniform branch.
+__device__ __forceinline__ bool apply_room(Lane &L, bool open, int sp, int max_stack) {
+    if (sp + 2 <= max_stack) return open;
+    L.drops += open ? 1u : 0u;
+    return false;
 }
 
 // Warp-coherent traversal: 32 key-consecutive targets per warp walk the tree
@@ -529,7 +537,7 @@ bh_traverse_kernel(TravArgs a) {
     if (n >= 2) {
         // The root is popped first, with an empty stack (sp = 0).
         const float4 R0 = __ldg(a.root), R1 = __ldg(a.root + 1);
-        const bool want = visit_child<COUNT>(L, a, R0, R1.x, n, s, 0, valid);
+        const bool want = apply_room(L, visit_child<COUNT>(L, a, R0, R1.x, n, s, valid), 0, a.max_stack);
         m = __ballot_sync(0xffffffffu, want);
     }
     while (m) {
@@ -542,8 +550,10 @@ bh_traverse_kernel(TravArgs a) {
             const float4 QR = __ldg(a.inode + 3 * k + 1);
             const float4 C = __ldg(a.inode + 3 * k + 2);
             if (COUNT) ++iters;
-            const bool wantR = visit_child<COUNT>(L, a, QR, C.y, __float_as_int(C.w), s, sp + 1, in);
-            const bool wantL = visit_child<COUNT>(L, a, QL, C.x, __float_as_int(C.z), s, sp, in);
+            const bool wantR = apply_room(L, visit_child<COUNT>(L, a, QR, C.y, __float_as_int(C.w), s, in),
+                                          sp + 1, a.max_stack);
+            const bool wantL = apply_room(L, visit_child<COUNT>(L, a, QL, C.x, __float_as_int(C.z), s, in), sp,
+                                          a.max_stack);
             const unsigned omL = __ballot_sync(0xffffffffu, wantL);
             const unsigned omR = __ballot_sync(0xffffffffu, wantR);
             if (omL) {

@@ -55,7 +55,11 @@ __device__ __forceinline__ float4 load_particle(const DirectArgs &a, int64_t i) 
 }
 
 // Force kernel for MODE_ACC / MODE_KDK.  NP packed target pairs per lane.
-// One packed pair per lane (NP = 1) fits 64 registers: 32 resident warps/SM.
+// The inner loop takes two sources per iteration into two accumulator sets
+// (independent dependency chains for the scheduler); the Kahan running sums
+// live in shared memory between source chunks, which keeps registers for
+// the interleave.  One pair per lane (NP = 1) fits 64 registers: 32
+// resident warps/SM.
 template <int NP, int WARPS, int MODE, bool KAHAN>
 __global__ void __launch_bounds__(WARPS * 32, NP == 1 ? 1024 / (WARPS * 32) : 1)
 direct_force_kernel(DirectArgs a) {
@@ -63,10 +67,13 @@ direct_force_kernel(DirectArgs a) {
     constexpr int TILE = 32 * K;
     constexpr int ST = WARPS * TILE;
     constexpr int JU = WARPS * 32;
+    constexpr int T = WARPS * 32;
     __shared__ ulonglong2 src[2 * JU];
+    __shared__ f2 kah[6 * NP][T];  // per thread: S{x,y,z}, C{x,y,z} per pair
 
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
+    const int tid = threadIdx.x;
     const int64_t c = blockIdx.x;
     const int64_t u_begin = unit_begin(a.U, a.P, c);
     const int64_t u_end = unit_begin(a.U, a.P, c + 1);
@@ -89,9 +96,8 @@ direct_force_kernel(DirectArgs a) {
             Y[p] = pack2(t0.y, t1.y);
             Z[p] = pack2(t0.z, t1.z);
         }
-        f2 SX[NP], SY[NP], SZ[NP], CX[NP], CY[NP], CZ[NP];
 #pragma unroll
-        for (int p = 0; p < NP; ++p) SX[p] = SY[p] = SZ[p] = CX[p] = CY[p] = CZ[p] = 0ull;
+        for (int v = 0; v < 6 * NP; ++v) kah[v][tid] = 0ull;
 
         for (; u < run_end; ++u) {
             const int64_t ju = u - st * a.num_ju;
@@ -101,40 +107,54 @@ direct_force_kernel(DirectArgs a) {
             src[2 * threadIdx.x + 1] = make_ulonglong2(pack2(s4.z, s4.z), pack2(s4.w, s4.w));
             __syncthreads();
 
-            f2 AX[NP], AY[NP], AZ[NP];
+            f2 AX[2][NP], AY[2][NP], AZ[2][NP];
 #pragma unroll
-            for (int p = 0; p < NP; ++p) AX[p] = AY[p] = AZ[p] = 0ull;
-#pragma unroll 4
-            for (int jj = 0; jj < JU; ++jj) {
-                const ulonglong2 A = src[2 * jj];
-                const ulonglong2 B = src[2 * jj + 1];
+            for (int p = 0; p < NP; ++p) AX[0][p] = AY[0][p] = AZ[0][p] = AX[1][p] = AY[1][p] = AZ[1][p] = 0ull;
+#pragma unroll 2
+            for (int jj = 0; jj < JU; jj += 2) {
 #pragma unroll
-                for (int p = 0; p < NP; ++p) {
-                    const f2 dx = sub2(A.x, X[p]);
-                    const f2 dy = sub2(A.y, Y[p]);
-                    const f2 dz = sub2(B.x, Z[p]);
-                    f2 r2 = fma2(dx, dx, E2);
-                    r2 = fma2(dy, dy, r2);
-                    r2 = fma2(dz, dz, r2);
-                    const f2 inv = rsqrt2(r2);
-                    const f2 inv2 = mul2(inv, inv);
-                    const f2 s = mul2(mul2(B.y, inv), inv2);
-                    AX[p] = fma2(s, dx, AX[p]);
-                    AY[p] = fma2(s, dy, AY[p]);
-                    AZ[p] = fma2(s, dz, AZ[p]);
+                for (int h = 0; h < 2; ++h) {
+                    const ulonglong2 A = src[2 * (jj + h)];
+                    const ulonglong2 B = src[2 * (jj + h) + 1];
+#pragma unroll
+                    for (int p = 0; p < NP; ++p) {
+                        const f2 dx = sub2(A.x, X[p]);
+                        const f2 dy = sub2(A.y, Y[p]);
+                        const f2 dz = sub2(B.x, Z[p]);
+                        f2 r2 = fma2(dx, dx, E2);
+                        r2 = fma2(dy, dy, r2);
+                        r2 = fma2(dz, dz, r2);
+                        const f2 inv = rsqrt2(r2);
+                        const f2 inv2 = mul2(inv, inv);
+                        const f2 sc = mul2(mul2(B.y, inv), inv2);
+                        AX[h][p] = fma2(sc, dx, AX[h][p]);
+                        AY[h][p] = fma2(sc, dy, AY[h][p]);
+                        AZ[h][p] = fma2(sc, dz, AZ[h][p]);
+                    }
                 }
             }
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
+                const f2 ax = add2(AX[0][p], AX[1][p]);
+                const f2 ay = add2(AY[0][p], AY[1][p]);
+                const f2 az = add2(AZ[0][p], AZ[1][p]);
+                f2 sx = kah[6 * p][tid], sy = kah[6 * p + 1][tid], sz = kah[6 * p + 2][tid];
                 if (KAHAN) {
-                    kahan_add2(SX[p], CX[p], AX[p]);
-                    kahan_add2(SY[p], CY[p], AY[p]);
-                    kahan_add2(SZ[p], CZ[p], AZ[p]);
+                    f2 cx = kah[6 * p + 3][tid], cy = kah[6 * p + 4][tid], cz = kah[6 * p + 5][tid];
+                    kahan_add2(sx, cx, ax);
+                    kahan_add2(sy, cy, ay);
+                    kahan_add2(sz, cz, az);
+                    kah[6 * p + 3][tid] = cx;
+                    kah[6 * p + 4][tid] = cy;
+                    kah[6 * p + 5][tid] = cz;
                 } else {
-                    SX[p] = add2(SX[p], AX[p]);
-                    SY[p] = add2(SY[p], AY[p]);
-                    SZ[p] = add2(SZ[p], AZ[p]);
+                    sx = add2(sx, ax);
+                    sy = add2(sy, ay);
+                    sz = add2(sz, az);
                 }
+                kah[6 * p][tid] = sx;
+                kah[6 * p + 1][tid] = sy;
+                kah[6 * p + 2][tid] = sz;
             }
         }
         // Flush the compensated partial: estimate = hi + lo with lo = -c.
@@ -142,17 +162,93 @@ direct_force_kernel(DirectArgs a) {
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
             float hx0, hx1, hy0, hy1, hz0, hz1, cx0, cx1, cy0, cy1, cz0, cz1;
-            unpack2(SX[p], hx0, hx1);
-            unpack2(SY[p], hy0, hy1);
-            unpack2(SZ[p], hz0, hz1);
-            unpack2(CX[p], cx0, cx1);
-            unpack2(CY[p], cy0, cy1);
-            unpack2(CZ[p], cz0, cz1);
+            unpack2(kah[6 * p][tid], hx0, hx1);
+            unpack2(kah[6 * p + 1][tid], hy0, hy1);
+            unpack2(kah[6 * p + 2][tid], hz0, hz1);
+            unpack2(kah[6 * p + 3][tid], cx0, cx1);
+            unpack2(kah[6 * p + 4][tid], cy0, cy1);
+            unpack2(kah[6 * p + 5][tid], cz0, cz1);
             const int64_t s0 = slot + (2 * p) * 32, s1 = s0 + 32;
             a.part[2 * s0] = make_float4(hx0, hy0, hz0, 0.f);
             a.part[2 * s0 + 1] = make_float4(-cx0, -cy0, -cz0, 0.f);
             a.part[2 * s1] = make_float4(hx1, hy1, hz1, 0.f);
             a.part[2 * s1 + 1] = make_float4(-cx1, -cy1, -cz1, 0.f);
+        }
+    }
+}
+
+// Scalar variant of the force kernel (same decomposition and Kahan
+// scheme): K = 2 * NP targets per lane in plain FP32 registers, one source
+// broadcast per shared-memory load.  Selected with gb_direct_set_variant.
+template <int NP, int WARPS, int MODE, bool KAHAN>
+__global__ void __launch_bounds__(WARPS * 32, NP == 1 ? 1024 / (WARPS * 32) : 1)
+direct_force_scalar_kernel(DirectArgs a) {
+    constexpr int K = 2 * NP;
+    constexpr int TILE = 32 * K;
+    constexpr int ST = WARPS * TILE;
+    constexpr int JU = WARPS * 32;
+    __shared__ float4 src[JU];
+
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int64_t c = blockIdx.x;
+    const int64_t u_begin = unit_begin(a.U, a.P, c);
+    const int64_t u_end = unit_begin(a.U, a.P, c + 1);
+    if (u_begin >= u_end) return;
+    const int64_t st0 = u_begin / a.num_ju;
+
+    int64_t u = u_begin;
+    while (u < u_end) {
+        const int64_t st = u / a.num_ju;
+        const int64_t run_end = min(u_end, (st + 1) * a.num_ju);
+        const int64_t tbase = st * ST + wib * TILE + lane;
+        float X[K], Y[K], Z[K], SX[K], SY[K], SZ[K], CX[K], CY[K], CZ[K];
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            const float4 t = load_particle<MODE>(a, tbase + q * 32);
+            X[q] = t.x; Y[q] = t.y; Z[q] = t.z;
+            SX[q] = SY[q] = SZ[q] = CX[q] = CY[q] = CZ[q] = 0.f;
+        }
+        for (; u < run_end; ++u) {
+            const int64_t ju = u - st * a.num_ju;
+            const float4 s4 = load_particle<MODE>(a, ju * JU + threadIdx.x);
+            __syncthreads();
+            src[threadIdx.x] = s4;
+            __syncthreads();
+            float AX[K], AY[K], AZ[K];
+#pragma unroll
+            for (int q = 0; q < K; ++q) AX[q] = AY[q] = AZ[q] = 0.f;
+#pragma unroll 4
+            for (int jj = 0; jj < JU; ++jj) {
+                const float4 sj = src[jj];
+#pragma unroll
+                for (int q = 0; q < K; ++q) {
+                    const float dx = sj.x - X[q], dy = sj.y - Y[q], dz = sj.z - Z[q];
+                    const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, a.eps2)));
+                    const float inv = rsqrt_approx(r2);
+                    const float sc = (sj.w * inv) * (inv * inv);
+                    AX[q] = __fmaf_rn(sc, dx, AX[q]);
+                    AY[q] = __fmaf_rn(sc, dy, AY[q]);
+                    AZ[q] = __fmaf_rn(sc, dz, AZ[q]);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < K; ++q) {
+                if (KAHAN) {
+                    kahan_add(SX[q], CX[q], AX[q]);
+                    kahan_add(SY[q], CY[q], AY[q]);
+                    kahan_add(SZ[q], CZ[q], AZ[q]);
+                } else {
+                    SX[q] += AX[q]; SY[q] += AY[q]; SZ[q] += AZ[q];
+                }
+            }
+        }
+        const int64_t slot = (c * a.smax + (st - st0)) * ST + wib * TILE + lane;
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            const int64_t sq = slot + q * 32;
+            a.part[2 * sq] = make_float4(SX[q], SY[q], SZ[q], 0.f);
+            a.part[2 * sq + 1] = make_float4(-CX[q], -CY[q], -CZ[q], 0.f);
         }
     }
 }
@@ -407,8 +503,18 @@ static int64_t plan_partials(const DirectPlan &p) { return 2 * p.P * p.smax * p.
 
 template <int NP, int WARPS>
 static cudaError_t launch_force(int mode, bool kahan, const DirectPlan &pl, const DirectArgs &a,
-                                cudaStream_t s) {
+                                cudaStream_t s, int packed) {
     const dim3 grid((unsigned)pl.P), block(WARPS * 32);
+    if (!packed) {
+        if (mode == MODE_ACC) {
+            if (kahan) direct_force_scalar_kernel<NP, WARPS, MODE_ACC, true><<<grid, block, 0, s>>>(a);
+            else direct_force_scalar_kernel<NP, WARPS, MODE_ACC, false><<<grid, block, 0, s>>>(a);
+        } else {
+            if (kahan) direct_force_scalar_kernel<NP, WARPS, MODE_KDK, true><<<grid, block, 0, s>>>(a);
+            else direct_force_scalar_kernel<NP, WARPS, MODE_KDK, false><<<grid, block, 0, s>>>(a);
+        }
+        return cudaGetLastError();
+    }
     if (mode == MODE_ACC) {
         if (kahan) direct_force_kernel<NP, WARPS, MODE_ACC, true><<<grid, block, 0, s>>>(a);
         else direct_force_kernel<NP, WARPS, MODE_ACC, false><<<grid, block, 0, s>>>(a);
@@ -421,7 +527,13 @@ static cudaError_t launch_force(int mode, bool kahan, const DirectPlan &pl, cons
 
 typedef const void *KernelPtr;
 
-static KernelPtr force_kernel_ptr(int np, int warps) {
+static KernelPtr force_kernel_ptr(int np, int warps, int packed) {
+    if (!packed) {
+        if (np == 1 && warps == 4) return (KernelPtr)direct_force_scalar_kernel<1, 4, MODE_KDK, true>;
+        if (np == 1 && warps == 8) return (KernelPtr)direct_force_scalar_kernel<1, 8, MODE_KDK, true>;
+        if (np == 2 && warps == 4) return (KernelPtr)direct_force_scalar_kernel<2, 4, MODE_KDK, true>;
+        return (KernelPtr)direct_force_scalar_kernel<2, 8, MODE_KDK, true>;
+    }
     if (np == 1 && warps == 4) return (KernelPtr)direct_force_kernel<1, 4, MODE_KDK, true>;
     if (np == 1 && warps == 8) return (KernelPtr)direct_force_kernel<1, 8, MODE_KDK, true>;
     if (np == 2 && warps == 4) return (KernelPtr)direct_force_kernel<2, 4, MODE_KDK, true>;
@@ -438,6 +550,7 @@ struct gb_direct {
     int sms;
     int64_t n_max;
     int np, warps, ctas_per_sm;  // tile shape (ctas_per_sm 0 = occupancy max)
+    int packed;                  // 1: .f32x2 inner loop, 0: scalar FP32
     float4 *part;
     int64_t part_cap;            // float4 elements
     float *phi;                  // n_max floats (energy scratch)
@@ -447,9 +560,9 @@ struct gb_direct {
     uint64_t launches;  // kernels launched by this handle (host count)
 };
 
-static int64_t grid_ctas(gb_direct_t *h, int np, int warps) {
+static int64_t grid_ctas(gb_direct_t *h, int np, int warps, int packed) {
     int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, force_kernel_ptr(np, warps), warps * 32, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, force_kernel_ptr(np, warps, packed), warps * 32, 0);
     if (occ < 1) occ = 1;
     const int per_sm = h->ctas_per_sm > 0 ? std::min(h->ctas_per_sm, occ) : occ;
     return (int64_t)h->sms * per_sm;
@@ -470,13 +583,14 @@ static int ensure_partials(gb_direct_t *h, int64_t need) {
 static int64_t max_partials(gb_direct_t *h, int64_t n) {
     int64_t need = 0;
     const int shapes[4][2] = {{1, 4}, {1, 8}, {2, 4}, {2, 8}};
-    for (auto &s : shapes) {
-        DirectPlan pl;
-        make_plan(n, s[0], s[1], grid_ctas(h, s[0], s[1]), &pl);
-        need = std::max(need, plan_partials(pl));
-        make_plan(n, 1, s[1], grid_ctas(h, s[0], s[1]), &pl);  // phi layout (K=2)
-        need = std::max(need, plan_partials(pl));
-    }
+    for (auto &s : shapes)
+        for (int packed = 0; packed < 2; ++packed) {
+            DirectPlan pl;
+            make_plan(n, s[0], s[1], grid_ctas(h, s[0], s[1], packed), &pl);
+            need = std::max(need, plan_partials(pl));
+            make_plan(n, 1, s[1], grid_ctas(h, s[0], s[1], packed), &pl);  // phi layout (K=2)
+            need = std::max(need, plan_partials(pl));
+        }
     return need;
 }
 
@@ -497,6 +611,7 @@ extern "C" int gb_direct_create(gb_direct_t **out, int64_t n_max) {
     h->np = 2;
     h->warps = 8;
     h->ctas_per_sm = 0;
+    h->packed = 0;
     int st = ensure_partials(h, max_partials(h, n_max));
     if (st == GB_OK && cudaMalloc(&h->phi, sizeof(float) * n_max) != cudaSuccess)
         st = fail(GB_ENOMEM, "phi scratch");
@@ -540,7 +655,7 @@ static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, f
                       int64_t n, float G, float eps2, float dt, int flags, cudaStream_t s) {
     DirectPlan pl;
     const int np = mode == MODE_PHI ? 1 : h->np;
-    make_plan(n, np, h->warps, grid_ctas(h, h->np, h->warps), &pl);
+    make_plan(n, np, h->warps, grid_ctas(h, h->np, h->warps, h->packed), &pl);
     if (plan_partials(pl) > h->part_cap) return fail(GB_EINVAL, "scratch too small for n=%lld", (long long)n);
     DirectArgs a;
     a.xm = xm;
@@ -568,9 +683,11 @@ static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, f
         }
         e = cudaGetLastError();
     } else if (pl.np == 1) {
-        e = pl.warps == 4 ? launch_force<1, 4>(mode, kahan, pl, a, s) : launch_force<1, 8>(mode, kahan, pl, a, s);
+        e = pl.warps == 4 ? launch_force<1, 4>(mode, kahan, pl, a, s, h->packed)
+                          : launch_force<1, 8>(mode, kahan, pl, a, s, h->packed);
     } else {
-        e = pl.warps == 4 ? launch_force<2, 4>(mode, kahan, pl, a, s) : launch_force<2, 8>(mode, kahan, pl, a, s);
+        e = pl.warps == 4 ? launch_force<2, 4>(mode, kahan, pl, a, s, h->packed)
+                          : launch_force<2, 8>(mode, kahan, pl, a, s, h->packed);
     }
     if (e != cudaSuccess) return fail(GB_ECUDA, "force launch: %s", cudaGetErrorString(e));
     FixArgs f;
@@ -674,6 +791,13 @@ extern "C" int gb_direct_acc_fp64(const float *xm, int64_t n, const int64_t *tar
 extern "C" int gb_direct_diag(gb_direct_t *h, gb_diag_t *out, int reset) {
     if (!h || !out) return fail(GB_EINVAL, "NULL argument");
     return read_diag(h->diag, out, reset);
+}
+
+extern "C" int gb_direct_set_variant(gb_direct_t *h, int packed) {
+    if (!h) return fail(GB_EINVAL, "handle is NULL");
+    if (packed != 0 && packed != 1) return fail(GB_EINVAL, "packed must be 0 or 1");
+    h->packed = packed;
+    return GB_OK;
 }
 
 extern "C" uint64_t gb_direct_launch_count(gb_direct_t *h) { return h ? h->launches : 0; }

@@ -51,8 +51,10 @@ class DirectGravity:
     def handle(self):
         return self._h
 
-    def set_tiles(self, k: int, warps: int, ctas_per_sm: int = 0):
+    def set_tiles(self, k: int, warps: int, ctas_per_sm: int = 0, packed: int | None = None):
         _lib.call("gb_direct_set_tiles", self._h, int(k), int(warps), int(ctas_per_sm))
+        if packed is not None:
+            _lib.call("gb_direct_set_variant", self._h, int(packed))
 
     # -- compute
     def acc(self, xm, acc, G, eps2, accumulate=False, plain=False):

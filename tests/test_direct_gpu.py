@@ -56,13 +56,14 @@ def test_golden_direct_acc(cuda_dev):
 
 @pytest.mark.parametrize("k,warps", [(2, 4), (2, 8), (4, 4), (4, 8)])
 @pytest.mark.parametrize("plain", [False, True])
-def test_config1_plummer_20k_all_tiles(cuda_dev, orc, k, warps, plain):
+@pytest.mark.parametrize("packed", [1, 0])
+def test_config1_plummer_20k_all_tiles(cuda_dev, orc, k, warps, plain, packed):
     """N = 20,000 Plummer sphere, G = 1, eps = 0.01 (the direct workload)."""
     _, grav, ic = _mods()
     pos, _, mass = ic.plummer(20000, seed=0)
     pos, mass = _f32(pos), _f32(mass)
     xm = _xm(pos, mass, cuda_dev)
-    a, _ = _acc(grav, xm, 1.0, 1e-4, tiles=(k, warps), plain=plain)
+    a, _ = _acc(grav, xm, 1.0, 1e-4, tiles=(k, warps, 0, packed), plain=plain)
     targets = np.random.default_rng(1).choice(20000, 2048, replace=False)
     ref = orc.direct_acc(pos, mass, 1.0, 1e-4, targets)
     rel = _rel(a[targets], ref)
