@@ -92,9 +92,14 @@ def plummer_pair(n_each: int, separation: float = 10.0, impact: float = 2.0,
                  seeds=(0, 1), G: float = 1.0):
     """Two unit Plummer spheres (a = 1, M = 1) whose centres are `separation`
     apart, approaching on a parabolic orbit (|v_rel| = sqrt(2 G (M1+M2) / d))
-    with impact parameter `impact`, in the centre-of-mass frame."""
+    with impact parameter `impact`, in the centre-of-mass frame.  Each sphere
+    is first moved to its own centre of mass and rest frame."""
     p1, v1, m1 = plummer(n_each, 1.0, 1.0, seeds[0], G)
     p2, v2, m2 = plummer(n_each, 1.0, 1.0, seeds[1], G)
+    p1 = p1 - np.average(p1, axis=0, weights=m1)
+    v1 = v1 - np.average(v1, axis=0, weights=m1)
+    p2 = p2 - np.average(p2, axis=0, weights=m2)
+    v2 = v2 - np.average(v2, axis=0, weights=m2)
     d = float(separation)
     vrel = np.sqrt(2.0 * G * 2.0 / d)
     sinb = impact / d
