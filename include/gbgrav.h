@@ -171,6 +171,26 @@ int gb_bh_timing(gb_bh_t *h, int enable);
 int gb_bh_stage_times(gb_bh_t *h, float *ms, int *steps);
 uint64_t gb_bh_launch_count(gb_bh_t *h);
 
+/* ------------------------------------------------- allocation-free call */
+/* No counterpart in the reference.  gb_direct_acc without a handle and
+ * without any device allocation, for callers that cannot call cudaMalloc:
+ * an application whose memory pool owns the whole GPU, a plug-in running in
+ * another framework's memory arena, or a loop that must never block
+ * (cudaMalloc/cudaFree can synchronise the device).  Same arguments and
+ * result as gb_direct_acc (flags GB_ACCUMULATE, GB_PLAIN_FP32); the caller
+ * still passes xm and acc.  Scratch is a 4 MiB file-scope device array that
+ * every GPU loading the library keeps until the process exits; it holds the
+ * partial sums of systems of at most GB_NOALLOC_MAX_N particles, and larger
+ * n is rejected with GB_EINVAL.  The first call on each device looks up the
+ * array's device address (with that device current); make that first call
+ * before any stream capture.  All calls on a device share the array: calls
+ * whose kernels overlap on the GPU (other streams or host threads) race and
+ * must be ordered by the caller. */
+#define GB_NOALLOC_MAX_N 65536
+#define GB_NOALLOC_MAX_DEVICES 64
+int gb_direct_acc_noalloc(const float *xm, float *acc, int64_t n, float G,
+                          float eps2, int flags, void *stream);
+
 /* ------------------------------------------------------------ calibration */
 /* Launches an FP32 FMA-throughput kernel (packed = 1: .f32x2 form) on
  * `stream`; *flops receives the FLOP count of the launch, which the caller

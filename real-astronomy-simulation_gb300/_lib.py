@@ -68,6 +68,7 @@ SIGNATURES = {
     "gb_direct_diag": (I32, [P, ctypes.POINTER(Diag), I32]),
     "gb_direct_launch_count": (ctypes.c_uint64, [P]),
     "gb_calib_fp32": (I32, [P, I32, I32, ctypes.POINTER(F64), P]),
+    "gb_direct_acc_noalloc": (I32, [P, P, I64, F32, F32, I32, P]),
     "gb_bh_create": (I32, [ctypes.POINTER(P), I64, I32]),
     "gb_bh_destroy": (I32, [P]),
     "gb_bh_build": (I32, [P, P, I64, P]),

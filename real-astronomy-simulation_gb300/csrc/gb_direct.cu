@@ -801,3 +801,92 @@ extern "C" int gb_direct_set_variant(gb_direct_t *h, int packed) {
 }
 
 extern "C" uint64_t gb_direct_launch_count(gb_direct_t *h) { return h ? h->launches : 0; }
+
+// ====================================================== allocation-free call
+// gb_direct_acc_noalloc: the direct force sum for callers that must not
+// allocate device memory (a host that hands its whole GPU memory to its own
+// pool, a plug-in living inside another framework's memory arena, or a loop
+// that must never stall: cudaMalloc and cudaFree can synchronise the device).
+// The stream-K partial sums, which gb_direct_acc keeps in its handle's
+// scratch, live here in one file-scope device array instead.  The launch
+// shape is fixed (256 CTAs of 4 warps, 2 targets per lane, scalar FP32 with
+// Kahan) so that the partials of any n up to GB_NOALLOC_MAX_N fit the array.
+//
+// The array is shared by every call in the process on a given device and
+// keeps whatever the previous call left in it.  Nothing in it has to start
+// at zero: each call writes every partial slot it later reads.  Two calls
+// whose kernels overlap on the GPU (different streams, or different host
+// threads) write the same slots and race; the caller must order them.
+constexpr int NOALLOC_CTAS = 256;
+constexpr int NOALLOC_NP = 1;     // 2 targets per lane
+constexpr int NOALLOC_WARPS = 4;  // supertile of 256 targets
+constexpr int64_t NOALLOC_PART = 2LL * NOALLOC_CTAS * 2 * (NOALLOC_WARPS * 32 * 2 * NOALLOC_NP);  // float4s
+
+static __device__ __align__(256) float4 g_noalloc_part[NOALLOC_PART];
+
+// Device address of g_noalloc_part per device: in host code the symbol name
+// is only a host-side stand-in, so the address is looked up once per device
+// (with that device current) and cached.
+static void *g_noalloc_addr[GB_NOALLOC_MAX_DEVICES];
+
+extern "C" int gb_direct_acc_noalloc(const float *xm, float *acc, int64_t n, float G, float eps2, int flags,
+                                     void *stream) {
+    if (n < 0 || n > GB_NOALLOC_MAX_N)
+        return fail(GB_EINVAL, "gb_direct_acc_noalloc: n=%lld outside [0, %d]; use gb_direct_acc for larger systems",
+                    (long long)n, GB_NOALLOC_MAX_N);
+    if (n == 0) return GB_OK;
+    GB_TRY(check_xm(xm, "xm"));
+    GB_TRY(check_xm(acc, "acc"));
+    if (!(eps2 > 0.f)) return fail(GB_EINVAL, "eps2 must be > 0");
+    int dev = 0;
+    GB_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= GB_NOALLOC_MAX_DEVICES) return fail(GB_EINVAL, "device index %d not supported", dev);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        GB_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_part));
+        g_noalloc_addr[dev] = p;
+    }
+    DirectPlan pl;
+    make_plan(n, NOALLOC_NP, NOALLOC_WARPS, NOALLOC_CTAS, &pl);
+    if (plan_partials(pl) > NOALLOC_PART)
+        return fail(GB_EINVAL, "gb_direct_acc_noalloc: partials for n=%lld exceed the static scratch", (long long)n);
+    DirectArgs a;
+    a.xm = (const float4 *)xm;
+    a.vel = nullptr;
+    a.acc = nullptr;
+    a.part = (float4 *)g_noalloc_addr[dev];
+    a.n = n;
+    a.num_ju = pl.num_ju;
+    a.U = pl.U;
+    a.P = pl.P;
+    a.smax = pl.smax;
+    a.eps2 = eps2;
+    a.h = 0.f;
+    a.dt = 0.f;
+    cudaStream_t s = (cudaStream_t)stream;
+    const dim3 grid((unsigned)pl.P), block(NOALLOC_WARPS * 32);
+    if (flags & GB_PLAIN_FP32)
+        direct_force_scalar_kernel<NOALLOC_NP, NOALLOC_WARPS, MODE_ACC, false><<<grid, block, 0, s>>>(a);
+    else
+        direct_force_scalar_kernel<NOALLOC_NP, NOALLOC_WARPS, MODE_ACC, true><<<grid, block, 0, s>>>(a);
+    GB_CUDA_TRY(cudaGetLastError());
+    FixArgs f;
+    f.part = a.part;
+    f.xm = const_cast<float4 *>(a.xm);
+    f.vel = nullptr;
+    f.acc = (float4 *)acc;
+    f.phi = nullptr;
+    f.n = n;
+    f.num_ju = pl.num_ju;
+    f.U = pl.U;
+    f.P = pl.P;
+    f.st_size = pl.st_size;
+    f.smax = pl.smax;
+    f.G = G;
+    f.h = 0.f;
+    f.dt = 0.f;
+    f.accumulate = (flags & GB_ACCUMULATE) ? 1 : 0;
+    direct_fixup_kernel<MODE_ACC><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(f);
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+}
