@@ -41,6 +41,7 @@ extern "C" {
 #define GB_ACCUMULATE 0x1  /* acc += result instead of acc = result */
 #define GB_PLAIN_FP32 0x2  /* plain FP32 accumulation (no Kahan compensation) */
 #define GB_COUNT_WORK 0x4  /* tree traversal also counts its work (gb_diag_t) */
+#define GB_USE_GRAPH 0x8   /* batched KDK: capture the step loop as one CUDA graph */
 
 /* Device diagnostic counters, read back by gb_*_diag (synchronising). */
 typedef struct gb_diag {
@@ -170,6 +171,57 @@ int gb_bh_diag(gb_bh_t *h, gb_diag_t *out, int reset);
 int gb_bh_timing(gb_bh_t *h, int enable);
 int gb_bh_stage_times(gb_bh_t *h, float *ms, int *steps);
 uint64_t gb_bh_launch_count(gb_bh_t *h);
+
+/* ------------------------------------------------ batched direct N^2 */
+/* Many independent systems of uneven size, concatenated in one set of
+ * float4 arrays (system s occupies particles off[s] .. off[s+1]-1 with off
+ * the prefix sum of sizes).  Each system is integrated exactly like
+ * Engine(gravity_mode="direct").step (core/engine.py:108-116) on its own;
+ * the reference has no batched form. */
+typedef struct gb_batch gb_batch_t;
+
+/* sizes: host array of nsys system sizes (each >= 1). */
+int gb_batch_create(gb_batch_t **out, const int64_t *sizes, int nsys);
+int gb_batch_destroy(gb_batch_t *h);
+/* Same meaning as gb_direct_set_tiles; chosen by the autotuner. */
+int gb_batch_set_tiles(gb_batch_t *h, int k, int warps, int ctas_per_sm);
+int64_t gb_batch_total(gb_batch_t *h);
+
+/* Direct accelerations of every system (compute_acc_direct per system,
+ * core/solvers/gravity.py:13-26), one persistent launch for all systems. */
+int gb_batch_acc(gb_batch_t *h, const float *xm, float *acc, float G,
+                 float eps2, int flags, void *stream);
+
+/* nsteps KDK steps of every system, in place; acc must hold the current
+ * accelerations.  One persistent force launch + one fix-up launch per step;
+ * with GB_USE_GRAPH the nsteps loop is captured once as a CUDA graph (kept
+ * until the pointers, parameters or tiles change) and replayed. */
+int gb_batch_kdk(gb_batch_t *h, float *xm, float *vel, float *acc, float G,
+                 float eps2, float dt, int64_t nsteps, int flags,
+                 void *stream);
+
+/* The same steps as a loop over systems of the single-system call
+ * gb_direct_kdk (two launches per system and step): the plain alternative
+ * the batched launch is measured against. */
+int gb_batch_kdk_loop(gb_batch_t *h, float *xm, float *vel, float *acc,
+                      float G, float eps2, float dt, int64_t nsteps,
+                      int flags, void *stream);
+uint64_t gb_batch_launch_count(gb_batch_t *h);
+
+/* --------------------------------------------------------------- adjoint */
+/* One reverse-mode step of the direct-sum KDK leapfrog (gb_direct_kdk),
+ * hand-written; the reference has no gradients.  xm holds the positions and
+ * masses at which the step evaluated its forces (the step's output
+ * positions).  On entry lx, lv, la are the adjoints of the step's outputs
+ * x', v', a'; on return they are the adjoints of its inputs x, v, a, and
+ * lm (n floats) has the step's mass gradient added:
+ *   w = la + (dt/2) lv;  (gx, gm) = VJP of the force at xm with w;
+ *   lx += gx;  lv += dt lx;  la = (dt/2) lv;  lm += gm.
+ * prime = 1 instead applies the priming force evaluation a0 = F(x0)
+ * (Engine.load_state, core/engine.py:81): w = la, lx += gx, lm += gm. */
+int gb_adjoint_step(gb_direct_t *h, const float *xm, float *lx, float *lv,
+                    float *la, float *lm, int64_t n, float G, float eps2,
+                    float dt, int prime, void *stream);
 
 /* ------------------------------------------------- allocation-free call */
 /* No counterpart in the reference.  gb_direct_acc without a handle and

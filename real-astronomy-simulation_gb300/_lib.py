@@ -28,6 +28,7 @@ GB_ENOTREADY = 6
 GB_ACCUMULATE = 0x1
 GB_PLAIN_FP32 = 0x2
 GB_COUNT_WORK = 0x4
+GB_USE_GRAPH = 0x8
 
 _STATUS = {GB_EINVAL: "GB_EINVAL", GB_ENOMEM: "GB_ENOMEM", GB_ESTACK: "GB_ESTACK",
            GB_ETIMEOUT: "GB_ETIMEOUT", GB_ECUDA: "GB_ECUDA",
@@ -80,6 +81,15 @@ SIGNATURES = {
     "gb_bh_timing": (I32, [P, I32]),
     "gb_bh_stage_times": (I32, [P, ctypes.POINTER(F32), ctypes.POINTER(I32)]),
     "gb_bh_launch_count": (ctypes.c_uint64, [P]),
+    "gb_batch_create": (I32, [ctypes.POINTER(P), P, I32]),
+    "gb_batch_destroy": (I32, [P]),
+    "gb_batch_set_tiles": (I32, [P, I32, I32, I32]),
+    "gb_batch_total": (I64, [P]),
+    "gb_batch_acc": (I32, [P, P, P, F32, F32, I32, P]),
+    "gb_batch_kdk": (I32, [P, P, P, P, F32, F32, F32, I64, I32, P]),
+    "gb_batch_kdk_loop": (I32, [P, P, P, P, F32, F32, F32, I64, I32, P]),
+    "gb_batch_launch_count": (ctypes.c_uint64, [P]),
+    "gb_adjoint_step": (I32, [P, P, P, P, P, P, I64, F32, F32, F32, I32, P]),
 }
 
 _lib = None

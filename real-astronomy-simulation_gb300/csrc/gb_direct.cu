@@ -23,7 +23,7 @@
 #include <algorithm>
 #include <cstdio>
 
-#include "gb_common.cuh"
+#include "gb_direct_core.cuh"
 
 namespace gb {
 
@@ -40,11 +40,6 @@ struct DirectArgs {
     float eps2, h, dt;
 };
 
-__device__ __forceinline__ int64_t unit_begin(int64_t U, int64_t P, int64_t c) { return U * c / P; }
-// CTA whose unit run contains unit u: the largest c with U*c/P <= u.
-__device__ __forceinline__ int64_t unit_owner(int64_t U, int64_t P, int64_t u) {
-    return ((u + 1) * P - 1) / U;
-}
 
 template <int MODE>
 __device__ __forceinline__ float4 load_particle(const DirectArgs &a, int64_t i) {
@@ -218,20 +213,7 @@ direct_force_scalar_kernel(DirectArgs a) {
             float AX[K], AY[K], AZ[K];
 #pragma unroll
             for (int q = 0; q < K; ++q) AX[q] = AY[q] = AZ[q] = 0.f;
-#pragma unroll 4
-            for (int jj = 0; jj < JU; ++jj) {
-                const float4 sj = src[jj];
-#pragma unroll
-                for (int q = 0; q < K; ++q) {
-                    const float dx = sj.x - X[q], dy = sj.y - Y[q], dz = sj.z - Z[q];
-                    const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, a.eps2)));
-                    const float inv = rsqrt_approx(r2);
-                    const float sc = (sj.w * inv) * (inv * inv);
-                    AX[q] = __fmaf_rn(sc, dx, AX[q]);
-                    AY[q] = __fmaf_rn(sc, dy, AY[q]);
-                    AZ[q] = __fmaf_rn(sc, dz, AZ[q]);
-                }
-            }
+            interact_chunk<K, JU>(src, X, Y, Z, AX, AY, AZ, a.eps2);
 #pragma unroll
             for (int q = 0; q < K; ++q) {
                 if (KAHAN) {
@@ -478,28 +460,6 @@ __global__ void direct_fp64_kernel(const float4 *__restrict__ xm, int64_t n,
 }
 
 // ------------------------------------------------------------------ host
-struct DirectPlan {
-    int np, warps;
-    int64_t n, st_size, num_st, num_ju, U, P;
-    int smax;
-};
-
-static void make_plan(int64_t n, int np, int warps, int64_t P, DirectPlan *p) {
-    p->np = np;
-    p->warps = warps;
-    p->n = n;
-    p->st_size = (int64_t)warps * 32 * 2 * np;
-    p->num_st = (n + p->st_size - 1) / p->st_size;
-    const int64_t ju = (int64_t)warps * 32;
-    p->num_ju = (n + ju - 1) / ju;
-    p->U = p->num_st * p->num_ju;
-    p->P = std::max<int64_t>(1, std::min<int64_t>(P, p->U));
-    const int64_t per = (p->U + p->P - 1) / p->P;
-    p->smax = (int)((per + p->num_ju - 1) / p->num_ju + 1);
-}
-
-// Scratch (float4 elements) a plan needs for its partials.
-static int64_t plan_partials(const DirectPlan &p) { return 2 * p.P * p.smax * p.st_size; }
 
 template <int NP, int WARPS>
 static cudaError_t launch_force(int mode, bool kahan, const DirectPlan &pl, const DirectArgs &a,
@@ -545,20 +505,6 @@ static KernelPtr force_kernel_ptr(int np, int warps, int packed) {
 // ================================================================ C ABI
 using namespace gb;
 
-struct gb_direct {
-    int device;
-    int sms;
-    int64_t n_max;
-    int np, warps, ctas_per_sm;  // tile shape (ctas_per_sm 0 = occupancy max)
-    int packed;                  // 1: .f32x2 inner loop, 0: scalar FP32
-    float4 *part;
-    int64_t part_cap;            // float4 elements
-    float *phi;                  // n_max floats (energy scratch)
-    double2 *epart;              // energy block partials
-    int epart_cap;
-    unsigned long long *diag;
-    uint64_t launches;  // kernels launched by this handle (host count)
-};
 
 static int64_t grid_ctas(gb_direct_t *h, int np, int warps, int packed) {
     int occ = 0;

@@ -1,0 +1,116 @@
+// Building blocks shared by the single-system and batched direct-sum kernels.
+#pragma once
+
+#include "gb_common.cuh"
+
+namespace gb {
+
+// ------------------------------------------------------------ stream-K plan
+// First unit of CTA c when U units are split into P equal contiguous runs.
+__device__ __forceinline__ int64_t unit_begin(int64_t U, int64_t P, int64_t c) { return U * c / P; }
+// CTA whose unit run contains unit u: the largest c with U*c/P <= u.
+__device__ __forceinline__ int64_t unit_owner(int64_t U, int64_t P, int64_t u) {
+    return ((u + 1) * P - 1) / U;
+}
+
+// Units are (target supertile of warps*32*2*np targets) x (source chunk of
+// warps*32 sources), supertile-major; smax bounds the supertiles one CTA run
+// touches, so a CTA's partials fit smax slots.
+struct DirectPlan {
+    int np, warps;
+    int64_t n, st_size, num_st, num_ju, U, P;
+    int smax;
+};
+
+static inline void make_plan(int64_t n, int np, int warps, int64_t P, DirectPlan *p) {
+    p->np = np;
+    p->warps = warps;
+    p->n = n;
+    p->st_size = (int64_t)warps * 32 * 2 * np;
+    p->num_st = (n + p->st_size - 1) / p->st_size;
+    const int64_t ju = (int64_t)warps * 32;
+    p->num_ju = (n + ju - 1) / ju;
+    p->U = p->num_st * p->num_ju;
+    p->P = P < 1 ? 1 : (P > p->U ? p->U : P);
+    const int64_t per = (p->U + p->P - 1) / p->P;
+    p->smax = (int)((per + p->num_ju - 1) / p->num_ju + 1);
+}
+
+// Scratch (float4 elements) a plan needs for its partials: (hi, lo) per
+// target slot.
+static inline int64_t plan_partials(const DirectPlan &p) { return 2 * p.P * p.smax * p.st_size; }
+
+// Adds the accelerations of JU staged sources (src, {x, y, z, m}) on K
+// targets per lane into AX/AY/AZ (FP32; G applied later):
+//   d = x_j - x_i, r2 = d.d + eps2, a += m_j rsqrt(r2)^3 d
+// (core/solvers/gravity.py:22-25).  Zero-mass padding sources add zero.
+template <int K, int JU>
+__device__ __forceinline__ void interact_chunk(const float4 *src, const float (&X)[K], const float (&Y)[K],
+                                               const float (&Z)[K], float (&AX)[K], float (&AY)[K],
+                                               float (&AZ)[K], float eps2) {
+#pragma unroll 4
+    for (int jj = 0; jj < JU; ++jj) {
+        const float4 sj = src[jj];
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            const float dx = sj.x - X[q], dy = sj.y - Y[q], dz = sj.z - Z[q];
+            const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, eps2)));
+            const float inv = rsqrt_approx(r2);
+            const float sc = (sj.w * inv) * (inv * inv);
+            AX[q] = __fmaf_rn(sc, dx, AX[q]);
+            AY[q] = __fmaf_rn(sc, dy, AY[q]);
+            AZ[q] = __fmaf_rn(sc, dz, AZ[q]);
+        }
+    }
+}
+
+// Merges the (hi, lo) partials of one target written by CTAs c_lo..c_hi at
+// slots slot_of(c) (Kahan, fixed CTA order) and returns the sum.
+template <typename SlotFn>
+__device__ __forceinline__ float3 merge_partials(const float4 *__restrict__ part, int64_t c_lo, int64_t c_hi,
+                                                 SlotFn slot_of) {
+    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+    for (int64_t c = c_lo; c <= c_hi; ++c) {
+        const int64_t slot = slot_of(c);
+        const float4 hi = part[2 * slot];
+        const float4 lo = part[2 * slot + 1];
+        kahan_add(sx, cx, hi.x);
+        kahan_add(sx, cx, lo.x);
+        kahan_add(sy, cy, hi.y);
+        kahan_add(sy, cy, lo.y);
+        kahan_add(sz, cz, hi.z);
+        kahan_add(sz, cz, lo.z);
+    }
+    return make_float3(sx - cx, sy - cy, sz - cz);
+}
+
+// Closing kick and in-place state write-back of one KDK step: the particle's
+// predicted position and half-kicked velocity are recomputed exactly as the
+// loaders computed them.
+__device__ __forceinline__ void kdk_writeback(float4 *xm, float4 *vel, float4 *acc, int64_t i, float4 an, float h,
+                                              float dt) {
+    const float4 x = xm[i], v = vel[i], a0 = acc[i];
+    const float vhx = kick(v.x, a0.x, h), vhy = kick(v.y, a0.y, h), vhz = kick(v.z, a0.z, h);
+    xm[i] = make_float4(drift(x.x, vhx, dt), drift(x.y, vhy, dt), drift(x.z, vhz, dt), x.w);
+    vel[i] = make_float4(kick(vhx, an.x, h), kick(vhy, an.y, h), kick(vhz, an.z, h), v.w);
+    acc[i] = an;
+}
+
+}  // namespace gb
+
+// Direct-sum handle (opaque in the C ABI), shared by the direct-sum and
+// adjoint translation units.
+struct gb_direct {
+    int device;
+    int sms;
+    int64_t n_max;
+    int np, warps, ctas_per_sm;  // tile shape (ctas_per_sm 0 = occupancy max)
+    int packed;                  // 1: .f32x2 inner loop, 0: scalar FP32
+    float4 *part;
+    int64_t part_cap;            // float4 elements
+    float *phi;                  // n_max floats (energy scratch)
+    double2 *epart;              // energy block partials
+    int epart_cap;
+    unsigned long long *diag;
+    uint64_t launches;  // kernels launched by this handle (host count)
+};

@@ -1,0 +1,119 @@
+"""Batched direct N^2 (many systems, one persistent launch per step) against
+the single-system path and the FP64 oracle.
+
+Tolerances: accelerations as in the direct tests (per-particle relative RMS
+<= 1e-5, max <= 1e-4 against FP64); trajectories of the batched launch and
+of the per-system loop differ only by FP32 summation order, so after a few
+steps positions agree to 1e-5 of the system size.
+"""
+import importlib
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import PKG_NAME
+
+pytestmark = pytest.mark.gpu
+
+
+def _mods():
+    return (importlib.import_module(PKG_NAME + ".batch"), importlib.import_module(PKG_NAME + ".ic"),
+            importlib.import_module(PKG_NAME + ".autotune"))
+
+
+def _systems(ic, sizes):
+    out = []
+    for s, n in enumerate(sizes):
+        p, v, m = ic.plummer(n, seed=100 + s)
+        f = lambda a: a.astype(np.float32).astype(np.float64)
+        out.append((f(p), f(v), f(m)))
+    return out
+
+
+def _rel(a, ref):
+    return np.linalg.norm(a - ref, axis=1) / np.maximum(np.linalg.norm(ref, axis=1), 1e-300)
+
+
+@pytest.mark.parametrize("tiles", [(2, 4), (2, 8), (4, 4), (4, 8)])
+def test_batch_acc_matches_oracle(cuda_dev, orc, tiles):
+    batch, ic, _ = _mods()
+    sizes = [1, 2, 33, 256, 1000, 1025, 3000, 700, 4096, 17]
+    systems = _systems(ic, sizes)
+    b = batch.DirectBatch(systems, G=1.0, softening=0.02, device=cuda_dev, tiles=tiles)
+    b.compute_acc()
+    acc = b.a4[:, :3].double().cpu().numpy()
+    for s, (p, v, m) in enumerate(systems):
+        o0, o1 = b.offsets[s], b.offsets[s + 1]
+        ref = orc.direct_acc(p, m, 1.0, 0.02 ** 2)
+        if sizes[s] == 1:
+            assert np.all(acc[o0:o1] == 0.0)
+            continue
+        rel = _rel(acc[o0:o1], ref)
+        assert np.sqrt((rel ** 2).mean()) < 1e-5 and rel.max() < 1e-4, (s, rel.max())
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_batch_kdk_matches_loop(cuda_dev, graph):
+    batch, ic, _ = _mods()
+    sizes = ic.batch_sizes(24, 256, 4096)
+    systems = _systems(ic, sizes)
+    b1 = batch.DirectBatch(systems, G=1.0, softening=0.02, device=cuda_dev)
+    b2 = batch.DirectBatch(systems, G=1.0, softening=0.02, device=cuda_dev)
+    b1.run(1e-3, 5, graph=graph)
+    b1.run(1e-3, 5, graph=graph)  # graph replay with the same key
+    b2.run_loop(1e-3, 10)
+    torch.cuda.synchronize()
+    x1 = b1.xm[:, :3].double().cpu().numpy()
+    x2 = b2.xm[:, :3].double().cpu().numpy()
+    assert np.abs(x1 - x2).max() < 1e-5 * np.abs(x2).max()
+    v1 = b1.v4[:, :3].double().cpu().numpy()
+    v2 = b2.v4[:, :3].double().cpu().numpy()
+    assert np.abs(v1 - v2).max() < 1e-4 * np.abs(v2).max()
+    assert b1.launch_count() == 2 * 10 + 2  # initial acc + 2 launches per step
+
+
+def test_batch_matches_oracle_kdk(cuda_dev, orc):
+    batch, ic, _ = _mods()
+    systems = _systems(ic, [300, 1200, 64])
+    b = batch.DirectBatch(systems, G=1.0, softening=0.02, device=cuda_dev)
+    b.run(1e-3, 8)
+    for s, (p, v, m) in enumerate(systems):
+        a0 = orc.direct_acc(p, m, 1.0, 4e-4)
+        pr, vr, _ = orc.kdk_direct(p, v, a0, m, 1.0, 4e-4, 1e-3, 8)
+        gp, gv, _ = b.system(s)
+        assert np.abs(gp - pr).max() < 2e-5 * np.abs(pr).max()
+        assert np.abs(gv - vr).max() < 1e-4 * np.abs(vr).max()
+
+
+def test_batch_energy_drift_and_autotune(cuda_dev):
+    batch, ic, tune = _mods()
+    grav = importlib.import_module(PKG_NAME + ".solvers.gravity")
+    sizes = ic.batch_sizes(16, 256, 2048)
+    systems = _systems(ic, sizes)
+    b = batch.DirectBatch(systems, G=1.0, softening=0.02, device=cuda_dev)
+    shape, times = tune.tune_batch(b, use_cache=False)
+    assert shape in tune.BATCH_SHAPES and len(times) == len(tune.BATCH_SHAPES)
+    g = grav.DirectGravity(int(max(sizes)), cuda_dev)
+
+    def energies():
+        out = []
+        for s in range(len(sizes)):
+            o0, o1 = int(b.offsets[s]), int(b.offsets[s + 1])
+            out.append(g.energies(b.xm[o0:o1], b.v4[o0:o1], 1.0, 4e-4)[2])
+        return np.array(out)
+
+    e0 = energies()
+    b.run(1e-3, 50)
+    e1 = energies()
+    assert np.abs((e1 - e0) / e0).max() < 1e-3
+
+
+def test_batch_bad_arguments(cuda_dev):
+    pkg = importlib.import_module(PKG_NAME)
+    batch, ic, _ = _mods()
+    b = batch.DirectBatch(_systems(ic, [10, 20]), device=cuda_dev)
+    with pytest.raises(pkg.GravityError):
+        b.set_tiles(3, 4)
+    with pytest.raises(ValueError):
+        batch.DirectBatch([], device=cuda_dev)
