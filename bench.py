@@ -401,6 +401,141 @@ def bench_merger(dev, drift_steps=1000):
             "gint_per_s": n * n * drift_steps / t / 1e9}
 
 
+def bench_batch(dev, steps=200, loop_steps=20):
+    """512 independent Plummer spheres (N_s = round(exp(U(ln 256, ln 16384))),
+    seed s), G = 1, eps = 0.02, dt = 1e-3: 200 KDK steps as one persistent
+    launch per step replayed from a CUDA graph, tile shape from the
+    autotuner; compared with the batched launches without the graph and with
+    a loop over systems of the single-system kernel."""
+    batch = importlib.import_module(PKG + ".batch")
+    ic = importlib.import_module(PKG + ".ic")
+    tune = importlib.import_module(PKG + ".autotune")
+    systems = [(_f32(p), _f32(v), _f32(m)) for p, v, m in ic.plummer_batch(512)]
+    b = batch.DirectBatch(systems, G=1.0, softening=0.02, device=dev)
+    shape, tune_ms = tune.tune_batch(b, use_cache=False)
+    inter = b.interactions_per_step()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        s.record()
+        fn()
+        e.record()
+        torch.cuda.synchronize()
+        return s.elapsed_time(e) / 1e3
+
+    b.run(1e-3, steps, graph=True)  # capture + first replay (warm-up)
+    saved = b.state_arrays()
+    l0 = b.launch_count()
+    t_graph = timed(lambda: b.run(1e-3, steps, graph=True))
+    launches = b.launch_count() - l0
+    b.restore(saved)
+    t_plain = timed(lambda: b.run(1e-3, loop_steps, graph=False))
+    b.restore(saved)
+    b.run_loop(1e-3, 2)
+    b.restore(saved)
+    t_loop = timed(lambda: b.run_loop(1e-3, loop_steps))
+    out = {"workload": "512 Plummer spheres, N log-uniform in [256, 16384] (seed s), G=1, eps=0.02, "
+                       f"dt=1e-3, {steps} KDK steps",
+           "n_total": b.n_total, "interactions_per_step": inter, "tiles": list(shape),
+           "autotune_ms_per_step": tune_ms,
+           "graph_gint_per_s": inter * steps / t_graph / 1e9, "graph_ms_per_step": t_graph / steps * 1e3,
+           "gpu_launches_graph": launches,
+           "batched_no_graph_gint_per_s": inter * loop_steps / t_plain / 1e9,
+           "per_system_loop_gint_per_s": inter * loop_steps / t_loop / 1e9,
+           "per_system_loop_ms_per_step": t_loop / loop_steps * 1e3}
+    out["speedup_vs_loop"] = out["graph_gint_per_s"] / out["per_system_loop_gint_per_s"]
+    b.close()
+    return out
+
+
+def bench_adjoint(dev, n=65536, steps=200, every=20):
+    """Adjoint of 200 direct-sum KDK steps on a 65,536-particle exponential
+    disk (Rd = 3, eps = 0.05, dt = 1e-3, galactic G), checkpoint every 20.
+    Loss: MSE of the final positions against a target snapshot made with
+    masses x lognormal(sigma = 0.05).  Reports forward and backward time per
+    step (backward = segment recompute + adjoint kernels)."""
+    adj = importlib.import_module(PKG + ".adjoint")
+    ic = importlib.import_module(PKG + ".ic")
+    grav = importlib.import_module(PKG + ".solvers.gravity")
+    units = importlib.import_module(PKG + ".units")
+    lib_mod = importlib.import_module(PKG + "._lib")
+    p, v, m = ic.exponential_disk(n, seed=0)
+    p, v, m = _f32(p), _f32(v), _f32(m)
+    solver = grav.DirectGravity(n, dev)
+    mt = m * np.random.default_rng(1).lognormal(0.0, 0.05, size=n)
+    with torch.no_grad():
+        xt, _ = adj.simulate(torch.tensor(p, device=dev, dtype=torch.float32),
+                             torch.tensor(v, device=dev, dtype=torch.float32),
+                             torch.tensor(mt, device=dev, dtype=torch.float32),
+                             G=units.G, softening=0.05, dt=1e-3, nsteps=steps, solver=solver)
+    target = xt.detach()
+    # Warm-up: one short differentiable run (module loading and autograd
+    # set-up happen on first use and are not part of a step).
+    xw = torch.tensor(p, device=dev, dtype=torch.float32, requires_grad=True)
+    xa, _ = adj.simulate(xw, torch.tensor(v, device=dev, dtype=torch.float32),
+                         torch.tensor(m, device=dev, dtype=torch.float32), G=units.G, softening=0.05,
+                         dt=1e-3, nsteps=2 * every, checkpoint_every=every, solver=solver)
+    (xa ** 2).mean().backward()
+    torch.cuda.synchronize()
+    x0 = torch.tensor(p, device=dev, dtype=torch.float32, requires_grad=True)
+    v0 = torch.tensor(v, device=dev, dtype=torch.float32, requires_grad=True)
+    m0 = torch.tensor(m, device=dev, dtype=torch.float32, requires_grad=True)
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    s.record()
+    xT, vT = adj.simulate(x0, v0, m0, G=units.G, softening=0.05, dt=1e-3, nsteps=steps,
+                          checkpoint_every=every, solver=solver)
+    e.record()
+    torch.cuda.synchronize()
+    t_fwd = s.elapsed_time(e) / 1e3
+    loss = ((xT - target) ** 2).mean()
+    torch.cuda.synchronize()
+    s.record()
+    loss.backward()
+    e.record()
+    torch.cuda.synchronize()
+    t_bwd = s.elapsed_time(e) / 1e3
+    # One adjoint step alone (no recompute) against one forward step.
+    xm = torch.zeros((n, 4), device=dev)
+    xm[:, :3] = x0.detach()
+    xm[:, 3] = m0.detach()
+    v4 = torch.zeros_like(xm)
+    a4 = torch.zeros_like(xm)
+    lx, lv, la = torch.ones_like(xm), torch.ones_like(xm), torch.ones_like(xm)
+    lm = torch.zeros(n, device=dev)
+    st = torch.cuda.current_stream().cuda_stream
+    reps = 10
+
+    def adj_step():
+        lib_mod.call("gb_adjoint_step", solver.handle, xm.data_ptr(), lx.data_ptr(), lv.data_ptr(),
+                     la.data_ptr(), lm.data_ptr(), n, units.G, 0.0025, 1e-3, 0, st)
+
+    adj_step()
+    solver.kdk(xm.clone(), v4, a4, units.G, 0.0025, 1e-3, 1)
+    xs = xm.clone()
+    s.record()
+    for _ in range(reps):
+        solver.kdk(xs, v4, a4, units.G, 0.0025, 1e-3, 1)
+    e.record()
+    torch.cuda.synchronize()
+    t_f1 = s.elapsed_time(e) / reps
+    s.record()
+    for _ in range(reps):
+        adj_step()
+    e.record()
+    torch.cuda.synchronize()
+    t_b1 = s.elapsed_time(e) / reps
+    g = [t.grad for t in (x0, v0, m0)]
+    return {"workload": f"adjoint of {steps} KDK steps, exponential disk N={n}, eps=0.05, dt=1e-3, "
+                        f"checkpoint every {every}; loss = MSE of final positions",
+            "forward_ms_per_step": t_fwd / steps * 1e3, "backward_ms_per_step": t_bwd / steps * 1e3,
+            "backward_over_forward": t_bwd / t_fwd,
+            "adjoint_kernel_over_force_step": t_b1 / t_f1,
+            "loss": float(loss.detach()),
+            "grad_finite": bool(all(torch.isfinite(t).all().item() for t in g))}
+
+
 # ------------------------------------------------------------------- main
 def run_reference(args):
     """Reference arm: the float64 CPU restatement of the reference's BH path
@@ -447,7 +582,7 @@ def main(argv=None):
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--drift-steps", type=int, default=1000)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
-    ap.add_argument("--only", choices=("direct", "merger"),
+    ap.add_argument("--only", choices=("direct", "merger", "batch", "adjoint"),
                     help="run one secondary workload alone (profiling runs)")
     args = ap.parse_args(argv)
     if args.warmup < 3:
@@ -470,7 +605,9 @@ def main(argv=None):
     if args.only:
         peak = fp32_peak_tflops(lib_mod, dev)
         fn = {"direct": lambda: bench_direct(dev, lib_mod, peak),
-              "merger": lambda: bench_merger(dev, args.drift_steps)}[args.only]
+              "merger": lambda: bench_merger(dev, args.drift_steps),
+              "batch": lambda: bench_batch(dev),
+              "adjoint": lambda: bench_adjoint(dev)}[args.only]
         print(json.dumps({"only": args.only, "fp32_peak_tflops_measured": peak,
                           "result": fn()}), flush=True)
         return 0
@@ -496,6 +633,8 @@ def main(argv=None):
             sec = {"fp32_peak_tflops_measured": peak}
             sec["direct"] = bench_direct(dev, lib_mod, peak)
             sec["merger"] = bench_merger(dev, args.drift_steps)
+            sec["batch"] = bench_batch(dev)
+            sec["adjoint"] = bench_adjoint(dev)
             line["secondary"] = sec
     if dist:
         dist.barrier()

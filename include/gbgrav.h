@@ -159,6 +159,11 @@ int gb_bh_export(gb_bh_t *h, int what, void *dst, void *stream);
 
 int gb_bh_diag(gb_bh_t *h, gb_diag_t *out, int reset);
 
+/* Traversal shape: targets per warp lane (1 or 2; default 1; 2 gives 64
+ * key-consecutive targets per warp).  Same results up to FP32 summation
+ * order; chosen by measurement. */
+int gb_bh_set_traversal(gb_bh_t *h, int targets_per_lane);
+
 /* Stage timing for measurement: with timing enabled, every build/step records
  * CUDA events on its stream at the boundaries of the GB_BH_STAGES stages
  * (0 bbox+keys, 1 sort, 2 gather+Karras, 3 summaries, 4 traversal).

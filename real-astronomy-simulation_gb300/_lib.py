@@ -79,6 +79,7 @@ SIGNATURES = {
     "gb_bh_export": (I32, [P, I32, P, P]),
     "gb_bh_diag": (I32, [P, ctypes.POINTER(Diag), I32]),
     "gb_bh_timing": (I32, [P, I32]),
+    "gb_bh_set_traversal": (I32, [P, I32]),
     "gb_bh_stage_times": (I32, [P, ctypes.POINTER(F32), ctypes.POINTER(I32)]),
     "gb_bh_launch_count": (ctypes.c_uint64, [P]),
     "gb_batch_create": (I32, [ctypes.POINTER(P), P, I32]),

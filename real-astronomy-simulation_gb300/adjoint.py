@@ -56,6 +56,7 @@ class DirectKDK(torch.autograd.Function):
             s.kdk(xm, v4, a4, cfg.G, cfg.eps2, cfg.dt, length)
         ctx.cfg = cfg
         ctx.ckpts = ckpts
+        ctx.x_final = xm.clone()
         return xm[:, :3].clone(), v4[:, :3].clone()
 
     @staticmethod
@@ -74,13 +75,15 @@ class DirectKDK(torch.autograd.Function):
         stream = stream_handle(dev)
         segs = _segments(cfg.nsteps, cfg.every)
         traj = torch.empty((cfg.every, n, 4), dtype=torch.float32, device=dev)
-        for (c, length), (xm, v4, a4) in zip(reversed(segs), reversed(ctx.ckpts)):
+        ends = [ck[0] for ck in ctx.ckpts[1:]] + [ctx.x_final]
+        for (c, length), (xm, v4, a4), x_end in zip(reversed(segs), reversed(ctx.ckpts), reversed(ends)):
             xm, v4, a4 = xm.clone(), v4.clone(), a4.clone()
-            for k in range(length):
+            for k in range(length - 1):
                 s.kdk(xm, v4, a4, cfg.G, cfg.eps2, cfg.dt, 1)
                 traj[k].copy_(xm)
             for k in reversed(range(length)):
-                _lib.call("gb_adjoint_step", s.handle, ptr(traj[k], "xm"), ptr(lx, "lx"), ptr(lv, "lv"),
+                xk = x_end if k == length - 1 else traj[k]
+                _lib.call("gb_adjoint_step", s.handle, ptr(xk, "xm"), ptr(lx, "lx"), ptr(lv, "lv"),
                           ptr(la, "la"), lm.data_ptr(), n, cfg.G, cfg.eps2, cfg.dt, 0, stream)
         _lib.call("gb_adjoint_step", s.handle, ptr(x0m, "xm"), ptr(lx, "lx"), ptr(lv, "lv"),
                   ptr(la, "la"), lm.data_ptr(), n, cfg.G, cfg.eps2, cfg.dt, 1, stream)

@@ -503,86 +503,115 @@ __device__ __forceinline__ bool apply_room(Lane &L, bool open, int sp, int max_s
     return false;
 }
 
-// Warp-coherent traversal: 32 key-consecutive targets per warp walk the tree
-// together.  The warp expands one internal node per iteration: it loads the
-// node's two-children record (48 B) and every lane of the node's mask visits
-// both children (right first, as the reference pops it first).  The right
-// child, if any lane opened it, is expanded next straight from registers; an
-// opened left child waits on a shared-memory stack of {node, mask, sp}.  sp,
-// the depth of the reference's per-particle stack when a node is popped,
-// depends only on the node's path (one pending left sibling per right turn),
-// so it travels with the node.
-template <bool KDK, bool COUNT>
+// Warp-coherent traversal: TPL x 32 key-consecutive targets per warp walk the
+// tree together (TPL targets per lane: slot q of lane l is target wbase +
+// 32 q + l).  The warp expands one internal node per iteration: it loads the
+// node's two-children record (48 B) and every lane visits both children for
+// each of its slots in the node's masks (right first, as the reference pops
+// it first).  The right child, if any slot opened it, is expanded next
+// straight from registers; an opened left child waits on a shared-memory
+// stack of {node, mask slot 0, mask slot 1, sp}.  sp, the depth of the
+// reference's per-particle stack when a node is popped, depends only on the
+// node's path (one pending left sibling per right turn), so it travels with
+// the node.
+template <bool KDK, bool COUNT, int TPL>
 __global__ void __launch_bounds__(TRAV_WARPS * 32)
 bh_traverse_kernel(TravArgs a) {
     __shared__ int4 stk[TRAV_WARPS][TRAV_STACK];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int wbase = (blockIdx.x * TRAV_WARPS + wid) * 32;
+    const int wbase = (blockIdx.x * TRAV_WARPS + wid) * (32 * TPL);
     if (wbase >= a.n) return;  // whole warp out of range
-    const int s = wbase + lane;
-    const bool valid = s < a.n;
     const int n = a.n;
-    Lane L;
-    L.px = L.py = L.pz = 0.f;
-    if (valid) {
-        const float4 p = __ldg(a.leaf + s);
-        L.px = p.x; L.py = p.y; L.pz = p.z;
+    int s[TPL];
+    bool valid[TPL];
+    Lane L[TPL];
+#pragma unroll
+    for (int q = 0; q < TPL; ++q) {
+        s[q] = wbase + 32 * q + lane;
+        valid[q] = s[q] < n;
+        L[q].px = L[q].py = L[q].pz = 0.f;
+        if (valid[q]) {
+            const float4 p = __ldg(a.leaf + s[q]);
+            L[q].px = p.x; L[q].py = p.y; L[q].pz = p.z;
+        }
+        L[q].ax = L[q].ay = L[q].az = 0.f;
+        L[q].n_int = L[q].n_test = L[q].drops = 0;
     }
-    L.ax = L.ay = L.az = 0.f;
-    L.n_int = L.n_test = L.drops = 0;
     unsigned overflow = 0, bad = 0, iters = 0;
     int top = 0;
     int k = 0, sp = 0;
-    unsigned m = 0;
+    unsigned m[TPL];
+    unsigned any = 0;
+#pragma unroll
+    for (int q = 0; q < TPL; ++q) m[q] = 0;
     if (n >= 2) {
         // The root is popped first, with an empty stack (sp = 0).
         const float4 R0 = __ldg(a.root), R1 = __ldg(a.root + 1);
-        const bool want = apply_room(L, visit_child<COUNT>(L, a, R0, R1.x, n, s, valid), 0, a.max_stack);
-        m = __ballot_sync(0xffffffffu, want);
+#pragma unroll
+        for (int q = 0; q < TPL; ++q) {
+            const bool want = apply_room(L[q], visit_child<COUNT>(L[q], a, R0, R1.x, n, s[q], valid[q]), 0,
+                                         a.max_stack);
+            m[q] = __ballot_sync(0xffffffffu, want);
+            any |= m[q];
+        }
     }
-    while (m) {
-        const bool in = (m >> lane) & 1u;
+    while (any) {
         if ((unsigned)k >= (unsigned)(n - 1)) {  // never for a consistent tree
-            bad += in ? 1u : 0u;
-            m = 0;
+#pragma unroll
+            for (int q = 0; q < TPL; ++q) bad += ((m[q] >> lane) & 1u);
+            any = 0;
         } else {
             const float4 QL = __ldg(a.inode + 3 * k);
             const float4 QR = __ldg(a.inode + 3 * k + 1);
             const float4 C = __ldg(a.inode + 3 * k + 2);
+            const int idL = __float_as_int(C.z), idR = __float_as_int(C.w);
             if (COUNT) ++iters;
-            const bool wantR = apply_room(L, visit_child<COUNT>(L, a, QR, C.y, __float_as_int(C.w), s, in),
-                                          sp + 1, a.max_stack);
-            const bool wantL = apply_room(L, visit_child<COUNT>(L, a, QL, C.x, __float_as_int(C.z), s, in), sp,
-                                          a.max_stack);
-            const unsigned omL = __ballot_sync(0xffffffffu, wantL);
-            const unsigned omR = __ballot_sync(0xffffffffu, wantR);
-            if (omL) {
+            unsigned omL[TPL], omR[TPL], anyL = 0, anyR = 0;
+#pragma unroll
+            for (int q = 0; q < TPL; ++q) {
+                const bool in = (m[q] >> lane) & 1u;
+                const bool wantR = apply_room(L[q], visit_child<COUNT>(L[q], a, QR, C.y, idR, s[q], in), sp + 1,
+                                              a.max_stack);
+                const bool wantL = apply_room(L[q], visit_child<COUNT>(L[q], a, QL, C.x, idL, s[q], in), sp,
+                                              a.max_stack);
+                omL[q] = __ballot_sync(0xffffffffu, wantL);
+                omR[q] = __ballot_sync(0xffffffffu, wantR);
+                anyL |= omL[q];
+                anyR |= omR[q];
+            }
+            if (anyL) {
                 if (top < TRAV_STACK) {
-                    if (lane == 0) stk[wid][top] = make_int4(__float_as_int(C.z) - n, (int)omL, sp, 0);
+                    if (lane == 0) stk[wid][top] = make_int4(idL - n, (int)omL[0], TPL > 1 ? (int)omL[TPL - 1] : 0, sp);
                     ++top;
                 } else {
-                    overflow += wantL ? 1u : 0u;
+#pragma unroll
+                    for (int q = 0; q < TPL; ++q) overflow += ((omL[q] >> lane) & 1u);
                 }
             }
-            if (omR) {  // expand the right child next
-                k = __float_as_int(C.w) - n;
-                m = omR;
+            if (anyR) {  // expand the right child next
+                k = idR - n;
+#pragma unroll
+                for (int q = 0; q < TPL; ++q) m[q] = omR[q];
                 sp = sp + 1;
                 continue;
             }
-            m = 0;
+            any = 0;
         }
         if (top > 0) {
             __syncwarp();
             const int4 e = stk[wid][--top];
             k = e.x;
-            m = (unsigned)e.y;
-            sp = e.z;
+            m[0] = (unsigned)e.y;
+            if (TPL > 1) m[TPL - 1] = (unsigned)e.z;
+            sp = e.w;
+            any = m[0] | m[TPL - 1];
             __syncwarp();
         }
     }
     // Counters: one atomic per warp and counter.
-    unsigned dsum = L.drops, osum = overflow, bsum = bad;
+    unsigned dsum = 0, osum = overflow, bsum = bad;
+#pragma unroll
+    for (int q = 0; q < TPL; ++q) dsum += L[q].drops;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
@@ -590,7 +619,12 @@ bh_traverse_kernel(TravArgs a) {
         bsum += __shfl_xor_sync(0xffffffffu, bsum, o);
     }
     if (COUNT) {
-        unsigned isum = L.n_int, tsum = L.n_test;
+        unsigned isum = 0, tsum = 0;
+#pragma unroll
+        for (int q = 0; q < TPL; ++q) {
+            isum += L[q].n_int;
+            tsum += L[q].n_test;
+        }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             isum += __shfl_xor_sync(0xffffffffu, isum, o);
@@ -609,20 +643,23 @@ bh_traverse_kernel(TravArgs a) {
         if (bsum) atomicAdd(a.diag + DIAG_BAD_TREE, (unsigned long long)bsum);
     }
     // Epilogue: scatter to the original particle index.
-    if (!valid) return;
-    const uint32_t p = __ldg(a.order + s);
-    if (p >= (uint32_t)n) return;
-    const float gx = a.G * L.ax, gy = a.G * L.ay, gz = a.G * L.az;
-    if (KDK) {
-        const float4 vh = a.vel[p];
-        a.vel[p] = make_float4(kick(vh.x, gx, a.h), kick(vh.y, gy, a.h), kick(vh.z, gz, a.h), vh.w);
-        a.acc[p] = make_float4(gx, gy, gz, 0.f);
-    } else if (a.accumulate) {
-        float4 o = a.acc[p];
-        o.x += gx; o.y += gy; o.z += gz;
-        a.acc[p] = o;
-    } else {
-        a.acc[p] = make_float4(gx, gy, gz, 0.f);
+#pragma unroll
+    for (int q = 0; q < TPL; ++q) {
+        if (!valid[q]) continue;
+        const uint32_t p = __ldg(a.order + s[q]);
+        if (p >= (uint32_t)n) continue;
+        const float gx = a.G * L[q].ax, gy = a.G * L[q].ay, gz = a.G * L[q].az;
+        if (KDK) {
+            const float4 vh = a.vel[p];
+            a.vel[p] = make_float4(kick(vh.x, gx, a.h), kick(vh.y, gy, a.h), kick(vh.z, gz, a.h), vh.w);
+            a.acc[p] = make_float4(gx, gy, gz, 0.f);
+        } else if (a.accumulate) {
+            float4 o = a.acc[p];
+            o.x += gx; o.y += gy; o.z += gz;
+            a.acc[p] = o;
+        } else {
+            a.acc[p] = make_float4(gx, gy, gz, 0.f);
+        }
     }
 }
 
@@ -729,6 +766,7 @@ struct gb_bh {
     cudaEvent_t ev[GB_BH_TIMING_STEPS * (GB_BH_STAGES + 1)];
     uint64_t launches;  // kernels launched by this handle (host count)
     int pending_slot;   // timing slot of the last gb_bh_build
+    int tpl;            // traversal targets per lane (1 or 2)
 };
 
 static void mark(gb_bh_t *h, int step_slot, int stage, cudaStream_t s) {
@@ -761,6 +799,7 @@ extern "C" int gb_bh_create(gb_bh_t **out, int64_t n_max, int key_bits) {
     h->sms = num_sms();
     h->n_max = n_max;
     h->key_bits = key_bits;
+    h->tpl = 1;
     h->n = -1;
     h->cur = 0;
     const int64_t nn = n_max, ni = std::max<int64_t>(n_max - 1, 1), nodes = 2 * n_max;
@@ -891,15 +930,20 @@ static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float theta, float eps
     a.max_stack = max_stack;
     a.accumulate = (flags & GB_ACCUMULATE) ? 1 : 0;
     a.diag = h->diag;
-    const int64_t warps = (n + 31) / 32;
+    const int tpl = h->tpl;
+    const int64_t warps = (n + 32 * tpl - 1) / (32 * tpl);
     const unsigned grid = (unsigned)((warps + TRAV_WARPS - 1) / TRAV_WARPS);
     const bool count = (flags & GB_COUNT_WORK) != 0;
-    if (kdk) {
-        if (count) bh_traverse_kernel<true, true><<<grid, TRAV_WARPS * 32, 0, s>>>(a);
-        else bh_traverse_kernel<true, false><<<grid, TRAV_WARPS * 32, 0, s>>>(a);
-    } else {
-        if (count) bh_traverse_kernel<false, true><<<grid, TRAV_WARPS * 32, 0, s>>>(a);
-        else bh_traverse_kernel<false, false><<<grid, TRAV_WARPS * 32, 0, s>>>(a);
+    const int sel = (kdk ? 4 : 0) + (count ? 2 : 0) + (tpl == 2 ? 1 : 0);
+    switch (sel) {
+        case 0: bh_traverse_kernel<false, false, 1><<<grid, TRAV_WARPS * 32, 0, s>>>(a); break;
+        case 1: bh_traverse_kernel<false, false, 2><<<grid, TRAV_WARPS * 32, 0, s>>>(a); break;
+        case 2: bh_traverse_kernel<false, true, 1><<<grid, TRAV_WARPS * 32, 0, s>>>(a); break;
+        case 3: bh_traverse_kernel<false, true, 2><<<grid, TRAV_WARPS * 32, 0, s>>>(a); break;
+        case 4: bh_traverse_kernel<true, false, 1><<<grid, TRAV_WARPS * 32, 0, s>>>(a); break;
+        case 5: bh_traverse_kernel<true, false, 2><<<grid, TRAV_WARPS * 32, 0, s>>>(a); break;
+        case 6: bh_traverse_kernel<true, true, 1><<<grid, TRAV_WARPS * 32, 0, s>>>(a); break;
+        default: bh_traverse_kernel<true, true, 2><<<grid, TRAV_WARPS * 32, 0, s>>>(a); break;
     }
     GB_CUDA_TRY(cudaGetLastError());
     mark(h, slot, 5, s);
@@ -1016,3 +1060,11 @@ extern "C" int gb_bh_stage_times(gb_bh_t *h, float *ms, int *steps) {
 }
 
 extern "C" uint64_t gb_bh_launch_count(gb_bh_t *h) { return h ? h->launches : 0; }
+
+extern "C" int gb_bh_set_traversal(gb_bh_t *h, int targets_per_lane) {
+    if (!h) return fail(GB_EINVAL, "handle is NULL");
+    if (targets_per_lane != 1 && targets_per_lane != 2)
+        return fail(GB_EINVAL, "targets_per_lane must be 1 or 2 (got %d)", targets_per_lane);
+    h->tpl = targets_per_lane;
+    return GB_OK;
+}

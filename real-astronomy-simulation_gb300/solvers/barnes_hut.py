@@ -104,6 +104,10 @@ class BarnesHut:
     def tree_arrays(self) -> dict:
         return {k: self.export(k) for k in EXPORTS}
 
+    def set_traversal(self, targets_per_lane: int) -> None:
+        """Targets per warp lane in the traversal (1 or 2)."""
+        _lib.call("gb_bh_set_traversal", self._h, int(targets_per_lane))
+
     # -- measurement hooks
     STAGES = ("keys", "sort", "build", "summaries", "traverse")
 

@@ -49,11 +49,12 @@ def _check_acc(a, ref):
     assert rel.max() < 1e-2, rel.max()
 
 
-def _run(bhmod, pos, mass, dev, theta=0.5, soft=0.05, bits=21, G=None, max_stack=64):
+def _run(bhmod, pos, mass, dev, theta=0.5, soft=0.05, bits=21, G=None, max_stack=64, tpl=2):
     kw = {} if G is None else {"G": G}
     n = pos.shape[0]
     b = bhmod.BarnesHut(n, theta=theta, softening=soft, max_stack=max_stack, key_bits=bits,
                         device=dev, **kw)
+    b.set_traversal(tpl)
     xm = _xm(pos, mass, dev)
     acc = torch.zeros_like(xm)
     b.compute(xm, acc)
@@ -62,11 +63,12 @@ def _run(bhmod, pos, mass, dev, theta=0.5, soft=0.05, bits=21, G=None, max_stack
 
 
 @pytest.mark.parametrize("bits", [21, 10])
-def test_golden_tree_bit_exact(cuda_dev, bits):
+@pytest.mark.parametrize("tpl", [1, 2])
+def test_golden_tree_bit_exact(cuda_dev, bits, tpl):
     _, bhmod, _, _ = _mods()
     g = load_golden("bh")
     pre = f"b{bits}_"
-    b, a = _run(bhmod, g["pos"], g["mass"], cuda_dev, bits=bits, G=float(g["G"]))
+    b, a = _run(bhmod, g["pos"], g["mass"], cuda_dev, bits=bits, G=float(g["G"]), tpl=tpl)
     t = b.tree_arrays()
     ref_sorted = g[pre + "code"][g[pre + "order"]]
     np.testing.assert_array_equal(t["code"], ref_sorted)
@@ -97,13 +99,14 @@ def test_golden_compute_and_duplicates(cuda_dev):
     _check_acc(a, g["dup_acc"])
 
 
-def test_stack_rule_matches_reference(cuda_dev, orc):
+@pytest.mark.parametrize("tpl", [1, 2])
+def test_stack_rule_matches_reference(cuda_dev, orc, tpl):
     """max_stack=6 silently drops subtrees in the reference (:212); the
     device applies the same rule per lane and counts the drops."""
     _, bhmod, _, _ = _mods()
     g = load_golden("bh")
     pos, mass = g["pos"][:400], g["mass"][:400]
-    b, a = _run(bhmod, pos, mass, cuda_dev, bits=21, G=float(g["G"]), max_stack=6)
+    b, a = _run(bhmod, pos, mass, cuda_dev, bits=21, G=float(g["G"]), max_stack=6, tpl=tpl)
     _check_acc(a, g["stk6_acc"])
     _, _, dropped = orc.bh_compute(pos, mass, 0.5, 0.05, float(g["G"]), max_stack=6)
     d = b.diag()["stack_drops"]
@@ -125,12 +128,13 @@ def test_engine_bh_golden(cuda_dev):
     assert np.abs(st.vel - g["vel"]).max() < 1e-4 * np.abs(g["vel"]).max()
 
 
-@pytest.mark.parametrize("n", [2, 3, 33, 256, 1000])
-def test_small_sizes(cuda_dev, orc, n):
+@pytest.mark.parametrize("n", [2, 3, 33, 64, 65, 256, 1000])
+@pytest.mark.parametrize("tpl", [1, 2])
+def test_small_sizes(cuda_dev, orc, n, tpl):
     _, bhmod, ic, _ = _mods()
     pos, _, mass = ic.exponential_disk(n, seed=n)
     pos, mass = _f32(pos), _f32(mass)
-    b, a = _run(bhmod, pos, mass, cuda_dev)
+    b, a = _run(bhmod, pos, mass, cuda_dev, tpl=tpl)
     ref, tree, _ = orc.bh_compute(pos, mass, 0.5, 0.05, b.G)
     t = b.tree_arrays()
     np.testing.assert_array_equal(t["order"], tree["order"])
@@ -138,8 +142,8 @@ def test_small_sizes(cuda_dev, orc, n):
     _check_acc(a, ref)
 
 
-@pytest.mark.parametrize("bits", [10, 21])
-def test_config2_disk_1m(cuda_dev, orc, bits):
+@pytest.mark.parametrize("bits,tpl", [(10, 2), (21, 1)])
+def test_config2_disk_1m(cuda_dev, orc, bits, tpl):
     """N = 1,000,000 exponential disk (M = 5, Rd = 3, z0 = 0.3, galactic G),
     theta = 0.5, eps = 0.05: keys, order, topology bit-exact at full size;
     forces on 4,096 seeded targets against FP64 direct and FP64 BH."""
@@ -147,7 +151,7 @@ def test_config2_disk_1m(cuda_dev, orc, bits):
     n = 1_000_000
     pos, _, mass = ic.exponential_disk(n, seed=0)
     pos, mass = _f32(pos), _f32(mass)
-    b, a = _run(bhmod, pos, mass, cuda_dev, bits=bits)
+    b, a = _run(bhmod, pos, mass, cuda_dev, bits=bits, tpl=tpl)
     t = b.tree_arrays()
     codes = orc.morton_codes(pos, bits)
     order = orc.stable_argsort(codes)
