@@ -114,6 +114,16 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
+def max_over_ranks(value: float, dist, device) -> float:
+    """The slowest rank's time (all ranks get it); identity without a
+    process group."""
+    if not dist:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def _events(k):
     return ([torch.cuda.Event(enable_timing=True) for _ in range(k)],
             [torch.cuda.Event(enable_timing=True) for _ in range(k)])
@@ -196,11 +206,7 @@ def bench_bh(args, dev, rank, world, dist):
     stages, nst = bh.stage_times()
     bh.timing(False)
     diag = bh.diag(reset=True)
-    total_ms = float(sum(step_ms))
-    if dist:
-        t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(float(sum(step_ms)), dist, dev)
     value = world * BH_N * args.steps / (total_ms / 1e3)
     res = {"value": value, "ms_per_step": total_ms / args.steps, "clocks": clk,
            "gpu_launches": int(launches), "diag": diag,
@@ -253,11 +259,7 @@ def bench_bh(args, dev, rank, world, dist):
         ha.copy_(a4, non_blocking=True)
         e_e[k].record()
     torch.cuda.synchronize()
-    e2e_ms = float(sum(s.elapsed_time(e) for s, e in zip(e_s, e_e)))
-    if dist:
-        t = torch.tensor([e2e_ms], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(float(sum(s.elapsed_time(e) for s, e in zip(e_s, e_e))), dist, dev)
     nbytes = 3 * BH_N * 16
     res["e2e"] = {"value": world * BH_N * args.steps / (e2e_ms / 1e3),
                   "unit": "particle-steps/s", "h2d_bytes_per_step": nbytes,
@@ -507,6 +509,8 @@ def bench_adjoint(dev, n=65536, steps=200, every=20):
     st = torch.cuda.current_stream().cuda_stream
     reps = 10
 
+    lib_mod.call("gb_adjoint_set_variant", solver.handle, 1)
+
     def adj_step():
         lib_mod.call("gb_adjoint_step", solver.handle, xm.data_ptr(), lx.data_ptr(), lv.data_ptr(),
                      la.data_ptr(), lm.data_ptr(), n, units.G, 0.0025, 1e-3, 0, st)
@@ -527,10 +531,23 @@ def bench_adjoint(dev, n=65536, steps=200, every=20):
     torch.cuda.synchronize()
     t_b1 = s.elapsed_time(e) / reps
     g = [t.grad for t in (x0, v0, m0)]
+    # The same backward with the per-target pair evaluation, for comparison.
+    x1 = x0.detach().clone().requires_grad_(True)
+    xT1, _ = adj.simulate(x1, v0.detach(), m0.detach(), G=units.G, softening=0.05, dt=1e-3,
+                          nsteps=steps, checkpoint_every=every, solver=solver, symmetric=False)
+    loss1 = ((xT1 - target) ** 2).mean()
+    torch.cuda.synchronize()
+    s.record()
+    loss1.backward()
+    e.record()
+    torch.cuda.synchronize()
+    t_bwd_pt = s.elapsed_time(e) / 1e3
+    lib_mod.call("gb_adjoint_set_variant", solver.handle, 1)
     return {"workload": f"adjoint of {steps} KDK steps, exponential disk N={n}, eps=0.05, dt=1e-3, "
                         f"checkpoint every {every}; loss = MSE of final positions",
             "forward_ms_per_step": t_fwd / steps * 1e3, "backward_ms_per_step": t_bwd / steps * 1e3,
             "backward_over_forward": t_bwd / t_fwd,
+            "backward_over_forward_per_target_form": t_bwd_pt / t_fwd,
             "adjoint_kernel_over_force_step": t_b1 / t_f1,
             "loss": float(loss.detach()),
             "grad_finite": bool(all(torch.isfinite(t).all().item() for t in g))}

@@ -228,6 +228,13 @@ int gb_adjoint_step(gb_direct_t *h, const float *xm, float *lx, float *lv,
                     float *la, float *lm, int64_t n, float G, float eps2,
                     float dt, int prime, void *stream);
 
+/* Pair evaluation of the adjoint: 1 (default) evaluates every unordered pair
+ * once and applies it to both particles (scratch grows as n^2 / 16 bytes,
+ * allocated on first use; beyond 3 GiB the call uses the other form), 0
+ * evaluates each ordered pair in one pass per target.  Both are
+ * deterministic; they differ by FP32 summation order. */
+int gb_adjoint_set_variant(gb_direct_t *h, int symmetric);
+
 /* ------------------------------------------------- allocation-free call */
 /* No counterpart in the reference.  gb_direct_acc without a handle and
  * without any device allocation, for callers that cannot call cudaMalloc:

@@ -91,6 +91,7 @@ SIGNATURES = {
     "gb_batch_kdk_loop": (I32, [P, P, P, P, F32, F32, F32, I64, I32, P]),
     "gb_batch_launch_count": (ctypes.c_uint64, [P]),
     "gb_adjoint_step": (I32, [P, P, P, P, P, P, I64, F32, F32, F32, I32, P]),
+    "gb_adjoint_set_variant": (I32, [P, I32]),
 }
 
 _lib = None

@@ -17,6 +17,24 @@ from . import _lib
 from ._dev import ptr, require_cuda, stream_handle
 
 
+def shard_systems(sizes, rank: int, world: int) -> list:
+    """Indices of the systems rank `rank` of `world` integrates when a batch
+    is split across GPUs: longest-processing-time assignment by N^2 (each
+    system whole on one rank, no exchange between ranks), deterministic on
+    every rank."""
+    if world < 1 or not (0 <= rank < world):
+        raise ValueError(f"bad rank {rank} of {world}")
+    cost = np.asarray(sizes, dtype=np.float64) ** 2
+    order = sorted(range(len(cost)), key=lambda s: (-cost[s], s))
+    load = [0.0] * world
+    owner = [0] * len(cost)
+    for s in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        owner[s] = r
+        load[r] += cost[s]
+    return [s for s in range(len(cost)) if owner[s] == rank]
+
+
 class DirectBatch:
     def __init__(self, systems, G: float = 1.0, softening: float = 0.02, device=None,
                  plain_fp32: bool = False, tiles=None):

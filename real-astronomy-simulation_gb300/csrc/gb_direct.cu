@@ -558,6 +558,7 @@ extern "C" int gb_direct_create(gb_direct_t **out, int64_t n_max) {
     h->warps = 8;
     h->ctas_per_sm = 0;
     h->packed = 0;
+    h->adj_variant = 1;
     int st = ensure_partials(h, max_partials(h, n_max));
     if (st == GB_OK && cudaMalloc(&h->phi, sizeof(float) * n_max) != cudaSuccess)
         st = fail(GB_ENOMEM, "phi scratch");
@@ -582,6 +583,7 @@ extern "C" int gb_direct_destroy(gb_direct_t *h) {
     cudaFree(h->phi);
     cudaFree(h->epart);
     cudaFree(h->diag);
+    cudaFree(h->sym);
     delete h;
     return GB_OK;
 }

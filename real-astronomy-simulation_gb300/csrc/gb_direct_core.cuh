@@ -113,4 +113,7 @@ struct gb_direct {
     int epart_cap;
     unsigned long long *diag;
     uint64_t launches;  // kernels launched by this handle (host count)
+    float4 *sym;        // symmetric adjoint partials (allocated on first use)
+    int64_t sym_cap;    // float4 elements
+    int adj_variant;    // 1: symmetric pair evaluation, 0: one pass per target
 };

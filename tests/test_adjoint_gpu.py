@@ -62,14 +62,14 @@ def _loss(x, v, target):
     return ((x - target) ** 2).mean() + 1e-6 * (v ** 2).mean()
 
 
-def _device_grads(p, v, m, target, nsteps, every, dev):
+def _device_grads(p, v, m, target, nsteps, every, dev, symmetric=True):
     adj, _, grav = _mods()
     x0 = torch.tensor(p, dtype=torch.float32, device=dev, requires_grad=True)
     v0 = torch.tensor(v, dtype=torch.float32, device=dev, requires_grad=True)
     m0 = torch.tensor(m, dtype=torch.float32, device=dev, requires_grad=True)
     solver = grav.DirectGravity(p.shape[0], dev)
     xT, vT = adj.simulate(x0, v0, m0, G=G, softening=EPS, dt=DT, nsteps=nsteps,
-                          checkpoint_every=every, solver=solver)
+                          checkpoint_every=every, solver=solver, symmetric=symmetric)
     loss = _loss(xT.double(), vT.double(), torch.tensor(target, device=dev))
     loss.backward()
     return [t.grad.double().cpu().numpy() for t in (x0, v0, m0)], float(loss.detach())
@@ -89,22 +89,43 @@ def _rel(a, b):
     return np.linalg.norm(a - b) / np.linalg.norm(b)
 
 
-def test_adjoint_matches_dense_autograd(cuda_dev):
+@pytest.mark.parametrize("symmetric", [True, False])
+def test_adjoint_matches_dense_autograd(cuda_dev, symmetric):
     p, v, m, target = _problem()
-    g_dev, l_dev = _device_grads(p, v, m, target, 200, 20, cuda_dev)
+    g_dev, l_dev = _device_grads(p, v, m, target, 200, 20, cuda_dev, symmetric)
     g_ref, l_ref = _dense_grads(p, v, m, target, 200)
     assert abs(l_dev - l_ref) < 1e-4 * abs(l_ref)
     for name, a, b in zip(("x0", "v0", "m"), g_dev, g_ref):
         assert _rel(a, b) < 2e-3, (name, _rel(a, b))
 
 
-def test_checkpoint_interval_does_not_change_gradients(cuda_dev):
+@pytest.mark.parametrize("symmetric", [True, False])
+def test_adjoint_ragged_tiles_match_dense(cuda_dev, symmetric):
+    """N = 520: two full 256-particle tiles and a partial one (diagonal,
+    off-diagonal and padded tile pairs of the symmetric form)."""
+    p, v, m, target = _problem(n=520, seed=13)
+    g_dev, _ = _device_grads(p, v, m, target, 30, 10, cuda_dev, symmetric)
+    g_ref, _ = _dense_grads(p, v, m, target, 30)
+    for name, a, b in zip(("x0", "v0", "m"), g_dev, g_ref):
+        assert _rel(a, b) < 2e-3, (name, _rel(a, b))
+
+
+@pytest.mark.parametrize("symmetric", [True, False])
+def test_checkpoint_interval_does_not_change_gradients(cuda_dev, symmetric):
     p, v, m, target = _problem(n=300, seed=5)
-    base, _ = _device_grads(p, v, m, target, 24, 24, cuda_dev)
+    base, _ = _device_grads(p, v, m, target, 24, 24, cuda_dev, symmetric)
     for every in (1, 5, 7):
-        g, _ = _device_grads(p, v, m, target, 24, every, cuda_dev)
+        g, _ = _device_grads(p, v, m, target, 24, every, cuda_dev, symmetric)
         for a, b in zip(g, base):
             assert np.array_equal(a, b)
+
+
+def test_symmetric_matches_per_target_form(cuda_dev):
+    p, v, m, target = _problem(n=3000, seed=17)
+    g1, _ = _device_grads(p, v, m, target, 10, 5, cuda_dev, True)
+    g0, _ = _device_grads(p, v, m, target, 10, 5, cuda_dev, False)
+    for a, b in zip(g1, g0):
+        assert _rel(a, b) < 1e-4
 
 
 def test_adjoint_matches_fp64_finite_differences(cuda_dev, orc):
