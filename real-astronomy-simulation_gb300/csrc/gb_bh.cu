@@ -472,23 +472,24 @@ struct Lane {
 // One child for one lane of the expanding mask (branch-free).  Leaves carry
 // size2 = -1 in the record, so the one comparison size2 < theta^2 (|d|^2 +
 // eps^2) accepts every leaf and applies the reference's test (:208) to
-// internal nodes; the self test id != s is true for every internal id (ids
-// >= n > s).  An accepted child adds its monopole unless it is the lane's own
-// particle; a rejected (internal) child is opened.  Returns "open".
+// internal nodes.  An accepted child adds its monopole; the lane's own leaf
+// (which the reference skips, :198) sits exactly at the lane's position, so
+// its term is d * (...) = +0 and needs no test.  A rejected (internal) child
+// is opened.  Returns "open".
 template <bool COUNT>
 __device__ __forceinline__ bool visit_child(Lane &L, const TravArgs &a, float4 q, float size2, int id, int s,
                                             bool in) {
     const float dx = q.x - L.px, dy = q.y - L.py, dz = q.z - L.pz;
     const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, a.eps2)));
     const bool accept = size2 < a.theta2 * r2;
-    const bool add = in && accept && id != s;
+    const bool add = in && accept;
     const float inv = rsqrt_approx(r2);
     const float sc = add ? q.w * inv * inv * inv : 0.f;
     L.ax = __fmaf_rn(sc, dx, L.ax);
     L.ay = __fmaf_rn(sc, dy, L.ay);
     L.az = __fmaf_rn(sc, dz, L.az);
     if (COUNT) {
-        L.n_int += add ? 1u : 0u;
+        L.n_int += (add && id != s) ? 1u : 0u;
         L.n_test += (in && size2 >= 0.f) ? 1u : 0u;
     }
     return in && !accept;
@@ -567,13 +568,23 @@ bh_traverse_kernel(TravArgs a) {
             const int idL = __float_as_int(C.z), idR = __float_as_int(C.w);
             if (COUNT) ++iters;
             unsigned omL[TPL], omR[TPL], anyL = 0, anyR = 0;
+            // Room for both children's pushes (the right child is popped at
+            // depth sp + 1): one warp-uniform test; the per-child rule only
+            // runs near max_stack.
+            const bool room2 = sp + 3 <= a.max_stack;
 #pragma unroll
             for (int q = 0; q < TPL; ++q) {
                 const bool in = (m[q] >> lane) & 1u;
-                const bool wantR = apply_room(L[q], visit_child<COUNT>(L[q], a, QR, C.y, idR, s[q], in), sp + 1,
-                                              a.max_stack);
-                const bool wantL = apply_room(L[q], visit_child<COUNT>(L[q], a, QL, C.x, idL, s[q], in), sp,
-                                              a.max_stack);
+                bool wantR, wantL;
+                if (room2) {
+                    wantR = visit_child<COUNT>(L[q], a, QR, C.y, idR, s[q], in);
+                    wantL = visit_child<COUNT>(L[q], a, QL, C.x, idL, s[q], in);
+                } else {
+                    wantR = apply_room(L[q], visit_child<COUNT>(L[q], a, QR, C.y, idR, s[q], in), sp + 1,
+                                       a.max_stack);
+                    wantL = apply_room(L[q], visit_child<COUNT>(L[q], a, QL, C.x, idL, s[q], in), sp,
+                                       a.max_stack);
+                }
                 omL[q] = __ballot_sync(0xffffffffu, wantL);
                 omR[q] = __ballot_sync(0xffffffffu, wantR);
                 anyL |= omL[q];
