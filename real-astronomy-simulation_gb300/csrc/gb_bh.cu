@@ -401,10 +401,11 @@ __device__ __forceinline__ unsigned arrive(unsigned *p) {
 }
 
 // Summarises every internal node k once both children are done and writes
-// the traversal record of its two children:
-//   inode[3k] = left {com, m}, inode[3k+1] = right {com, m},
-//   inode[3k+2] = {size2 left, size2 right, left id, right id} (ids as bits;
-//   size2 = -1 marks a leaf child).
+// the traversal record of its two children as (left, right) pairs:
+//   inode[3k] = {x_L, x_R, y_L, y_R}, inode[3k+1] = {z_L, z_R, m_L, m_R},
+//   inode[3k+2] = {size2_L, size2_R, id_L, id_R} (ids as bits; size2 = -1
+//   marks a leaf child), so the traversal loads both children pre-packed for
+//   .f32x2 arithmetic.
 __global__ void bh_bottomup_kernel(const float4 *__restrict__ leaf, const int2 *__restrict__ child,
                                    const int *__restrict__ parent, int n, unsigned *__restrict__ arrivals,
                                    float4 *__restrict__ sums, float4 *__restrict__ bmin, float4 *__restrict__ bmax,
@@ -436,8 +437,9 @@ __global__ void bh_bottomup_kernel(const float4 *__restrict__ leaf, const int2 *
         sums[k] = make_float4(s.m, s.sx, s.sy, s.sz);
         bmin[k] = make_float4(s.lx, s.ly, s.lz, 0.f);
         bmax[k] = make_float4(s.hx, s.hy, s.hz, 0.f);
-        inode[3 * k] = trav_com(a);
-        inode[3 * k + 1] = trav_com(b);
+        const float4 ca = trav_com(a), cb = trav_com(b);
+        inode[3 * k] = make_float4(ca.x, cb.x, ca.y, cb.y);
+        inode[3 * k + 1] = make_float4(ca.z, cb.z, ca.w, cb.w);
         inode[3 * k + 2] = make_float4(c.x < n ? -1.f : size2_of(a), c.y < n ? -1.f : size2_of(b),
                                        __int_as_float(c.x), __int_as_float(c.y));
         const int up = __ldg(parent + node);
@@ -466,6 +468,8 @@ struct TravArgs {
 
 struct Lane {
     float px, py, pz, ax, ay, az;
+    f2 PX, PY, PZ;  // (p, p) pairs
+    f2 AX, AY, AZ;  // accumulators for (left, right) children
     unsigned n_int, n_test, drops;
 };
 
@@ -493,6 +497,39 @@ __device__ __forceinline__ bool visit_child(Lane &L, const TravArgs &a, float4 q
         L.n_test += (in && size2 >= 0.f) ? 1u : 0u;
     }
     return in && !accept;
+}
+
+// Both children of an expanded node for one lane, on packed (left, right)
+// pairs: the same test and monopole as visit_child, two children per
+// instruction.  Sets openL / openR.
+template <bool COUNT>
+__device__ __forceinline__ void visit_pair(Lane &L, const TravArgs &a, ulonglong2 A, ulonglong2 B, float4 C, int s,
+                                           bool in, f2 E2, f2 TH2, bool &openL, bool &openR) {
+    const f2 dx = sub2(A.x, L.PX), dy = sub2(A.y, L.PY), dz = sub2(B.x, L.PZ);
+    f2 r2 = fma2(dx, dx, E2);
+    r2 = fma2(dy, dy, r2);
+    r2 = fma2(dz, dz, r2);
+    const f2 t = mul2(TH2, r2);
+    float r2L, r2R, tL, tR;
+    unpack2(r2, r2L, r2R);
+    unpack2(t, tL, tR);
+    const bool accL = C.x < tL, accR = C.y < tR;
+    const f2 inv = pack2(rsqrt_approx(r2L), rsqrt_approx(r2R));
+    const f2 sc = mul2(mul2(B.y, inv), mul2(inv, inv));
+    float scL, scR;
+    unpack2(sc, scL, scR);
+    const f2 scm = pack2((in && accL) ? scL : 0.f, (in && accR) ? scR : 0.f);
+    L.AX = fma2(scm, dx, L.AX);
+    L.AY = fma2(scm, dy, L.AY);
+    L.AZ = fma2(scm, dz, L.AZ);
+    if (COUNT) {
+        L.n_int += (in && accL && __float_as_int(C.z) != s) ? 1u : 0u;
+        L.n_int += (in && accR && __float_as_int(C.w) != s) ? 1u : 0u;
+        L.n_test += (in && C.x >= 0.f) ? 1u : 0u;
+        L.n_test += (in && C.y >= 0.f) ? 1u : 0u;
+    }
+    openL = in && !accL;
+    openR = in && !accR;
 }
 
 // The reference's push rule (:212): a lane that opens a node popped at stack
@@ -536,8 +573,13 @@ bh_traverse_kernel(TravArgs a) {
             L[q].px = p.x; L[q].py = p.y; L[q].pz = p.z;
         }
         L[q].ax = L[q].ay = L[q].az = 0.f;
+        L[q].PX = pack2(L[q].px, L[q].px);
+        L[q].PY = pack2(L[q].py, L[q].py);
+        L[q].PZ = pack2(L[q].pz, L[q].pz);
+        L[q].AX = L[q].AY = L[q].AZ = 0ull;
         L[q].n_int = L[q].n_test = L[q].drops = 0;
     }
+    const f2 E2 = pack2(a.eps2, a.eps2), TH2 = pack2(a.theta2, a.theta2);
     unsigned overflow = 0, bad = 0, iters = 0;
     int top = 0;
     int k = 0, sp = 0;
@@ -562,8 +604,8 @@ bh_traverse_kernel(TravArgs a) {
             for (int q = 0; q < TPL; ++q) bad += ((m[q] >> lane) & 1u);
             any = 0;
         } else {
-            const float4 QL = __ldg(a.inode + 3 * k);
-            const float4 QR = __ldg(a.inode + 3 * k + 1);
+            const ulonglong2 A = __ldg(reinterpret_cast<const ulonglong2 *>(a.inode + 3 * k));
+            const ulonglong2 B = __ldg(reinterpret_cast<const ulonglong2 *>(a.inode + 3 * k + 1));
             const float4 C = __ldg(a.inode + 3 * k + 2);
             const int idL = __float_as_int(C.z), idR = __float_as_int(C.w);
             if (COUNT) ++iters;
@@ -576,14 +618,10 @@ bh_traverse_kernel(TravArgs a) {
             for (int q = 0; q < TPL; ++q) {
                 const bool in = (m[q] >> lane) & 1u;
                 bool wantR, wantL;
-                if (room2) {
-                    wantR = visit_child<COUNT>(L[q], a, QR, C.y, idR, s[q], in);
-                    wantL = visit_child<COUNT>(L[q], a, QL, C.x, idL, s[q], in);
-                } else {
-                    wantR = apply_room(L[q], visit_child<COUNT>(L[q], a, QR, C.y, idR, s[q], in), sp + 1,
-                                       a.max_stack);
-                    wantL = apply_room(L[q], visit_child<COUNT>(L[q], a, QL, C.x, idL, s[q], in), sp,
-                                       a.max_stack);
+                visit_pair<COUNT>(L[q], a, A, B, C, s[q], in, E2, TH2, wantL, wantR);
+                if (!room2) {
+                    wantR = apply_room(L[q], wantR, sp + 1, a.max_stack);
+                    wantL = apply_room(L[q], wantL, sp, a.max_stack);
                 }
                 omL[q] = __ballot_sync(0xffffffffu, wantL);
                 omR[q] = __ballot_sync(0xffffffffu, wantR);
@@ -659,7 +697,12 @@ bh_traverse_kernel(TravArgs a) {
         if (!valid[q]) continue;
         const uint32_t p = __ldg(a.order + s[q]);
         if (p >= (uint32_t)n) continue;
-        const float gx = a.G * L[q].ax, gy = a.G * L[q].ay, gz = a.G * L[q].az;
+        float xl, xr, yl, yr, zl, zr;
+        unpack2(L[q].AX, xl, xr);
+        unpack2(L[q].AY, yl, yr);
+        unpack2(L[q].AZ, zl, zr);
+        const float gx = a.G * (L[q].ax + (xl + xr)), gy = a.G * (L[q].ay + (yl + yr)),
+                    gz = a.G * (L[q].az + (zl + zr));
         if (KDK) {
             const float4 vh = a.vel[p];
             a.vel[p] = make_float4(kick(vh.x, gx, a.h), kick(vh.y, gy, a.h), kick(vh.z, gz, a.h), vh.w);
