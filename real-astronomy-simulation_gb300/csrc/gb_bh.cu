@@ -105,13 +105,37 @@ bh_bbox_kernel(float4 *xm, float4 *vel, const float4 *acc, int64_t n, float h, f
         is_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
     }
     __syncthreads();
-    if (!is_last || threadIdx.x != 0) return;
+    if (!is_last) return;
+    // Last CTA: merge every CTA's partial with all its threads (strided L2
+    // reads, then the same warp/CTA reduction).
     __threadfence();
-    float4 a = __ldcg(part), b = __ldcg(part + 1);
-    for (unsigned k = 1; k < gridDim.x; ++k) {
+    float4 a = make_float4(INFINITY, INFINITY, INFINITY, 0.f), b = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
+    for (unsigned k = threadIdx.x; k < gridDim.x; k += BBOX_THREADS) {
         const float4 c = __ldcg(part + 2 * k), d = __ldcg(part + 2 * k + 1);
         a.x = fminf(a.x, c.x); a.y = fminf(a.y, c.y); a.z = fminf(a.z, c.z);
         b.x = fmaxf(b.x, d.x); b.y = fmaxf(b.y, d.y); b.z = fmaxf(b.z, d.z);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a.x = fminf(a.x, __shfl_xor_sync(0xffffffffu, a.x, o));
+        a.y = fminf(a.y, __shfl_xor_sync(0xffffffffu, a.y, o));
+        a.z = fminf(a.z, __shfl_xor_sync(0xffffffffu, a.z, o));
+        b.x = fmaxf(b.x, __shfl_xor_sync(0xffffffffu, b.x, o));
+        b.y = fmaxf(b.y, __shfl_xor_sync(0xffffffffu, b.y, o));
+        b.z = fmaxf(b.z, __shfl_xor_sync(0xffffffffu, b.z, o));
+    }
+    __syncthreads();  // smn/smx reused
+    if (lane == 0) {
+        smn[wid] = a;
+        smx[wid] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    a = smn[0];
+    b = smx[0];
+    for (int w = 1; w < BBOX_THREADS / 32; ++w) {
+        a.x = fminf(a.x, smn[w].x); a.y = fminf(a.y, smn[w].y); a.z = fminf(a.z, smn[w].z);
+        b.x = fmaxf(b.x, smx[w].x); b.y = fmaxf(b.y, smx[w].y); b.z = fmaxf(b.z, smx[w].z);
     }
     // span = largest per-axis extent (:41); 1.0 when not > 0 (:42).
     const double lo0 = a.x, lo1 = a.y, lo2 = a.z;
