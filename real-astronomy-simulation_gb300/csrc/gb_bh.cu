@@ -652,20 +652,27 @@ bh_traverse_kernel(TravArgs a) {
                 anyL |= omL[q];
                 anyR |= omR[q];
             }
-            if (anyL) {
-                if (top < TRAV_STACK) {
-                    if (lane == 0) stk[wid][top] = make_int4(idL - n, (int)omL[0], TPL > 1 ? (int)omL[TPL - 1] : 0, sp);
-                    ++top;
-                } else {
+            if (anyR) {  // expand the right child next; a left child waits on the stack
+                if (anyL) {
+                    if (top < TRAV_STACK) {
+                        // Every lane stores the same entry (no lane predicate).
+                        stk[wid][top] = make_int4(idL - n, (int)omL[0], TPL > 1 ? (int)omL[TPL - 1] : 0, sp);
+                        ++top;
+                    } else {
 #pragma unroll
-                    for (int q = 0; q < TPL; ++q) overflow += ((omL[q] >> lane) & 1u);
+                        for (int q = 0; q < TPL; ++q) overflow += ((omL[q] >> lane) & 1u);
+                    }
                 }
-            }
-            if (anyR) {  // expand the right child next
                 k = idR - n;
 #pragma unroll
                 for (int q = 0; q < TPL; ++q) m[q] = omR[q];
                 sp = sp + 1;
+                continue;
+            }
+            if (anyL) {  // only the left child was opened: expand it next directly
+                k = idL - n;
+#pragma unroll
+                for (int q = 0; q < TPL; ++q) m[q] = omL[q];
                 continue;
             }
             any = 0;
