@@ -14,7 +14,7 @@ __device__ __forceinline__ int64_t unit_owner(int64_t U, int64_t P, int64_t u) {
 }
 
 // Units are (target supertile of warps*32*2*np targets) x (source chunk of
-// warps*32 sources), supertile-major; smax bounds the supertiles one CTA run
+// unit_src sources), supertile-major; smax bounds the supertiles one CTA run
 // touches, so a CTA's partials fit smax slots.
 struct DirectPlan {
     int np, warps;
@@ -22,13 +22,13 @@ struct DirectPlan {
     int smax;
 };
 
-static inline void make_plan(int64_t n, int np, int warps, int64_t P, DirectPlan *p) {
+static inline void make_plan(int64_t n, int np, int warps, int64_t P, DirectPlan *p, int unit_src = 0) {
     p->np = np;
     p->warps = warps;
     p->n = n;
     p->st_size = (int64_t)warps * 32 * 2 * np;
     p->num_st = (n + p->st_size - 1) / p->st_size;
-    const int64_t ju = (int64_t)warps * 32;
+    const int64_t ju = unit_src > 0 ? unit_src : (int64_t)warps * 32;
     p->num_ju = (n + ju - 1) / ju;
     p->U = p->num_st * p->num_ju;
     p->P = P < 1 ? 1 : (P > p->U ? p->U : P);
@@ -63,6 +63,10 @@ __device__ __forceinline__ void interact_chunk(const float4 *src, const float (&
         }
     }
 }
+
+// Sources per stream-K unit of the scalar force kernel: one warp-width
+// sub-chunk, so CTA runs split the work evenly even at small N.
+constexpr int SCALAR_UNIT = 32;
 
 // Merges the (hi, lo) partials of one target written by CTAs c_lo..c_hi at
 // slots slot_of(c) (Kahan, fixed CTA order) and returns the sum.
