@@ -509,7 +509,7 @@ def bench_adjoint(dev, n=65536, steps=200, every=20):
     st = torch.cuda.current_stream().cuda_stream
     reps = 10
 
-    lib_mod.call("gb_adjoint_set_variant", solver.handle, 1)
+    lib_mod.call("gb_adjoint_set_variant", solver.handle, 2)
 
     def adj_step():
         lib_mod.call("gb_adjoint_step", solver.handle, xm.data_ptr(), lx.data_ptr(), lv.data_ptr(),
@@ -531,23 +531,30 @@ def bench_adjoint(dev, n=65536, steps=200, every=20):
     torch.cuda.synchronize()
     t_b1 = s.elapsed_time(e) / reps
     g = [t.grad for t in (x0, v0, m0)]
-    # The same backward with the per-target pair evaluation, for comparison.
-    x1 = x0.detach().clone().requires_grad_(True)
-    xT1, _ = adj.simulate(x1, v0.detach(), m0.detach(), G=units.G, softening=0.05, dt=1e-3,
-                          nsteps=steps, checkpoint_every=every, solver=solver, symmetric=False)
-    loss1 = ((xT1 - target) ** 2).mean()
-    torch.cuda.synchronize()
-    s.record()
-    loss1.backward()
-    e.record()
-    torch.cuda.synchronize()
-    t_bwd_pt = s.elapsed_time(e) / 1e3
-    lib_mod.call("gb_adjoint_set_variant", solver.handle, 1)
+
+    def backward_time(symmetric, packed):
+        """The same backward with another pair evaluation, for comparison."""
+        x1 = x0.detach().clone().requires_grad_(True)
+        xT1, _ = adj.simulate(x1, v0.detach(), m0.detach(), G=units.G, softening=0.05, dt=1e-3,
+                              nsteps=steps, checkpoint_every=every, solver=solver, symmetric=symmetric,
+                              packed=packed)
+        loss1 = ((xT1 - target) ** 2).mean()
+        torch.cuda.synchronize()
+        s.record()
+        loss1.backward()
+        e.record()
+        torch.cuda.synchronize()
+        return s.elapsed_time(e) / 1e3
+
+    t_bwd_pt = backward_time(False, True)
+    t_bwd_sc = backward_time(True, False)
+    lib_mod.call("gb_adjoint_set_variant", solver.handle, 2)
     return {"workload": f"adjoint of {steps} KDK steps, exponential disk N={n}, eps=0.05, dt=1e-3, "
                         f"checkpoint every {every}; loss = MSE of final positions",
             "forward_ms_per_step": t_fwd / steps * 1e3, "backward_ms_per_step": t_bwd / steps * 1e3,
             "backward_over_forward": t_bwd / t_fwd,
             "backward_over_forward_per_target_form": t_bwd_pt / t_fwd,
+            "backward_over_forward_scalar_symmetric_form": t_bwd_sc / t_fwd,
             "adjoint_kernel_over_force_step": t_b1 / t_f1,
             "loss": float(loss.detach()),
             "grad_finite": bool(all(torch.isfinite(t).all().item() for t in g))}

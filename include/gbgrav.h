@@ -228,12 +228,16 @@ int gb_adjoint_step(gb_direct_t *h, const float *xm, float *lx, float *lv,
                     float *la, float *lm, int64_t n, float G, float eps2,
                     float dt, int prime, void *stream);
 
-/* Pair evaluation of the adjoint: 1 (default) evaluates every unordered pair
- * once and applies it to both particles (scratch grows as n^2 / 16 bytes,
- * allocated on first use; beyond 3 GiB the call uses the other form), 0
- * evaluates each ordered pair in one pass per target.  Both are
- * deterministic; they differ by FP32 summation order. */
-int gb_adjoint_set_variant(gb_direct_t *h, int symmetric);
+/* Pair evaluation of the adjoint:
+ *   2 (default) every unordered pair once, applied to both particles, in
+ *     packed FP32x2 arithmetic with CTAs taking tile-pair units from a
+ *     counter (scratch about n^2 / 16 bytes, allocated on first use);
+ *   1 every unordered pair once, scalar FP32, static runs per CTA (scratch
+ *     about n^2 / 32 bytes);
+ *   0 each ordered pair, one pass per target (no extra scratch).
+ * A symmetric form whose scratch would pass 3 GiB falls back to 0.  All
+ * are deterministic; they differ by FP32 summation order. */
+int gb_adjoint_set_variant(gb_direct_t *h, int variant);
 
 /* ------------------------------------------------- allocation-free call */
 /* No counterpart in the reference.  gb_direct_acc without a handle and

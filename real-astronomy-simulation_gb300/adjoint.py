@@ -92,13 +92,15 @@ class DirectKDK(torch.autograd.Function):
 
 def simulate(x0: torch.Tensor, v0: torch.Tensor, m: torch.Tensor, *, G: float, softening: float,
              dt: float, nsteps: int, checkpoint_every: int = 20, solver: DirectGravity | None = None,
-             symmetric: bool = True):
+             symmetric: bool = True, packed: bool = True):
     """(x_T, v_T) after nsteps KDK steps; differentiable in x0, v0 and m.
     symmetric selects the adjoint's pair evaluation (each unordered pair once,
-    or each ordered pair in one pass per target)."""
+    or each ordered pair in one pass per target); packed selects, for the
+    symmetric form, FP32x2 arithmetic with dynamically fetched tile-pair
+    units over the scalar form with static CTA runs."""
     require_cuda(x0.device)
     if solver is None:
         solver = DirectGravity(x0.shape[0], x0.device)
-    _lib.call("gb_adjoint_set_variant", solver.handle, 1 if symmetric else 0)
+    _lib.call("gb_adjoint_set_variant", solver.handle, (2 if packed else 1) if symmetric else 0)
     cfg = KDKConfig(G, softening, dt, nsteps, checkpoint_every, solver)
     return DirectKDK.apply(x0, v0, m, cfg)

@@ -355,6 +355,244 @@ __global__ void __launch_bounds__(SYM_WARPS * 32) adjoint_vjp_sym_kernel(SymArgs
     }
 }
 
+// ------------------------------------- symmetric evaluation, packed pairs
+// The pair algebra of adjoint_vjp_sym_kernel in .f32x2 arithmetic, where one
+// instruction serves two (target, source) pairs.  Tiles of SYM2_T = 512
+// particles; 4 warps, 4 targets per lane held as two packed pairs (targets
+// q = 0, 1 and q = 2, 3; lane l of warp w owns targets 128 w + 32 q + l).
+// A unit is one unordered tile pair (I <= J) and one of Q source slices of
+// tile J (512 / Q sources, G = 16 / Q groups of 32).  CTAs take units from
+// an atomic counter, so CTAs that the schedulers favour take more units and
+// all of them stay resident until the work runs out; each unit writes its
+// own row slot (tile I's sums over the slice) and its slice of the pair's
+// column slot, and the fix-up adds the slots in a fixed order, so results
+// do not depend on which CTA did which unit.  In round r warp w takes group
+// g = (G/4 w + r) mod G of the slice (distinct across the warps of a round)
+// and at step k lane l source 32 g + (l + k) mod 32, so no two lanes update
+// one source accumulator at once.  Target sums N = sum sv v (and sum sv
+// d.w_source) stay in registers and are written negated.  On the diagonal
+// tile a pair (t, s) counts when t < s; the self pair is exactly zero.
+constexpr int SYM2_T = 512;
+constexpr int SYM2_WARPS = 4;
+
+struct Sym2Args {
+    const float4 *__restrict__ xm;
+    const float4 *__restrict__ lv;
+    const float4 *__restrict__ la;
+    float4 *__restrict__ rowpart;  // NP * Q x SYM2_T
+    float4 *__restrict__ colpart;  // NP x SYM2_T
+    unsigned long long *counter;   // zero at launch
+    int64_t n, nt, NP;
+    float eps2, h;
+    int prime;
+};
+
+__device__ __forceinline__ float4 sym2_w(const Sym2Args &a, int64_t i) {
+    if (i >= a.n) return make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 la = __ldg(a.la + i);
+    if (a.prime) return la;
+    const float4 lv = __ldg(a.lv + i);
+    return make_float4(__fmaf_rn(a.h, lv.x, la.x), __fmaf_rn(a.h, lv.y, la.y), __fmaf_rn(a.h, lv.z, la.z), 0.f);
+}
+
+// One round of sym2 pair steps: lane l at step k takes source jj =
+// 32 g + (l + k) mod 32 of the staged tile against its 4 targets.  DIAG
+// masks the pairs with target index >= source index (diagonal tile).
+template <bool DIAG>
+__device__ __forceinline__ void sym2_round(const float4 *__restrict__ sxm, const float4 *__restrict__ sw,
+                                           float4 *sacc, int g, int lane, int wib, f2 EPS2, f2 NEG3,
+                                           const f2 (&TX)[2], const f2 (&TY)[2], const f2 (&TZ)[2],
+                                           const f2 (&TNM)[2], const f2 (&TWX)[2], const f2 (&TWY)[2],
+                                           const f2 (&TWZ)[2], f2 (&NX)[2], f2 (&NY)[2], f2 (&NZ)[2],
+                                           f2 (&NG)[2]) {
+#pragma unroll 2
+    for (int k = 0; k < 32; ++k) {
+        const int jj = g * 32 + ((lane + k) & 31);
+        const float4 xs = sxm[jj], ws = sw[jj];
+        const f2 sx = pack2(xs.x, xs.x), sy = pack2(xs.y, xs.y), sz = pack2(xs.z, xs.z);
+        const f2 sm = pack2(xs.w, xs.w);
+        const f2 swx = pack2(ws.x, ws.x), swy = pack2(ws.y, ws.y), swz = pack2(ws.z, ws.z);
+        f2 PX = 0ull, PY = 0ull, PZ = 0ull, PG = 0ull;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const f2 dx = sub2(sx, TX[h]), dy = sub2(sy, TY[h]), dz = sub2(sz, TZ[h]);
+            const f2 r2 = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, EPS2)));
+            const f2 inv = rsqrt2(r2);
+            const f2 inv2 = mul2(inv, inv);
+            f2 sv = mul2(inv, inv2);
+            if (DIAG) {
+                // Target index 128 w + 64 h + 32 e + lane < source index jj.
+                float s0, s1;
+                unpack2(sv, s0, s1);
+                const int t0 = 128 * wib + 64 * h + lane;
+                s0 = t0 < jj ? s0 : 0.f;
+                s1 = t0 + 32 < jj ? s1 : 0.f;
+                sv = pack2(s0, s1);
+            }
+            // u = m_s w_t - m_t w_s; v = u - 3 inv2 (d.u) d.
+            const f2 ux = fma2(TNM[h], swx, mul2(sm, TWX[h]));
+            const f2 uy = fma2(TNM[h], swy, mul2(sm, TWY[h]));
+            const f2 uz = fma2(TNM[h], swz, mul2(sm, TWZ[h]));
+            const f2 du = fma2(dz, uz, fma2(dy, uy, mul2(dx, ux)));
+            const f2 ne = mul2(mul2(NEG3, inv2), du);
+            const f2 vx = fma2(ne, dx, ux), vy = fma2(ne, dy, uy), vz = fma2(ne, dz, uz);
+            const f2 dwt = fma2(dz, TWZ[h], fma2(dy, TWY[h], mul2(dx, TWX[h])));
+            const f2 dws = fma2(dz, swz, fma2(dy, swy, mul2(dx, swx)));
+            NX[h] = fma2(sv, vx, NX[h]);
+            NY[h] = fma2(sv, vy, NY[h]);
+            NZ[h] = fma2(sv, vz, NZ[h]);
+            NG[h] = fma2(sv, dws, NG[h]);
+            PX = fma2(sv, vx, PX);
+            PY = fma2(sv, vy, PY);
+            PZ = fma2(sv, vz, PZ);
+            PG = fma2(sv, dwt, PG);
+        }
+        float4 acc = sacc[jj];
+        float lo, hi;
+        unpack2(PX, lo, hi);
+        acc.x += lo + hi;
+        unpack2(PY, lo, hi);
+        acc.y += lo + hi;
+        unpack2(PZ, lo, hi);
+        acc.z += lo + hi;
+        unpack2(PG, lo, hi);
+        acc.w += lo + hi;
+        sacc[jj] = acc;
+        __syncwarp();
+    }
+}
+
+template <int Q>
+__global__ void __launch_bounds__(SYM2_WARPS * 32, 4) adjoint_vjp_sym2_kernel(Sym2Args a) {
+    constexpr int G = 16 / Q, SPAN = G * 32;
+    __shared__ float4 sxm[SYM2_T], sw[SYM2_T], sacc[SYM2_T];
+    __shared__ long long s_unit;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, tid = threadIdx.x;
+    const int64_t NU = a.NP * Q;
+    const f2 EPS2 = pack2(a.eps2, a.eps2), NEG3 = pack2(-3.f, -3.f);
+    for (;;) {
+        __syncthreads();  // the previous unit is done with s_unit and shared memory
+        if (tid == 0) s_unit = (long long)atomicAdd(a.counter, 1ull);
+        __syncthreads();
+        f2 TX[2], TY[2], TZ[2], TNM[2], TWX[2], TWY[2], TWZ[2], NX[2], NY[2], NZ[2], NG[2];
+        bool diag;
+        int gbase;
+        {
+        // Unit bookkeeping is re-read from shared memory after the pair
+        // loop, so none of it stays in registers across the loop.
+        const int64_t u = s_unit;
+        if (u >= NU) break;
+        const int64_t p = u / Q;
+        const int sl = (int)(u - p * Q);
+        const int64_t I = sym_row(p, a.nt);
+        const int64_t J = I + (p - sym_base(I, a.nt));
+        diag = J == I;
+        gbase = sl * G;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            float4 x[2], w[2];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int64_t i = I * SYM2_T + 128 * wib + 32 * (2 * h + e) + lane;
+                x[e] = i < a.n ? __ldg(a.xm + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+                w[e] = sym2_w(a, i);
+            }
+            TX[h] = pack2(x[0].x, x[1].x);
+            TY[h] = pack2(x[0].y, x[1].y);
+            TZ[h] = pack2(x[0].z, x[1].z);
+            TNM[h] = pack2(-x[0].w, -x[1].w);
+            TWX[h] = pack2(w[0].x, w[1].x);
+            TWY[h] = pack2(w[0].y, w[1].y);
+            TWZ[h] = pack2(w[0].z, w[1].z);
+            NX[h] = NY[h] = NZ[h] = NG[h] = 0ull;
+        }
+        // Stage the slice's sources (tile-local indices sl*SPAN .. +SPAN-1).
+        for (int t = tid; t < SPAN; t += SYM2_WARPS * 32) {
+            const int tt = sl * SPAN + t;
+            const int64_t j = J * SYM2_T + tt;
+            sxm[tt] = j < a.n ? __ldg(a.xm + j) : make_float4(0.f, 0.f, 0.f, 0.f);
+            sw[tt] = sym2_w(a, j);
+            sacc[tt] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        }
+        __syncthreads();
+        for (int r = 0; r < G; ++r) {
+            const int g = gbase + (((G / 4) * wib + r) & (G - 1));
+            // Diagonal tile: targets 128 w .. 128 w + 127 against sources
+            // 32 g .. 32 g + 31; no pair has t < s when 4 w > g.
+            // Warp-uniform branches; every warp still reaches the barrier.
+            if (!diag)
+                sym2_round<false>(sxm, sw, sacc, g, lane, wib, EPS2, NEG3, TX, TY, TZ, TNM, TWX, TWY, TWZ, NX, NY,
+                                  NZ, NG);
+            else if (4 * wib <= g)
+                sym2_round<true>(sxm, sw, sacc, g, lane, wib, EPS2, NEG3, TX, TY, TZ, TNM, TWX, TWY, TWZ, NX, NY,
+                                 NZ, NG);
+            __syncthreads();
+        }
+        const int64_t u = s_unit;
+        const int64_t p = u / Q;
+        const int sl = (int)(u - p * Q);
+        for (int t = tid; t < SPAN; t += SYM2_WARPS * 32) {
+            const int tt = sl * SPAN + t;
+            a.colpart[p * SYM2_T + tt] = sacc[tt];
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            float x0, x1, y0, y1, z0, z1, g0, g1;
+            unpack2(NX[h], x0, x1);
+            unpack2(NY[h], y0, y1);
+            unpack2(NZ[h], z0, z1);
+            unpack2(NG[h], g0, g1);
+            float4 *row = a.rowpart + u * SYM2_T + 128 * wib + 64 * h + lane;
+            row[0] = make_float4(-x0, -y0, -z0, -g0);
+            row[32] = make_float4(-x1, -y1, -z1, -g1);
+        }
+    }
+}
+
+struct Sym2Fix {
+    const float4 *__restrict__ rowpart;
+    const float4 *__restrict__ colpart;
+    float4 *lx, *lv, *la;
+    float *lm;
+    int64_t n, nt;
+    int Q;
+    float G, h, dt;
+    int prime;
+};
+
+// Adds particle i's slots in a fixed order: its row units (I, J, slice) for
+// J = I .. nt-1, then its column slots (I', I) for I' = 0 .. I; then applies
+// the elementwise part of the backward step.
+__global__ void adjoint_sym2_fixup_kernel(Sym2Fix f) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= f.n) return;
+    const int64_t I = i / SYM2_T, r = i - I * SYM2_T;
+    const int64_t u0 = sym_base(I, f.nt) * f.Q, u1 = (sym_base(I, f.nt) + (f.nt - I)) * f.Q;
+    float gx = 0.f, gy = 0.f, gz = 0.f, gm = 0.f;
+    for (int64_t u = u0; u < u1; ++u) {
+        const float4 v = f.rowpart[u * SYM2_T + r];
+        gx += v.x; gy += v.y; gz += v.z; gm += v.w;
+    }
+    for (int64_t I2 = 0; I2 <= I; ++I2) {
+        const float4 v = f.colpart[(sym_base(I2, f.nt) + (I - I2)) * SYM2_T + r];
+        gx += v.x; gy += v.y; gz += v.z; gm += v.w;
+    }
+    gx *= f.G; gy *= f.G; gz *= f.G; gm *= f.G;
+    f.lm[i] += gm;
+    const float4 lx = f.lx[i];
+    const float tx = lx.x + gx, ty = lx.y + gy, tz = lx.z + gz;
+    if (f.prime) {
+        f.lx[i] = make_float4(tx, ty, tz, 0.f);
+        return;
+    }
+    const float4 lv = f.lv[i];
+    const float hx = __fmaf_rn(f.dt, tx, lv.x), hy = __fmaf_rn(f.dt, ty, lv.y), hz = __fmaf_rn(f.dt, tz, lv.z);
+    f.lx[i] = make_float4(tx, ty, tz, 0.f);
+    f.lv[i] = make_float4(hx, hy, hz, 0.f);
+    f.la[i] = make_float4(f.h * hx, f.h * hy, f.h * hz, 0.f);
+}
+
 struct SymFix {
     const float4 *__restrict__ rowpart;
     const float4 *__restrict__ colpart;
@@ -398,6 +636,18 @@ __global__ void adjoint_sym_fixup_kernel(SymFix f) {
 // Symmetric scratch above this size falls back to the per-target kernel.
 constexpr int64_t SYM_MAX_BYTES = 3LL << 30;
 
+// Grows the handle's symmetric scratch to at least need float4 elements.
+static int ensure_sym(gb_direct_t *h, int64_t need) {
+    if (need <= h->sym_cap) return GB_OK;
+    if (h->sym) cudaFree(h->sym);
+    h->sym = nullptr;
+    h->sym_cap = 0;
+    if (cudaMalloc(&h->sym, sizeof(float4) * need) != cudaSuccess)
+        return fail(GB_ENOMEM, "symmetric adjoint scratch (%lld bytes)", (long long)(need * 16));
+    h->sym_cap = need;
+    return GB_OK;
+}
+
 }  // namespace gb
 
 using namespace gb;
@@ -417,6 +667,57 @@ extern "C" int gb_adjoint_step(gb_direct_t *h, const float *xm, float *lx, float
     if (!lm) return fail(GB_EINVAL, "lm is NULL");
     if (!(eps2 > 0.f)) return fail(GB_EINVAL, "eps2 must be > 0");
     cudaStream_t s = (cudaStream_t)stream;
+    if (h->adj_variant == 2) {
+        const int64_t nt = (n + SYM2_T - 1) / SYM2_T, NP = nt * (nt + 1) / 2;
+        int occs = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occs, adjoint_vjp_sym2_kernel<1>, SYM2_WARPS * 32, 0);
+        const int64_t slots = (int64_t)h->sms * std::max(occs, 1);
+        // Source slices per tile pair: enough units that the last ones are a
+        // small share of each CTA's work.
+        int Q = 1;
+        while (Q < 4 && NP * Q < 16 * slots) Q *= 2;
+        const int64_t NU = NP * Q, P = std::min(slots, NU);
+        const int64_t need = NU * SYM2_T + NP * SYM2_T + 1;  // + the unit counter
+        if (need * (int64_t)sizeof(float4) <= SYM_MAX_BYTES) {
+            GB_TRY(ensure_sym(h, need));
+            Sym2Args a;
+            a.xm = (const float4 *)xm;
+            a.lv = (const float4 *)lv;
+            a.la = (const float4 *)la;
+            a.rowpart = h->sym;
+            a.colpart = h->sym + NU * SYM2_T;
+            a.counter = (unsigned long long *)(h->sym + need - 1);
+            a.n = n;
+            a.nt = nt;
+            a.NP = NP;
+            a.eps2 = eps2;
+            a.h = 0.5f * dt;
+            a.prime = prime ? 1 : 0;
+            GB_CUDA_TRY(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), s));
+            if (Q == 1) adjoint_vjp_sym2_kernel<1><<<(unsigned)P, SYM2_WARPS * 32, 0, s>>>(a);
+            else if (Q == 2) adjoint_vjp_sym2_kernel<2><<<(unsigned)P, SYM2_WARPS * 32, 0, s>>>(a);
+            else adjoint_vjp_sym2_kernel<4><<<(unsigned)P, SYM2_WARPS * 32, 0, s>>>(a);
+            GB_CUDA_TRY(cudaGetLastError());
+            Sym2Fix f;
+            f.rowpart = a.rowpart;
+            f.colpart = a.colpart;
+            f.lx = (float4 *)lx;
+            f.lv = (float4 *)lv;
+            f.la = (float4 *)la;
+            f.lm = lm;
+            f.n = n;
+            f.nt = nt;
+            f.Q = Q;
+            f.G = G;
+            f.h = 0.5f * dt;
+            f.dt = dt;
+            f.prime = a.prime;
+            adjoint_sym2_fixup_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(f);
+            GB_CUDA_TRY(cudaGetLastError());
+            h->launches += 2;
+            return GB_OK;
+        }
+    }
     if (h->adj_variant == 1) {
         const int64_t nt = (n + SYM_T - 1) / SYM_T, NP = nt * (nt + 1) / 2;
         int occs = 0;
@@ -424,14 +725,7 @@ extern "C" int gb_adjoint_step(gb_direct_t *h, const float *xm, float *lx, float
         const int64_t P = std::max<int64_t>(1, std::min<int64_t>((int64_t)h->sms * std::max(occs, 1), NP));
         const int64_t need = (nt + P) * SYM_T + NP * SYM_T;
         if (need * (int64_t)sizeof(float4) <= SYM_MAX_BYTES) {
-            if (need > h->sym_cap) {
-                if (h->sym) cudaFree(h->sym);
-                h->sym = nullptr;
-                h->sym_cap = 0;
-                if (cudaMalloc(&h->sym, sizeof(float4) * need) != cudaSuccess)
-                    return fail(GB_ENOMEM, "symmetric adjoint scratch (%lld bytes)", (long long)(need * 16));
-                h->sym_cap = need;
-            }
+            GB_TRY(ensure_sym(h, need));
             SymArgs a;
             a.xm = (const float4 *)xm;
             a.lv = (const float4 *)lv;
@@ -515,9 +809,9 @@ extern "C" int gb_adjoint_step(gb_direct_t *h, const float *xm, float *lx, float
     return GB_OK;
 }
 
-extern "C" int gb_adjoint_set_variant(gb_direct_t *h, int symmetric) {
+extern "C" int gb_adjoint_set_variant(gb_direct_t *h, int variant) {
     if (!h) return fail(GB_EINVAL, "handle is NULL");
-    if (symmetric != 0 && symmetric != 1) return fail(GB_EINVAL, "symmetric must be 0 or 1");
-    h->adj_variant = symmetric;
+    if (variant < 0 || variant > 2) return fail(GB_EINVAL, "variant must be 0, 1 or 2 (got %d)", variant);
+    h->adj_variant = variant;
     return GB_OK;
 }

@@ -598,7 +598,7 @@ extern "C" int gb_direct_create(gb_direct_t **out, int64_t n_max) {
     h->warps = 8;
     h->ctas_per_sm = 0;
     h->packed = 0;
-    h->adj_variant = 1;
+    h->adj_variant = 2;
     int st = ensure_partials(h, max_partials(h, n_max));
     if (st == GB_OK && cudaMalloc(&h->phi, sizeof(float) * n_max) != cudaSuccess)
         st = fail(GB_ENOMEM, "phi scratch");

@@ -119,5 +119,5 @@ struct gb_direct {
     uint64_t launches;  // kernels launched by this handle (host count)
     float4 *sym;        // symmetric adjoint partials (allocated on first use)
     int64_t sym_cap;    // float4 elements
-    int adj_variant;    // 1: symmetric pair evaluation, 0: one pass per target
+    int adj_variant;    // 2: symmetric packed, 1: symmetric scalar, 0: one pass per target
 };

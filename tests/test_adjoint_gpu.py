@@ -62,14 +62,19 @@ def _loss(x, v, target):
     return ((x - target) ** 2).mean() + 1e-6 * (v ** 2).mean()
 
 
-def _device_grads(p, v, m, target, nsteps, every, dev, symmetric=True):
+# Adjoint pair evaluations: (symmetric, packed) arguments of adjoint.simulate.
+FORMS = {"packed": (True, True), "scalar": (True, False), "per_target": (False, True)}
+
+
+def _device_grads(p, v, m, target, nsteps, every, dev, form="packed"):
     adj, _, grav = _mods()
+    symmetric, packed = FORMS[form]
     x0 = torch.tensor(p, dtype=torch.float32, device=dev, requires_grad=True)
     v0 = torch.tensor(v, dtype=torch.float32, device=dev, requires_grad=True)
     m0 = torch.tensor(m, dtype=torch.float32, device=dev, requires_grad=True)
     solver = grav.DirectGravity(p.shape[0], dev)
     xT, vT = adj.simulate(x0, v0, m0, G=G, softening=EPS, dt=DT, nsteps=nsteps,
-                          checkpoint_every=every, solver=solver, symmetric=symmetric)
+                          checkpoint_every=every, solver=solver, symmetric=symmetric, packed=packed)
     loss = _loss(xT.double(), vT.double(), torch.tensor(target, device=dev))
     loss.backward()
     return [t.grad.double().cpu().numpy() for t in (x0, v0, m0)], float(loss.detach())
@@ -89,43 +94,75 @@ def _rel(a, b):
     return np.linalg.norm(a - b) / np.linalg.norm(b)
 
 
-@pytest.mark.parametrize("symmetric", [True, False])
-def test_adjoint_matches_dense_autograd(cuda_dev, symmetric):
+@pytest.mark.parametrize("form", list(FORMS))
+def test_adjoint_matches_dense_autograd(cuda_dev, form):
     p, v, m, target = _problem()
-    g_dev, l_dev = _device_grads(p, v, m, target, 200, 20, cuda_dev, symmetric)
+    g_dev, l_dev = _device_grads(p, v, m, target, 200, 20, cuda_dev, form)
     g_ref, l_ref = _dense_grads(p, v, m, target, 200)
     assert abs(l_dev - l_ref) < 1e-4 * abs(l_ref)
     for name, a, b in zip(("x0", "v0", "m"), g_dev, g_ref):
         assert _rel(a, b) < 2e-3, (name, _rel(a, b))
 
 
-@pytest.mark.parametrize("symmetric", [True, False])
-def test_adjoint_ragged_tiles_match_dense(cuda_dev, symmetric):
-    """N = 520: two full 256-particle tiles and a partial one (diagonal,
-    off-diagonal and padded tile pairs of the symmetric form)."""
+@pytest.mark.parametrize("form", list(FORMS))
+def test_adjoint_ragged_tiles_match_dense(cuda_dev, form):
+    """N = 520: diagonal, off-diagonal and padded tile pairs of the symmetric
+    forms (two full 256-particle tiles and a partial one; one full
+    512-particle tile and a partial one)."""
     p, v, m, target = _problem(n=520, seed=13)
-    g_dev, _ = _device_grads(p, v, m, target, 30, 10, cuda_dev, symmetric)
+    g_dev, _ = _device_grads(p, v, m, target, 30, 10, cuda_dev, form)
     g_ref, _ = _dense_grads(p, v, m, target, 30)
     for name, a, b in zip(("x0", "v0", "m"), g_dev, g_ref):
         assert _rel(a, b) < 2e-3, (name, _rel(a, b))
 
 
-@pytest.mark.parametrize("symmetric", [True, False])
-def test_checkpoint_interval_does_not_change_gradients(cuda_dev, symmetric):
+@pytest.mark.parametrize("form", list(FORMS))
+def test_checkpoint_interval_does_not_change_gradients(cuda_dev, form):
     p, v, m, target = _problem(n=300, seed=5)
-    base, _ = _device_grads(p, v, m, target, 24, 24, cuda_dev, symmetric)
+    base, _ = _device_grads(p, v, m, target, 24, 24, cuda_dev, form)
     for every in (1, 5, 7):
-        g, _ = _device_grads(p, v, m, target, 24, every, cuda_dev, symmetric)
+        g, _ = _device_grads(p, v, m, target, 24, every, cuda_dev, form)
         for a, b in zip(g, base):
             assert np.array_equal(a, b)
 
 
-def test_symmetric_matches_per_target_form(cuda_dev):
+@pytest.mark.parametrize("form", ["packed", "scalar"])
+def test_symmetric_matches_per_target_form(cuda_dev, form):
     p, v, m, target = _problem(n=3000, seed=17)
-    g1, _ = _device_grads(p, v, m, target, 10, 5, cuda_dev, True)
-    g0, _ = _device_grads(p, v, m, target, 10, 5, cuda_dev, False)
+    g1, _ = _device_grads(p, v, m, target, 10, 5, cuda_dev, form)
+    g0, _ = _device_grads(p, v, m, target, 10, 5, cuda_dev, "per_target")
     for a, b in zip(g1, g0):
         assert _rel(a, b) < 1e-4
+
+
+@pytest.mark.parametrize("n", [65536, 80000])
+def test_adjoint_step_forms_agree_at_large_n(cuda_dev, n):
+    """One backward step of each pair evaluation on the same inputs.  The
+    packed form splits tile pairs into 2 source slices at N = 65,536 and
+    none at N = 80,000 (the small cases above use 4 slices)."""
+    _, ic, grav = _mods()
+    lib = importlib.import_module(PKG_NAME + "._lib")
+    p, _, m = ic.exponential_disk(n, total_mass=5.0, seed=2)
+    xm = torch.zeros((n, 4), dtype=torch.float32, device=cuda_dev)
+    xm[:, :3] = torch.tensor(p, device=cuda_dev)
+    xm[:, 3] = torch.tensor(m, device=cuda_dev)
+    gen = torch.Generator().manual_seed(4)
+    base = [torch.randn((n, 4), generator=gen).to(cuda_dev) for _ in range(3)]
+    solver = grav.DirectGravity(n, cuda_dev)
+    stream = torch.cuda.current_stream(cuda_dev).cuda_stream
+    out = {}
+    for variant in (2, 1, 0):
+        lib.call("gb_adjoint_set_variant", solver.handle, variant)
+        lx, lv, la = [b.clone() for b in base]
+        lm = torch.zeros(n, dtype=torch.float32, device=cuda_dev)
+        lib.call("gb_adjoint_step", solver.handle, xm.data_ptr(), lx.data_ptr(), lv.data_ptr(), la.data_ptr(),
+                 lm.data_ptr(), n, G, EPS * EPS, DT, 0, stream)
+        out[variant] = [t.double().cpu().numpy() for t in (lx[:, :3], lv[:, :3], la[:, :3], lm)]
+    solver.close()
+    for variant in (2, 1):
+        for a, b in zip(out[variant], out[0]):
+            assert np.all(np.isfinite(a))
+            assert _rel(a, b) < 1e-5, (variant, _rel(a, b))
 
 
 def test_adjoint_matches_fp64_finite_differences(cuda_dev, orc):
