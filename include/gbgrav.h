@@ -259,6 +259,45 @@ int gb_adjoint_set_variant(gb_direct_t *h, int variant);
 int gb_direct_acc_noalloc(const float *xm, float *acc, int64_t n, float G,
                           float eps2, int flags, void *stream);
 
+/* ---------------------------------------------- analytic galaxy potential */
+/* The fixed analytic potential that the living-galaxy and gas-disk engines
+ * add after self-gravity (grav_analytic, core/living_galaxy_engine.py:
+ * 124-151; add_analytic, core/gas_disk_engine.py:54-81): a Miyamoto-Nagai
+ * disk (mass M_d, scale lengths a, b), a Hernquist (is_hernquist = 1) or
+ * Plummer (0) halo (M_h, a_h) and, when smbh_mass > 0, a point mass at the
+ * origin softened as in the reference.  Same fields as the engines' `pot`
+ * dict; masses in the units of G.  Evaluated in FP32 with G folded into the
+ * masses. */
+typedef struct gb_potential {
+    double M_d, a, b, M_h, a_h, smbh_mass;
+    int32_t is_hernquist;
+    int32_t reserved; /* must be 0 */
+} gb_potential_t;
+
+/* acc += the potential's acceleration at every particle (acc = it without
+ * GB_ACCUMULATE): grav_analytic / add_analytic, for callers whose
+ * self-gravity comes from elsewhere. */
+int gb_analytic_acc(const float *xm, float *acc, int64_t n, float G,
+                    const gb_potential_t *pot, int flags, void *stream);
+
+/* gb_direct_acc with the potential added in the same pass that writes the
+ * results (the fix-up).  With GB_ACCUMULATE this is add_grav_ext
+ * (core/gas_disk_engine.py:20-51), and grav_self_direct followed by
+ * grav_analytic (core/living_galaxy_engine.py:1016-1027).  pot = NULL gives
+ * gb_direct_acc. */
+int gb_direct_acc_ext(gb_direct_t *h, const float *xm, float *acc, int64_t n,
+                      float G, float eps2, const gb_potential_t *pot,
+                      int flags, void *stream);
+
+/* gb_bh_accel with the potential added in the traversal's epilogue: the
+ * tree branch of the engines' force pass, BarnesHut.compute + add_field /
+ * add_acc + add_analytic / grav_analytic (core/gas_disk_engine.py:216-225,
+ * core/living_galaxy_engine.py:1013-1027), with GB_ACCUMULATE.  pot = NULL
+ * gives gb_bh_accel. */
+int gb_bh_accel_ext(gb_bh_t *h, float *acc, float theta, float eps2, float G,
+                    int max_stack, const gb_potential_t *pot, int flags,
+                    void *stream);
+
 /* ------------------------------------------------------------ calibration */
 /* Launches an FP32 FMA-throughput kernel (packed = 1: .f32x2 form) on
  * `stream`; *flops receives the FLOP count of the launch, which the caller

@@ -140,6 +140,75 @@ void orc_kdk_direct(double *pos, double *vel, double *acc, const double *mass,
     }
 }
 
+/* ----------------------------------------------------- analytic potential
+ * The analytic galaxy potential of grav_analytic
+ * (core/living_galaxy_engine.py:124-151) and add_analytic
+ * (core/gas_disk_engine.py:54-81), added to av in the reference's order:
+ * Miyamoto-Nagai disk, then the Hernquist (hern = 1) or Plummer halo, then
+ * the softened central point mass when smbh > 0. */
+static void analytic_add(const double *p, double G, double M_d, double a,
+                         double b, double M_h, double a_h, int hern,
+                         double smbh, double *av) {
+    const double x = p[0], y = p[1], z = p[2];
+    const double R2 = x * x + y * y;
+    const double S = sqrt(z * z + b * b);
+    const double aS = a + S;
+    const double invD3 = pow(R2 + aS * aS, -1.5);
+    const double gmd = -G * M_d;
+    av[0] += gmd * x * invD3;
+    av[1] += gmd * y * invD3;
+    av[2] += gmd * z * aS * invD3 / S;
+    if (hern == 1) {
+        const double r = sqrt(x * x + y * y + z * z);
+        const double rs = r > 1e-6 ? r : 1e-6;
+        const double c = -(G * M_h / (pow(rs + a_h, 2.0) * rs));
+        av[0] += c * x;
+        av[1] += c * y;
+        av[2] += c * z;
+    } else {
+        const double rh = R2 + z * z + a_h * a_h;
+        const double c = -(G * M_h * pow(rh, -1.5));
+        av[0] += c * x;
+        av[1] += c * y;
+        av[2] += c * z;
+    }
+    if (smbh > 0.0) {
+        const double rs = sqrt(x * x + y * y + z * z) + 1e-6;
+        const double c = -(G * smbh / (rs * rs * rs));
+        av[0] += c * x;
+        av[1] += c * y;
+        av[2] += c * z;
+    }
+}
+
+/* grav_analytic / add_analytic: acc[i] += av (analytic part only). */
+void orc_analytic_acc(const double *pos, double *acc, int64_t n, double G,
+                      double M_d, double a, double b, double M_h, double a_h,
+                      int hern, double smbh) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        double av[3] = {0.0, 0.0, 0.0};
+        analytic_add(pos + 3 * i, G, M_d, a, b, M_h, a_h, hern, smbh, av);
+        for (int k = 0; k < 3; ++k) acc[3 * i + k] += av[k];
+    }
+}
+
+/* add_grav_ext (core/gas_disk_engine.py:20-51): av = softened direct
+ * self-gravity over all j (as compute_acc_direct), then the analytic terms,
+ * then acc[i] += av. */
+void orc_grav_ext_acc(const double *pos, const double *mass, double *acc,
+                      int64_t n, double G, double eps2, double M_d, double a,
+                      double b, double M_h, double a_h, int hern,
+                      double smbh) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        double av[3];
+        direct_one(pos, mass, n, G, eps2, i, av);
+        analytic_add(pos + 3 * i, G, M_d, a, b, M_h, a_h, hern, smbh, av);
+        for (int k = 0; k < 3; ++k) acc[3 * i + k] += av[k];
+    }
+}
+
 /* ------------------------------------------------------------------ Morton
  * core/solvers/barnes_hut.py:27-46.  lo = per-axis min, span = the largest
  * per-axis extent (1.0 if not > 0), scale = (2^bits-1)/(span*1.0000001),

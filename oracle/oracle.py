@@ -73,6 +73,8 @@ def _declare(L):
     L.orc_potential_energy.argtypes = [P, P, I64, D, D]
     L.orc_potential_energy.restype = D
     L.orc_kdk_direct.argtypes = [P, P, P, P, I64, D, D, D, I64]
+    L.orc_analytic_acc.argtypes = [P, P, I64, D, D, D, D, D, D, I32, D]
+    L.orc_grav_ext_acc.argtypes = [P, P, P, I64, D, D, D, D, D, D, D, I32, D]
     L.orc_morton.argtypes = [P, I64, I32, P, P, P]
     L.orc_stable_argsort_u64.argtypes = [P, I64, P]
     L.orc_build_radix.argtypes = [P, I32, P, P, P]
@@ -142,6 +144,30 @@ def kdk_direct(pos, vel, acc, mass, G, eps2, dt, nsteps):
     lib().orc_kdk_direct(_p(pos), _p(vel), _p(acc), _p(mass), pos.shape[0], G,
                          eps2, dt, nsteps)
     return pos, vel, acc
+
+
+# ------------------------------------------------------ analytic potential
+def _pot_args(pot):
+    return (float(pot["M_d"]), float(pot["a"]), float(pot["b"]), float(pot["M_h"]),
+            float(pot["a_h"]), int(pot.get("is_hernquist", 0)), float(pot.get("smbh_mass", 0.0)))
+
+
+def analytic_acc(pos, G, pot, acc=None):
+    """acc + the analytic disk/halo/point-mass acceleration (grav_analytic,
+    add_analytic); acc defaults to zero.  Returns a new (n, 3) array."""
+    pos = _f64(pos, (-1, 3))
+    out = np.zeros_like(pos) if acc is None else _f64(acc, (-1, 3)).copy()
+    lib().orc_analytic_acc(_p(pos), _p(out), pos.shape[0], G, *_pot_args(pot))
+    return out
+
+
+def grav_ext_acc(pos, mass, G, eps2, pot, acc=None):
+    """acc + direct self-gravity + the analytic potential (add_grav_ext)."""
+    pos = _f64(pos, (-1, 3))
+    mass = _f64(mass, (-1,))
+    out = np.zeros_like(pos) if acc is None else _f64(acc, (-1, 3)).copy()
+    lib().orc_grav_ext_acc(_p(pos), _p(mass), _p(out), pos.shape[0], G, eps2, *_pot_args(pot))
+    return out
 
 
 # ------------------------------------------------------------------ Morton

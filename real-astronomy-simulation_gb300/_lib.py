@@ -54,6 +54,14 @@ class Diag(ctypes.Structure):
 
 
 # name -> (restype, argtypes)
+class Potential(ctypes.Structure):
+    """gb_potential_t: the analytic galaxy potential (Miyamoto-Nagai disk,
+    Hernquist or Plummer halo, optional central point mass)."""
+    _fields_ = [("M_d", ctypes.c_double), ("a", ctypes.c_double), ("b", ctypes.c_double),
+                ("M_h", ctypes.c_double), ("a_h", ctypes.c_double), ("smbh_mass", ctypes.c_double),
+                ("is_hernquist", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
 SIGNATURES = {
     "gb_last_error_string": (ctypes.c_char_p, []),
     "gb_version": (I32, []),
@@ -92,6 +100,9 @@ SIGNATURES = {
     "gb_batch_launch_count": (ctypes.c_uint64, [P]),
     "gb_adjoint_step": (I32, [P, P, P, P, P, P, I64, F32, F32, F32, I32, P]),
     "gb_adjoint_set_variant": (I32, [P, I32]),
+    "gb_analytic_acc": (I32, [P, P, I64, F32, P, I32, P]),
+    "gb_direct_acc_ext": (I32, [P, P, P, I64, F32, F32, P, I32, P]),
+    "gb_bh_accel_ext": (I32, [P, P, F32, F32, F32, I32, P, I32, P]),
 }
 
 _lib = None

@@ -488,6 +488,7 @@ struct TravArgs {
     int max_stack;
     int accumulate;
     unsigned long long *diag;
+    ExtPot pot;  // analytic potential added in the epilogue (pot.on)
 };
 
 struct Lane {
@@ -732,8 +733,9 @@ bh_traverse_kernel(TravArgs a) {
         unpack2(L[q].AX, xl, xr);
         unpack2(L[q].AY, yl, yr);
         unpack2(L[q].AZ, zl, zr);
-        const float gx = a.G * (L[q].ax + (xl + xr)), gy = a.G * (L[q].ay + (yl + yr)),
-                    gz = a.G * (L[q].az + (zl + zr));
+        float gx = a.G * (L[q].ax + (xl + xr)), gy = a.G * (L[q].ay + (yl + yr)),
+              gz = a.G * (L[q].az + (zl + zr));
+        if (a.pot.on) ext_acc_add(a.pot, L[q].px, L[q].py, L[q].pz, gx, gy, gz);
         if (KDK) {
             const float4 vh = a.vel[p];
             a.vel[p] = make_float4(kick(vh.x, gx, a.h), kick(vh.y, gy, a.h), kick(vh.z, gz, a.h), vh.w);
@@ -997,7 +999,7 @@ static int check_ptr(const void *p, const char *name) {
 }
 
 static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float theta, float eps2, float G, float dt, int max_stack,
-                    int flags, bool kdk, cudaStream_t s, int slot) {
+                    int flags, bool kdk, cudaStream_t s, int slot, const ExtPot &pot = ExtPot{}) {
     const int64_t n = h->n;
     if (n <= 0) return GB_OK;
     TravArgs a;
@@ -1015,6 +1017,7 @@ static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float theta, float eps
     a.max_stack = max_stack;
     a.accumulate = (flags & GB_ACCUMULATE) ? 1 : 0;
     a.diag = h->diag;
+    a.pot = pot;
     const int tpl = h->tpl;
     const int64_t warps = (n + 32 * tpl - 1) / (32 * tpl);
     const unsigned grid = (unsigned)((warps + TRAV_WARPS - 1) / TRAV_WARPS);
@@ -1063,6 +1066,19 @@ extern "C" int gb_bh_accel(gb_bh_t *h, float *acc, float theta, float eps2, floa
     GB_TRY(check_params(theta, eps2, max_stack));
     return traverse(h, (float4 *)acc, nullptr, theta, eps2, G, 0.f, max_stack, flags, false, (cudaStream_t)stream,
                     h->pending_slot);
+}
+
+extern "C" int gb_bh_accel_ext(gb_bh_t *h, float *acc, float theta, float eps2, float G, int max_stack,
+                               const gb_potential_t *pot, int flags, void *stream) {
+    if (!h) return fail(GB_EINVAL, "handle is NULL");
+    ExtPot ep;
+    GB_TRY(make_extpot(pot, G, &ep));
+    if (h->n < 0) return fail(GB_ENOTREADY, "gb_bh_accel_ext before gb_bh_build");
+    if (h->n == 0) return GB_OK;
+    GB_TRY(check_ptr(acc, "acc"));
+    GB_TRY(check_params(theta, eps2, max_stack));
+    return traverse(h, (float4 *)acc, nullptr, theta, eps2, G, 0.f, max_stack, flags, false, (cudaStream_t)stream,
+                    h->pending_slot, ep);
 }
 
 extern "C" int gb_bh_compute(gb_bh_t *h, const float *xm, float *acc, int64_t n, float theta, float eps2, float G,

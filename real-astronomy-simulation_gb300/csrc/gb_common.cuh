@@ -122,4 +122,55 @@ __device__ __forceinline__ float4 predict_xm(float4 xm, float4 v, float4 a, floa
 
 __device__ __forceinline__ float4 ldg4(const float4 *p) { return __ldg(p); }
 
+// ------------------------------------------------ analytic external potential
+// The analytic galaxy potential that grav_analytic
+// (core/living_galaxy_engine.py:124-151), add_analytic
+// (core/gas_disk_engine.py:54-81) and add_grav_ext (:20-51) add after
+// self-gravity, in FP32 with G folded into the masses: a Miyamoto-Nagai disk
+// (gmd, a, b), a Hernquist (hernquist = 1) or Plummer halo (gmh, ah) and a
+// softened central point mass (gmbh, when smbh = 1).
+struct ExtPot {
+    float gmd, a, b, gmh, ah, gmbh;
+    int hernquist, smbh, on;
+};
+
+// Host: checks *pot (NULL gives on = 0) and folds G into the masses.
+int make_extpot(const gb_potential_t *pot, float G, ExtPot *out);
+
+// Adds the potential's acceleration at (x, y, z) to (ax, ay, az).  Same terms
+// and guards as the reference: r clamped to 1e-6 in the Hernquist term,
+// r + 1e-6 in the point-mass term.
+__device__ __forceinline__ void ext_acc_add(const ExtPot &p, float x, float y, float z, float &ax, float &ay,
+                                            float &az) {
+    const float R2 = x * x + y * y;
+    const float S = sqrtf(z * z + p.b * p.b);
+    const float aS = p.a + S;
+    const float invD = rsqrtf(R2 + aS * aS);
+    const float cd = -p.gmd * (invD * invD * invD);
+    float ex = cd * x, ey = cd * y, ez = cd * z * aS / S;
+    const float r = sqrtf(R2 + z * z);
+    float ch;
+    if (p.hernquist) {
+        const float rs = fmaxf(r, 1e-6f);
+        const float q = rs + p.ah;
+        ch = -p.gmh / (q * q * rs);
+    } else {
+        const float invH = rsqrtf(R2 + z * z + p.ah * p.ah);
+        ch = -p.gmh * (invH * invH * invH);
+    }
+    ex += ch * x;
+    ey += ch * y;
+    ez += ch * z;
+    if (p.smbh) {
+        const float rs = r + 1e-6f;
+        const float cb = -p.gmbh / (rs * rs * rs);
+        ex += cb * x;
+        ey += cb * y;
+        ez += cb * z;
+    }
+    ax += ex;
+    ay += ey;
+    az += ez;
+}
+
 }  // namespace gb

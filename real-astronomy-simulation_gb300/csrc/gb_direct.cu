@@ -333,6 +333,7 @@ struct FixArgs {
     int smax;
     float G, h, dt;
     int accumulate;
+    ExtPot pot;  // ACC: analytic potential added to the result (pot.on)
 };
 
 template <int MODE>
@@ -363,8 +364,12 @@ __global__ void direct_fixup_kernel(FixArgs f) {
         f.phi[i] = tx;
         return;
     }
-    const float4 an = make_float4(f.G * tx, f.G * ty, f.G * tz, 0.f);
+    float4 an = make_float4(f.G * tx, f.G * ty, f.G * tz, 0.f);
     if (MODE == MODE_ACC) {
+        if (f.pot.on) {
+            const float4 x = f.xm[i];
+            ext_acc_add(f.pot, x.x, x.y, x.z, an.x, an.y, an.z);
+        }
         if (f.accumulate) {
             float4 o = f.acc[i];
             o.x += an.x; o.y += an.y; o.z += an.z;
@@ -640,7 +645,8 @@ extern "C" int gb_direct_set_tiles(gb_direct_t *h, int k, int warps, int ctas_pe
 }
 
 static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, float4 *acc, float *phi,
-                      int64_t n, float G, float eps2, float dt, int flags, cudaStream_t s) {
+                      int64_t n, float G, float eps2, float dt, int flags, cudaStream_t s,
+                      const ExtPot &pot = ExtPot{}) {
     DirectPlan pl;
     const int np = mode == MODE_PHI ? 1 : h->np;
     const int64_t ctas = grid_ctas(h, h->np, h->warps, h->packed);
@@ -696,6 +702,7 @@ static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, f
     f.h = 0.5f * dt;
     f.dt = dt;
     f.accumulate = (flags & GB_ACCUMULATE) ? 1 : 0;
+    f.pot = pot;
     const unsigned fb = 256, fg = (unsigned)((n + fb - 1) / fb);
     if (mode == MODE_ACC) direct_fixup_kernel<MODE_ACC><<<fg, fb, 0, s>>>(f);
     else if (mode == MODE_KDK) direct_fixup_kernel<MODE_KDK><<<fg, fb, 0, s>>>(f);
@@ -721,6 +728,19 @@ extern "C" int gb_direct_acc(gb_direct_t *h, const float *xm, float *acc, int64_
     if (!(eps2 > 0.f)) return fail(GB_EINVAL, "eps2 must be > 0");
     return run_direct(h, MODE_ACC, (const float4 *)xm, nullptr, (float4 *)acc, nullptr, n, G, eps2, 0.f,
                       flags, (cudaStream_t)stream);
+}
+
+extern "C" int gb_direct_acc_ext(gb_direct_t *h, const float *xm, float *acc, int64_t n, float G, float eps2,
+                                 const gb_potential_t *pot, int flags, void *stream) {
+    GB_TRY(check_n(h, n));
+    ExtPot ep;
+    GB_TRY(make_extpot(pot, G, &ep));
+    if (n == 0) return GB_OK;
+    GB_TRY(check_xm(xm, "xm"));
+    GB_TRY(check_xm(acc, "acc"));
+    if (!(eps2 > 0.f)) return fail(GB_EINVAL, "eps2 must be > 0");
+    return run_direct(h, MODE_ACC, (const float4 *)xm, nullptr, (float4 *)acc, nullptr, n, G, eps2, 0.f,
+                      flags, (cudaStream_t)stream, ep);
 }
 
 extern "C" int gb_direct_kdk(gb_direct_t *h, float *xm, float *vel, float *acc, int64_t n, float G, float eps2,
@@ -876,6 +896,7 @@ extern "C" int gb_direct_acc_noalloc(const float *xm, float *acc, int64_t n, flo
     f.h = 0.f;
     f.dt = 0.f;
     f.accumulate = (flags & GB_ACCUMULATE) ? 1 : 0;
+    f.pot = ExtPot{};
     direct_fixup_kernel<MODE_ACC><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(f);
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;

@@ -1,4 +1,5 @@
 // Host runtime shared by every entry point: error reporting and device info.
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 
@@ -21,6 +22,27 @@ int fail(int code, const char *fmt, ...) {
     vsnprintf(g_err, sizeof(g_err), fmt, ap);
     va_end(ap);
     return code;
+}
+
+int make_extpot(const gb_potential_t *pot, float G, ExtPot *out) {
+    *out = ExtPot{};
+    if (!pot) return GB_OK;
+    const double v[] = {pot->M_d, pot->a, pot->b, pot->M_h, pot->a_h, pot->smbh_mass};
+    for (double x : v)
+        if (!std::isfinite(x)) return fail(GB_EINVAL, "potential parameters must be finite");
+    if (pot->reserved != 0) return fail(GB_EINVAL, "gb_potential_t.reserved must be 0");
+    if (pot->is_hernquist != 0 && pot->is_hernquist != 1)
+        return fail(GB_EINVAL, "is_hernquist must be 0 or 1 (got %d)", (int)pot->is_hernquist);
+    out->gmd = (float)((double)G * pot->M_d);
+    out->a = (float)pot->a;
+    out->b = (float)pot->b;
+    out->gmh = (float)((double)G * pot->M_h);
+    out->ah = (float)pot->a_h;
+    out->gmbh = (float)((double)G * pot->smbh_mass);
+    out->hernquist = pot->is_hernquist;
+    out->smbh = pot->smbh_mass > 0.0 ? 1 : 0;
+    out->on = 1;
+    return GB_OK;
 }
 
 int num_sms() {

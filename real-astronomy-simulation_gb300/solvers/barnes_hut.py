@@ -62,6 +62,10 @@ class BarnesHut:
             raise ValueError(f"BarnesHut was sized for n={self.n}, got {n}")
         return n
 
+    @property
+    def handle(self):
+        return self._h
+
     def build(self, xm: torch.Tensor) -> None:
         self._last_n = self._n(xm)
         _lib.call("gb_bh_build", self._h, ptr(xm, "xm"), self._last_n, stream_handle(self.device))

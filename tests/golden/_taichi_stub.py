@@ -24,13 +24,30 @@ import numpy as np
 
 
 class Field(np.ndarray):
-    """numpy array with Taichi's host-transfer methods."""
+    """numpy array with Taichi's host-transfer methods; a row of a vector
+    field also has Taichi's ``.x/.y/.z`` and ``.norm()``."""
 
     def from_numpy(self, arr):
         self[...] = np.asarray(arr).reshape(self.shape)
 
     def to_numpy(self):
         return np.array(self)
+
+    @property
+    def x(self):
+        return np.float64(self[0])
+
+    @property
+    def y(self):
+        return np.float64(self[1])
+
+    @property
+    def z(self):
+        return np.float64(self[2])
+
+    def norm(self):
+        x, y, z = (np.float64(self[k]) for k in range(3))
+        return np.sqrt(x * x + y * y + z * z)
 
 
 def _field(dtype, shape):
@@ -66,6 +83,8 @@ def make_module() -> types.ModuleType:
     ti.template = lambda: None
     ti.static = lambda x: x
     ti.sqrt = math.sqrt
+    ti.max = max
+    ti.min = min
     ti.init = lambda **kw: None
     ti.Vector = _Vector()
     ti.field = lambda dtype, shape: _field(dtype, shape)

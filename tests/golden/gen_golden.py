@@ -41,11 +41,14 @@ def _load_reference(ref_root: str):
     import core.ic.plummer as plummer
     import core.ic.disk as disk
     import core.engine as engine
+    import core.living_galaxy_engine as living
+    import core.gas_disk_engine as gasdisk
     # _accumulate: atomics -> in-place updates (the only source rewrite).
     src = _taichi_stub.rewrite_atomics(inspect.getsource(bh._accumulate))
     exec(compile(src, bh.__file__, "exec"), bh.__dict__)
     return dict(units=units, gravity=gravity, bh=bh, leapfrog=leapfrog,
-                plummer=plummer, disk=disk, engine=engine, stub=_taichi_stub)
+                plummer=plummer, disk=disk, engine=engine, living=living,
+                gasdisk=gasdisk, stub=_taichi_stub)
 
 
 def _f32(a):
@@ -232,12 +235,67 @@ def gen_engine_bh(R, out):
                             vel=eng.vel.to_numpy(), acc=eng.acc.to_numpy())
 
 
+# Potentials of the fixtures: the engines' default (core/gas_disk_engine.py:
+# 130), the giant-impact scenario's halo + black hole (core/scenarios.py:331)
+# and both together.
+POTENTIALS = {
+    "mn_plummer": dict(M_d=5.0, a=3.0, b=0.3, M_h=12.0, a_h=8.0,
+                       is_hernquist=0, smbh_mass=0.0),
+    "hernquist_smbh": dict(M_d=0.0, a=1.0, b=1.0, M_h=40.0, a_h=15.0,
+                           is_hernquist=1, smbh_mass=0.1),
+    "mn_hernquist_smbh": dict(M_d=5.0, a=3.0, b=0.3, M_h=40.0, a_h=15.0,
+                              is_hernquist=1, smbh_mass=0.1),
+}
+
+
+def gen_analytic(R, out):
+    """The analytic galaxy potential added after self-gravity:
+    grav_analytic (core/living_galaxy_engine.py:124-151), add_analytic
+    (core/gas_disk_engine.py:54-81) and add_grav_ext (self-gravity +
+    analytic, :20-51), each adding into an acc array that already holds
+    values.  Particle 0 sits at the origin and particle 1 on the z axis."""
+    lg, gd, stub, units = R["living"], R["gasdisk"], R["stub"], R["units"]
+    pos, mass = _disk_positions(R, 240, seed=31)
+    pos[0] = 0.0
+    pos[1, :2] = 0.0
+    n = pos.shape[0]
+    rng = np.random.default_rng(32)
+    acc0 = _f32(rng.normal(0.0, 1.0e4, (n, 3)))
+    eps2 = 0.05 ** 2
+    d = dict(pos=pos, mass=mass, acc0=acc0, G=units.G, eps2=eps2)
+    fp, fm = _field_from(stub, pos), _field_from(stub, mass)
+    for name, pot in POTENTIALS.items():
+        args = (pot["M_d"], pot["a"], pot["b"], pot["M_h"], pot["a_h"],
+                pot["is_hernquist"], pot["smbh_mass"])
+        for k, v in pot.items():
+            d[f"{name}_{k}"] = v
+        fa = _field_from(stub, acc0)
+        lg.grav_analytic(fp, fa, n, *args)
+        d[f"{name}_grav_analytic"] = fa.to_numpy()
+        fa = _field_from(stub, acc0)
+        gd.add_analytic(fp, fa, n, *args)
+        d[f"{name}_add_analytic"] = fa.to_numpy()
+        fa = _field_from(stub, acc0)
+        gd.add_grav_ext(fp, fm, fa, n, eps2, *args)
+        d[f"{name}_add_grav_ext"] = fa.to_numpy()
+    d["names"] = np.array(list(POTENTIALS))
+    out["analytic"] = d
+
+
+GENERATORS = (gen_plummer_ic, gen_direct, gen_engine_direct, gen_morton,
+              gen_bh, gen_engine_bh, gen_analytic)
+
+
 def main(argv):
+    """argv: [script, reference root, generator names...]; no names runs
+    every generator."""
     ref_root = argv[1] if len(argv) > 1 else "/root/reference"
     R = _load_reference(ref_root)
     out = {}
-    for fn in (gen_plummer_ic, gen_direct, gen_engine_direct, gen_morton,
-               gen_bh, gen_engine_bh):
+    wanted = set(argv[2:])
+    for fn in GENERATORS:
+        if wanted and fn.__name__ not in wanted:
+            continue
         t0 = time.time()
         fn(R, out)
         print(f"{fn.__name__}: {time.time() - t0:.1f}s", flush=True)

@@ -88,3 +88,20 @@ def test_state_contract():
     st = pkg.State.from_arrays(np.zeros((5, 3), np.float32), np.ones((5, 3)), np.ones(5))
     assert st.pos.dtype == np.float64 and st.ids.dtype == np.int64
     assert st.ptype.dtype == np.int32 and st.n == 5
+
+
+def test_potential_struct_layout_and_dict(pkg):
+    """gb_potential_t: six doubles then two int32 (56 bytes), filled from the
+    engines' `pot` dict."""
+    import ctypes
+    lib_mod = importlib.import_module(PKG_NAME + "._lib")
+    ext = importlib.import_module(PKG_NAME + ".solvers.external")
+    assert ctypes.sizeof(lib_mod.Potential) == 56
+    assert lib_mod.Potential.is_hernquist.offset == 48
+    p = ext.Potential.from_dict(dict(M_d=5.0, a=3.0, b=0.3, M_h=12.0, a_h=8.0))
+    c = p.to_c()
+    assert (c.M_d, c.a, c.b, c.M_h, c.a_h, c.smbh_mass, c.is_hernquist, c.reserved) == \
+        (5.0, 3.0, 0.3, 12.0, 8.0, 0.0, 0, 0)
+    q = ext.Potential.from_dict(dict(M_d=0.0, a=1.0, b=1.0, M_h=40.0, a_h=15.0, is_hernquist=1,
+                                     smbh_mass=0.1))
+    assert q.is_hernquist == 1 and q.smbh_mass == 0.1

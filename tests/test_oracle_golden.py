@@ -128,3 +128,21 @@ def test_engine_bh_matches_reference(orc):
         vel = vel + acc * (0.5 * dt)
     np.testing.assert_allclose(pos, g["pos"], rtol=1e-10, atol=1e-10)
     np.testing.assert_allclose(vel, g["vel"], rtol=1e-9, atol=1e-7)
+
+
+def _potential(g, name):
+    return {k: g[f"{name}_{k}"].item() for k in ("M_d", "a", "b", "M_h", "a_h", "is_hernquist", "smbh_mass")}
+
+
+@pytest.mark.parametrize("name", ["mn_plummer", "hernquist_smbh", "mn_hernquist_smbh"])
+def test_analytic_potential_matches_reference(orc, name):
+    """grav_analytic / add_analytic bit for bit; add_grav_ext to FP64
+    rounding of its self-gravity sum."""
+    g = load_golden("analytic")
+    pot = _potential(g, name)
+    G, eps2 = float(g["G"]), float(g["eps2"])
+    acc = orc.analytic_acc(g["pos"], G, pot, g["acc0"])
+    np.testing.assert_array_equal(acc, g[f"{name}_grav_analytic"])
+    np.testing.assert_array_equal(acc, g[f"{name}_add_analytic"])
+    ext = orc.grav_ext_acc(g["pos"], g["mass"], G, eps2, pot, g["acc0"])
+    np.testing.assert_allclose(ext, g[f"{name}_add_grav_ext"], rtol=1e-13, atol=1e-10)
