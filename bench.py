@@ -24,6 +24,7 @@ import ctypes
 import importlib
 import json
 import os
+import re
 import subprocess
 import sys
 import tempfile
@@ -55,6 +56,19 @@ def _peaks():
         return float(p["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def _profiled_traffic(summary: str):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum)
+    of the ncu capture summarised in profiles/<summary>, taken on the same
+    workload as the bench line; None when the summary is absent."""
+    try:
+        with open(os.path.join(ROOT, "profiles", summary)) as f:
+            txt = f.read()
+    except OSError:
+        return None
+    m = re.search(r"traffic per launch[^|]*\|\s*([0-9]+) bytes", txt)
+    return int(m.group(1)) if m else None
 
 
 class ClockSampler:
@@ -234,6 +248,11 @@ def bench_bh(args, dev, rank, world, dist):
                        "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
                        "algorithmic_bytes_per_launch": bytes_launch,
                        "launch_ms": trav_ms}
+    traffic = _profiled_traffic("bh_traverse_1M_disk.md")
+    if traffic is not None and BH_N == 1_000_000 and BH_BITS == 10:
+        res["roofline"]["traffic"] = traffic
+        res["roofline"]["traffic_source"] = ("ncu dram bytes of one launch on this workload "
+                                             "(profiles/bh_traverse_1M_disk.md)")
     # The same launch seen as FP32 work: 20 flop per monopole term, 10 per
     # acceptance test.
     flops = 20 * per_step["lane_interactions"] + 10 * per_step["lane_tests"]
