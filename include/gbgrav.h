@@ -298,6 +298,46 @@ int gb_bh_accel_ext(gb_bh_t *h, float *acc, float theta, float eps2, float G,
                     int max_stack, const gb_potential_t *pot, int flags,
                     void *stream);
 
+/* ------------------------------------------------- SPH neighbour grid */
+/* Uniform grid over the gas particles for the SPH neighbour walk, rebuilt on
+ * the device: NeighborGrid (core/solvers/neighbor_grid.py:35-136), whose
+ * rebuild the reference runs in host numpy.  Outputs are bit-identical to
+ * the reference's for the same float32 inputs: gsort (gas indices in stable
+ * cell order, zero-padded to n) and cell_start (max_cells + 1 entries, cell
+ * c's first slot in gsort for c <= n_cells, zero above), with
+ * max_cells = max(64, 4 n) and the cell size max(2 h_max, min_radius) grown
+ * by 1.3 until the grid fits. */
+typedef struct gb_grid gb_grid_t;
+
+typedef struct gb_grid_info {
+    int64_t ngas, n_cells;
+    int32_t nx, ny, nz;
+    int32_t status;       /* 0 ok, 1 non-finite input, 2 no fitting grid */
+    double lo[3], cell, inv_cell;
+} gb_grid_info_t;
+
+/* NeighborGrid.__init__(n, min_radius) (:38-48): scratch for n particles. */
+int gb_grid_create(gb_grid_t **out, int64_t n, double min_radius);
+int gb_grid_destroy(gb_grid_t *h);
+/* max(64, 4 n): cell_start needs max_cells + 1 entries. */
+int64_t gb_grid_max_cells(gb_grid_t *h);
+
+/* rebuild (is_star != NULL; gas = is_star == 0) or rebuild_all (is_star =
+ * NULL; every particle is gas) (:49-136).  xm: n float4 {x, y, z, m};
+ * hsml: n smoothing lengths; is_star: n int32; gsort: int32[max(n, 1)];
+ * cell_start: int32[max_cells + 1] (device, caller-owned, like the
+ * reference's fields).  Asynchronous on `stream`; a rebuild without gas
+ * leaves gsort, cell_start and the geometry unchanged, as the reference
+ * does.  When info is not NULL the call waits for the stream and fills it
+ * (the reference's return value ngas and its nx, ny, nz, lo, inv_cell), and
+ * a non-finite gas position or smoothing length returns GB_EINVAL. */
+int gb_grid_rebuild(gb_grid_t *h, const float *xm, const float *hsml,
+                    const int32_t *is_star, int32_t *gsort, int32_t *cell_start,
+                    gb_grid_info_t *info, void *stream);
+
+/* Kernels launched through this handle (measurement support). */
+uint64_t gb_grid_launch_count(gb_grid_t *h);
+
 /* ------------------------------------------------------------ calibration */
 /* Launches an FP32 FMA-throughput kernel (packed = 1: .f32x2 form) on
  * `stream`; *flops receives the FLOP count of the launch, which the caller

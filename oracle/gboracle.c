@@ -465,3 +465,81 @@ int64_t orc_traverse(const double *pos, const int32_t *order, const double *com,
     }
     return dropped;
 }
+
+/* ------------------------------------------------------- neighbour grid
+ * NeighborGrid.rebuild / rebuild_all (core/solvers/neighbor_grid.py:49-136):
+ * gas = particles with is_star == 0 (all when is_star is NULL), in index
+ * order; cell = max(2 h_max, min_radius), 1 if not > 1e-9; lo / span from
+ * the gas positions; dims = max(int64(floor(span / cell)) + 1, 1), the cell
+ * grown by 1.3 while prod(dims) > max_cells; key = (i dy + j) dz + k with
+ * ijk = clip(int64((x - lo) / cell), 0, dims - 1); gsort = gas in stable key
+ * order (zero-padded to n), cell_start = exclusive prefix of the per-cell
+ * counts (n_cells + 1 entries, zero above).  Returns ngas; with no gas the
+ * outputs are left untouched.  int64 casts follow numpy on x86-64
+ * (truncation, INT64_MIN for NaN and out-of-range values). */
+static int64_t np_i64(double t) {
+    if (!(t < 9223372036854775808.0 && t > -9223372036854775808.0)) return INT64_MIN;
+    return (int64_t)t;
+}
+
+int64_t orc_grid_rebuild(const double *pos, const double *h, const int32_t *is_star,
+                         int64_t n, double min_radius, int64_t max_cells,
+                         int32_t *gsort, int32_t *cell_start, int64_t *dims_out,
+                         double *lo_out, double *inv_cell_out) {
+    int64_t ngas = 0;
+    for (int64_t i = 0; i < n; ++i) ngas += (!is_star || is_star[i] == 0);
+    if (ngas == 0) return 0;
+    int32_t *gas = (int32_t *)malloc(sizeof(int32_t) * (size_t)ngas);
+    double hmax = -INFINITY, lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    int64_t g = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        if (is_star && is_star[i] != 0) continue;
+        gas[g++] = (int32_t)i;
+        if (h[i] > hmax) hmax = h[i];
+        for (int a = 0; a < 3; ++a) {
+            const double x = pos[3 * i + a];
+            if (x < lo[a]) lo[a] = x;
+            if (x > hi[a]) hi[a] = x;
+        }
+    }
+    double cell = 2.0 * hmax > min_radius ? 2.0 * hmax : min_radius;
+    cell = cell > 1e-9 ? cell : 1.0;
+    double span[3];
+    for (int a = 0; a < 3; ++a) span[a] = hi[a] - lo[a];
+    int64_t dims[3];
+    for (;;) {
+        for (int a = 0; a < 3; ++a) {
+            const int64_t f = np_i64(floor(span[a] / cell));
+            dims[a] = (f != INT64_MIN && f + 1 > 1) ? f + 1 : 1;
+        }
+        if ((double)dims[0] * (double)dims[1] * (double)dims[2] <= (double)max_cells) break;
+        cell *= 1.3;
+    }
+    const int64_t n_cells = dims[0] * dims[1] * dims[2];
+    int64_t *key = (int64_t *)malloc(sizeof(int64_t) * (size_t)ngas);
+    int64_t *cnt = (int64_t *)calloc((size_t)n_cells + 1, sizeof(int64_t));
+    for (int64_t p = 0; p < ngas; ++p) {
+        const int64_t i = gas[p];
+        int64_t q[3];
+        for (int a = 0; a < 3; ++a) {
+            int64_t v = np_i64((pos[3 * i + a] - lo[a]) / cell);
+            q[a] = v < 0 ? 0 : (v > dims[a] - 1 ? dims[a] - 1 : v);
+        }
+        key[p] = (q[0] * dims[1] + q[1]) * dims[2] + q[2];
+        cnt[key[p] + 1] += 1;
+    }
+    for (int64_t c = 0; c <= max_cells; ++c) cell_start[c] = 0;
+    for (int64_t c = 0; c < n_cells; ++c) cnt[c + 1] += cnt[c];
+    for (int64_t c = 0; c <= n_cells; ++c) cell_start[c] = (int32_t)cnt[c];
+    for (int64_t p = 0; p < ngas; ++p) gsort[cnt[key[p]]++] = gas[p]; /* stable */
+    for (int64_t p = ngas; p < n; ++p) gsort[p] = 0;
+    for (int a = 0; a < 3; ++a) {
+        dims_out[a] = dims[a];
+        lo_out[a] = lo[a];
+    }
+    *inv_cell_out = 1.0 / cell;
+    free(gas);
+    free(key);
+    free(cnt);
+    return ngas;
+}

@@ -74,6 +74,8 @@ def _declare(L):
     L.orc_potential_energy.restype = D
     L.orc_kdk_direct.argtypes = [P, P, P, P, I64, D, D, D, I64]
     L.orc_analytic_acc.argtypes = [P, P, I64, D, D, D, D, D, D, I32, D]
+    L.orc_grid_rebuild.argtypes = [P, P, P, I64, D, I64, P, P, P, P, P]
+    L.orc_grid_rebuild.restype = I64
     L.orc_grav_ext_acc.argtypes = [P, P, P, I64, D, D, D, D, D, D, D, I32, D]
     L.orc_morton.argtypes = [P, I64, I32, P, P, P]
     L.orc_stable_argsort_u64.argtypes = [P, I64, P]
@@ -167,6 +169,32 @@ def grav_ext_acc(pos, mass, G, eps2, pot, acc=None):
     mass = _f64(mass, (-1,))
     out = np.zeros_like(pos) if acc is None else _f64(acc, (-1, 3)).copy()
     lib().orc_grav_ext_acc(_p(pos), _p(mass), _p(out), pos.shape[0], G, eps2, *_pot_args(pot))
+    return out
+
+
+# ------------------------------------------------------ neighbour grid
+def grid_rebuild(pos, h, is_star=None, min_radius=0.0, state=None):
+    """NeighborGrid(n, min_radius).rebuild(pos, h, is_star) (or rebuild_all
+    when is_star is None).  state: a previous result whose gsort/cell_start/
+    geometry a rebuild without gas leaves in place.  Returns a dict with
+    ngas, gsort, cell_start, dims, lo, inv_cell."""
+    pos = _f64(pos, (-1, 3))
+    n = pos.shape[0]
+    h = _f64(h, (-1,))
+    max_cells = max(64, 4 * n)
+    if state is None:
+        state = dict(gsort=np.zeros(max(n, 1), np.int32), cell_start=np.zeros(max_cells + 1, np.int32),
+                     dims=np.ones(3, np.int64), lo=np.zeros(3), inv_cell=1.0)
+    out = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in state.items()}
+    star = None if is_star is None else np.ascontiguousarray(is_star, dtype=np.int32)
+    dims = out["dims"]
+    lo = out["lo"]
+    inv = np.array([out["inv_cell"]], np.float64)
+    ngas = lib().orc_grid_rebuild(_p(pos), _p(h), _p(star) if star is not None else None, n,
+                                  float(min_radius), max_cells, _p(out["gsort"]), _p(out["cell_start"]),
+                                  _p(dims), _p(lo), _p(inv))
+    out["inv_cell"] = float(inv[0])
+    out["ngas"] = int(ngas)
     return out
 
 

@@ -62,6 +62,13 @@ class Potential(ctypes.Structure):
                 ("is_hernquist", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
+class GridInfo(ctypes.Structure):
+    """gb_grid_info_t: the geometry of the last neighbour-grid rebuild."""
+    _fields_ = [("ngas", ctypes.c_int64), ("n_cells", ctypes.c_int64), ("nx", ctypes.c_int32),
+                ("ny", ctypes.c_int32), ("nz", ctypes.c_int32), ("status", ctypes.c_int32),
+                ("lo", ctypes.c_double * 3), ("cell", ctypes.c_double), ("inv_cell", ctypes.c_double)]
+
+
 SIGNATURES = {
     "gb_last_error_string": (ctypes.c_char_p, []),
     "gb_version": (I32, []),
@@ -103,6 +110,11 @@ SIGNATURES = {
     "gb_analytic_acc": (I32, [P, P, I64, F32, P, I32, P]),
     "gb_direct_acc_ext": (I32, [P, P, P, I64, F32, F32, P, I32, P]),
     "gb_bh_accel_ext": (I32, [P, P, F32, F32, F32, I32, P, I32, P]),
+    "gb_grid_create": (I32, [ctypes.POINTER(P), I64, F64]),
+    "gb_grid_destroy": (I32, [P]),
+    "gb_grid_max_cells": (I64, [P]),
+    "gb_grid_rebuild": (I32, [P, P, P, P, P, P, P, P]),
+    "gb_grid_launch_count": (ctypes.c_uint64, [P]),
 }
 
 _lib = None

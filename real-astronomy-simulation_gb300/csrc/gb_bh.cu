@@ -30,6 +30,7 @@
 #include <cstdio>
 
 #include "gb_common.cuh"
+#include "gb_sort.cuh"
 
 namespace gb {
 
@@ -41,11 +42,6 @@ struct BHParams {
 
 
 constexpr int BBOX_THREADS = 256;
-constexpr int RS_THREADS = 256;
-constexpr int RS_WARPS = RS_THREADS / 32;
-constexpr int RS_ITEMS = 16;
-constexpr int RS_TILE = RS_THREADS * RS_ITEMS;  // 4096 keys per CTA
-constexpr int RS_BINS = 256;
 constexpr int TRAV_WARPS = 4;
 constexpr int TRAV_STACK = 128;  // > maximum Karras depth (63 + 31 levels)
 constexpr int MAX_DEPTH = 128;
@@ -183,134 +179,6 @@ __global__ void bh_morton_kernel(const float4 *__restrict__ xm, int64_t n, const
     const uint32_t qz = quantise(x.z, prm->lo[2], sc, qmax);
     keys[i] = (KeyT)interleave3<BITS>(qx, qy, qz);
     vals[i] = (uint32_t)i;
-}
-
-// ------------------------------------------------------------ radix sort
-template <typename KeyT>
-__global__ void __launch_bounds__(RS_THREADS)
-rs_upsweep_kernel(const KeyT *__restrict__ keys, int64_t n, int shift, uint32_t *__restrict__ hist, int nb) {
-    __shared__ uint32_t h[RS_BINS];
-    for (int d = threadIdx.x; d < RS_BINS; d += RS_THREADS) h[d] = 0;
-    __syncthreads();
-    const int64_t base = (int64_t)blockIdx.x * RS_TILE;
-    for (int k = threadIdx.x; k < RS_TILE; k += RS_THREADS) {
-        const int64_t i = base + k;
-        if (i < n) atomicAdd(&h[(uint32_t)(keys[i] >> shift) & 0xFFu], 1u);
-    }
-    __syncthreads();
-    for (int d = threadIdx.x; d < RS_BINS; d += RS_THREADS) hist[(int64_t)d * nb + blockIdx.x] = h[d];
-}
-
-// Exclusive scan of 256 values held one per thread of a 256-thread CTA.
-__device__ __forceinline__ uint32_t cta256_exclusive_scan(uint32_t v, uint32_t *wsum) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    uint32_t inc = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += t;
-    }
-    if (lane == 31) wsum[wid] = inc;
-    __syncthreads();
-    if (wid == 0) {
-        const uint32_t w = lane < RS_WARPS ? wsum[lane] : 0u;
-        uint32_t wi = w;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
-            if (lane >= o) wi += t;
-        }
-        if (lane < RS_WARPS) wsum[lane] = wi - w;
-    }
-    __syncthreads();
-    return wsum[wid] + inc - v;
-}
-
-// Row scan: CTA d turns row d of the digit-major histogram (one count per
-// tile) into exclusive offsets within the digit and stores the digit total.
-__global__ void __launch_bounds__(RS_THREADS) rs_rowscan_kernel(uint32_t *hist, int nb, uint32_t *totals) {
-    __shared__ uint32_t wsum[RS_WARPS];
-    uint32_t *row = hist + (int64_t)blockIdx.x * nb;
-    const int per = (nb + RS_THREADS - 1) / RS_THREADS;
-    const int b0 = min(nb, (int)threadIdx.x * per), b1 = min(nb, b0 + per);
-    uint32_t v = 0;
-    for (int b = b0; b < b1; ++b) v += row[b];
-    const uint32_t excl = cta256_exclusive_scan(v, wsum);
-    uint32_t run = excl;
-    for (int b = b0; b < b1; ++b) {
-        const uint32_t t = row[b];
-        row[b] = run;
-        run += t;
-    }
-    if (threadIdx.x == RS_THREADS - 1) totals[blockIdx.x] = excl + v;
-}
-
-// Stable scatter: elements of a tile are ranked in index order (warp, round,
-// lane) among equal digits with match/ballot, then written to the scanned
-// global offset of (digit, tile).
-template <typename KeyT>
-__global__ void __launch_bounds__(RS_THREADS)
-rs_downsweep_kernel(const KeyT *__restrict__ kin, const uint32_t *__restrict__ vin, KeyT *__restrict__ kout,
-                    uint32_t *__restrict__ vout, int64_t n, int shift, const uint32_t *__restrict__ hist, int nb,
-                    const uint32_t *__restrict__ totals, unsigned long long *diag) {
-    static_assert(RS_THREADS == RS_BINS, "one thread per digit");
-    __shared__ uint32_t whist[RS_WARPS][RS_BINS];
-    __shared__ uint32_t boff[RS_BINS];
-    __shared__ uint32_t wsum[RS_WARPS];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    {
-        const int d = threadIdx.x;
-        const uint32_t base = cta256_exclusive_scan(totals[d], wsum);
-        boff[d] = base + hist[(int64_t)d * nb + blockIdx.x];
-#pragma unroll
-        for (int w = 0; w < RS_WARPS; ++w) whist[w][d] = 0;
-    }
-    __syncthreads();
-    const int64_t wbase = (int64_t)blockIdx.x * RS_TILE + (int64_t)wid * (RS_ITEMS * 32);
-    const uint32_t lt_mask = (1u << lane) - 1u;
-    KeyT key[RS_ITEMS];
-    uint32_t val[RS_ITEMS];
-    uint32_t rank[RS_ITEMS];
-#pragma unroll
-    for (int r = 0; r < RS_ITEMS; ++r) {
-        const int64_t i = wbase + r * 32 + lane;
-        const bool ok = i < n;
-        key[r] = ok ? kin[i] : (KeyT)0;
-        val[r] = ok ? vin[i] : 0u;
-        const uint32_t dig = (uint32_t)(key[r] >> shift) & 0xFFu;
-        const uint32_t tag = ok ? dig : (0x100u | (uint32_t)lane);
-        const uint32_t peers = __match_any_sync(0xffffffffu, tag);
-        const uint32_t before = ok ? whist[wid][dig] : 0u;
-        rank[r] = before + __popc(peers & lt_mask);
-        __syncwarp();
-        if (ok && (peers & lt_mask) == 0) whist[wid][dig] = before + __popc(peers);
-        __syncwarp();
-    }
-    __syncthreads();
-    for (int d = threadIdx.x; d < RS_BINS; d += RS_THREADS) {
-        uint32_t run = 0;
-#pragma unroll
-        for (int w = 0; w < RS_WARPS; ++w) {
-            const uint32_t t = whist[w][d];
-            whist[w][d] = run;
-            run += t;
-        }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < RS_ITEMS; ++r) {
-        const int64_t i = wbase + r * 32 + lane;
-        if (i < n) {
-            const uint32_t dig = (uint32_t)(key[r] >> shift) & 0xFFu;
-            const uint32_t dst = boff[dig] + whist[wid][dig] + rank[r];
-            if (dst < n) {
-                kout[dst] = key[r];
-                vout[dst] = val[r];
-            } else {
-                atomicAdd(diag + DIAG_BAD_TREE, 1ull);
-            }
-        }
-    }
 }
 
 // ----------------------------------------------------------------- gather
@@ -945,17 +813,12 @@ static int build_impl(gb_bh_t *h, float4 *xm, float4 *vel, const float4 *acc, in
     uint32_t *v0 = h->vals[0], *v1 = h->vals[1];
     bh_morton_kernel<KeyT, BITS><<<g256, 256, 0, s>>>(xm, n, h->prm, k0, v0);
     mark(h, slot, 1, s);
-    const int nb = (int)((n + RS_TILE - 1) / RS_TILE);
     const int passes = (3 * BITS + 7) / 8;
-    for (int p = 0; p < passes; ++p) {
-        rs_upsweep_kernel<KeyT><<<nb, RS_THREADS, 0, s>>>(k0, n, 8 * p, h->hist, nb);
-        rs_rowscan_kernel<<<RS_BINS, RS_THREADS, 0, s>>>(h->hist, nb, h->totals);
-        rs_downsweep_kernel<KeyT><<<nb, RS_THREADS, 0, s>>>(k0, v0, k1, v1, n, 8 * p, h->hist, nb, h->totals,
-                                                            h->diag);
-        std::swap(k0, k1);
-        std::swap(v0, v1);
-    }
-    h->cur = (k0 == (KeyT *)h->keys[0]) ? 0 : 1;
+    KeyT *kk[2] = {k0, k1};
+    uint32_t *vv[2] = {v0, v1};
+    h->cur = radix_sort_pairs<KeyT>(kk, vv, n, passes, h->hist, h->totals, h->diag, s);
+    k0 = kk[h->cur];
+    v0 = vv[h->cur];
     mark(h, slot, 2, s);
     bh_gather_kernel<<<g256, 256, 0, s>>>(xm, v0, n, h->leaf, h->diag);
     const int ni = (int)std::max<int64_t>(n - 1, 1);

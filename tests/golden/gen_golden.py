@@ -43,12 +43,13 @@ def _load_reference(ref_root: str):
     import core.engine as engine
     import core.living_galaxy_engine as living
     import core.gas_disk_engine as gasdisk
+    import core.solvers.neighbor_grid as ngrid
     # _accumulate: atomics -> in-place updates (the only source rewrite).
     src = _taichi_stub.rewrite_atomics(inspect.getsource(bh._accumulate))
     exec(compile(src, bh.__file__, "exec"), bh.__dict__)
     return dict(units=units, gravity=gravity, bh=bh, leapfrog=leapfrog,
                 plummer=plummer, disk=disk, engine=engine, living=living,
-                gasdisk=gasdisk, stub=_taichi_stub)
+                gasdisk=gasdisk, ngrid=ngrid, stub=_taichi_stub)
 
 
 def _f32(a):
@@ -282,8 +283,60 @@ def gen_analytic(R, out):
     out["analytic"] = d
 
 
+def gen_neighbor_grid(R, out):
+    """NeighborGrid.rebuild / rebuild_all (core/solvers/neighbor_grid.py:
+    35-136) on float32-rounded inputs.  Cases: a disk with 30% stars; the
+    same with rebuild_all and a dominant min_radius; smoothing lengths so
+    small that the cell-growth loop runs; a rebuild without gas after a
+    normal one (the fields must stay as they were); points on exact cell
+    boundaries with duplicates; zero smoothing lengths (cell falls back to
+    1); a single gas particle."""
+    ng, stub = R["ngrid"], R["stub"]
+    rng = np.random.default_rng(41)
+    d = {}
+
+    def run(name, pos, h, is_star=None, min_radius=0.0, grid=None):
+        n = pos.shape[0]
+        g = grid if grid is not None else ng.NeighborGrid(n, min_radius=min_radius)
+        fp, fh = _field_from(stub, pos), _field_from(stub, h)
+        if is_star is None:
+            ngas = g.rebuild_all(fp, fh)
+        else:
+            ngas = g.rebuild(fp, fh, _field_from(stub, is_star, "i32"))
+        d[f"{name}_pos"], d[f"{name}_h"] = pos, h
+        if is_star is not None:
+            d[f"{name}_is_star"] = is_star
+        d[f"{name}_min_radius"] = min_radius
+        d[f"{name}_ngas"] = ngas
+        d[f"{name}_gsort"] = g.gsort.to_numpy()
+        d[f"{name}_cell_start"] = g.cell_start.to_numpy()
+        d[f"{name}_dims"] = np.array([g.nx, g.ny, g.nz], np.int64)
+        d[f"{name}_lo"] = np.array(g.lo, np.float64)
+        d[f"{name}_inv_cell"] = g.inv_cell
+        return g
+
+    pos, _ = _disk_positions(R, 3000, seed=43)
+    h = _f32(rng.lognormal(np.log(0.3), 0.4, 3000))
+    star = (rng.random(3000) < 0.3).astype(np.int32)
+    g = run("disk", pos, h, star)
+    run("disk_all", pos, h, None, min_radius=1.5)
+    run("tiny_h", _f32(rng.normal(0.0, 2.0, (500, 3))), _f32(np.full(500, 1e-4)), None)
+    nostar = np.ones(3000, np.int32)
+    run("nogas", pos, h, nostar, grid=g)  # after "disk": fields unchanged
+    lat = _f32(np.stack(np.meshgrid(np.arange(8), np.arange(5), np.arange(3), indexing="ij"),
+                        -1).reshape(-1, 3) * 0.5)
+    lat = np.concatenate([lat, lat[::7]])  # duplicates
+    run("lattice", lat, _f32(np.full(lat.shape[0], 0.25)), np.zeros(lat.shape[0], np.int32))
+    run("zero_h", pos[:400], _f32(np.zeros(400)), star[:400])
+    one = np.ones(50, np.int32)
+    one[17] = 0
+    run("single_gas", pos[:50], h[:50], one)
+    d["names"] = np.array(["disk", "disk_all", "tiny_h", "nogas", "lattice", "zero_h", "single_gas"])
+    out["neighbor_grid"] = d
+
+
 GENERATORS = (gen_plummer_ic, gen_direct, gen_engine_direct, gen_morton,
-              gen_bh, gen_engine_bh, gen_analytic)
+              gen_bh, gen_engine_bh, gen_analytic, gen_neighbor_grid)
 
 
 def main(argv):

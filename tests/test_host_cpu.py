@@ -105,3 +105,9 @@ def test_potential_struct_layout_and_dict(pkg):
     q = ext.Potential.from_dict(dict(M_d=0.0, a=1.0, b=1.0, M_h=40.0, a_h=15.0, is_hernquist=1,
                                      smbh_mass=0.1))
     assert q.is_hernquist == 1 and q.smbh_mass == 0.1
+
+
+def test_grid_info_struct_layout():
+    lib_mod = importlib.import_module(PKG_NAME + "._lib")
+    assert ctypes.sizeof(lib_mod.GridInfo) == 72
+    assert lib_mod.GridInfo.lo.offset == 32 and lib_mod.GridInfo.inv_cell.offset == 64

@@ -146,3 +146,22 @@ def test_analytic_potential_matches_reference(orc, name):
     np.testing.assert_array_equal(acc, g[f"{name}_add_analytic"])
     ext = orc.grav_ext_acc(g["pos"], g["mass"], G, eps2, pot, g["acc0"])
     np.testing.assert_allclose(ext, g[f"{name}_add_grav_ext"], rtol=1e-13, atol=1e-10)
+
+
+def test_neighbor_grid_matches_reference(orc):
+    """NeighborGrid.rebuild / rebuild_all: every output bit for bit on the
+    seven fixture cases (the no-gas case runs on the disk case's grid)."""
+    g = load_golden("neighbor_grid")
+    prev = None
+    for name in g["names"]:
+        star = g.get(f"{name}_is_star")
+        r = orc.grid_rebuild(g[f"{name}_pos"], g[f"{name}_h"], star, float(g[f"{name}_min_radius"]),
+                             state=prev if name == "nogas" else None)
+        assert r["ngas"] == int(g[f"{name}_ngas"]), name
+        np.testing.assert_array_equal(r["gsort"], g[f"{name}_gsort"])
+        np.testing.assert_array_equal(r["cell_start"], g[f"{name}_cell_start"])
+        np.testing.assert_array_equal(r["dims"], g[f"{name}_dims"])
+        np.testing.assert_array_equal(r["lo"], g[f"{name}_lo"])
+        assert r["inv_cell"] == float(g[f"{name}_inv_cell"])
+        if name == "disk":
+            prev = r
