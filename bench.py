@@ -579,6 +579,55 @@ def bench_adjoint(dev, n=65536, steps=200, every=20):
             "grad_finite": bool(all(torch.isfinite(t).all().item() for t in g))}
 
 
+def bench_grid(dev, n=1_000_000, reps=20):
+    """SPH neighbour-grid rebuild (NeighborGrid.rebuild) of a 1M exponential
+    disk with 30% stars: device rebuild alone (CUDA events, L2 flushed), the
+    call with its gas-count readback, and the oracle's C restatement on one
+    host core (the reference's rebuild is host numpy)."""
+    ic = importlib.import_module(PKG + ".ic")
+    ngm = importlib.import_module(PKG + ".solvers.neighbor_grid")
+    pos, _, mass = ic.exponential_disk(n, seed=5)
+    rng = np.random.default_rng(6)
+    h = rng.lognormal(np.log(0.05), 0.5, n).astype(np.float32)
+    star = (rng.random(n) < 0.3).astype(np.int32)
+    xm = _xm(pos, mass, dev)
+    hs = torch.tensor(h, device=dev)
+    st = torch.tensor(star, device=dev)
+    grid = ngm.NeighborGrid(n, min_radius=0.02, device=dev)
+    for _ in range(3):
+        ngas = grid.rebuild(xm, hs, st)
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    starts, ends = _events(reps)
+    l0 = grid.launch_count()
+    for k in range(reps):
+        flush.zero_()
+        starts[k].record()
+        grid.rebuild_async(xm, hs, st)
+        ends[k].record()
+    torch.cuda.synchronize()
+    launches = (grid.launch_count() - l0) // reps
+    dev_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        grid.rebuild(xm, hs, st)
+    sync_ms = (time.perf_counter() - t0) / reps * 1e3
+    from oracle import oracle as orc
+    orc.build()
+    pos64 = pos.astype(np.float32).astype(np.float64)
+    t0 = time.perf_counter()
+    ref = orc.grid_rebuild(pos64, h.astype(np.float64), star, 0.02)
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    same = bool(ref["ngas"] == ngas and np.array_equal(ref["gsort"], grid.gsort.cpu().numpy())
+                and np.array_equal(ref["cell_start"], grid.cell_start.cpu().numpy()))
+    grid.close()
+    return {"workload": f"NeighborGrid.rebuild, exponential disk N={n}, 30% stars, h lognormal(0.05, 0.5), "
+                        "min_radius 0.02", "ngas": int(ngas), "dims": [grid.nx, grid.ny, grid.nz],
+            "rebuild_ms": dev_ms, "rebuild_with_gas_count_readback_ms": sync_ms,
+            "launches_per_rebuild": int(launches),
+            "cpu_port_ms": cpu_ms, "cpu_port": "oracle C restatement, 1 host core",
+            "identical_to_oracle": same}
+
+
 # ------------------------------------------------------------------- main
 def run_reference(args):
     """Reference arm: the float64 CPU restatement of the reference's BH path
@@ -625,7 +674,7 @@ def main(argv=None):
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--drift-steps", type=int, default=1000)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
-    ap.add_argument("--only", choices=("direct", "merger", "batch", "adjoint"),
+    ap.add_argument("--only", choices=("direct", "merger", "batch", "adjoint", "grid"),
                     help="run one secondary workload alone (profiling runs)")
     args = ap.parse_args(argv)
     if args.warmup < 3:
@@ -650,7 +699,8 @@ def main(argv=None):
         fn = {"direct": lambda: bench_direct(dev, lib_mod, peak),
               "merger": lambda: bench_merger(dev, args.drift_steps),
               "batch": lambda: bench_batch(dev),
-              "adjoint": lambda: bench_adjoint(dev)}[args.only]
+              "adjoint": lambda: bench_adjoint(dev),
+              "grid": lambda: bench_grid(dev)}[args.only]
         print(json.dumps({"only": args.only, "fp32_peak_tflops_measured": peak,
                           "result": fn()}), flush=True)
         return 0
@@ -678,6 +728,7 @@ def main(argv=None):
             sec["merger"] = bench_merger(dev, args.drift_steps)
             sec["batch"] = bench_batch(dev)
             sec["adjoint"] = bench_adjoint(dev)
+            sec["neighbor_grid"] = bench_grid(dev)
             line["secondary"] = sec
     if dist:
         dist.barrier()

@@ -327,7 +327,7 @@ extern "C" int gb_grid_rebuild(gb_grid_t *h, const float *xm, const float *hsml,
         const unsigned gc = (unsigned)((h->max_cells + 1 + GRID_THREADS - 1) / GRID_THREADS);
         grid_start_kernel<<<gc, GRID_THREADS, 0, s>>>(h->keys[cur], h->geom, h->max_cells, cell_start);
         GB_CUDA_TRY(cudaGetLastError());
-        h->launches += 5 + 3 * h->passes;
+        h->launches += 4 + 3 * h->passes;
     }
     if (info) {
         GridGeom g;
