@@ -94,16 +94,19 @@ class Engine:
             self.xm = pack_xm(state.pos, state.mass, self.device)
             self.v4 = pack_vec(state.vel, self.device)
             self.a4 = empty4(self.n, self.device)
-            if self._direct is None or self._direct.n_max < max(self.n, 1):
-                self._direct = DirectGravity(max(self.n, 1), self.device)
-            if self.gravity_mode == "bh" and self.n >= BH_MIN_N:
-                from .solvers.barnes_hut import BarnesHut
-                self._bh = BarnesHut(self.n, theta=self.theta, softening=self.softening,
-                                     max_stack=self.max_stack, key_bits=self.key_bits,
-                                     G=self.G, device=self.device)
-            else:
-                self._bh = None
+            self._make_solvers()
             self._compute_acc()
+
+    def _make_solvers(self) -> None:
+        if self._direct is None or self._direct.n_max < max(self.n, 1):
+            self._direct = DirectGravity(max(self.n, 1), self.device)
+        if self.gravity_mode == "bh" and self.n >= BH_MIN_N:
+            from .solvers.barnes_hut import BarnesHut
+            self._bh = BarnesHut(self.n, theta=self.theta, softening=self.softening,
+                                 max_stack=self.max_stack, key_bits=self.key_bits,
+                                 G=self.G, device=self.device)
+        else:
+            self._bh = None
 
     def to_state(self) -> State:
         """Download the state into a host State (core/engine.py:83-98)."""
@@ -113,6 +116,38 @@ class Engine:
                      ids=self._ids, time=self.time, step=self.step_count, seed=self.seed,
                      age=self._age, temperature=self._temperature,
                      metallicity=self._metallicity, meta=dict(self.meta))
+
+    def to_device_state(self) -> dict:
+        """The state without a host copy: device tensor views of the engine's
+        float32 records (pos, vel, acc: (n, 3); mass: (n,)) plus time and
+        step.  The views change as the engine steps; copy them to keep a
+        snapshot (see snapshot.SnapshotWriter)."""
+        return {"pos": self.xm[:, :3], "vel": self.v4[:, :3], "mass": self.xm[:, 3],
+                "acc": self.a4[:, :3], "time": self.time, "step": self.step_count}
+
+    def load_device_state(self, pos: torch.Tensor, vel: torch.Tensor, mass: torch.Tensor, *,
+                          time: float = 0.0, step: int = 0, seed: int = 0, ptype=None, ids=None,
+                          meta: dict | None = None) -> None:
+        """load_state from device tensors (copied device to device, no host
+        round trip) and prime the accelerations."""
+        n = int(pos.shape[0])
+        self.n = n
+        self.time = float(time)
+        self.step_count = int(step)
+        self.seed = int(seed)
+        self.meta = dict(meta or {})
+        self._ptype = np.zeros(n, np.int32) if ptype is None else np.asarray(ptype, np.int32).copy()
+        self._ids = np.arange(n, dtype=np.int64) if ids is None else np.asarray(ids, np.int64).copy()
+        self._age = self._temperature = self._metallicity = None
+        with torch.cuda.device(self.device):
+            self.xm = empty4(n, self.device)
+            self.xm[:, :3] = pos.to(self.device, torch.float32)
+            self.xm[:, 3] = mass.to(self.device, torch.float32)
+            self.v4 = empty4(n, self.device)
+            self.v4[:, :3] = vel.to(self.device, torch.float32)
+            self.a4 = empty4(n, self.device)
+            self._make_solvers()
+            self._compute_acc()
 
     # -------------------------------------------------------------- stepping
     def _compute_acc(self) -> None:

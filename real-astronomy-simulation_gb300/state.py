@@ -70,6 +70,32 @@ class State:
                     f.create_dataset(name, data=np.asarray(arr, dtype=np.float64),
                                      compression="gzip")
 
+    def save_npz(self, path: str) -> None:
+        """The same datasets and attributes as save(), in a numpy .npz file
+        (for hosts without h5py)."""
+        arrays = {name: getattr(self, name) for name in ("pos", "vel", "mass", "ptype", "ids")}
+        for name in _OPTIONAL:
+            arr = getattr(self, name)
+            if arr is not None:
+                arrays[name] = np.asarray(arr, dtype=np.float64)
+        attrs = {"time": float(self.time), "step": int(self.step), "seed": int(self.seed),
+                 "n": int(self.n)}
+        for k, v in attrs.items():
+            arrays[f"attr_{k}"] = np.asarray(v)
+        for k, v in self.meta.items():
+            arrays[f"meta_{k}"] = np.asarray(v if np.isscalar(v) else str(v))
+        with open(path, "wb") as f:
+            np.savez(f, **arrays)
+
+    @classmethod
+    def load_npz(cls, path: str) -> "State":
+        with np.load(path, allow_pickle=False) as z:
+            meta = {k[len("meta_"):]: z[k].item() for k in z.files if k.startswith("meta_")}
+            optional = {name: z[name] for name in _OPTIONAL if name in z.files}
+            return cls(pos=z["pos"], vel=z["vel"], mass=z["mass"], ptype=z["ptype"], ids=z["ids"],
+                       time=float(z["attr_time"]), step=int(z["attr_step"]), seed=int(z["attr_seed"]),
+                       meta=meta, **optional)
+
     @classmethod
     def load(cls, path: str) -> "State":
         import h5py

@@ -111,3 +111,18 @@ def test_grid_info_struct_layout():
     lib_mod = importlib.import_module(PKG_NAME + "._lib")
     assert ctypes.sizeof(lib_mod.GridInfo) == 72
     assert lib_mod.GridInfo.lo.offset == 32 and lib_mod.GridInfo.inv_cell.offset == 64
+
+
+def test_state_npz_roundtrip(tmp_path):
+    st_mod = importlib.import_module(PKG_NAME + ".state")
+    rng = np.random.default_rng(3)
+    s = st_mod.State.from_arrays(rng.normal(size=(50, 3)), rng.normal(size=(50, 3)), rng.random(50),
+                                 time=1.25, step=7, seed=3, u=rng.random(50),
+                                 meta={"level": "small", "dt": 1e-3})
+    p = str(tmp_path / "snap.npz")
+    s.save_npz(p)
+    t = st_mod.State.load_npz(p)
+    for name in ("pos", "vel", "mass", "ptype", "ids", "u"):
+        np.testing.assert_array_equal(getattr(t, name), getattr(s, name))
+    assert (t.time, t.step, t.seed) == (1.25, 7, 3)
+    assert t.meta["level"] == "small" and t.meta["dt"] == 1e-3 and t.temperature is None
