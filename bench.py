@@ -628,6 +628,50 @@ def bench_grid(dev, n=1_000_000, reps=20):
             "identical_to_oracle": same}
 
 
+def bench_snapshot(dev, n=1_000_000, steps=100, every=20):
+    """Snapshot cost in the step loop: the 1M-disk BH engine runs `steps`
+    KDK steps with a snapshot every `every` steps, written (a) the
+    reference's way (to_state, then the file, the loop waiting) and (b) by
+    snapshot.run_with_snapshots (device copy on the compute stream, copy
+    stream + host thread for the rest); (c) without snapshots.  Files are
+    .npz in a temporary directory (h5py is not installed here)."""
+    pkg = importlib.import_module(PKG)
+    snap = importlib.import_module(PKG + ".snapshot")
+    ic = importlib.import_module(PKG + ".ic")
+    st = importlib.import_module(PKG + ".state")
+    pos, vel, mass = ic.exponential_disk(n, seed=0)
+    s0 = st.State.from_arrays(pos, vel, mass)
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for mode in ("none", "sync", "async"):
+            eng = pkg.Engine(softening=BH_EPS, gravity_mode="bh", theta=BH_THETA, key_bits=BH_BITS,
+                             device=dev)
+            eng.load_state(s0)
+            eng.run(BH_DT, 3)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if mode == "async":
+                snap.run_with_snapshots(eng, BH_DT, steps, os.path.join(tmp, mode), snap_every=every)
+            else:
+                os.makedirs(os.path.join(tmp, mode), exist_ok=True)
+                frame = 0
+                if mode == "sync":
+                    eng.to_state().save_npz(os.path.join(tmp, mode, f"snap_{frame:04d}.npz"))
+                for k in range(steps // every):
+                    eng.run(BH_DT, every)
+                    if mode == "sync":
+                        frame += 1
+                        eng.to_state().save_npz(os.path.join(tmp, mode, f"snap_{frame:04d}.npz"))
+                torch.cuda.synchronize()
+            out[f"{mode}_s"] = time.perf_counter() - t0
+    return {"workload": f"BH engine, 1M exponential disk, {steps} KDK steps, snapshot every {every} "
+                        f"({steps // every + 1} files of {n} particles, .npz)",
+            "wall_s_no_snapshots": out["none_s"], "wall_s_synchronous_snapshots": out["sync_s"],
+            "wall_s_async_snapshots": out["async_s"],
+            "snapshot_cost_per_file_ms": {"synchronous": (out["sync_s"] - out["none_s"]) / (steps // every + 1) * 1e3,
+                                          "async": (out["async_s"] - out["none_s"]) / (steps // every + 1) * 1e3}}
+
+
 # ------------------------------------------------------------------- main
 def run_reference(args):
     """Reference arm: the float64 CPU restatement of the reference's BH path
@@ -674,7 +718,7 @@ def main(argv=None):
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--drift-steps", type=int, default=1000)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
-    ap.add_argument("--only", choices=("direct", "merger", "batch", "adjoint", "grid"),
+    ap.add_argument("--only", choices=("direct", "merger", "batch", "adjoint", "grid", "snapshot"),
                     help="run one secondary workload alone (profiling runs)")
     args = ap.parse_args(argv)
     if args.warmup < 3:
@@ -700,7 +744,8 @@ def main(argv=None):
               "merger": lambda: bench_merger(dev, args.drift_steps),
               "batch": lambda: bench_batch(dev),
               "adjoint": lambda: bench_adjoint(dev),
-              "grid": lambda: bench_grid(dev)}[args.only]
+              "grid": lambda: bench_grid(dev),
+              "snapshot": lambda: bench_snapshot(dev)}[args.only]
         print(json.dumps({"only": args.only, "fp32_peak_tflops_measured": peak,
                           "result": fn()}), flush=True)
         return 0
@@ -729,6 +774,7 @@ def main(argv=None):
             sec["batch"] = bench_batch(dev)
             sec["adjoint"] = bench_adjoint(dev)
             sec["neighbor_grid"] = bench_grid(dev)
+            sec["snapshot"] = bench_snapshot(dev)
             line["secondary"] = sec
     if dist:
         dist.barrier()
