@@ -159,9 +159,13 @@ int gb_bh_export(gb_bh_t *h, int what, void *dst, void *stream);
 
 int gb_bh_diag(gb_bh_t *h, gb_diag_t *out, int reset);
 
-/* Traversal shape: targets per warp lane (1 or 2; default 1; 2 gives 64
- * key-consecutive targets per warp).  Same results up to FP32 summation
- * order; chosen by measurement. */
+/* Traversal shape.  1 (default) and 2: warp-coherent, the warp's 32 (or 64,
+ * two per lane) key-consecutive targets walk the tree together, one node
+ * record per warp step.  0: per lane, each lane walks its own target with
+ * its own stack (max_stack <= 127 and n <= 2^25 + 1; otherwise mode 1
+ * runs).  All modes give bit-identical results: each target meets its
+ * nodes in the same order.  Mode 1 is fastest on the 1M disk (per-lane
+ * record loads diverge). */
 int gb_bh_set_traversal(gb_bh_t *h, int targets_per_lane);
 
 /* Stage timing for measurement: with timing enabled, every build/step records

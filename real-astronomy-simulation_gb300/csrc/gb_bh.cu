@@ -618,6 +618,143 @@ bh_traverse_kernel(TravArgs a) {
     }
 }
 
+// Per-lane traversal: each lane walks the tree for its own target, exactly
+// the reference's per-particle loop (:185-217) on the two-children records:
+// expanding node k tests both children (the reference pushes both and then
+// tests each when popped; the decisions do not depend on when a child is
+// tested), continues into an opened right child directly (the reference pops
+// the right child first) and keeps an opened left child on the lane's own
+// shared-memory stack.  Lanes of a warp are at different nodes, so a warp
+// runs as many iterations as its busiest lane, instead of the union of all
+// its lanes' nodes as the warp-coherent kernel does.  Stack entries hold
+// the internal index (25 bits) and the reference's stack depth d when the
+// node is popped (7 bits): a right child is popped at d + 1 and a left child
+// at d, which gives the max_stack rule exactly.  Layout [depth][thread]:
+// every lane hits its own bank whatever its depth.
+constexpr int LANE_THREADS = 128;
+constexpr int LANE_KBITS = 25;
+constexpr int LANE_MAX_STACK = 127;
+
+template <bool KDK, bool COUNT>
+__global__ void __launch_bounds__(LANE_THREADS)
+bh_traverse_lane_kernel(TravArgs a) {
+    extern __shared__ int lstk[];  // [max_stack][LANE_THREADS]
+    const int tid = threadIdx.x;
+    const int n = a.n;
+    const int s = blockIdx.x * LANE_THREADS + tid;
+    const bool valid = s < n;
+    Lane L;
+    L.px = L.py = L.pz = 0.f;
+    if (valid) {
+        const float4 p = __ldg(a.leaf + s);
+        L.px = p.x; L.py = p.y; L.pz = p.z;
+    }
+    L.ax = L.ay = L.az = 0.f;
+    L.PX = pack2(L.px, L.px);
+    L.PY = pack2(L.py, L.py);
+    L.PZ = pack2(L.pz, L.pz);
+    L.AX = L.AY = L.AZ = 0ull;
+    L.n_int = L.n_test = L.drops = 0;
+    const f2 E2 = pack2(a.eps2, a.eps2), TH2 = pack2(a.theta2, a.theta2);
+    unsigned overflow = 0, bad = 0, reads = 0;
+    int k = 0, d = 0, top = 0;
+    bool active = false;
+    if (valid && n >= 2) {
+        // The root is popped first, with an empty stack (d = 0).
+        const float4 R0 = __ldg(a.root), R1 = __ldg(a.root + 1);
+        active = apply_room(L, visit_child<COUNT>(L, a, R0, R1.x, n, s, true), 0, a.max_stack);
+    }
+    for (;;) {
+        if (!active) {
+            if (top == 0) break;
+            const unsigned e = (unsigned)lstk[(--top) * LANE_THREADS + tid];
+            k = (int)(e & ((1u << LANE_KBITS) - 1u));
+            d = (int)(e >> LANE_KBITS);
+            active = true;
+        }
+        if ((unsigned)k >= (unsigned)(n - 1)) {  // never for a consistent tree
+            ++bad;
+            break;
+        }
+        const ulonglong2 A = __ldg(reinterpret_cast<const ulonglong2 *>(a.inode + 3 * k));
+        const ulonglong2 B = __ldg(reinterpret_cast<const ulonglong2 *>(a.inode + 3 * k + 1));
+        const float4 C = __ldg(a.inode + 3 * k + 2);
+        if (COUNT) ++reads;
+        bool wantL, wantR;
+        visit_pair<COUNT>(L, a, A, B, C, s, true, E2, TH2, wantL, wantR);
+        if (d + 3 > a.max_stack) {  // the rule only bites near max_stack
+            wantR = apply_room(L, wantR, d + 1, a.max_stack);
+            wantL = apply_room(L, wantL, d, a.max_stack);
+        }
+        if (wantR) {
+            if (wantL) {
+                if (top < a.max_stack) {
+                    lstk[(top++) * LANE_THREADS + tid] =
+                        (int)((unsigned)(__float_as_int(C.z) - n) | ((unsigned)d << LANE_KBITS));
+                } else {
+                    ++overflow;
+                }
+            }
+            k = __float_as_int(C.w) - n;
+            d = d + 1;
+        } else if (wantL) {
+            k = __float_as_int(C.z) - n;
+        } else {
+            active = false;
+        }
+    }
+    // Counters: one atomic per warp and counter.
+    unsigned dsum = L.drops, osum = overflow, bsum = bad;
+    const int lane = tid & 31;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+        osum += __shfl_xor_sync(0xffffffffu, osum, o);
+        bsum += __shfl_xor_sync(0xffffffffu, bsum, o);
+    }
+    if (COUNT) {
+        unsigned isum = L.n_int, tsum = L.n_test, rsum = reads, vsum = (valid && n >= 2) ? 1u : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            isum += __shfl_xor_sync(0xffffffffu, isum, o);
+            tsum += __shfl_xor_sync(0xffffffffu, tsum, o);
+            rsum += __shfl_xor_sync(0xffffffffu, rsum, o);
+            vsum += __shfl_xor_sync(0xffffffffu, vsum, o);
+        }
+        if (lane == 0) {
+            atomicAdd(a.diag + DIAG_NODE_READS, (unsigned long long)rsum);
+            atomicAdd(a.diag + DIAG_ROOT_READS, (unsigned long long)vsum);
+            atomicAdd(a.diag + DIAG_INTERACTIONS, (unsigned long long)isum);
+            atomicAdd(a.diag + DIAG_TESTS, (unsigned long long)tsum);
+        }
+    }
+    if (lane == 0) {
+        if (dsum) atomicAdd(a.diag + DIAG_STACK_DROPS, (unsigned long long)dsum);
+        if (osum) atomicAdd(a.diag + DIAG_STACK_OVERFLOW, (unsigned long long)osum);
+        if (bsum) atomicAdd(a.diag + DIAG_BAD_TREE, (unsigned long long)bsum);
+    }
+    if (!valid) return;
+    const uint32_t p = __ldg(a.order + s);
+    if (p >= (uint32_t)n) return;
+    float xl, xr, yl, yr, zl, zr;
+    unpack2(L.AX, xl, xr);
+    unpack2(L.AY, yl, yr);
+    unpack2(L.AZ, zl, zr);
+    float gx = a.G * (L.ax + (xl + xr)), gy = a.G * (L.ay + (yl + yr)), gz = a.G * (L.az + (zl + zr));
+    if (a.pot.on) ext_acc_add(a.pot, L.px, L.py, L.pz, gx, gy, gz);
+    if (KDK) {
+        const float4 vh = a.vel[p];
+        a.vel[p] = make_float4(kick(vh.x, gx, a.h), kick(vh.y, gy, a.h), kick(vh.z, gz, a.h), vh.w);
+        a.acc[p] = make_float4(gx, gy, gz, 0.f);
+    } else if (a.accumulate) {
+        float4 o = a.acc[p];
+        o.x += gx; o.y += gy; o.z += gz;
+        a.acc[p] = o;
+    } else {
+        a.acc[p] = make_float4(gx, gy, gz, 0.f);
+    }
+}
+
 // ----------------------------------------------------------------- export
 // Tree arrays in the reference's layout for parity checks.
 enum ExportWhat {
@@ -755,6 +892,19 @@ extern "C" int gb_bh_create(gb_bh_t **out, int64_t n_max, int key_bits) {
     h->n_max = n_max;
     h->key_bits = key_bits;
     h->tpl = 1;
+    {
+        const int smem_max = (int)sizeof(int) * LANE_MAX_STACK * LANE_THREADS;
+        const void *lk[] = {(const void *)bh_traverse_lane_kernel<false, false>,
+                            (const void *)bh_traverse_lane_kernel<false, true>,
+                            (const void *)bh_traverse_lane_kernel<true, false>,
+                            (const void *)bh_traverse_lane_kernel<true, true>};
+        for (const void *f : lk) {
+            if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max) != cudaSuccess) {
+                delete h;
+                return fail(GB_ECUDA, "gb_bh_create: cannot enable %d bytes of shared memory", smem_max);
+            }
+        }
+    }
     h->n = -1;
     h->cur = 0;
     const int64_t nn = n_max, ni = std::max<int64_t>(n_max - 1, 1), nodes = 2 * n_max;
@@ -881,10 +1031,25 @@ static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float theta, float eps
     a.accumulate = (flags & GB_ACCUMULATE) ? 1 : 0;
     a.diag = h->diag;
     a.pot = pot;
-    const int tpl = h->tpl;
+    const bool count = (flags & GB_COUNT_WORK) != 0;
+    if (h->tpl == 0 && max_stack <= LANE_MAX_STACK && n - 1 <= ((int64_t)1 << LANE_KBITS)) {
+        const unsigned grid = (unsigned)((n + LANE_THREADS - 1) / LANE_THREADS);
+        const size_t smem = sizeof(int) * (size_t)std::max(max_stack, 1) * LANE_THREADS;
+        const int sel = (kdk ? 2 : 0) + (count ? 1 : 0);
+        switch (sel) {
+            case 0: bh_traverse_lane_kernel<false, false><<<grid, LANE_THREADS, smem, s>>>(a); break;
+            case 1: bh_traverse_lane_kernel<false, true><<<grid, LANE_THREADS, smem, s>>>(a); break;
+            case 2: bh_traverse_lane_kernel<true, false><<<grid, LANE_THREADS, smem, s>>>(a); break;
+            default: bh_traverse_lane_kernel<true, true><<<grid, LANE_THREADS, smem, s>>>(a); break;
+        }
+        GB_CUDA_TRY(cudaGetLastError());
+        mark(h, slot, 5, s);
+        h->launches += 1;
+        return GB_OK;
+    }
+    const int tpl = h->tpl == 2 ? 2 : 1;
     const int64_t warps = (n + 32 * tpl - 1) / (32 * tpl);
     const unsigned grid = (unsigned)((warps + TRAV_WARPS - 1) / TRAV_WARPS);
-    const bool count = (flags & GB_COUNT_WORK) != 0;
     const int sel = (kdk ? 4 : 0) + (count ? 2 : 0) + (tpl == 2 ? 1 : 0);
     switch (sel) {
         case 0: bh_traverse_kernel<false, false, 1><<<grid, TRAV_WARPS * 32, 0, s>>>(a); break;
@@ -1027,8 +1192,8 @@ extern "C" uint64_t gb_bh_launch_count(gb_bh_t *h) { return h ? h->launches : 0;
 
 extern "C" int gb_bh_set_traversal(gb_bh_t *h, int targets_per_lane) {
     if (!h) return fail(GB_EINVAL, "handle is NULL");
-    if (targets_per_lane != 1 && targets_per_lane != 2)
-        return fail(GB_EINVAL, "targets_per_lane must be 1 or 2 (got %d)", targets_per_lane);
+    if (targets_per_lane < 0 || targets_per_lane > 2)
+        return fail(GB_EINVAL, "traversal mode must be 0, 1 or 2 (got %d)", targets_per_lane);
     h->tpl = targets_per_lane;
     return GB_OK;
 }

@@ -109,7 +109,8 @@ class BarnesHut:
         return {k: self.export(k) for k in EXPORTS}
 
     def set_traversal(self, targets_per_lane: int) -> None:
-        """Targets per warp lane in the traversal (1 or 2)."""
+        """Traversal shape: 1 (default) or 2 targets per lane, warp-coherent;
+        0 per-lane walks.  Results are bit-identical across shapes."""
         _lib.call("gb_bh_set_traversal", self._h, int(targets_per_lane))
 
     # -- measurement hooks

@@ -63,7 +63,7 @@ def _run(bhmod, pos, mass, dev, theta=0.5, soft=0.05, bits=21, G=None, max_stack
 
 
 @pytest.mark.parametrize("bits", [21, 10])
-@pytest.mark.parametrize("tpl", [1, 2])
+@pytest.mark.parametrize("tpl", [0, 1, 2])
 def test_golden_tree_bit_exact(cuda_dev, bits, tpl):
     _, bhmod, _, _ = _mods()
     g = load_golden("bh")
@@ -99,7 +99,7 @@ def test_golden_compute_and_duplicates(cuda_dev):
     _check_acc(a, g["dup_acc"])
 
 
-@pytest.mark.parametrize("tpl", [1, 2])
+@pytest.mark.parametrize("tpl", [0, 1, 2])
 def test_stack_rule_matches_reference(cuda_dev, orc, tpl):
     """max_stack=6 silently drops subtrees in the reference (:212); the
     device applies the same rule per lane and counts the drops."""
@@ -129,7 +129,7 @@ def test_engine_bh_golden(cuda_dev):
 
 
 @pytest.mark.parametrize("n", [2, 3, 33, 64, 65, 256, 1000])
-@pytest.mark.parametrize("tpl", [1, 2])
+@pytest.mark.parametrize("tpl", [0, 1, 2])
 def test_small_sizes(cuda_dev, orc, n, tpl):
     _, bhmod, ic, _ = _mods()
     pos, _, mass = ic.exponential_disk(n, seed=n)
@@ -142,7 +142,7 @@ def test_small_sizes(cuda_dev, orc, n, tpl):
     _check_acc(a, ref)
 
 
-@pytest.mark.parametrize("bits,tpl", [(10, 2), (21, 1)])
+@pytest.mark.parametrize("bits,tpl", [(10, 2), (21, 1), (10, 0)])
 def test_config2_disk_1m(cuda_dev, orc, bits, tpl):
     """N = 1,000,000 exponential disk (M = 5, Rd = 3, z0 = 0.3, galactic G),
     theta = 0.5, eps = 0.05: keys, order, topology bit-exact at full size;
@@ -223,3 +223,17 @@ def test_bad_arguments(cuda_dev):
         b.compute(torch.zeros((200, 4), device=cuda_dev), torch.zeros((200, 4), device=cuda_dev))
     with pytest.raises(pkg.GravityError, match="key_bits"):
         bhmod.BarnesHut(100, key_bits=16, device=cuda_dev)
+
+
+def test_traversal_modes_bit_identical(cuda_dev):
+    """Per-lane (0) and warp-coherent (1, 2) traversals visit each target's
+    nodes in the same order, so their accelerations agree bit for bit."""
+    ic = importlib.import_module(PKG_NAME + ".ic")
+    bhmod = importlib.import_module(PKG_NAME + ".solvers.barnes_hut")
+    pos, _, mass = ic.exponential_disk(20000, seed=12)
+    out = []
+    for tpl in (0, 1, 2):
+        b, a = _run(bhmod, pos, mass, cuda_dev, tpl=tpl)
+        out.append(a)
+        b.close()
+    assert np.array_equal(out[0], out[1]) and np.array_equal(out[1], out[2])
