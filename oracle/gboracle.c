@@ -1,7 +1,7 @@
 /*
  * ORACLE — test infrastructure only.  A float64 CPU restatement of the
  * reference's self-gravity hot path (Khaserdene/real-astronomy-simulation),
- * used as the checker for the GPU engine and as the timed CPU baseline.
+ * that the tests compare the GPU engine against, and the timed CPU baseline.
  * Nothing in the shipped package links or calls this file.
  *
  * Pinned against golden fixtures produced by running the reference's own

@@ -1,4 +1,5 @@
-"""ORACLE — test infrastructure only (the checker, never the product).
+"""ORACLE — test infrastructure only (what the tests compare against, never
+the product).
 
 Python front end of the float64 CPU restatement of the reference's hot path
 (``gboracle.c``), plus a numpy restatement of the reference's Morton keys.
@@ -18,6 +19,9 @@ Every function follows a reference function line by line:
 * ``summaries``           core/solvers/barnes_hut.py:124-177
 * ``traverse``            core/solvers/barnes_hut.py:180-217
 * ``bh_compute``          core/solvers/barnes_hut.py:242-259
+* ``analytic_acc``        core/living_galaxy_engine.py:124-151, core/gas_disk_engine.py:54-81
+* ``grav_ext_acc``        core/gas_disk_engine.py:20-51
+* ``grid_rebuild``        core/solvers/neighbor_grid.py:49-136
 """
 from __future__ import annotations
 
