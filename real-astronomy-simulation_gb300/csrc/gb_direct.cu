@@ -34,6 +34,7 @@ struct DirectArgs {
     const float4 *__restrict__ vel;
     const float4 *__restrict__ acc;
     float4 *__restrict__ part;
+    int *st0tab;  // per CTA: its first supertile (read by the fix-up)
     int64_t n, num_ju, U;
     int64_t P;
     int smax;
@@ -74,6 +75,7 @@ direct_force_kernel(DirectArgs a) {
     const int64_t u_end = unit_begin(a.U, a.P, c + 1);
     if (u_begin >= u_end) return;  // whole CTA idle (tiny n)
     const int64_t st0 = u_begin / a.num_ju;
+    if (threadIdx.x == 0) a.st0tab[c] = (int)st0;
     const f2 E2 = pack2(a.eps2, a.eps2);
 
     int64_t u = u_begin;
@@ -194,6 +196,7 @@ direct_force_scalar_kernel(DirectArgs a) {
     const int64_t u_end = unit_begin(a.U, a.P, c + 1);
     if (u_begin >= u_end) return;
     const int64_t st0 = u_begin / a.num_ju;
+    if (threadIdx.x == 0) a.st0tab[c] = (int)st0;
 
     int64_t u = u_begin;
     while (u < u_end) {
@@ -271,6 +274,7 @@ direct_phi_kernel(DirectArgs a) {
     const int64_t u_end = unit_begin(a.U, a.P, c + 1);
     if (u_begin >= u_end) return;
     const int64_t st0 = u_begin / a.num_ju;
+    if (threadIdx.x == 0) a.st0tab[c] = (int)st0;
 
     int64_t u = u_begin;
     while (u < u_end) {
@@ -325,6 +329,7 @@ direct_phi_kernel(DirectArgs a) {
 
 struct FixArgs {
     const float4 *__restrict__ part;
+    const int *__restrict__ st0tab;  // first supertile of each CTA
     float4 *xm;   // KDK: in/out positions
     float4 *vel;  // KDK: in/out velocities
     float4 *acc;  // ACC/KDK: output accelerations (KDK: in = previous)
@@ -346,7 +351,7 @@ __global__ void direct_fixup_kernel(FixArgs f) {
     const int64_t c_hi = unit_owner(f.U, f.P, (st + 1) * f.num_ju - 1);
     float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
     for (int64_t c = c_lo; c <= c_hi; ++c) {
-        const int64_t st0c = unit_begin(f.U, f.P, c) / f.num_ju;
+        const int64_t st0c = __ldg(f.st0tab + c);
         const int64_t slot = (c * f.smax + (st - st0c)) * f.st_size + off;
         const float4 hi = f.part[2 * slot];
         const float4 lo = f.part[2 * slot + 1];
@@ -605,6 +610,9 @@ extern "C" int gb_direct_create(gb_direct_t **out, int64_t n_max) {
     h->packed = 0;
     h->adj_variant = 2;
     int st = ensure_partials(h, max_partials(h, n_max));
+    h->st0_cap = h->sms * 64;  // above every plan's CTA count (ctas_per_sm <= 32)
+    if (st == GB_OK && cudaMalloc(&h->st0tab, sizeof(int) * h->st0_cap) != cudaSuccess)
+        st = fail(GB_ENOMEM, "CTA table");
     if (st == GB_OK && cudaMalloc(&h->phi, sizeof(float) * n_max) != cudaSuccess)
         st = fail(GB_ENOMEM, "phi scratch");
     h->epart_cap = 4 * h->sms;
@@ -625,6 +633,7 @@ extern "C" int gb_direct_create(gb_direct_t **out, int64_t n_max) {
 extern "C" int gb_direct_destroy(gb_direct_t *h) {
     if (!h) return GB_OK;
     cudaFree(h->part);
+    cudaFree(h->st0tab);
     cudaFree(h->phi);
     cudaFree(h->epart);
     cudaFree(h->diag);
@@ -653,11 +662,13 @@ static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, f
     const bool fine = mode != MODE_PHI && !h->packed && use_fine_units(n, np, h->warps, ctas);
     make_plan(n, np, h->warps, ctas, &pl, fine ? SCALAR_UNIT : 0);
     if (plan_partials(pl) > h->part_cap) return fail(GB_EINVAL, "scratch too small for n=%lld", (long long)n);
+    if (pl.P > h->st0_cap) return fail(GB_EINVAL, "%lld CTAs exceed the handle's table", (long long)pl.P);
     DirectArgs a;
     a.xm = xm;
     a.vel = vel;
     a.acc = acc;
     a.part = h->part;
+    a.st0tab = h->st0tab;
     a.n = n;
     a.num_ju = pl.num_ju;
     a.U = pl.U;
@@ -688,6 +699,7 @@ static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, f
     if (e != cudaSuccess) return fail(GB_ECUDA, "force launch: %s", cudaGetErrorString(e));
     FixArgs f;
     f.part = h->part;
+    f.st0tab = h->st0tab;
     f.xm = const_cast<float4 *>(xm);
     f.vel = vel;
     f.acc = acc;
@@ -833,11 +845,13 @@ constexpr int NOALLOC_WARPS = 4;  // supertile of 256 targets
 constexpr int64_t NOALLOC_PART = 2LL * NOALLOC_CTAS * 2 * (NOALLOC_WARPS * 32 * 2 * NOALLOC_NP);  // float4s
 
 static __device__ __align__(256) float4 g_noalloc_part[NOALLOC_PART];
+static __device__ int g_noalloc_tab[NOALLOC_CTAS];  // first supertile per CTA
 
-// Device address of g_noalloc_part per device: in host code the symbol name
-// is only a host-side stand-in, so the address is looked up once per device
-// (with that device current) and cached.
+// Device addresses of g_noalloc_part and g_noalloc_tab per device: in host
+// code the symbol names are only host-side stand-ins, so the addresses are
+// looked up once per device (with that device current) and cached.
 static void *g_noalloc_addr[GB_NOALLOC_MAX_DEVICES];
+static void *g_noalloc_tab_addr[GB_NOALLOC_MAX_DEVICES];
 
 extern "C" int gb_direct_acc_noalloc(const float *xm, float *acc, int64_t n, float G, float eps2, int flags,
                                      void *stream) {
@@ -852,8 +866,10 @@ extern "C" int gb_direct_acc_noalloc(const float *xm, float *acc, int64_t n, flo
     GB_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= GB_NOALLOC_MAX_DEVICES) return fail(GB_EINVAL, "device index %d not supported", dev);
     if (!g_noalloc_addr[dev]) {
-        void *p = nullptr;
+        void *p = nullptr, *t = nullptr;
         GB_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_part));
+        GB_CUDA_TRY(cudaGetSymbolAddress(&t, g_noalloc_tab));
+        g_noalloc_tab_addr[dev] = t;
         g_noalloc_addr[dev] = p;
     }
     DirectPlan pl;
@@ -866,6 +882,7 @@ extern "C" int gb_direct_acc_noalloc(const float *xm, float *acc, int64_t n, flo
     a.vel = nullptr;
     a.acc = nullptr;
     a.part = (float4 *)g_noalloc_addr[dev];
+    a.st0tab = (int *)g_noalloc_tab_addr[dev];
     a.n = n;
     a.num_ju = pl.num_ju;
     a.U = pl.U;
@@ -882,6 +899,7 @@ extern "C" int gb_direct_acc_noalloc(const float *xm, float *acc, int64_t n, flo
     GB_CUDA_TRY(cudaGetLastError());
     FixArgs f;
     f.part = a.part;
+    f.st0tab = a.st0tab;
     f.xm = const_cast<float4 *>(a.xm);
     f.vel = nullptr;
     f.acc = (float4 *)acc;

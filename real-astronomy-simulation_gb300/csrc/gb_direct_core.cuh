@@ -112,6 +112,8 @@ struct gb_direct {
     int packed;                  // 1: .f32x2 inner loop, 0: scalar FP32
     float4 *part;
     int64_t part_cap;            // float4 elements
+    int *st0tab;                 // first supertile of each CTA of the last launch
+    int st0_cap;
     float *phi;                  // n_max floats (energy scratch)
     double2 *epart;              // energy block partials
     int epart_cap;
