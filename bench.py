@@ -226,6 +226,17 @@ def bench_bh(args, dev, rank, world, dist):
            "gpu_launches": int(launches), "diag": diag,
            "stages_ms_per_step": {k: v / max(nst, 1) for k, v in stages.items()}}
 
+    # Tree forces of the final state against FP64 direct sums on 4,096 seeded
+    # targets (untimed).
+    grav = importlib.import_module(PKG + ".solvers.gravity")
+    targets = np.random.default_rng(1234).choice(BH_N, 4096, replace=False)
+    ref = grav.acc_fp64_targets(xm, targets, units.G, BH_EPS * BH_EPS)
+    got = a4[torch.as_tensor(targets, device=dev), :3].double().cpu().numpy()
+    rel = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    res["force_error_vs_fp64_direct"] = {"targets": 4096, "median": float(np.median(rel)),
+                                         "p99": float(np.percentile(rel, 99)), "max": float(rel.max()),
+                                         "rms": float(np.sqrt((rel ** 2).mean()))}
+
     # Work of one traversal, counted by an extra untimed evaluation with the
     # counting kernel variant on the final state of the timed steps.
     tmp = torch.zeros_like(a4)
@@ -761,6 +772,7 @@ def main(argv=None):
             "stages_ms_per_step": res["stages_ms_per_step"],
             "traverse_work_per_step": res["work_per_step"],
             "traverse_fp32_tflops": res["traverse_fp32_tflops"],
+            "force_error_vs_fp64_direct": res["force_error_vs_fp64_direct"],
             "diag": {k: res["diag"][k] for k in ("stack_drops", "stack_overflow", "nonfinite",
                                                   "bad_tree")}}
     if rank == 0 and world == 1:
