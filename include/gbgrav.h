@@ -150,6 +150,14 @@ int gb_bh_kdk(gb_bh_t *h, float *xm, float *vel, float *acc, int64_t n,
               float theta, float eps2, float G, float dt, int64_t nsteps,
               int max_stack, void *stream);
 
+/* gb_bh_kdk replays one captured step as a CUDA graph (on = 1, default)
+ * instead of launching its kernels one by one (on = 0).  The graph is
+ * captured on the first call and again whenever the pointers, n or a
+ * parameter change; results are identical (measured 13% faster per step
+ * at N = 3,000, 6% at 100,000, 1% at 1,000,000).  While stage timing
+ * (gb_bh_timing) is on, the kernels are launched directly. */
+int gb_bh_set_graph(gb_bh_t *h, int on);
+
 /* Copies one array of the last build, in the reference's layout, to device
  * memory dst: 0 codes (uint64[n], key order), 1 order (int32[n]), 2 left,
  * 3 right (int32[n-1]), 4 parent (int32[2n-1]), 5 mass (double[2n-1]),

@@ -859,6 +859,24 @@ struct gb_bh {
     uint64_t launches;  // kernels launched by this handle (host count)
     int pending_slot;   // timing slot of the last gb_bh_build
     int tpl;            // traversal targets per lane (1 or 2)
+    // One KDK step captured as a CUDA graph (gb_bh_kdk), replayed per step
+    // on the handle's own stream and joined to the caller's by events.
+    int use_graph;
+    cudaStream_t gstream;
+    cudaEvent_t gev_in, gev_out;
+    cudaGraphExec_t gexec;
+    bool has_graph;
+    struct Key {
+        const void *xm, *vel, *acc;
+        int64_t n;
+        float theta, eps2, G, dt;
+        int max_stack, tpl;
+        bool operator==(const Key &o) const {
+            return xm == o.xm && vel == o.vel && acc == o.acc && n == o.n && theta == o.theta && eps2 == o.eps2 &&
+                   G == o.G && dt == o.dt && max_stack == o.max_stack && tpl == o.tpl;
+        }
+    } gkey;
+    uint64_t graph_launches;  // kernels in the captured step
 };
 
 static void mark(gb_bh_t *h, int step_slot, int stage, cudaStream_t s) {
@@ -875,6 +893,10 @@ extern "C" int gb_bh_destroy(gb_bh_t *h) {
                     h->inode, h->root, h->totals, h->diag};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    if (h->has_graph) cudaGraphExecDestroy(h->gexec);
+    if (h->gev_in) cudaEventDestroy(h->gev_in);
+    if (h->gev_out) cudaEventDestroy(h->gev_out);
+    if (h->gstream) cudaStreamDestroy(h->gstream);
     for (auto &e : h->ev)
         if (e) cudaEventDestroy(e);
     delete h;
@@ -892,6 +914,7 @@ extern "C" int gb_bh_create(gb_bh_t **out, int64_t n_max, int key_bits) {
     h->n_max = n_max;
     h->key_bits = key_bits;
     h->tpl = 1;
+    h->use_graph = 1;
     {
         const int smem_max = (int)sizeof(int) * LANE_MAX_STACK * LANE_THREADS;
         const void *lk[] = {(const void *)bh_traverse_lane_kernel<false, false>,
@@ -1120,6 +1143,15 @@ extern "C" int gb_bh_compute(gb_bh_t *h, const float *xm, float *acc, int64_t n,
     return gb_bh_accel(h, acc, theta, eps2, G, max_stack, flags, stream);
 }
 
+// One KDK step: tree build with the fused kick and drift, then the traversal
+// with the closing kick.
+static int kdk_step(gb_bh_t *h, float4 *xm, float4 *vel, float4 *acc, int64_t n, float theta, float eps2, float G,
+                    float dt, int max_stack, cudaStream_t s) {
+    const int slot = next_slot(h);
+    GB_TRY(build_any(h, xm, vel, acc, n, dt, true, s, slot));
+    return traverse(h, acc, vel, theta, eps2, G, dt, max_stack, 0, true, s, slot);
+}
+
 extern "C" int gb_bh_kdk(gb_bh_t *h, float *xm, float *vel, float *acc, int64_t n, float theta, float eps2, float G,
                          float dt, int64_t nsteps, int max_stack, void *stream) {
     GB_TRY(check_bh(h, n));
@@ -1130,11 +1162,53 @@ extern "C" int gb_bh_kdk(gb_bh_t *h, float *xm, float *vel, float *acc, int64_t 
     GB_TRY(check_ptr(acc, "acc"));
     GB_TRY(check_params(theta, eps2, max_stack));
     cudaStream_t s = (cudaStream_t)stream;
-    for (int64_t k = 0; k < nsteps; ++k) {
-        const int slot = next_slot(h);
-        GB_TRY(build_any(h, (float4 *)xm, (float4 *)vel, (const float4 *)acc, n, dt, true, s, slot));
-        GB_TRY(traverse(h, (float4 *)acc, (float4 *)vel, theta, eps2, G, dt, max_stack, 0, true, s, slot));
+    float4 *x = (float4 *)xm, *v = (float4 *)vel, *a = (float4 *)acc;
+    if (!h->use_graph || h->timing) {
+        for (int64_t k = 0; k < nsteps; ++k) GB_TRY(kdk_step(h, x, v, a, n, theta, eps2, G, dt, max_stack, s));
+        return GB_OK;
     }
+    const gb_bh::Key key{xm, vel, acc, n, theta, eps2, G, dt, max_stack, h->tpl};
+    if (!h->has_graph || !(h->gkey == key)) {
+        if (h->has_graph) {
+            cudaGraphExecDestroy(h->gexec);
+            h->has_graph = false;
+        }
+        if (!h->gstream) {
+            GB_CUDA_TRY(cudaStreamCreateWithFlags(&h->gstream, cudaStreamNonBlocking));
+            GB_CUDA_TRY(cudaEventCreateWithFlags(&h->gev_in, cudaEventDisableTiming));
+            GB_CUDA_TRY(cudaEventCreateWithFlags(&h->gev_out, cudaEventDisableTiming));
+        }
+        GB_CUDA_TRY(cudaStreamBeginCapture(h->gstream, cudaStreamCaptureModeThreadLocal));
+        const uint64_t l0 = h->launches;
+        const int st = kdk_step(h, x, v, a, n, theta, eps2, G, dt, max_stack, h->gstream);
+        h->graph_launches = h->launches - l0;
+        h->launches = l0;
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(h->gstream, &graph);
+        if (st != GB_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return st;
+        }
+        if (e != cudaSuccess) return fail(GB_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+        const cudaError_t ei = cudaGraphInstantiate(&h->gexec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) return fail(GB_ECUDA, "graph instantiate: %s", cudaGetErrorString(ei));
+        h->has_graph = true;
+        h->gkey = key;
+    }
+    GB_CUDA_TRY(cudaEventRecord(h->gev_in, s));
+    GB_CUDA_TRY(cudaStreamWaitEvent(h->gstream, h->gev_in, 0));
+    for (int64_t k = 0; k < nsteps; ++k) GB_CUDA_TRY(cudaGraphLaunch(h->gexec, h->gstream));
+    GB_CUDA_TRY(cudaEventRecord(h->gev_out, h->gstream));
+    GB_CUDA_TRY(cudaStreamWaitEvent(s, h->gev_out, 0));
+    h->launches += h->graph_launches * (uint64_t)nsteps;
+    h->n = n;
+    return GB_OK;
+}
+
+extern "C" int gb_bh_set_graph(gb_bh_t *h, int on) {
+    if (!h) return fail(GB_EINVAL, "handle is NULL");
+    h->use_graph = on ? 1 : 0;
     return GB_OK;
 }
 

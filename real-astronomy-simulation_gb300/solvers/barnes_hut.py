@@ -108,6 +108,11 @@ class BarnesHut:
     def tree_arrays(self) -> dict:
         return {k: self.export(k) for k in EXPORTS}
 
+    def set_graph(self, on: bool = True) -> None:
+        """kdk() replays one captured step as a CUDA graph (identical
+        results, fewer launches)."""
+        _lib.call("gb_bh_set_graph", self._h, 1 if on else 0)
+
     def set_traversal(self, targets_per_lane: int) -> None:
         """Traversal shape: 1 (default) or 2 targets per lane, warp-coherent;
         0 per-lane walks.  Results are bit-identical across shapes."""
