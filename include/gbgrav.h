@@ -41,7 +41,7 @@ extern "C" {
 #define GB_ACCUMULATE 0x1  /* acc += result instead of acc = result */
 #define GB_PLAIN_FP32 0x2  /* plain FP32 accumulation (no Kahan compensation) */
 #define GB_COUNT_WORK 0x4  /* tree traversal also counts its work (gb_diag_t) */
-#define GB_USE_GRAPH 0x8   /* batched KDK: capture the step loop as one CUDA graph */
+#define GB_USE_GRAPH 0x8   /* KDK calls: replay captured steps as a CUDA graph */
 
 /* Device diagnostic counters, read back by gb_*_diag (synchronising). */
 typedef struct gb_diag {
@@ -86,7 +86,10 @@ int gb_direct_acc(gb_direct_t *h, const float *xm, float *acc, int64_t n,
 /* nsteps kick-drift-kick leapfrog steps with direct forces, in place.
  * acc must hold the accelerations of the current positions on entry.
  * Replaces Engine.step (core/engine.py:108-116) with kick/drift
- * (core/integrators/leapfrog.py:11-22) fused into the force pass. */
+ * (core/integrators/leapfrog.py:11-22) fused into the force pass.  With
+ * GB_USE_GRAPH one step is captured as a CUDA graph (again whenever the
+ * pointers, n, a parameter or the tile shape change) and replayed nsteps
+ * times: identical results, less launch overhead at small n. */
 int gb_direct_kdk(gb_direct_t *h, float *xm, float *vel, float *acc, int64_t n,
                   float G, float eps2, float dt, int64_t nsteps, int flags,
                   void *stream);

@@ -632,6 +632,10 @@ extern "C" int gb_direct_create(gb_direct_t **out, int64_t n_max) {
 
 extern "C" int gb_direct_destroy(gb_direct_t *h) {
     if (!h) return GB_OK;
+    if (h->has_graph) cudaGraphExecDestroy(h->gexec);
+    if (h->gev_in) cudaEventDestroy(h->gev_in);
+    if (h->gev_out) cudaEventDestroy(h->gev_out);
+    if (h->gstream) cudaStreamDestroy(h->gstream);
     cudaFree(h->part);
     cudaFree(h->st0tab);
     cudaFree(h->phi);
@@ -764,9 +768,50 @@ extern "C" int gb_direct_kdk(gb_direct_t *h, float *xm, float *vel, float *acc, 
     GB_TRY(check_xm(vel, "vel"));
     GB_TRY(check_xm(acc, "acc"));
     if (!(eps2 > 0.f)) return fail(GB_EINVAL, "eps2 must be > 0");
-    for (int64_t s = 0; s < nsteps; ++s)
-        GB_TRY(run_direct(h, MODE_KDK, (const float4 *)xm, (float4 *)vel, (float4 *)acc, nullptr, n, G, eps2,
-                          dt, flags & GB_PLAIN_FP32, (cudaStream_t)stream));
+    cudaStream_t s = (cudaStream_t)stream;
+    const int plain = flags & GB_PLAIN_FP32;
+    if (!(flags & GB_USE_GRAPH)) {
+        for (int64_t k = 0; k < nsteps; ++k)
+            GB_TRY(run_direct(h, MODE_KDK, (const float4 *)xm, (float4 *)vel, (float4 *)acc, nullptr, n, G, eps2,
+                              dt, plain, s));
+        return GB_OK;
+    }
+    // One step captured on the handle's stream and replayed nsteps times.
+    const gb_direct::Key key{xm, vel, acc, n, G, eps2, dt, plain, h->np, h->warps, h->ctas_per_sm, h->packed};
+    if (!h->has_graph || !(h->gkey == key)) {
+        if (h->has_graph) {
+            cudaGraphExecDestroy(h->gexec);
+            h->has_graph = false;
+        }
+        if (!h->gstream) {
+            GB_CUDA_TRY(cudaStreamCreateWithFlags(&h->gstream, cudaStreamNonBlocking));
+            GB_CUDA_TRY(cudaEventCreateWithFlags(&h->gev_in, cudaEventDisableTiming));
+            GB_CUDA_TRY(cudaEventCreateWithFlags(&h->gev_out, cudaEventDisableTiming));
+        }
+        GB_CUDA_TRY(cudaStreamBeginCapture(h->gstream, cudaStreamCaptureModeThreadLocal));
+        const uint64_t l0 = h->launches;
+        const int st = run_direct(h, MODE_KDK, (const float4 *)xm, (float4 *)vel, (float4 *)acc, nullptr, n, G,
+                                  eps2, dt, plain, h->gstream);
+        h->launches = l0;
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(h->gstream, &graph);
+        if (st != GB_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return st;
+        }
+        if (e != cudaSuccess) return fail(GB_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+        const cudaError_t ei = cudaGraphInstantiate(&h->gexec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) return fail(GB_ECUDA, "graph instantiate: %s", cudaGetErrorString(ei));
+        h->has_graph = true;
+        h->gkey = key;
+    }
+    GB_CUDA_TRY(cudaEventRecord(h->gev_in, s));
+    GB_CUDA_TRY(cudaStreamWaitEvent(h->gstream, h->gev_in, 0));
+    for (int64_t k = 0; k < nsteps; ++k) GB_CUDA_TRY(cudaGraphLaunch(h->gexec, h->gstream));
+    GB_CUDA_TRY(cudaEventRecord(h->gev_out, h->gstream));
+    GB_CUDA_TRY(cudaStreamWaitEvent(s, h->gev_out, 0));
+    h->launches += 2 * (uint64_t)nsteps;
     return GB_OK;
 }
 

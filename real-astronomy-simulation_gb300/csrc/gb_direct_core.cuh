@@ -122,4 +122,21 @@ struct gb_direct {
     float4 *sym;        // symmetric adjoint partials (allocated on first use)
     int64_t sym_cap;    // float4 elements
     int adj_variant;    // 2: symmetric packed, 1: symmetric scalar, 0: one pass per target
+    // One KDK step captured as a CUDA graph (gb_direct_kdk with
+    // GB_USE_GRAPH), replayed per step on the handle's own stream.
+    cudaStream_t gstream;
+    cudaEvent_t gev_in, gev_out;
+    cudaGraphExec_t gexec;
+    bool has_graph;
+    struct Key {
+        const void *xm, *vel, *acc;
+        int64_t n;
+        float G, eps2, dt;
+        int plain, np, warps, ctas_per_sm, packed;
+        bool operator==(const Key &o) const {
+            return xm == o.xm && vel == o.vel && acc == o.acc && n == o.n && G == o.G && eps2 == o.eps2 &&
+                   dt == o.dt && plain == o.plain && np == o.np && warps == o.warps &&
+                   ctas_per_sm == o.ctas_per_sm && packed == o.packed;
+        }
+    } gkey;
 };

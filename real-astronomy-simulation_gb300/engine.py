@@ -175,7 +175,7 @@ class Engine:
                     self._bh.kdk(self.xm, self.v4, self.a4, dt, nsteps)
                 else:
                     self._direct.kdk(self.xm, self.v4, self.a4, self.G, self.eps2, dt, nsteps,
-                                     plain=self.plain_fp32)
+                                     plain=self.plain_fp32, graph=True)
         self.time += dt * nsteps
         self.step_count += nsteps
 

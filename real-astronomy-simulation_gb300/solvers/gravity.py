@@ -64,11 +64,13 @@ class DirectGravity:
                   float(G), float(eps2), flags, stream_handle(self.device))
         return acc
 
-    def kdk(self, xm, vel, acc, G, eps2, dt, nsteps=1, plain=False):
+    def kdk(self, xm, vel, acc, G, eps2, dt, nsteps=1, plain=False, graph=False):
+        """nsteps fused KDK steps in place; graph=True replays one captured
+        step as a CUDA graph (identical results, fewer launches)."""
         n = xm.shape[0]
+        flags = (_lib.GB_PLAIN_FP32 if plain else 0) | (_lib.GB_USE_GRAPH if graph else 0)
         _lib.call("gb_direct_kdk", self._h, ptr(xm, "xm"), ptr(vel, "vel"), ptr(acc, "acc"),
-                  n, float(G), float(eps2), float(dt), int(nsteps),
-                  _lib.GB_PLAIN_FP32 if plain else 0, stream_handle(self.device))
+                  n, float(G), float(eps2), float(dt), int(nsteps), flags, stream_handle(self.device))
 
     def phi(self, xm, eps2, out=None, plain=False):
         n = xm.shape[0]

@@ -194,3 +194,29 @@ def test_bad_arguments_raise(cuda_dev):
         s.acc(xm[:10], acc[:10], 1.0, 0.0)
     with pytest.raises(pkg.GravityError):
         s.set_tiles(3, 8)
+
+
+def test_kdk_graph_replay_matches_direct_launches(cuda_dev):
+    """gb_direct_kdk with GB_USE_GRAPH (one captured step replayed) and with
+    direct launches: identical trajectories, including recaptures when dt
+    and the tile shape change."""
+    grav = importlib.import_module(PKG_NAME + ".solvers.gravity")
+    ic = importlib.import_module(PKG_NAME + ".ic")
+    p, v, m = ic.plummer(3000, seed=9)
+    out = []
+    for graph in (True, False):
+        xm = torch.tensor(np.column_stack((p, m)), dtype=torch.float32, device=cuda_dev)
+        v4 = torch.zeros_like(xm)
+        v4[:, :3] = torch.tensor(v, dtype=torch.float32, device=cuda_dev)
+        a4 = torch.zeros_like(xm)
+        s = grav.DirectGravity(3000, cuda_dev)
+        s.acc(xm, a4, 1.0, 1e-4)
+        s.kdk(xm, v4, a4, 1.0, 1e-4, 1e-3, 4, graph=graph)
+        s.kdk(xm, v4, a4, 1.0, 1e-4, 2e-3, 3, graph=graph)
+        s.set_tiles(2, 4)
+        s.kdk(xm, v4, a4, 1.0, 1e-4, 1e-3, 2, graph=graph)
+        torch.cuda.synchronize()
+        out.append((xm.clone(), v4.clone(), a4.clone()))
+        s.close()
+    for u, w in zip(*out):
+        assert torch.equal(u, w)
