@@ -1,1 +1,3 @@
-"""Gravity solvers: direct N^2 (gravity) and LBVH Barnes-Hut (barnes_hut)."""
+"""Gravity solvers: direct N^2 (gravity), LBVH Barnes-Hut (barnes_hut), the
+analytic galaxy potential (external) and the SPH neighbour grid
+(neighbor_grid)."""
