@@ -86,3 +86,45 @@ class FieldView:
     def __array__(self, dtype=None, copy=None):
         a = self.to_numpy()
         return a.astype(dtype) if dtype is not None else a
+
+
+def field_values(x, device) -> torch.Tensor:
+    """float32 device tensor of a reference-style field (anything with
+    ``to_numpy``), a FieldView, a numpy array or a torch tensor."""
+    if isinstance(x, FieldView):
+        t = x.tensor
+    elif isinstance(x, torch.Tensor):
+        t = x
+    elif hasattr(x, "to_numpy"):
+        t = torch.from_numpy(np.ascontiguousarray(x.to_numpy()))
+    else:
+        t = torch.as_tensor(np.asarray(x))
+    return t.to(device=device, dtype=torch.float32)
+
+
+def write_rows(dst, values: torch.Tensor) -> None:
+    """Write values (device, rows 0..len-1) into the first rows of dst: a
+    FieldView, a torch tensor, a numpy array or a reference-style field
+    (``to_numpy`` / ``from_numpy``)."""
+    n = values.shape[0]
+    if isinstance(dst, FieldView):
+        dst._buf[:n, dst._cols] = values.to(dst._buf.dtype)
+    elif isinstance(dst, torch.Tensor):
+        dst[:n] = values.to(device=dst.device, dtype=dst.dtype)
+    elif isinstance(dst, np.ndarray):
+        dst[:n] = values.double().cpu().numpy().reshape(dst[:n].shape)
+    else:
+        full = np.array(dst.to_numpy())
+        full[:n] = values.double().cpu().numpy().reshape(full[:n].shape)
+        dst.from_numpy(full)
+
+
+def pick_device(*xs) -> torch.device:
+    """The CUDA device of the first CUDA tensor (or FieldView) among xs,
+    else the current CUDA device."""
+    for x in xs:
+        if isinstance(x, FieldView):
+            return x.tensor.device
+        if isinstance(x, torch.Tensor) and x.is_cuda:
+            return x.device
+    return require_cuda()

@@ -16,7 +16,7 @@ import numpy as np
 import torch
 
 from .. import _lib, units
-from .._dev import ptr, require_cuda, stream_handle
+from .._dev import empty4, field_values, pick_device, ptr, require_cuda, stream_handle, write_rows
 
 EXPORTS = {"code": (0, np.uint64, 1, 0), "order": (1, np.int32, 1, 0),
            "left": (2, np.int32, 1, -1), "right": (3, np.int32, 1, -1),
@@ -76,11 +76,29 @@ class BarnesHut:
                   stream_handle(self.device))
         return acc
 
-    def compute(self, xm: torch.Tensor, acc: torch.Tensor, accumulate: bool = False,
-                count_work: bool = False) -> torch.Tensor:
-        """acc <- tree accelerations of the particles in xm
-        (core/solvers/barnes_hut.py:242-259).  count_work adds the traversal
-        work counters to diag() (a slightly slower kernel variant)."""
+    def compute(self, *args, accumulate: bool = False, count_work: bool = False):
+        """acc <- tree accelerations (core/solvers/barnes_hut.py:242-259).
+        Call forms: ``compute(pos_field, mass_field, acc_field)``, the
+        reference's (fields, numpy arrays or tensors; acc filled in place),
+        or ``compute(xm, acc)`` on (n, 4) float32 device records.
+        count_work adds the traversal work counters to diag() (a slightly
+        slower kernel variant)."""
+        if len(args) == 3:
+            pos, mass, acc_out = args
+            dev = pick_device(pos, mass, acc_out)
+            xm = empty4(self.n, dev)
+            xm[:, :3] = field_values(pos, dev)[: self.n].reshape(self.n, 3)
+            xm[:, 3] = field_values(mass, dev)[: self.n].reshape(self.n)
+            acc = empty4(self.n, dev)
+            if accumulate:
+                acc[:, :3] = field_values(acc_out, dev)[: self.n].reshape(self.n, 3)
+            self._compute(xm, acc, accumulate, count_work)
+            write_rows(acc_out, acc[:, :3])
+            return acc_out
+        xm, acc = args
+        return self._compute(xm, acc, accumulate, count_work)
+
+    def _compute(self, xm, acc, accumulate, count_work):
         self._last_n = self._n(xm)
         flags = (_lib.GB_ACCUMULATE if accumulate else 0) | (_lib.GB_COUNT_WORK if count_work else 0)
         _lib.call("gb_bh_compute", self._h, ptr(xm, "xm"), ptr(acc, "acc"), self._last_n,

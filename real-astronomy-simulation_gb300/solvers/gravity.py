@@ -18,7 +18,7 @@ import numpy as np
 import torch
 
 from .. import _lib
-from .._dev import ptr, require_cuda, stream_handle
+from .._dev import empty4, field_values, pick_device, ptr, require_cuda, stream_handle, write_rows
 
 
 class DirectGravity:
@@ -124,21 +124,64 @@ def _solver_for(xm: torch.Tensor) -> DirectGravity:
     return s
 
 
-def compute_acc_direct(xm, acc, n, grav, eps2):
-    """acc[:n] = G sum_j m_j d_ij / (|d_ij|^2 + eps2)^{3/2} (core/solvers/gravity.py:13-26)."""
+def _pack(pos, mass, n) -> torch.Tensor:
+    """(n, 4) float32 device records from separate position and mass fields."""
+    dev = pick_device(pos, mass)
+    xm = empty4(n, dev)
+    xm[:, :3] = field_values(pos, dev)[:n].reshape(n, 3)
+    xm[:, 3] = field_values(mass, dev)[:n].reshape(n)
+    return xm
+
+
+def _is_records(x) -> bool:
+    return isinstance(x, torch.Tensor) and x.dim() == 2 and x.shape[1] == 4
+
+
+def compute_acc_direct(*args):
+    """acc[:n] = G sum_j m_j d_ij / (|d_ij|^2 + eps2)^{3/2}
+    (core/solvers/gravity.py:13-26).  Two call forms:
+
+    * ``compute_acc_direct(pos, mass, acc, n, grav, eps2)``, the reference's:
+      pos / acc (n, 3) and mass (n,) as reference-style fields (``to_numpy``
+      / ``from_numpy``), numpy arrays or torch tensors; acc is filled in
+      place (rows 0..n-1);
+    * ``compute_acc_direct(xm, acc, n, grav, eps2)`` on (n, 4) float32 device
+      records (no copies)."""
+    if len(args) == 6:
+        pos, mass, acc, n, grav, eps2 = args
+        n = int(n)
+        xm = _pack(pos, mass, n)
+        out = empty4(n, xm.device)
+        _solver_for(xm).acc(xm, out, grav, eps2)
+        write_rows(acc, out[:, :3])
+        return
+    xm, acc, n, grav, eps2 = args
     xm_n = xm[:n] if n != xm.shape[0] else xm
     acc_n = acc[:n] if n != acc.shape[0] else acc
     _solver_for(xm).acc(xm_n, acc_n, grav, eps2)
 
 
-def kinetic_energy(vel, xm, n, grav=1.0, eps2=1.0):
-    """1/2 sum m |v|^2 in FP64 (core/solvers/gravity.py:29-36)."""
-    return _solver_for(xm).energies(xm[:n], vel[:n], grav, eps2)[0]
+def kinetic_energy(vel, mass, n, grav=1.0, eps2=1.0):
+    """1/2 sum m |v|^2 in FP64 (core/solvers/gravity.py:29-36).  ``mass``
+    is the reference's (n,) mass field or, with device records, the (n, 4)
+    ``xm`` tensor; vel is a reference-style field, array or tensor."""
+    n = int(n)
+    xm = mass[:n] if _is_records(mass) else _pack(torch.zeros((n, 3)), mass, n)
+    v = field_values(vel, xm.device)[:n]
+    v4 = empty4(n, xm.device)
+    v4[:, :3] = v[:, :3] if v.dim() == 2 else v.reshape(n, 3)
+    return _solver_for(xm).energies(xm, v4, grav, eps2)[0]
 
 
-def potential_energy(xm, n, grav, eps2, vel=None):
+def potential_energy(*args, vel=None):
     """-1/2 G sum_i m_i sum_{j != i} m_j / sqrt(r^2 + eps2)
-    (core/solvers/gravity.py:39-57); FP32 pair sums, FP64 reduction."""
-    if vel is None:
-        vel = torch.zeros_like(xm)
-    return _solver_for(xm).energies(xm[:n], vel[:n], grav, eps2)[1]
+    (core/solvers/gravity.py:39-57); FP32 pair sums, FP64 reduction.  Call
+    forms: ``potential_energy(pos, mass, n, grav, eps2)`` (the reference's)
+    or ``potential_energy(xm, n, grav, eps2)`` on device records."""
+    if len(args) == 5:
+        pos, mass, n, grav, eps2 = args
+        xm = _pack(pos, mass, int(n))
+    else:
+        xm, n, grav, eps2 = args
+        xm = xm[:n]
+    return _solver_for(xm).energies(xm, torch.zeros_like(xm), grav, eps2)[1]
