@@ -94,6 +94,14 @@ int gb_direct_kdk(gb_direct_t *h, float *xm, float *vel, float *acc, int64_t n,
                   float G, float eps2, float dt, int64_t nsteps, int flags,
                   void *stream);
 
+/* Standalone leapfrog halves on n float4 records, for callers that step
+ * outside the fused KDK path: vel += acc * dt_half (kick, core/integrators/
+ * leapfrog.py:11-15) and xm.xyz += vel * dt (drift, :18-22; the mass column
+ * is untouched).  Same FMA forms as the fused step, so kick -> drift ->
+ * gb_direct_acc -> kick equals gb_direct_kdk bit for bit. */
+int gb_kick(float *vel, const float *acc, int64_t n, float dt_half, void *stream);
+int gb_drift(float *xm, const float *vel, int64_t n, float dt, void *stream);
+
 /* phi_i = sum_{j != i} m_j / sqrt(|x_j - x_i|^2 + eps2) (FP32, Kahan): the
  * inner sum of potential_energy (core/solvers/gravity.py:47-55). */
 int gb_direct_phi(gb_direct_t *h, const float *xm, float *phi, int64_t n,

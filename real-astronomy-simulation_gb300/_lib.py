@@ -111,6 +111,8 @@ SIGNATURES = {
     "gb_direct_acc_ext": (I32, [P, P, P, I64, F32, F32, P, I32, P]),
     "gb_bh_accel_ext": (I32, [P, P, F32, F32, F32, I32, P, I32, P]),
     "gb_bh_set_graph": (I32, [P, I32]),
+    "gb_kick": (I32, [P, P, I64, F32, P]),
+    "gb_drift": (I32, [P, P, I64, F32, P]),
     "gb_grid_create": (I32, [ctypes.POINTER(P), I64, F64]),
     "gb_grid_destroy": (I32, [P]),
     "gb_grid_max_cells": (I64, [P]),

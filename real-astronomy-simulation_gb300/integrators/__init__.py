@@ -1,1 +1,1 @@
-"""Leapfrog integrator entry points."""
+"""Integrators: the leapfrog halves (leapfrog)."""
