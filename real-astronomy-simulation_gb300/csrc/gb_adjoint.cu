@@ -405,12 +405,16 @@ __device__ __forceinline__ void sym2_round(const float4 *__restrict__ sxm, const
                                            const f2 (&TNM)[2], const f2 (&TWX)[2], const f2 (&TWY)[2],
                                            const f2 (&TWZ)[2], f2 (&NX)[2], f2 (&NY)[2], f2 (&NZ)[2],
                                            f2 (&NG)[2]) {
+    // 3 m_t for the lane's targets: d.u = m_s d.w_t - m_t d.w_s, so
+    // -3 d.u = (-3 m_s) d.w_t + (3 m_t) d.w_s from the two dot products.
+    const f2 TM3[2] = {mul2(TNM[0], NEG3), mul2(TNM[1], NEG3)};
 #pragma unroll 2
     for (int k = 0; k < 32; ++k) {
         const int jj = g * 32 + ((lane + k) & 31);
         const float4 xs = sxm[jj], ws = sw[jj];
         const f2 sx = pack2(xs.x, xs.x), sy = pack2(xs.y, xs.y), sz = pack2(xs.z, xs.z);
         const f2 sm = pack2(xs.w, xs.w);
+        const f2 sm3 = mul2(sm, NEG3);
         const f2 swx = pack2(ws.x, ws.x), swy = pack2(ws.y, ws.y), swz = pack2(ws.z, ws.z);
         f2 PX = 0ull, PY = 0ull, PZ = 0ull, PG = 0ull;
 #pragma unroll
@@ -433,11 +437,10 @@ __device__ __forceinline__ void sym2_round(const float4 *__restrict__ sxm, const
             const f2 ux = fma2(TNM[h], swx, mul2(sm, TWX[h]));
             const f2 uy = fma2(TNM[h], swy, mul2(sm, TWY[h]));
             const f2 uz = fma2(TNM[h], swz, mul2(sm, TWZ[h]));
-            const f2 du = fma2(dz, uz, fma2(dy, uy, mul2(dx, ux)));
-            const f2 ne = mul2(mul2(NEG3, inv2), du);
-            const f2 vx = fma2(ne, dx, ux), vy = fma2(ne, dy, uy), vz = fma2(ne, dz, uz);
             const f2 dwt = fma2(dz, TWZ[h], fma2(dy, TWY[h], mul2(dx, TWX[h])));
             const f2 dws = fma2(dz, swz, fma2(dy, swy, mul2(dx, swx)));
+            const f2 ne = mul2(inv2, fma2(sm3, dwt, mul2(TM3[h], dws)));  // -3 inv2 d.u
+            const f2 vx = fma2(ne, dx, ux), vy = fma2(ne, dy, uy), vz = fma2(ne, dz, uz);
             NX[h] = fma2(sv, vx, NX[h]);
             NY[h] = fma2(sv, vy, NY[h]);
             NZ[h] = fma2(sv, vz, NZ[h]);
