@@ -683,6 +683,58 @@ def bench_snapshot(dev, n=1_000_000, steps=100, every=20):
                                           "async": (out["async_s"] - out["none_s"]) / (steps // every + 1) * 1e3}}
 
 
+def bench_scaling(dev, sizes=(10_000, 100_000, 1_000_000, 4_000_000, 16_000_000)):
+    """BH KDK step time and force error against N (exponential disk, theta
+    0.5, eps 0.05, 30-bit keys; error against FP64 direct sums on 256 seeded
+    targets), and one direct N^2 force evaluation at N = 1M."""
+    ic = importlib.import_module(PKG + ".ic")
+    bhmod = importlib.import_module(PKG + ".solvers.barnes_hut")
+    grav = importlib.import_module(PKG + ".solvers.gravity")
+    units = importlib.import_module(PKG + ".units")
+    rows = []
+    direct_ms = None
+    for n in sizes:
+        pos, vel, mass = ic.exponential_disk(n, seed=1)
+        xm, v4 = _xm(pos, mass, dev), _v4(vel, dev)
+        a4 = torch.zeros_like(xm)
+        bh = bhmod.BarnesHut(n, theta=BH_THETA, softening=BH_EPS, key_bits=BH_BITS, G=units.G, device=dev)
+        bh.compute(xm, a4)
+        targets = np.random.default_rng(2).choice(n, 256, replace=False)
+        ref = grav.acc_fp64_targets(xm, targets, units.G, BH_EPS * BH_EPS)
+        got = a4[torch.as_tensor(targets, device=dev), :3].double().cpu().numpy()
+        rel = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
+        for _ in range(3):
+            bh.kdk(xm, v4, a4, BH_DT, 1)
+        reps = 10 if n <= 4_000_000 else 3
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        s.record()
+        bh.kdk(xm, v4, a4, BH_DT, reps)
+        e.record()
+        torch.cuda.synchronize()
+        ms = s.elapsed_time(e) / reps
+        d = bh.diag(reset=True)
+        rows.append({"n": n, "bh_step_ms": ms, "particle_steps_per_s": n / ms * 1e3,
+                     "force_error_median": float(np.median(rel)), "p99": float(np.percentile(rel, 99)),
+                     "max": float(rel.max()),
+                     "stack_drops": d["stack_drops"], "bad_tree": d["bad_tree"]})
+        bh.close()
+        if n == 1_000_000:
+            g = grav.DirectGravity(n, dev)
+            acc = torch.zeros_like(xm)
+            g.acc(xm, acc, units.G, BH_EPS * BH_EPS)
+            s.record()
+            g.acc(xm, acc, units.G, BH_EPS * BH_EPS)
+            e.record()
+            torch.cuda.synchronize()
+            direct_ms = s.elapsed_time(e)
+            g.close()
+        del xm, v4, a4
+        torch.cuda.empty_cache()
+    return {"workload": "BH KDK step against N, exponential disk, theta 0.5, eps 0.05, 30-bit keys",
+            "rows": rows, "direct_force_ms_at_1m": direct_ms}
+
+
 # ------------------------------------------------------------------- main
 def run_reference(args):
     """Reference arm: the float64 CPU restatement of the reference's BH path
@@ -729,7 +781,7 @@ def main(argv=None):
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--drift-steps", type=int, default=1000)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
-    ap.add_argument("--only", choices=("direct", "merger", "batch", "adjoint", "grid", "snapshot"),
+    ap.add_argument("--only", choices=("direct", "merger", "batch", "adjoint", "grid", "snapshot", "scaling"),
                     help="run one secondary workload alone (profiling runs)")
     args = ap.parse_args(argv)
     if args.warmup < 3:
@@ -756,7 +808,8 @@ def main(argv=None):
               "batch": lambda: bench_batch(dev),
               "adjoint": lambda: bench_adjoint(dev),
               "grid": lambda: bench_grid(dev),
-              "snapshot": lambda: bench_snapshot(dev)}[args.only]
+              "snapshot": lambda: bench_snapshot(dev),
+              "scaling": lambda: bench_scaling(dev)}[args.only]
         print(json.dumps({"only": args.only, "fp32_peak_tflops_measured": peak,
                           "result": fn()}), flush=True)
         return 0
