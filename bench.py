@@ -347,7 +347,9 @@ def cpu_bh_step(budget_s: float = 20.0):
 # ------------------------------------------------------------- secondary
 def bench_direct(dev, lib_mod, peak_tflops):
     """Direct N^2 Plummer, N = 20,000, G = 1, eps = 0.01, dt = 1e-3, 100 KDK
-    steps; plus the force kernel's own FP32 fraction at N = 20k and 262k."""
+    steps through the Engine (symmetric pass); plus the per-target force
+    kernel's own FP32 fraction at N = 20k and 262k, and the symmetric pass
+    at the same sizes."""
     pkg = importlib.import_module(PKG)
     ic = importlib.import_module(PKG + ".ic")
     grav = importlib.import_module(PKG + ".solvers.gravity")
@@ -392,6 +394,19 @@ def bench_direct(dev, lib_mod, peak_tflops):
         tf = 20.0 * nk * nk / tk / 1e12
         kern[str(nk)] = {"ms": tk * 1e3, "gint_per_s": nk * nk / tk / 1e9, "tflops_20flop": tf,
                          "frac_of_fp32_peak": tf / peak_tflops}
+        # Symmetric variant (the Engine's default): n^2/2 pair evaluations;
+        # gint_per_s counts the n^2 ordered interactions it delivers.
+        g.set_variant(2)
+        for _ in range(3):
+            g.acc(xm, acc, 1.0, 1e-4)
+        s.record()
+        for _ in range(reps):
+            g.acc(xm, acc, 1.0, 1e-4)
+        e.record()
+        torch.cuda.synchronize()
+        ts = s.elapsed_time(e) / reps / 1e3
+        kern[str(nk)]["symmetric"] = {"ms": ts * 1e3, "gint_per_s": nk * nk / ts / 1e9,
+                                      "speedup_vs_per_target": tk / ts}
         g.close()
     out["force_kernel"] = kern
     return out
@@ -554,6 +569,15 @@ def bench_adjoint(dev, n=65536, steps=200, every=20):
     e.record()
     torch.cuda.synchronize()
     t_f1 = s.elapsed_time(e) / reps
+    solver.set_variant(2)  # the symmetric force pass, for comparison
+    solver.kdk(xs, v4, a4, units.G, 0.0025, 1e-3, 1)
+    s.record()
+    for _ in range(reps):
+        solver.kdk(xs, v4, a4, units.G, 0.0025, 1e-3, 1)
+    e.record()
+    torch.cuda.synchronize()
+    t_f1s = s.elapsed_time(e) / reps
+    solver.set_variant(0)
     s.record()
     for _ in range(reps):
         adj_step()
@@ -586,6 +610,7 @@ def bench_adjoint(dev, n=65536, steps=200, every=20):
             "backward_over_forward_per_target_form": t_bwd_pt / t_fwd,
             "backward_over_forward_scalar_symmetric_form": t_bwd_sc / t_fwd,
             "adjoint_kernel_over_force_step": t_b1 / t_f1,
+            "adjoint_kernel_over_symmetric_force_step": t_b1 / t_f1s,
             "loss": float(loss.detach()),
             "grad_finite": bool(all(torch.isfinite(t).all().item() for t in g))}
 

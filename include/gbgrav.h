@@ -72,8 +72,12 @@ int gb_direct_destroy(gb_direct_t *h);
  * SM (0 = occupancy maximum).  Chosen by the autotuner. */
 int gb_direct_set_tiles(gb_direct_t *h, int k, int warps, int ctas_per_sm);
 
-/* Inner-loop form: 0 = scalar FP32 (default), 1 = packed .f32x2 FP32.  Same
- * results up to FP32 rounding order; chosen by the autotuner. */
+/* Inner-loop form: 0 = scalar FP32 (default), 1 = packed .f32x2 FP32, one
+ * pass per target; 2 = symmetric packed .f32x2, each unordered pair once,
+ * applied to both particles (tile-pair scratch of N^2/32 bytes at large N,
+ * up to 5 N^2/64 at small N; where that passes 3 GiB, N above about
+ * 310,000, the scalar pass runs).  Same results up to FP32 rounding order;
+ * gb_direct_phi always runs the per-target pass. */
 int gb_direct_set_variant(gb_direct_t *h, int packed);
 
 /* acc_i = G sum_j m_j (x_j - x_i) / (|x_j - x_i|^2 + eps2)^{3/2}, all j

@@ -16,7 +16,8 @@ import torch
 from . import _buildlib
 
 CACHE = os.path.join(_buildlib.BUILD, "autotune.json")
-DIRECT_SHAPES = [(k, w, packed) for k in (2, 4) for w in (4, 8) for packed in (0, 1)]
+# (k, warps, variant); the symmetric variant 2 has one tile shape of its own.
+DIRECT_SHAPES = [(k, w, packed) for k in (2, 4) for w in (4, 8) for packed in (0, 1)] + [(2, 4, 2)]
 BATCH_SHAPES = [(k, w) for k in (2, 4) for w in (4, 8)]
 
 

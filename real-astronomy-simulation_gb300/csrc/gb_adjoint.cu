@@ -178,17 +178,6 @@ constexpr int VJP_WARPS = 8;
 constexpr int SYM_T = 256;
 constexpr int SYM_WARPS = 4;
 
-__device__ __forceinline__ int64_t sym_base(int64_t I, int64_t nt) { return I * nt - I * (I - 1) / 2; }
-
-__device__ __forceinline__ int64_t sym_row(int64_t p, int64_t nt) {
-    int64_t lo = 0, hi = nt - 1;
-    while (lo < hi) {
-        const int64_t mid = (lo + hi + 1) >> 1;
-        if (sym_base(mid, nt) <= p) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
 
 struct SymArgs {
     const float4 *__restrict__ xm;
@@ -636,20 +625,8 @@ __global__ void adjoint_sym_fixup_kernel(SymFix f) {
     f.la[i] = make_float4(f.h * hx, f.h * hy, f.h * hz, 0.f);
 }
 
-// Symmetric scratch above this size falls back to the per-target kernel.
-constexpr int64_t SYM_MAX_BYTES = 3LL << 30;
 
 // Grows the handle's symmetric scratch to at least need float4 elements.
-static int ensure_sym(gb_direct_t *h, int64_t need) {
-    if (need <= h->sym_cap) return GB_OK;
-    if (h->sym) cudaFree(h->sym);
-    h->sym = nullptr;
-    h->sym_cap = 0;
-    if (cudaMalloc(&h->sym, sizeof(float4) * need) != cudaSuccess)
-        return fail(GB_ENOMEM, "symmetric adjoint scratch (%lld bytes)", (long long)(need * 16));
-    h->sym_cap = need;
-    return GB_OK;
-}
 
 }  // namespace gb
 

@@ -660,10 +660,17 @@ extern "C" int gb_direct_set_tiles(gb_direct_t *h, int k, int warps, int ctas_pe
 static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, float4 *acc, float *phi,
                       int64_t n, float G, float eps2, float dt, int flags, cudaStream_t s,
                       const ExtPot &pot = ExtPot{}) {
+    if (mode != MODE_PHI && h->packed == 2) {
+        bool done = false;
+        GB_TRY(run_direct_sym(h, mode, xm, vel, acc, n, G, eps2, dt, flags, s, pot, &done));
+        if (done) return GB_OK;
+    }
+    // Variant 2 beyond the tile-pair scratch limit runs the scalar pass.
+    const int packed = h->packed == 1 ? 1 : 0;
     DirectPlan pl;
     const int np = mode == MODE_PHI ? 1 : h->np;
-    const int64_t ctas = grid_ctas(h, h->np, h->warps, h->packed);
-    const bool fine = mode != MODE_PHI && !h->packed && use_fine_units(n, np, h->warps, ctas);
+    const int64_t ctas = grid_ctas(h, h->np, h->warps, packed);
+    const bool fine = mode != MODE_PHI && !packed && use_fine_units(n, np, h->warps, ctas);
     make_plan(n, np, h->warps, ctas, &pl, fine ? SCALAR_UNIT : 0);
     if (plan_partials(pl) > h->part_cap) return fail(GB_EINVAL, "scratch too small for n=%lld", (long long)n);
     if (pl.P > h->st0_cap) return fail(GB_EINVAL, "%lld CTAs exceed the handle's table", (long long)pl.P);
@@ -694,11 +701,11 @@ static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, f
         }
         e = cudaGetLastError();
     } else if (pl.np == 1) {
-        e = pl.warps == 4 ? launch_force<1, 4>(mode, kahan, pl, a, s, h->packed, fine)
-                          : launch_force<1, 8>(mode, kahan, pl, a, s, h->packed, fine);
+        e = pl.warps == 4 ? launch_force<1, 4>(mode, kahan, pl, a, s, packed, fine)
+                          : launch_force<1, 8>(mode, kahan, pl, a, s, packed, fine);
     } else {
-        e = pl.warps == 4 ? launch_force<2, 4>(mode, kahan, pl, a, s, h->packed, fine)
-                          : launch_force<2, 8>(mode, kahan, pl, a, s, h->packed, fine);
+        e = pl.warps == 4 ? launch_force<2, 4>(mode, kahan, pl, a, s, packed, fine)
+                          : launch_force<2, 8>(mode, kahan, pl, a, s, packed, fine);
     }
     if (e != cudaSuccess) return fail(GB_ECUDA, "force launch: %s", cudaGetErrorString(e));
     FixArgs f;
@@ -777,7 +784,11 @@ extern "C" int gb_direct_kdk(gb_direct_t *h, float *xm, float *vel, float *acc, 
         return GB_OK;
     }
     // One step captured on the handle's stream and replayed nsteps times.
-    const gb_direct::Key key{xm, vel, acc, n, G, eps2, dt, plain, h->np, h->warps, h->ctas_per_sm, h->packed};
+    // Tile-pair scratch is sized before the capture (no allocation inside
+    // it); its address is part of the key, since the adjoint may regrow it.
+    if (h->packed == 2) GB_TRY(reserve_direct_sym(h, n));
+    const gb_direct::Key key{xm, vel, acc, h->sym, n, G, eps2, dt, plain, h->np, h->warps, h->ctas_per_sm,
+                             h->packed};
     if (!h->has_graph || !(h->gkey == key)) {
         if (h->has_graph) {
             cudaGraphExecDestroy(h->gexec);
@@ -862,7 +873,7 @@ extern "C" int gb_direct_diag(gb_direct_t *h, gb_diag_t *out, int reset) {
 
 extern "C" int gb_direct_set_variant(gb_direct_t *h, int packed) {
     if (!h) return fail(GB_EINVAL, "handle is NULL");
-    if (packed != 0 && packed != 1) return fail(GB_EINVAL, "packed must be 0 or 1");
+    if (packed < 0 || packed > 2) return fail(GB_EINVAL, "variant must be 0, 1 or 2");
     h->packed = packed;
     return GB_OK;
 }

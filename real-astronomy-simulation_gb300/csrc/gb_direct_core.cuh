@@ -68,6 +68,21 @@ __device__ __forceinline__ void interact_chunk(const float4 *src, const float (&
 // sub-chunk, so CTA runs split the work evenly even at small N.
 constexpr int SCALAR_UNIT = 32;
 
+// ------------------------------------------------ unordered tile pairs
+// Tile pairs (I <= J) of nt tiles numbered row-major: row I starts at
+// sym_base(I); sym_row(p) is the row of pair p.
+__device__ __forceinline__ int64_t sym_base(int64_t I, int64_t nt) { return I * nt - I * (I - 1) / 2; }
+
+__device__ __forceinline__ int64_t sym_row(int64_t p, int64_t nt) {
+    int64_t lo = 0, hi = nt - 1;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        if (sym_base(mid, nt) <= p) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 // Merges the (hi, lo) partials of one target written by CTAs c_lo..c_hi at
 // slots slot_of(c) (Kahan, fixed CTA order) and returns the sum.
 template <typename SlotFn>
@@ -100,6 +115,10 @@ __device__ __forceinline__ void kdk_writeback(float4 *xm, float4 *vel, float4 *a
     acc[i] = an;
 }
 
+// Symmetric (tile-pair) scratch above this size is not used: the callers
+// fall back to their per-target forms.
+constexpr int64_t SYM_MAX_BYTES = 3LL << 30;
+
 }  // namespace gb
 
 // Direct-sum handle (opaque in the C ABI), shared by the direct-sum and
@@ -109,7 +128,7 @@ struct gb_direct {
     int sms;
     int64_t n_max;
     int np, warps, ctas_per_sm;  // tile shape (ctas_per_sm 0 = occupancy max)
-    int packed;                  // 1: .f32x2 inner loop, 0: scalar FP32
+    int packed;                  // 2: symmetric .f32x2 pairs, 1: .f32x2 per target, 0: scalar FP32
     float4 *part;
     int64_t part_cap;            // float4 elements
     int *st0tab;                 // first supertile of each CTA of the last launch
@@ -129,14 +148,40 @@ struct gb_direct {
     cudaGraphExec_t gexec;
     bool has_graph;
     struct Key {
-        const void *xm, *vel, *acc;
+        const void *xm, *vel, *acc, *sym;
         int64_t n;
         float G, eps2, dt;
         int plain, np, warps, ctas_per_sm, packed;
         bool operator==(const Key &o) const {
-            return xm == o.xm && vel == o.vel && acc == o.acc && n == o.n && G == o.G && eps2 == o.eps2 &&
+            return xm == o.xm && vel == o.vel && acc == o.acc && sym == o.sym && n == o.n && G == o.G && eps2 == o.eps2 &&
                    dt == o.dt && plain == o.plain && np == o.np && warps == o.warps &&
                    ctas_per_sm == o.ctas_per_sm && packed == o.packed;
         }
     } gkey;
 };
+
+namespace gb {
+
+// Grows the handle's tile-pair scratch (shared by the symmetric force pass
+// and the symmetric adjoint, which run in stream order) to need float4s.
+inline int ensure_sym(gb_direct *h, int64_t need) {
+    if (need <= h->sym_cap) return GB_OK;
+    if (h->sym) cudaFree(h->sym);
+    h->sym = nullptr;
+    h->sym_cap = 0;
+    if (cudaMalloc(&h->sym, sizeof(float4) * need) != cudaSuccess)
+        return fail(GB_ENOMEM, "tile-pair scratch (%lld bytes)", (long long)(need * 16));
+    h->sym_cap = need;
+    return GB_OK;
+}
+
+// Symmetric direct-sum force pass (gb_direct_sym.cu): mode 0 acceleration,
+// 1 fused KDK.  Returns GB_OK with *done = false when the scratch it needs
+// passes SYM_MAX_BYTES (the caller then runs the per-target pass).
+int run_direct_sym(gb_direct *h, int mode, const float4 *xm, float4 *vel, float4 *acc, int64_t n, float G,
+                   float eps2, float dt, int flags, cudaStream_t s, const ExtPot &pot, bool *done);
+// Sizes the tile-pair scratch run_direct_sym needs for n particles (nothing
+// when that passes SYM_MAX_BYTES).
+int reserve_direct_sym(gb_direct *h, int64_t n);
+
+}  // namespace gb

@@ -1,0 +1,341 @@
+// Symmetric direct-sum forces: every unordered pair {t, s} is evaluated
+// once and applied to both particles (Newton's third law), in packed
+// FP32x2 arithmetic.  The sum is that of compute_acc_direct
+// (core/solvers/gravity.py:13-26):
+//   d = x_s - x_t, r2 = d.d + eps2, c = rsqrt(r2)^3,
+//   a_t += m_s c d,   a_s -= m_t c d,
+// with the self pair (d = 0) adding nothing.  Per two pairs: 16 packed
+// instructions and 2 rsqrt, against 24 FP32 instructions and 2 rsqrt for
+// two ordered pairs of the per-target kernel.
+//
+// Layout and schedule are those of adjoint_vjp_sym2_kernel: tiles of 512
+// particles, 4 warps, 4 targets per lane as two packed pairs (targets
+// q = 0, 1 and 2, 3 of lane l in warp w: 128 w + 32 q + l); CTAs take units
+// (tile pair I <= J, one of Q source slices of tile J) from an atomic
+// counter; in round r warp w takes source group (G/4 w + r) mod G of the
+// slice and at step k lane l source 32 g + (l + k) mod 32, so the per-source
+// shared-memory sums have one writer at a time.  Each unit writes its own
+// row slot (tile I's sums over the slice) and its slice of the pair's column
+// slot; the fix-up adds a particle's slots in a fixed order (Kahan unless
+// GB_PLAIN_FP32), scales by G and writes the result (or, fused KDK, applies
+// the closing kick and writes x', v', a').  In the fused KDK form both sides
+// load the leapfrog prediction x' = x + (v + a dt/2) dt with the same FMAs as
+// the per-target kernel, so the two forms see identical positions.
+#include "gb_direct_core.cuh"
+
+namespace gb {
+
+#ifndef DS_MIN_CTAS
+#define DS_MIN_CTAS 6  // minimum resident CTAs per SM (register budget)
+#endif
+#ifndef DS_UNROLL
+#define DS_UNROLL 4
+#endif
+
+constexpr int DS_T = 512;
+constexpr int DS_K_UNROLL = DS_UNROLL;
+constexpr int DS_WARPS = 4;
+constexpr int DS_ACC = 0, DS_KDK = 1;
+
+struct DsArgs {
+    const float4 *__restrict__ xm;
+    const float4 *__restrict__ vel;  // fused KDK: v and a of the step start
+    const float4 *__restrict__ acc;
+    float4 *__restrict__ rowpart;  // NP * Q x DS_T
+    float4 *__restrict__ colpart;  // NP x DS_T
+    unsigned long long *counter;   // zero at launch
+    int64_t n, nt, NP;
+    float eps2, h, dt;
+};
+
+template <int MODE>
+__device__ __forceinline__ float4 ds_load(const DsArgs &a, int64_t i) {
+    if (i >= a.n) return make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 x = __ldg(a.xm + i);
+    if (MODE == DS_KDK) x = predict_xm(x, __ldg(a.vel + i), __ldg(a.acc + i), a.h, a.dt);
+    return x;
+}
+
+// One round: lane l at step k takes source jj = 32 g + (l + k) mod 32 of the
+// staged tile against its 4 targets.  DIAG zeroes the pairs with target
+// index >= source index (diagonal tile).
+template <bool DIAG>
+__device__ __forceinline__ void ds_round(const float4 *__restrict__ sxm, float4 *sacc, int g, int lane, int wib,
+                                         f2 EPS2, const f2 (&TX)[2], const f2 (&TY)[2], const f2 (&TZ)[2],
+                                         const f2 (&TM)[2], f2 (&NX)[2], f2 (&NY)[2], f2 (&NZ)[2]) {
+#pragma unroll DS_K_UNROLL
+    for (int k = 0; k < 32; ++k) {
+        const int jj = g * 32 + ((lane + k) & 31);
+        const float4 xs = sxm[jj];
+        const f2 sx = pack2(xs.x, xs.x), sy = pack2(xs.y, xs.y), sz = pack2(xs.z, xs.z);
+        const f2 sm = pack2(xs.w, xs.w);
+        f2 PX = 0ull, PY = 0ull, PZ = 0ull;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const f2 dx = sub2(sx, TX[h]), dy = sub2(sy, TY[h]), dz = sub2(sz, TZ[h]);
+            const f2 r2 = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, EPS2)));
+            const f2 inv = rsqrt2(r2);
+            f2 c = mul2(inv, mul2(inv, inv));
+            if (DIAG) {
+                float c0, c1;
+                unpack2(c, c0, c1);
+                const int t0 = 128 * wib + 64 * h + lane;
+                c0 = t0 < jj ? c0 : 0.f;
+                c1 = t0 + 32 < jj ? c1 : 0.f;
+                c = pack2(c0, c1);
+            }
+            const f2 ct = mul2(sm, c);     // m_s c: the targets' side
+            const f2 cs = mul2(TM[h], c);  // m_t c: the source's side (subtracted)
+            NX[h] = fma2(ct, dx, NX[h]);
+            NY[h] = fma2(ct, dy, NY[h]);
+            NZ[h] = fma2(ct, dz, NZ[h]);
+            PX = fma2(cs, dx, PX);
+            PY = fma2(cs, dy, PY);
+            PZ = fma2(cs, dz, PZ);
+        }
+        float4 acc = sacc[jj];
+        float lo, hi;
+        unpack2(PX, lo, hi);
+        acc.x -= lo + hi;
+        unpack2(PY, lo, hi);
+        acc.y -= lo + hi;
+        unpack2(PZ, lo, hi);
+        acc.z -= lo + hi;
+        sacc[jj] = acc;
+        __syncwarp();
+    }
+}
+
+template <int Q, int MODE>
+__global__ void __launch_bounds__(DS_WARPS * 32, DS_MIN_CTAS) direct_sym_kernel(DsArgs a) {
+    constexpr int G = 16 / Q, SPAN = G * 32;
+    __shared__ float4 sxm[DS_T], sacc[DS_T];
+    __shared__ long long s_unit;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, tid = threadIdx.x;
+    const int64_t NU = a.NP * Q;
+    const f2 EPS2 = pack2(a.eps2, a.eps2);
+    for (;;) {
+        __syncthreads();  // the previous unit is done with s_unit and shared memory
+        if (tid == 0) s_unit = (long long)atomicAdd(a.counter, 1ull);
+        __syncthreads();
+        f2 TX[2], TY[2], TZ[2], TM[2], NX[2], NY[2], NZ[2];
+        bool diag;
+        int gbase;
+        {
+            // Unit bookkeeping is re-read from shared memory after the pair
+            // loop, so none of it stays in registers across the loop.
+            const int64_t u = s_unit;
+            if (u >= NU) break;
+            const int64_t p = u / Q;
+            const int sl = (int)(u - p * Q);
+            const int64_t I = sym_row(p, a.nt);
+            const int64_t J = I + (p - sym_base(I, a.nt));
+            diag = J == I;
+            gbase = sl * G;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const float4 x0 = ds_load<MODE>(a, I * DS_T + 128 * wib + 64 * h + lane);
+                const float4 x1 = ds_load<MODE>(a, I * DS_T + 128 * wib + 64 * h + 32 + lane);
+                TX[h] = pack2(x0.x, x1.x);
+                TY[h] = pack2(x0.y, x1.y);
+                TZ[h] = pack2(x0.z, x1.z);
+                TM[h] = pack2(x0.w, x1.w);
+                NX[h] = NY[h] = NZ[h] = 0ull;
+            }
+            for (int t = tid; t < SPAN; t += DS_WARPS * 32) {
+                const int tt = sl * SPAN + t;
+                sxm[tt] = ds_load<MODE>(a, J * DS_T + tt);
+                sacc[tt] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        }
+        __syncthreads();
+        for (int r = 0; r < G; ++r) {
+            const int g = gbase + (((G / 4) * wib + r) & (G - 1));
+            // Diagonal tile: targets 128 w .. 128 w + 127 against sources
+            // 32 g .. 32 g + 31; no pair has t < s when 4 w > g.
+            // Warp-uniform branches; every warp still reaches the barrier.
+            if (!diag)
+                ds_round<false>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX, NY, NZ);
+            else if (4 * wib <= g)
+                ds_round<true>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX, NY, NZ);
+            __syncthreads();
+        }
+        const int64_t u = s_unit;
+        const int64_t p = u / Q;
+        const int sl = (int)(u - p * Q);
+        for (int t = tid; t < SPAN; t += DS_WARPS * 32) {
+            const int tt = sl * SPAN + t;
+            a.colpart[p * DS_T + tt] = sacc[tt];
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            float x0, x1, y0, y1, z0, z1;
+            unpack2(NX[h], x0, x1);
+            unpack2(NY[h], y0, y1);
+            unpack2(NZ[h], z0, z1);
+            float4 *row = a.rowpart + u * DS_T + 128 * wib + 64 * h + lane;
+            row[0] = make_float4(x0, y0, z0, 0.f);
+            row[32] = make_float4(x1, y1, z1, 0.f);
+        }
+    }
+}
+
+struct DsFix {
+    const float4 *__restrict__ rowpart;
+    const float4 *__restrict__ colpart;
+    float4 *xm, *vel, *acc;
+    int64_t n, nt;
+    int Q;
+    float G, h, dt;
+    int accumulate;
+    ExtPot pot;
+};
+
+// Particle i's slots, in a fixed order: its row units (I, J, slice) for
+// J = I .. nt-1, then its column slots (I', I) for I' = 0 .. I.  A CTA of
+// DS_FIX_WARPS warps takes 32 consecutive particles (one tile I); warp w adds
+// slots w, w + DS_FIX_WARPS, ... (coalesced 512-byte rows), and warp 0 adds
+// the warps' sums in warp order.
+constexpr int DS_FIX_WARPS = 8;
+
+template <int MODE, bool KAHAN>
+__global__ void __launch_bounds__(DS_FIX_WARPS * 32) direct_sym_fixup_kernel(DsFix f) {
+    __shared__ float3 part[DS_FIX_WARPS][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t i = (int64_t)blockIdx.x * 32 + lane;
+    const int64_t I = ((int64_t)blockIdx.x * 32) / DS_T, r = i - I * DS_T;
+    const int64_t b = sym_base(I, f.nt);
+    const int64_t R = (f.nt - I) * f.Q, C = I + 1;
+    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+    auto add = [&](float4 v) {
+        if (KAHAN) {
+            kahan_add(sx, cx, v.x);
+            kahan_add(sy, cy, v.y);
+            kahan_add(sz, cz, v.z);
+        } else {
+            sx += v.x; sy += v.y; sz += v.z;
+        }
+    };
+    // Rows of padded particles (i >= n) are zero-mass records: reading them
+    // stays inside the scratch; their sums are dropped below.
+    for (int64_t k = w; k < R; k += DS_FIX_WARPS) add(f.rowpart[(b * f.Q + k) * DS_T + r]);
+    for (int64_t k = (R + DS_FIX_WARPS - 1 - w) / DS_FIX_WARPS * DS_FIX_WARPS + w - R; k < C; k += DS_FIX_WARPS)
+        add(f.colpart[(sym_base(k, f.nt) + (I - k)) * DS_T + r]);
+    part[w][lane] = make_float3(sx - cx, sy - cy, sz - cz);
+    __syncthreads();
+    if (w != 0 || i >= f.n) return;
+    sx = sy = sz = cx = cy = cz = 0.f;
+#pragma unroll
+    for (int q = 0; q < DS_FIX_WARPS; ++q) {
+        const float3 v = part[q][lane];
+        add(make_float4(v.x, v.y, v.z, 0.f));
+    }
+    float4 an = make_float4(f.G * (sx - cx), f.G * (sy - cy), f.G * (sz - cz), 0.f);
+    if (MODE == DS_ACC) {
+        if (f.pot.on) {
+            const float4 x = f.xm[i];
+            ext_acc_add(f.pot, x.x, x.y, x.z, an.x, an.y, an.z);
+        }
+        if (f.accumulate) {
+            float4 o = f.acc[i];
+            o.x += an.x; o.y += an.y; o.z += an.z;
+            f.acc[i] = o;
+        } else {
+            f.acc[i] = an;
+        }
+        return;
+    }
+    kdk_writeback(f.xm, f.vel, f.acc, i, an, f.h, f.dt);
+}
+
+template <int Q, int MODE>
+static void launch_ds(unsigned grid, const DsArgs &a, cudaStream_t s) {
+    direct_sym_kernel<Q, MODE><<<grid, DS_WARPS * 32, 0, s>>>(a);
+}
+
+struct DsPlan {
+    int64_t nt, NP, NU, P, need;  // need: float4s of scratch (+1 for the unit counter)
+    int Q;
+};
+
+static DsPlan ds_plan(const gb_direct *h, int64_t n) {
+    DsPlan p;
+    p.nt = (n + DS_T - 1) / DS_T;
+    p.NP = p.nt * (p.nt + 1) / 2;
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, direct_sym_kernel<1, DS_ACC>, DS_WARPS * 32, 0);
+    const int64_t slots = (int64_t)h->sms * std::max(occ, 1);
+    // Source slices per tile pair: enough units that the last ones are a
+    // small share of each CTA's work.
+    p.Q = 1;
+    while (p.Q < 4 && p.NP * p.Q < 16 * slots) p.Q *= 2;
+    p.NU = p.NP * p.Q;
+    p.P = std::min(slots, p.NU);
+    p.need = p.NU * DS_T + p.NP * DS_T + 1;
+    return p;
+}
+
+int reserve_direct_sym(gb_direct *h, int64_t n) {
+    const DsPlan p = ds_plan(h, n);
+    if (p.need * (int64_t)sizeof(float4) > SYM_MAX_BYTES) return GB_OK;
+    return ensure_sym(h, p.need);
+}
+
+int run_direct_sym(gb_direct *h, int mode, const float4 *xm, float4 *vel, float4 *acc, int64_t n, float G,
+                   float eps2, float dt, int flags, cudaStream_t s, const ExtPot &pot, bool *done) {
+    *done = false;
+    const DsPlan pl = ds_plan(h, n);
+    const int64_t nt = pl.nt, NP = pl.NP, NU = pl.NU, P = pl.P, need = pl.need;
+    const int Q = pl.Q;
+    if (need * (int64_t)sizeof(float4) > SYM_MAX_BYTES) return GB_OK;
+    GB_TRY(ensure_sym(h, need));
+    DsArgs a;
+    a.xm = xm;
+    a.vel = vel;
+    a.acc = acc;
+    a.rowpart = h->sym;
+    a.colpart = h->sym + NU * DS_T;
+    a.counter = (unsigned long long *)(h->sym + need - 1);
+    a.n = n;
+    a.nt = nt;
+    a.NP = NP;
+    a.eps2 = eps2;
+    a.h = 0.5f * dt;
+    a.dt = dt;
+    GB_CUDA_TRY(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), s));
+    const unsigned grid = (unsigned)P;
+    const bool kdk = mode == DS_KDK;
+    if (Q == 1) kdk ? launch_ds<1, DS_KDK>(grid, a, s) : launch_ds<1, DS_ACC>(grid, a, s);
+    else if (Q == 2) kdk ? launch_ds<2, DS_KDK>(grid, a, s) : launch_ds<2, DS_ACC>(grid, a, s);
+    else kdk ? launch_ds<4, DS_KDK>(grid, a, s) : launch_ds<4, DS_ACC>(grid, a, s);
+    GB_CUDA_TRY(cudaGetLastError());
+    DsFix f;
+    f.rowpart = a.rowpart;
+    f.colpart = a.colpart;
+    f.xm = const_cast<float4 *>(xm);
+    f.vel = vel;
+    f.acc = acc;
+    f.n = n;
+    f.nt = nt;
+    f.Q = Q;
+    f.G = G;
+    f.h = 0.5f * dt;
+    f.dt = dt;
+    f.accumulate = (flags & GB_ACCUMULATE) ? 1 : 0;
+    f.pot = pot;
+    const bool kahan = !(flags & GB_PLAIN_FP32);
+    const unsigned fg = (unsigned)((n + 31) / 32), fb = DS_FIX_WARPS * 32;
+    if (kdk) {
+        if (kahan) direct_sym_fixup_kernel<DS_KDK, true><<<fg, fb, 0, s>>>(f);
+        else direct_sym_fixup_kernel<DS_KDK, false><<<fg, fb, 0, s>>>(f);
+    } else {
+        if (kahan) direct_sym_fixup_kernel<DS_ACC, true><<<fg, fb, 0, s>>>(f);
+        else direct_sym_fixup_kernel<DS_ACC, false><<<fg, fb, 0, s>>>(f);
+    }
+    GB_CUDA_TRY(cudaGetLastError());
+    h->launches += 2;
+    *done = true;
+    return GB_OK;
+}
+
+}  // namespace gb

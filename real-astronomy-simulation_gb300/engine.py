@@ -7,7 +7,9 @@ float4 records and every force evaluation running in the sm_103a CUDA
 library.  Extra keyword arguments: ``G`` (default core/units.py:21),
 ``key_bits`` (Morton key width of the tree path; the reference uses 21),
 ``max_stack`` (traversal stack rule, reference default 64), ``plain_fp32``
-(disable Kahan accumulation), ``device``.
+(disable Kahan accumulation), ``symmetric`` (direct sum: evaluate each
+unordered pair once and update both particles, default; False runs one pass
+per target), ``device``.
 
 As in the reference (core/engine.py:75-80), gravity_mode="bh" uses the tree
 only for n >= 256; smaller systems use the direct sum.
@@ -34,7 +36,8 @@ def init_taichi(arch: str = "cuda") -> None:
 class Engine:
     def __init__(self, softening: float = 0.05, gravity_mode: str = "direct",
                  theta: float = 0.6, *, G: float = units.G, key_bits: int = 21,
-                 max_stack: int = 64, plain_fp32: bool = False, device=None):
+                 max_stack: int = 64, plain_fp32: bool = False, symmetric: bool = True,
+                 device=None):
         if gravity_mode not in ("direct", "bh"):
             raise ValueError(f"gravity_mode must be 'direct' or 'bh', got {gravity_mode!r}")
         self.softening = float(softening)
@@ -44,6 +47,7 @@ class Engine:
         self.key_bits = int(key_bits)
         self.max_stack = int(max_stack)
         self.plain_fp32 = bool(plain_fp32)
+        self.symmetric = bool(symmetric)
         self.device = require_cuda(device)
         self._bh = None
         self._direct = None
@@ -100,6 +104,7 @@ class Engine:
     def _make_solvers(self) -> None:
         if self._direct is None or self._direct.n_max < max(self.n, 1):
             self._direct = DirectGravity(max(self.n, 1), self.device)
+            self._direct.set_variant(2 if self.symmetric else 0)
         if self.gravity_mode == "bh" and self.n >= BH_MIN_N:
             from .solvers.barnes_hut import BarnesHut
             self._bh = BarnesHut(self.n, theta=self.theta, softening=self.softening,

@@ -56,6 +56,13 @@ class DirectGravity:
         if packed is not None:
             _lib.call("gb_direct_set_variant", self._h, int(packed))
 
+    def set_variant(self, variant: int):
+        """Force-pass form: 0 scalar per target (default), 1 packed per
+        target, 2 symmetric (each unordered pair once, both particles
+        updated; needs N^2/32 bytes of scratch at large N, runs the scalar
+        pass where that passes 3 GiB).  The potential pass is per target."""
+        _lib.call("gb_direct_set_variant", self._h, int(variant))
+
     # -- compute
     def acc(self, xm, acc, G, eps2, accumulate=False, plain=False):
         flags = (_lib.GB_ACCUMULATE if accumulate else 0) | (_lib.GB_PLAIN_FP32 if plain else 0)

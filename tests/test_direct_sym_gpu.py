@@ -1,0 +1,159 @@
+"""Symmetric direct-sum pass (gb_direct_set_variant 2: each unordered pair
+once, applied to both particles) against the FP64 oracle.
+
+Same tolerances as the per-target pass (per-particle relative error, RMS
+<= 1e-5, max <= 1e-4); the fused KDK form is checked against the oracle's
+leapfrog and, bit for bit, against itself under CUDA-graph replay.
+"""
+import importlib
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import PKG_NAME
+
+pytestmark = pytest.mark.gpu
+
+RMS_TOL = 1e-5
+MAX_TOL = 1e-4
+SYM = 2
+
+
+def _mods():
+    grav = importlib.import_module(PKG_NAME + ".solvers.gravity")
+    ic = importlib.import_module(PKG_NAME + ".ic")
+    return grav, ic
+
+
+def _f32(a):
+    return np.asarray(a, np.float64).astype(np.float32).astype(np.float64)
+
+
+def _xm(pos, mass, dev):
+    return torch.tensor(np.column_stack((pos, mass)), dtype=torch.float32, device=dev)
+
+
+def _rel(a, ref):
+    return np.linalg.norm(a - ref, axis=1) / np.maximum(np.linalg.norm(ref, axis=1), 1e-300)
+
+
+def _sym_solver(grav, n, dev):
+    s = grav.DirectGravity(n, dev)
+    s.set_tiles(2, 4, 0, SYM)
+    return s
+
+
+@pytest.mark.parametrize("plain", [False, True])
+def test_plummer_20k_matches_oracle(cuda_dev, orc, plain):
+    grav, ic = _mods()
+    pos, _, mass = ic.plummer(20000, seed=0)
+    pos, mass = _f32(pos), _f32(mass)
+    xm = _xm(pos, mass, cuda_dev)
+    s = _sym_solver(grav, 20000, cuda_dev)
+    acc = torch.zeros_like(xm)
+    s.acc(xm, acc, 1.0, 1e-4, plain=plain)
+    a = acc[:, :3].double().cpu().numpy()
+    targets = np.random.default_rng(1).choice(20000, 2048, replace=False)
+    ref = orc.direct_acc(pos, mass, 1.0, 1e-4, targets)
+    rel = _rel(a[targets], ref)
+    assert np.sqrt((rel ** 2).mean()) < RMS_TOL, np.sqrt((rel ** 2).mean())
+    assert rel.max() < MAX_TOL, rel.max()
+    s.close()
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 33, 511, 512, 513, 1025, 4099, 9000])
+def test_ragged_sizes(cuda_dev, orc, n):
+    """Ragged last tiles, one tile, and the three source-slice counts."""
+    grav, ic = _mods()
+    pos, _, mass = ic.plummer(max(n, 2), seed=n)
+    pos, mass = _f32(pos[:n]), _f32(mass[:n])
+    xm = _xm(pos, mass, cuda_dev)
+    s = _sym_solver(grav, n, cuda_dev)
+    acc = torch.full_like(xm, 7.0)
+    s.acc(xm, acc, 2.5, 0.05 ** 2)
+    a = acc[:, :3].double().cpu().numpy()
+    assert torch.all(acc[:, 3] == 0.0)
+    if n == 1:
+        assert np.all(a == 0.0)
+        return
+    ref = orc.direct_acc(pos, mass, 2.5, 0.05 ** 2)
+    assert _rel(a, ref).max() < MAX_TOL
+    s.close()
+
+
+def test_matches_per_target_pass_and_is_deterministic(cuda_dev):
+    grav, ic = _mods()
+    pos, _, mass = ic.plummer(30000, seed=3)
+    xm = _xm(pos, mass, cuda_dev)
+    s = _sym_solver(grav, 30000, cuda_dev)
+    a1, a2, a3 = (torch.zeros_like(xm) for _ in range(3))
+    s.acc(xm, a1, 1.0, 1e-4)
+    s.acc(xm, a2, 1.0, 1e-4)
+    s.set_tiles(2, 4, 0, 0)
+    s.acc(xm, a3, 1.0, 1e-4)
+    torch.cuda.synchronize()
+    assert torch.equal(a1, a2)
+    rel = _rel(a1[:, :3].double().cpu().numpy(), a3[:, :3].double().cpu().numpy())
+    assert np.sqrt((rel ** 2).mean()) < RMS_TOL and rel.max() < MAX_TOL, rel.max()
+    s.close()
+
+
+def test_accumulate_and_potential(cuda_dev, orc):
+    grav, ic = _mods()
+    ext = importlib.import_module(PKG_NAME + ".solvers.external")
+    pos, _, mass = ic.plummer(3000, seed=4)
+    pos, mass = _f32(pos), _f32(mass)
+    xm = _xm(pos, mass, cuda_dev)
+    s = _sym_solver(grav, 3000, cuda_dev)
+    acc = torch.zeros_like(xm)
+    acc[:, 0] = 1.0
+    s.acc(xm, acc, 1.0, 1e-4, accumulate=True)
+    a = acc[:, :3].double().cpu().numpy()
+    ref = orc.direct_acc(pos, mass, 1.0, 1e-4)
+    ref[:, 0] += 1.0
+    assert _rel(a, ref).max() < MAX_TOL
+    p = {"M_d": 5.0, "a": 3.0, "b": 0.3, "M_h": 50.0, "a_h": 20.0, "smbh_mass": 0.1, "is_hernquist": True}
+    pot = ext.Potential.from_dict(p)
+    base = np.zeros((3000, 3))
+    acc2 = torch.zeros_like(xm)
+    ext.direct_acc_ext(s, xm, acc2, 1.0, 1e-4, pot, accumulate=False)
+    got = acc2[:, :3].double().cpu().numpy()
+    ref2 = orc.grav_ext_acc(pos, mass, 1.0, 1e-4, p, base)
+    assert _rel(got, ref2).max() < MAX_TOL
+    s.close()
+
+
+def test_kdk_matches_oracle_and_graph_replay(cuda_dev, orc):
+    grav, ic = _mods()
+    pos, vel, mass = ic.plummer(2048, seed=6)
+    pos, vel, mass = _f32(pos), _f32(vel), _f32(mass)
+    out = []
+    for graph in (False, True):
+        xm = _xm(pos, mass, cuda_dev)
+        v4 = torch.zeros_like(xm)
+        v4[:, :3] = torch.tensor(vel, dtype=torch.float32, device=cuda_dev)
+        a4 = torch.zeros_like(xm)
+        s = _sym_solver(grav, 2048, cuda_dev)
+        s.acc(xm, a4, 1.0, 1e-4)
+        s.kdk(xm, v4, a4, 1.0, 1e-4, 1e-3, 6, graph=graph)
+        s.kdk(xm, v4, a4, 1.0, 1e-4, 1e-3, 4, graph=graph)
+        torch.cuda.synchronize()
+        out.append((xm.clone(), v4.clone(), a4.clone()))
+        s.close()
+    for u, w in zip(*out):
+        assert torch.equal(u, w)
+    a0 = orc.direct_acc(pos, mass, 1.0, 1e-4)
+    p, v, _ = orc.kdk_direct(pos, vel, a0, mass, 1.0, 1e-4, 1e-3, 10)
+    xm, v4, _ = out[0]
+    assert np.abs(xm[:, :3].double().cpu().numpy() - p).max() < 2e-5 * np.abs(p).max()
+    assert np.abs(v4[:, :3].double().cpu().numpy() - v).max() < 1e-4 * np.abs(v).max()
+
+
+def test_variant_out_of_range_is_rejected(cuda_dev):
+    pkg = importlib.import_module(PKG_NAME)
+    grav, _ = _mods()
+    s = grav.DirectGravity(64, cuda_dev)
+    with pytest.raises(pkg.GravityError):
+        s.set_tiles(2, 4, 0, 3)
+    s.close()
