@@ -603,6 +603,25 @@ def bench_adjoint(dev, n=65536, steps=200, every=20):
     t_bwd_pt = backward_time(False, True)
     t_bwd_sc = backward_time(True, False)
     lib_mod.call("gb_adjoint_set_variant", solver.handle, 2)
+    # The same run with the symmetric force pass in the forward steps and the
+    # backward's segment recompute.
+    solver.set_variant(2)
+    xs0 = x0.detach().clone().requires_grad_(True)
+    torch.cuda.synchronize()
+    s.record()
+    xTs, _ = adj.simulate(xs0, v0.detach(), m0.detach(), G=units.G, softening=0.05, dt=1e-3,
+                          nsteps=steps, checkpoint_every=every, solver=solver)
+    e.record()
+    torch.cuda.synchronize()
+    t_fwd_s = s.elapsed_time(e) / 1e3
+    loss_s = ((xTs - target) ** 2).mean()
+    torch.cuda.synchronize()
+    s.record()
+    loss_s.backward()
+    e.record()
+    torch.cuda.synchronize()
+    t_bwd_s = s.elapsed_time(e) / 1e3
+    solver.set_variant(0)
     return {"workload": f"adjoint of {steps} KDK steps, exponential disk N={n}, eps=0.05, dt=1e-3, "
                         f"checkpoint every {every}; loss = MSE of final positions",
             "forward_ms_per_step": t_fwd / steps * 1e3, "backward_ms_per_step": t_bwd / steps * 1e3,
@@ -611,6 +630,9 @@ def bench_adjoint(dev, n=65536, steps=200, every=20):
             "backward_over_forward_scalar_symmetric_form": t_bwd_sc / t_fwd,
             "adjoint_kernel_over_force_step": t_b1 / t_f1,
             "adjoint_kernel_over_symmetric_force_step": t_b1 / t_f1s,
+            "with_symmetric_force_pass": {"forward_ms_per_step": t_fwd_s / steps * 1e3,
+                                          "backward_ms_per_step": t_bwd_s / steps * 1e3,
+                                          "backward_over_forward": t_bwd_s / t_fwd_s},
             "loss": float(loss.detach()),
             "grad_finite": bool(all(torch.isfinite(t).all().item() for t in g))}
 

@@ -127,6 +127,7 @@ def _solver_for(xm: torch.Tensor) -> DirectGravity:
     s = _CACHE.get(key)
     if s is None or s.n_max < xm.shape[0]:
         s = DirectGravity(max(xm.shape[0], 1), xm.device)
+        s.set_variant(2)  # the symmetric pass, as the Engine uses
         _CACHE[key] = s
     return s
 
