@@ -451,9 +451,10 @@ def bench_merger(dev, drift_steps=1000):
 def bench_batch(dev, steps=200, loop_steps=20):
     """512 independent Plummer spheres (N_s = round(exp(U(ln 256, ln 16384))),
     seed s), G = 1, eps = 0.02, dt = 1e-3: 200 KDK steps as one persistent
-    launch per step replayed from a CUDA graph, tile shape from the
-    autotuner; compared with the batched launches without the graph and with
-    a loop over systems of the single-system kernel."""
+    launch per step replayed from a CUDA graph, tile shape and force-pass
+    form (per target or symmetric) from the autotuner; compared with the
+    batched launches without the graph, with the other form, and with a loop
+    over systems of the single-system kernel."""
     batch = importlib.import_module(PKG + ".batch")
     ic = importlib.import_module(PKG + ".ic")
     tune = importlib.import_module(PKG + ".autotune")
@@ -478,6 +479,21 @@ def bench_batch(dev, steps=200, loop_steps=20):
     launches = b.launch_count() - l0
     b.restore(saved)
     t_plain = timed(lambda: b.run(1e-3, loop_steps, graph=False))
+    # The other force-pass form, for comparison: best per-target tile shape
+    # against the symmetric pass.
+    per_target = min((k for k in tune_ms if k.endswith(",0")), key=tune_ms.get)
+    forms = {}
+    for v in (0, 1):
+        if v == 0:
+            kk, ww, _ = (int(x) for x in per_target.split(","))
+            b.set_tiles(kk, ww)
+        b.set_variant(v)
+        b.restore(saved)
+        b.run(1e-3, steps, graph=True)
+        b.restore(saved)
+        forms[v] = inter * steps / timed(lambda: b.run(1e-3, steps, graph=True)) / 1e9
+    b.set_tiles(shape[0], shape[1])
+    b.set_variant(shape[2])
     b.restore(saved)
     b.run_loop(1e-3, 2)
     b.restore(saved)
@@ -488,6 +504,7 @@ def bench_batch(dev, steps=200, loop_steps=20):
            "autotune_ms_per_step": tune_ms,
            "graph_gint_per_s": inter * steps / t_graph / 1e9, "graph_ms_per_step": t_graph / steps * 1e3,
            "gpu_launches_graph": launches,
+           "graph_gint_per_s_per_target_pass": forms[0], "graph_gint_per_s_symmetric_pass": forms[1],
            "batched_no_graph_gint_per_s": inter * loop_steps / t_plain / 1e9,
            "per_system_loop_gint_per_s": inter * loop_steps / t_loop / 1e9,
            "per_system_loop_ms_per_step": t_loop / loop_steps * 1e3}

@@ -217,6 +217,13 @@ int gb_batch_create(gb_batch_t **out, const int64_t *sizes, int nsys);
 int gb_batch_destroy(gb_batch_t *h);
 /* Same meaning as gb_direct_set_tiles; chosen by the autotuner. */
 int gb_batch_set_tiles(gb_batch_t *h, int k, int warps, int ctas_per_sm);
+/* Force-pass form: 0 = one pass per target (default); 1 = symmetric packed
+ * .f32x2 (each unordered pair of a system once, both particles updated; the
+ * same tile-pair pass as gb_direct_set_variant 2, over all systems in one
+ * launch from an atomic unit counter).  Selecting 1 allocates its scratch
+ * (about 16 KB per 512 x 512 tile pair of every system) and fails with
+ * GB_EINVAL above 3 GiB of it.  Same results up to FP32 rounding order. */
+int gb_batch_set_variant(gb_batch_t *h, int variant);
 int64_t gb_batch_total(gb_batch_t *h);
 
 /* Direct accelerations of every system (compute_acc_direct per system,

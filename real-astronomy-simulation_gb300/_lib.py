@@ -100,6 +100,7 @@ SIGNATURES = {
     "gb_batch_create": (I32, [ctypes.POINTER(P), P, I32]),
     "gb_batch_destroy": (I32, [P]),
     "gb_batch_set_tiles": (I32, [P, I32, I32, I32]),
+    "gb_batch_set_variant": (I32, [P, I32]),
     "gb_batch_total": (I64, [P]),
     "gb_batch_acc": (I32, [P, P, P, F32, F32, I32, P]),
     "gb_batch_kdk": (I32, [P, P, P, P, F32, F32, F32, I64, I32, P]),

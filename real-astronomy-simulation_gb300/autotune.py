@@ -18,7 +18,8 @@ from . import _buildlib
 CACHE = os.path.join(_buildlib.BUILD, "autotune.json")
 # (k, warps, variant); the symmetric variant 2 has one tile shape of its own.
 DIRECT_SHAPES = [(k, w, packed) for k in (2, 4) for w in (4, 8) for packed in (0, 1)] + [(2, 4, 2)]
-BATCH_SHAPES = [(k, w) for k in (2, 4) for w in (4, 8)]
+# (k, warps, variant); variant 1 is the symmetric batched pass (one shape).
+BATCH_SHAPES = [(k, w, 0) for k in (2, 4) for w in (4, 8)] + [(2, 4, 1)]
 
 
 def _load():
@@ -79,25 +80,28 @@ def tune_direct(solver, xm, G=1.0, eps2=1e-4, reps=3, use_cache=True):
 
 
 def tune_batch(batch, dt=1e-3, reps=2, use_cache=True):
-    """Pick (k, warps) for a DirectBatch by timing one KDK step per shape on
-    a copy of its state (the batch is restored afterwards)."""
+    """Pick (k, warps, variant) for a DirectBatch by timing one KDK step per
+    candidate on a copy of its state (the batch is restored afterwards)."""
     sig = f"{batch.n_total}:{len(batch.sizes)}:{int(batch.sizes.max())}:{batch.interactions_per_step()}"
     key = _key("batch", sig)
     cache = _load() if use_cache else {}
-    if key in cache:
-        k, w = cache[key]["best"]
+    if key in cache and len(cache[key]["best"]) == 3:
+        k, w, v = cache[key]["best"]
         batch.set_tiles(k, w)
-        return (k, w), cache[key]["ms"]
+        batch.set_variant(v)
+        return (k, w, v), cache[key]["ms"]
     saved = batch.state_arrays()
     times = {}
-    for k, w in BATCH_SHAPES:
+    for k, w, v in BATCH_SHAPES:
         batch.set_tiles(k, w)
-        times[f"{k},{w}"] = _time(lambda: batch.run(dt, 1, graph=False), reps)
+        batch.set_variant(v)
+        times[f"{k},{w},{v}"] = _time(lambda: batch.run(dt, 1, graph=False), reps)
         batch.restore(saved)
     best = min(times, key=times.get)
-    k, w = (int(x) for x in best.split(","))
+    k, w, v = (int(x) for x in best.split(","))
     batch.set_tiles(k, w)
+    batch.set_variant(v)
     cache = _load()
-    cache[key] = {"best": [k, w], "ms": times, "when": time.time()}
+    cache[key] = {"best": [k, w, v], "ms": times, "when": time.time()}
     _save(cache)
-    return (k, w), times
+    return (k, w, v), times

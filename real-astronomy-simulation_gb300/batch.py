@@ -5,6 +5,8 @@ separate Engine(gravity_mode="direct") would (core/engine.py:108-116).
     b = DirectBatch([pos_vel_mass, ...], G=1.0, softening=0.02)
     b.run(dt, nsteps)              # one persistent launch per step, CUDA graph
     b.run_loop(dt, nsteps)         # per-system loop of the plain kernel
+
+variant=1 runs the symmetric pass (each unordered pair of a system once).
 """
 from __future__ import annotations
 
@@ -37,7 +39,7 @@ def shard_systems(sizes, rank: int, world: int) -> list:
 
 class DirectBatch:
     def __init__(self, systems, G: float = 1.0, softening: float = 0.02, device=None,
-                 plain_fp32: bool = False, tiles=None):
+                 plain_fp32: bool = False, tiles=None, variant: int = 0):
         if not systems:
             raise ValueError("DirectBatch needs at least one system")
         self.device = require_cuda(device)
@@ -66,6 +68,8 @@ class DirectBatch:
             self.a4 = torch.zeros_like(self.xm)
             if tiles is not None:
                 self.set_tiles(*tiles)
+            if variant:
+                self.set_variant(variant)
             self.compute_acc()
 
     @property
@@ -85,6 +89,11 @@ class DirectBatch:
 
     def set_tiles(self, k: int, warps: int, ctas_per_sm: int = 0):
         _lib.call("gb_batch_set_tiles", self._h, int(k), int(warps), int(ctas_per_sm))
+
+    def set_variant(self, variant: int):
+        """Force pass: 0 one pass per target (default), 1 symmetric (each
+        unordered pair of a system once; allocates its tile-pair scratch)."""
+        _lib.call("gb_batch_set_variant", self._h, int(variant))
 
     def _flags(self, graph=False):
         return (_lib.GB_PLAIN_FP32 if self.plain else 0) | (_lib.GB_USE_GRAPH if graph else 0)

@@ -38,17 +38,6 @@ struct BatchArgs {
     float eps2, h, dt;
 };
 
-// Largest s in [0, nsys) with base[s] <= x (base is non-decreasing).
-__device__ __forceinline__ int find_sys(const int64_t *__restrict__ base, int nsys, int64_t x) {
-    int lo = 0, hi = nsys - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (__ldg(base + mid) <= x) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
 template <int MODE>
 __device__ __forceinline__ float4 load_b(const BatchArgs &a, int64_t o, int64_t n_s, int64_t li) {
     if (li >= n_s) return make_float4(0.f, 0.f, 0.f, 0.f);
@@ -69,7 +58,7 @@ batch_force_kernel(BatchArgs a) {
     const int64_t c = blockIdx.x;
     const int64_t u_begin = a.U * c / a.P, u_end = a.U * (c + 1) / a.P;
     if (u_begin >= u_end) return;
-    int s = find_sys(a.ubase, a.nsys, u_begin);
+    int s = find_base(a.ubase, a.nsys, u_begin);
     int64_t u = u_begin;
     while (u < u_end) {
         while (s + 1 < a.nsys && u >= __ldg(a.ubase + s + 1)) ++s;
@@ -134,7 +123,7 @@ template <int MODE>
 __global__ void batch_fixup_kernel(BatchFix f) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= f.ntot) return;
-    const int s = find_sys(f.off, f.nsys, i);
+    const int s = find_base(f.off, f.nsys, i);
     const int64_t o = __ldg(f.off + s), n_s = __ldg(f.off + s + 1) - o;
     const int64_t li = i - o;
     const int64_t nju = (n_s + f.ju - 1) / f.ju;
@@ -185,11 +174,11 @@ struct GraphKey {
     const void *xm, *vel, *acc;
     float G, eps2, dt;
     int64_t nsteps;
-    int np, warps, ctas_per_sm, flags;
+    int np, warps, ctas_per_sm, flags, variant;
     bool operator==(const GraphKey &o) const {
         return xm == o.xm && vel == o.vel && acc == o.acc && G == o.G && eps2 == o.eps2 && dt == o.dt &&
                nsteps == o.nsteps && np == o.np && warps == o.warps && ctas_per_sm == o.ctas_per_sm &&
-               flags == o.flags;
+               flags == o.flags && variant == o.variant;
     }
 };
 
@@ -210,7 +199,64 @@ struct gb_batch {
     bool has_graph;
     gb_direct_t *loop;  // per-system handle for gb_batch_kdk_loop (lazy)
     uint64_t launches;
+    // Symmetric pass (variant 1): its tables (unit, column-slot and fix-up
+    // block bases, nsys + 1 each) and scratch, allocated on first selection.
+    int variant;
+    int64_t *d_symtab;
+    float4 *sym;
+    SymBatch symb;
 };
+
+// Tables and scratch of the symmetric pass (tiles of SYM_TILE particles;
+// units are system after system, tile pairs row-major, Q slices each).
+static int batch_sym_plan(gb_batch_t *h) {
+    if (h->sym) return GB_OK;
+    const int ns = h->nsys;
+    std::vector<int64_t> tab(3 * (ns + 1), 0);
+    int64_t *ub = tab.data(), *cb = ub + ns + 1, *fb = cb + ns + 1;
+    int64_t pairs = 0;
+    for (int s = 0; s < ns; ++s) {
+        const int64_t n = h->off[s + 1] - h->off[s], nt = (n + SYM_TILE - 1) / SYM_TILE;
+        pairs += nt * (nt + 1) / 2;
+    }
+    const int64_t slots = direct_sym_slots(h->sms);
+    const int Q = direct_sym_slices(pairs, slots);
+    for (int s = 0; s < ns; ++s) {
+        const int64_t n = h->off[s + 1] - h->off[s], nt = (n + SYM_TILE - 1) / SYM_TILE;
+        ub[s + 1] = ub[s] + nt * (nt + 1) / 2 * Q;
+        cb[s + 1] = cb[s] + nt * (nt + 1) / 2;
+        fb[s + 1] = fb[s] + (n + 31) / 32;
+    }
+    const int64_t NU = ub[ns], need = (NU + pairs) * SYM_TILE + 1;
+    if (need * (int64_t)sizeof(float4) > SYM_MAX_BYTES)
+        return fail(GB_EINVAL, "symmetric batch pass needs %lld bytes of scratch (limit %lld)",
+                    (long long)(need * 16), (long long)SYM_MAX_BYTES);
+    if (fb[ns] > INT32_MAX) return fail(GB_EINVAL, "too many particles for the symmetric batch fix-up");
+    if (cudaMalloc(&h->d_symtab, sizeof(int64_t) * tab.size()) != cudaSuccess) {
+        h->d_symtab = nullptr;
+        return fail(GB_ENOMEM, "symmetric batch tables");
+    }
+    if (cudaMalloc(&h->sym, sizeof(float4) * need) != cudaSuccess) {
+        h->sym = nullptr;
+        cudaFree(h->d_symtab);
+        h->d_symtab = nullptr;
+        return fail(GB_ENOMEM, "symmetric batch scratch (%lld bytes)", (long long)(need * 16));
+    }
+    GB_CUDA_TRY(cudaMemcpy(h->d_symtab, tab.data(), sizeof(int64_t) * tab.size(), cudaMemcpyHostToDevice));
+    SymBatch &b = h->symb;
+    b.off = h->d_off;
+    b.ubase = h->d_symtab;
+    b.cbase = h->d_symtab + ns + 1;
+    b.fbase = h->d_symtab + 2 * (ns + 1);
+    b.nsys = ns;
+    b.Q = Q;
+    b.NU = NU;
+    b.NPtot = pairs;
+    b.nfb = fb[ns];
+    b.P = std::min<int64_t>(slots, NU);
+    b.scratch = h->sym;
+    return GB_OK;
+}
 
 // Unit and supertile tables for the current tile shape (host, uploaded).
 static int batch_plan(gb_batch_t *h, int np, int warps, int ctas_per_sm, bool upload) {
@@ -257,6 +303,8 @@ extern "C" int gb_batch_destroy(gb_batch_t *h) {
     cudaFree(h->d_ubase);
     cudaFree(h->d_stbase);
     cudaFree(h->part);
+    cudaFree(h->d_symtab);
+    cudaFree(h->sym);
     if (h->loop) gb_direct_destroy(h->loop);
     delete h;
     return GB_OK;
@@ -312,10 +360,23 @@ extern "C" int gb_batch_set_tiles(gb_batch_t *h, int k, int warps, int ctas_per_
     return batch_plan(h, k / 2, warps, ctas_per_sm, true);
 }
 
+extern "C" int gb_batch_set_variant(gb_batch_t *h, int variant) {
+    if (!h) return fail(GB_EINVAL, "handle is NULL");
+    if (variant != 0 && variant != 1) return fail(GB_EINVAL, "variant must be 0 or 1 (got %d)", variant);
+    if (variant == 1) GB_TRY(batch_sym_plan(h));
+    h->variant = variant;
+    return GB_OK;
+}
+
 extern "C" int64_t gb_batch_total(gb_batch_t *h) { return h ? h->ntot : -1; }
 
 static int batch_step(gb_batch_t *h, int mode, const float4 *xm, float4 *vel, float4 *acc, float G, float eps2,
                       float dt, int flags, cudaStream_t s) {
+    if (h->variant == 1) {
+        GB_TRY(run_batch_sym(h->symb, mode, xm, vel, acc, G, eps2, dt, flags, s));
+        h->launches += 2;
+        return GB_OK;
+    }
     BatchArgs a;
     a.xm = xm;
     a.vel = vel;
@@ -397,7 +458,7 @@ extern "C" int gb_batch_kdk(gb_batch_t *h, float *xm, float *vel, float *acc, fl
             GB_TRY(batch_step(h, BMODE_KDK, (const float4 *)xm, (float4 *)vel, (float4 *)acc, G, eps2, dt, flags, s));
         return GB_OK;
     }
-    const GraphKey key{xm, vel, acc, G, eps2, dt, nsteps, h->np, h->warps, h->ctas_per_sm, flags};
+    const GraphKey key{xm, vel, acc, G, eps2, dt, nsteps, h->np, h->warps, h->ctas_per_sm, flags, h->variant};
     if (!h->has_graph || !(h->gkey == key)) {
         if (h->has_graph) {
             cudaGraphExecDestroy(h->graph);

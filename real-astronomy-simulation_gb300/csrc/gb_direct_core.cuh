@@ -69,6 +69,17 @@ __device__ __forceinline__ void interact_chunk(const float4 *src, const float (&
 constexpr int SCALAR_UNIT = 32;
 
 // ------------------------------------------------ unordered tile pairs
+// Largest s in [0, nsys) with base[s] <= x (base is non-decreasing).
+__device__ __forceinline__ int find_base(const int64_t *__restrict__ base, int nsys, int64_t x) {
+    int lo = 0, hi = nsys - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(base + mid) <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 // Tile pairs (I <= J) of nt tiles numbered row-major: row I starts at
 // sym_base(I); sym_row(p) is the row of pair p.
 __device__ __forceinline__ int64_t sym_base(int64_t I, int64_t nt) { return I * nt - I * (I - 1) / 2; }
@@ -183,5 +194,25 @@ int run_direct_sym(gb_direct *h, int mode, const float4 *xm, float4 *vel, float4
 // Sizes the tile-pair scratch run_direct_sym needs for n particles (nothing
 // when that passes SYM_MAX_BYTES).
 int reserve_direct_sym(gb_direct *h, int64_t n);
+
+// The symmetric pass over many systems at once (gb_batch_set_variant 1).
+// Device tables of nsys + 1 entries: particle offsets, unit bases (units of
+// system s: its tile pairs x Q slices), column-slot bases (its tile pairs)
+// and fix-up block bases (ceil(n_s / 32) blocks per system).  scratch holds
+// NU row slots and NPtot column slots of SYM_TILE float4s, then the unit
+// counter.
+constexpr int SYM_TILE = 512;
+struct SymBatch {
+    const int64_t *off, *ubase, *cbase, *fbase;
+    int nsys, Q;
+    int64_t NU, NPtot, nfb, P;
+    float4 *scratch;
+};
+// Resident CTAs of the symmetric kernel on a device with sms SMs, and the
+// source slices per tile pair for a pass of the given tile-pair count.
+int direct_sym_slots(int sms);
+int direct_sym_slices(int64_t pairs, int64_t slots);
+int run_batch_sym(const SymBatch &b, int mode, const float4 *xm, float4 *vel, float4 *acc, float G, float eps2,
+                  float dt, int flags, cudaStream_t s);
 
 }  // namespace gb

@@ -32,7 +32,7 @@ namespace gb {
 #define DS_UNROLL 4
 #endif
 
-constexpr int DS_T = 512;
+constexpr int DS_T = SYM_TILE;
 constexpr int DS_K_UNROLL = DS_UNROLL;
 constexpr int DS_WARPS = 4;
 constexpr int DS_ACC = 0, DS_KDK = 1;
@@ -41,18 +41,24 @@ struct DsArgs {
     const float4 *__restrict__ xm;
     const float4 *__restrict__ vel;  // fused KDK: v and a of the step start
     const float4 *__restrict__ acc;
-    float4 *__restrict__ rowpart;  // NP * Q x DS_T
-    float4 *__restrict__ colpart;  // NP x DS_T
+    float4 *__restrict__ rowpart;  // NU x DS_T (one row slot per unit)
+    float4 *__restrict__ colpart;  // tile pairs x DS_T
     unsigned long long *counter;   // zero at launch
-    int64_t n, nt, NP;
+    int64_t n, nt, NU;             // one system: particles, tiles; units in all
+    // Many systems (BATCH): nsys + 1 particle offsets, unit bases and
+    // column-slot bases; units are numbered system after system.
+    const int64_t *__restrict__ off;
+    const int64_t *__restrict__ ubase;
+    const int64_t *__restrict__ cbase;
+    int nsys;
     float eps2, h, dt;
 };
 
 template <int MODE>
-__device__ __forceinline__ float4 ds_load(const DsArgs &a, int64_t i) {
-    if (i >= a.n) return make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 x = __ldg(a.xm + i);
-    if (MODE == DS_KDK) x = predict_xm(x, __ldg(a.vel + i), __ldg(a.acc + i), a.h, a.dt);
+__device__ __forceinline__ float4 ds_load(const DsArgs &a, int64_t o, int64_t n_s, int64_t i) {
+    if (i >= n_s) return make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 x = __ldg(a.xm + o + i);
+    if (MODE == DS_KDK) x = predict_xm(x, __ldg(a.vel + o + i), __ldg(a.acc + o + i), a.h, a.dt);
     return x;
 }
 
@@ -106,17 +112,28 @@ __device__ __forceinline__ void ds_round(const float4 *__restrict__ sxm, float4 
     }
 }
 
-template <int Q, int MODE>
+template <int Q, int MODE, bool BATCH>
 __global__ void __launch_bounds__(DS_WARPS * 32, DS_MIN_CTAS) direct_sym_kernel(DsArgs a) {
     constexpr int G = 16 / Q, SPAN = G * 32;
     __shared__ float4 sxm[DS_T], sacc[DS_T];
-    __shared__ long long s_unit;
+    // The unit and, for a batch, its system's offset, size, local unit and
+    // column-slot base (decoded once by thread 0).
+    __shared__ long long s_unit, s_off, s_n, s_local, s_cb;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, tid = threadIdx.x;
-    const int64_t NU = a.NP * Q;
     const f2 EPS2 = pack2(a.eps2, a.eps2);
     for (;;) {
-        __syncthreads();  // the previous unit is done with s_unit and shared memory
-        if (tid == 0) s_unit = (long long)atomicAdd(a.counter, 1ull);
+        __syncthreads();  // the previous unit is done with the shared state
+        if (tid == 0) {
+            const long long u = (long long)atomicAdd(a.counter, 1ull);
+            s_unit = u;
+            if (BATCH && u < a.NU) {
+                const int sy = find_base(a.ubase, a.nsys, u);
+                s_off = __ldg(a.off + sy);
+                s_n = __ldg(a.off + sy + 1) - s_off;
+                s_local = u - __ldg(a.ubase + sy);
+                s_cb = __ldg(a.cbase + sy);
+            }
+        }
         __syncthreads();
         f2 TX[2], TY[2], TZ[2], TM[2], NX[2], NY[2], NZ[2];
         bool diag;
@@ -125,17 +142,20 @@ __global__ void __launch_bounds__(DS_WARPS * 32, DS_MIN_CTAS) direct_sym_kernel(
             // Unit bookkeeping is re-read from shared memory after the pair
             // loop, so none of it stays in registers across the loop.
             const int64_t u = s_unit;
-            if (u >= NU) break;
-            const int64_t p = u / Q;
-            const int sl = (int)(u - p * Q);
-            const int64_t I = sym_row(p, a.nt);
-            const int64_t J = I + (p - sym_base(I, a.nt));
+            if (u >= a.NU) break;
+            const int64_t o = BATCH ? s_off : 0, n_s = BATCH ? s_n : a.n;
+            const int64_t nt = BATCH ? (n_s + DS_T - 1) / DS_T : a.nt;
+            const int64_t lu = BATCH ? s_local : u;
+            const int64_t p = lu / Q;
+            const int sl = (int)(lu - p * Q);
+            const int64_t I = sym_row(p, nt);
+            const int64_t J = I + (p - sym_base(I, nt));
             diag = J == I;
             gbase = sl * G;
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                const float4 x0 = ds_load<MODE>(a, I * DS_T + 128 * wib + 64 * h + lane);
-                const float4 x1 = ds_load<MODE>(a, I * DS_T + 128 * wib + 64 * h + 32 + lane);
+                const float4 x0 = ds_load<MODE>(a, o, n_s, I * DS_T + 128 * wib + 64 * h + lane);
+                const float4 x1 = ds_load<MODE>(a, o, n_s, I * DS_T + 128 * wib + 64 * h + 32 + lane);
                 TX[h] = pack2(x0.x, x1.x);
                 TY[h] = pack2(x0.y, x1.y);
                 TZ[h] = pack2(x0.z, x1.z);
@@ -144,7 +164,7 @@ __global__ void __launch_bounds__(DS_WARPS * 32, DS_MIN_CTAS) direct_sym_kernel(
             }
             for (int t = tid; t < SPAN; t += DS_WARPS * 32) {
                 const int tt = sl * SPAN + t;
-                sxm[tt] = ds_load<MODE>(a, J * DS_T + tt);
+                sxm[tt] = ds_load<MODE>(a, o, n_s, J * DS_T + tt);
                 sacc[tt] = make_float4(0.f, 0.f, 0.f, 0.f);
             }
         }
@@ -161,11 +181,13 @@ __global__ void __launch_bounds__(DS_WARPS * 32, DS_MIN_CTAS) direct_sym_kernel(
             __syncthreads();
         }
         const int64_t u = s_unit;
-        const int64_t p = u / Q;
-        const int sl = (int)(u - p * Q);
+        const int64_t lu = BATCH ? s_local : u;
+        const int64_t p = lu / Q;
+        const int sl = (int)(lu - p * Q);
+        const int64_t col = (BATCH ? s_cb : 0) + p;
         for (int t = tid; t < SPAN; t += DS_WARPS * 32) {
             const int tt = sl * SPAN + t;
-            a.colpart[p * DS_T + tt] = sacc[tt];
+            a.colpart[col * DS_T + tt] = sacc[tt];
         }
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
@@ -186,6 +208,13 @@ struct DsFix {
     float4 *xm, *vel, *acc;
     int64_t n, nt;
     int Q;
+    // Many systems (BATCH): as in DsArgs, plus each system's first fix-up
+    // block (blocks of 32 particles never straddle two systems).
+    const int64_t *__restrict__ off;
+    const int64_t *__restrict__ ubase;
+    const int64_t *__restrict__ cbase;
+    const int64_t *__restrict__ fbase;
+    int nsys;
     float G, h, dt;
     int accumulate;
     ExtPot pot;
@@ -198,14 +227,24 @@ struct DsFix {
 // the warps' sums in warp order.
 constexpr int DS_FIX_WARPS = 8;
 
-template <int MODE, bool KAHAN>
+template <int MODE, bool KAHAN, bool BATCH>
 __global__ void __launch_bounds__(DS_FIX_WARPS * 32) direct_sym_fixup_kernel(DsFix f) {
     __shared__ float3 part[DS_FIX_WARPS][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int64_t i = (int64_t)blockIdx.x * 32 + lane;
-    const int64_t I = ((int64_t)blockIdx.x * 32) / DS_T, r = i - I * DS_T;
-    const int64_t b = sym_base(I, f.nt);
-    const int64_t R = (f.nt - I) * f.Q, C = I + 1;
+    int64_t o = 0, n_s = f.n, nt = f.nt, li0 = (int64_t)blockIdx.x * 32, ub = 0, cb = 0;
+    if (BATCH) {
+        const int sy = find_base(f.fbase, f.nsys, (int64_t)blockIdx.x);
+        o = __ldg(f.off + sy);
+        n_s = __ldg(f.off + sy + 1) - o;
+        nt = (n_s + DS_T - 1) / DS_T;
+        li0 = ((int64_t)blockIdx.x - __ldg(f.fbase + sy)) * 32;
+        ub = __ldg(f.ubase + sy);
+        cb = __ldg(f.cbase + sy);
+    }
+    const int64_t li = li0 + lane;
+    const int64_t I = li0 / DS_T, r = li - I * DS_T;
+    const int64_t b = sym_base(I, nt);
+    const int64_t R = (nt - I) * f.Q, C = I + 1;
     float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
     auto add = [&](float4 v) {
         if (KAHAN) {
@@ -216,14 +255,15 @@ __global__ void __launch_bounds__(DS_FIX_WARPS * 32) direct_sym_fixup_kernel(DsF
             sx += v.x; sy += v.y; sz += v.z;
         }
     };
-    // Rows of padded particles (i >= n) are zero-mass records: reading them
-    // stays inside the scratch; their sums are dropped below.
-    for (int64_t k = w; k < R; k += DS_FIX_WARPS) add(f.rowpart[(b * f.Q + k) * DS_T + r]);
+    // Rows of padded particles (li >= n_s) are zero-mass records: reading
+    // them stays inside the scratch; their sums are dropped below.
+    for (int64_t k = w; k < R; k += DS_FIX_WARPS) add(f.rowpart[(ub + b * f.Q + k) * DS_T + r]);
     for (int64_t k = (R + DS_FIX_WARPS - 1 - w) / DS_FIX_WARPS * DS_FIX_WARPS + w - R; k < C; k += DS_FIX_WARPS)
-        add(f.colpart[(sym_base(k, f.nt) + (I - k)) * DS_T + r]);
+        add(f.colpart[(cb + sym_base(k, nt) + (I - k)) * DS_T + r]);
     part[w][lane] = make_float3(sx - cx, sy - cy, sz - cz);
     __syncthreads();
-    if (w != 0 || i >= f.n) return;
+    if (w != 0 || li >= n_s) return;
+    const int64_t i = o + li;
     sx = sy = sz = cx = cy = cz = 0.f;
 #pragma unroll
     for (int q = 0; q < DS_FIX_WARPS; ++q) {
@@ -237,9 +277,9 @@ __global__ void __launch_bounds__(DS_FIX_WARPS * 32) direct_sym_fixup_kernel(DsF
             ext_acc_add(f.pot, x.x, x.y, x.z, an.x, an.y, an.z);
         }
         if (f.accumulate) {
-            float4 o = f.acc[i];
-            o.x += an.x; o.y += an.y; o.z += an.z;
-            f.acc[i] = o;
+            float4 v = f.acc[i];
+            v.x += an.x; v.y += an.y; v.z += an.z;
+            f.acc[i] = v;
         } else {
             f.acc[i] = an;
         }
@@ -248,9 +288,37 @@ __global__ void __launch_bounds__(DS_FIX_WARPS * 32) direct_sym_fixup_kernel(DsF
     kdk_writeback(f.xm, f.vel, f.acc, i, an, f.h, f.dt);
 }
 
-template <int Q, int MODE>
-static void launch_ds(unsigned grid, const DsArgs &a, cudaStream_t s) {
-    direct_sym_kernel<Q, MODE><<<grid, DS_WARPS * 32, 0, s>>>(a);
+template <bool BATCH>
+static void launch_pass(int Q, bool kdk, bool kahan, unsigned grid, unsigned fgrid, const DsArgs &a,
+                        const DsFix &f, cudaStream_t s) {
+    const unsigned b = DS_WARPS * 32, fb = DS_FIX_WARPS * 32;
+    if (Q == 1) kdk ? direct_sym_kernel<1, DS_KDK, BATCH><<<grid, b, 0, s>>>(a)
+                    : direct_sym_kernel<1, DS_ACC, BATCH><<<grid, b, 0, s>>>(a);
+    else if (Q == 2) kdk ? direct_sym_kernel<2, DS_KDK, BATCH><<<grid, b, 0, s>>>(a)
+                         : direct_sym_kernel<2, DS_ACC, BATCH><<<grid, b, 0, s>>>(a);
+    else kdk ? direct_sym_kernel<4, DS_KDK, BATCH><<<grid, b, 0, s>>>(a)
+             : direct_sym_kernel<4, DS_ACC, BATCH><<<grid, b, 0, s>>>(a);
+    if (kdk) {
+        if (kahan) direct_sym_fixup_kernel<DS_KDK, true, BATCH><<<fgrid, fb, 0, s>>>(f);
+        else direct_sym_fixup_kernel<DS_KDK, false, BATCH><<<fgrid, fb, 0, s>>>(f);
+    } else {
+        if (kahan) direct_sym_fixup_kernel<DS_ACC, true, BATCH><<<fgrid, fb, 0, s>>>(f);
+        else direct_sym_fixup_kernel<DS_ACC, false, BATCH><<<fgrid, fb, 0, s>>>(f);
+    }
+}
+
+int direct_sym_slots(int sms) {
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, direct_sym_kernel<1, DS_ACC, false>, DS_WARPS * 32, 0);
+    return sms * std::max(occ, 1);
+}
+
+int direct_sym_slices(int64_t pairs, int64_t slots) {
+    // Source slices per tile pair: enough units that the last ones are a
+    // small share of each CTA's work.
+    int Q = 1;
+    while (Q < 4 && pairs * Q < 16 * slots) Q *= 2;
+    return Q;
 }
 
 struct DsPlan {
@@ -262,13 +330,8 @@ static DsPlan ds_plan(const gb_direct *h, int64_t n) {
     DsPlan p;
     p.nt = (n + DS_T - 1) / DS_T;
     p.NP = p.nt * (p.nt + 1) / 2;
-    int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, direct_sym_kernel<1, DS_ACC>, DS_WARPS * 32, 0);
-    const int64_t slots = (int64_t)h->sms * std::max(occ, 1);
-    // Source slices per tile pair: enough units that the last ones are a
-    // small share of each CTA's work.
-    p.Q = 1;
-    while (p.Q < 4 && p.NP * p.Q < 16 * slots) p.Q *= 2;
+    const int64_t slots = direct_sym_slots(h->sms);
+    p.Q = direct_sym_slices(p.NP, slots);
     p.NU = p.NP * p.Q;
     p.P = std::min(slots, p.NU);
     p.need = p.NU * DS_T + p.NP * DS_T + 1;
@@ -285,56 +348,80 @@ int run_direct_sym(gb_direct *h, int mode, const float4 *xm, float4 *vel, float4
                    float eps2, float dt, int flags, cudaStream_t s, const ExtPot &pot, bool *done) {
     *done = false;
     const DsPlan pl = ds_plan(h, n);
-    const int64_t nt = pl.nt, NP = pl.NP, NU = pl.NU, P = pl.P, need = pl.need;
-    const int Q = pl.Q;
-    if (need * (int64_t)sizeof(float4) > SYM_MAX_BYTES) return GB_OK;
-    GB_TRY(ensure_sym(h, need));
-    DsArgs a;
+    if (pl.need * (int64_t)sizeof(float4) > SYM_MAX_BYTES) return GB_OK;
+    GB_TRY(ensure_sym(h, pl.need));
+    DsArgs a{};
     a.xm = xm;
     a.vel = vel;
     a.acc = acc;
     a.rowpart = h->sym;
-    a.colpart = h->sym + NU * DS_T;
-    a.counter = (unsigned long long *)(h->sym + need - 1);
+    a.colpart = h->sym + pl.NU * DS_T;
+    a.counter = (unsigned long long *)(h->sym + pl.need - 1);
     a.n = n;
-    a.nt = nt;
-    a.NP = NP;
+    a.nt = pl.nt;
+    a.NU = pl.NU;
     a.eps2 = eps2;
     a.h = 0.5f * dt;
     a.dt = dt;
-    GB_CUDA_TRY(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), s));
-    const unsigned grid = (unsigned)P;
-    const bool kdk = mode == DS_KDK;
-    if (Q == 1) kdk ? launch_ds<1, DS_KDK>(grid, a, s) : launch_ds<1, DS_ACC>(grid, a, s);
-    else if (Q == 2) kdk ? launch_ds<2, DS_KDK>(grid, a, s) : launch_ds<2, DS_ACC>(grid, a, s);
-    else kdk ? launch_ds<4, DS_KDK>(grid, a, s) : launch_ds<4, DS_ACC>(grid, a, s);
-    GB_CUDA_TRY(cudaGetLastError());
-    DsFix f;
+    DsFix f{};
     f.rowpart = a.rowpart;
     f.colpart = a.colpart;
     f.xm = const_cast<float4 *>(xm);
     f.vel = vel;
     f.acc = acc;
     f.n = n;
-    f.nt = nt;
-    f.Q = Q;
+    f.nt = pl.nt;
+    f.Q = pl.Q;
     f.G = G;
     f.h = 0.5f * dt;
     f.dt = dt;
     f.accumulate = (flags & GB_ACCUMULATE) ? 1 : 0;
     f.pot = pot;
-    const bool kahan = !(flags & GB_PLAIN_FP32);
-    const unsigned fg = (unsigned)((n + 31) / 32), fb = DS_FIX_WARPS * 32;
-    if (kdk) {
-        if (kahan) direct_sym_fixup_kernel<DS_KDK, true><<<fg, fb, 0, s>>>(f);
-        else direct_sym_fixup_kernel<DS_KDK, false><<<fg, fb, 0, s>>>(f);
-    } else {
-        if (kahan) direct_sym_fixup_kernel<DS_ACC, true><<<fg, fb, 0, s>>>(f);
-        else direct_sym_fixup_kernel<DS_ACC, false><<<fg, fb, 0, s>>>(f);
-    }
+    GB_CUDA_TRY(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), s));
+    launch_pass<false>(pl.Q, mode == DS_KDK, !(flags & GB_PLAIN_FP32), (unsigned)pl.P, (unsigned)((n + 31) / 32),
+                       a, f, s);
     GB_CUDA_TRY(cudaGetLastError());
     h->launches += 2;
     *done = true;
+    return GB_OK;
+}
+
+int run_batch_sym(const SymBatch &b, int mode, const float4 *xm, float4 *vel, float4 *acc, float G, float eps2,
+                  float dt, int flags, cudaStream_t s) {
+    DsArgs a{};
+    a.xm = xm;
+    a.vel = vel;
+    a.acc = acc;
+    a.rowpart = b.scratch;
+    a.colpart = b.scratch + b.NU * DS_T;
+    a.counter = (unsigned long long *)(b.scratch + (b.NU + b.NPtot) * DS_T);
+    a.NU = b.NU;
+    a.off = b.off;
+    a.ubase = b.ubase;
+    a.cbase = b.cbase;
+    a.nsys = b.nsys;
+    a.eps2 = eps2;
+    a.h = 0.5f * dt;
+    a.dt = dt;
+    DsFix f{};
+    f.rowpart = a.rowpart;
+    f.colpart = a.colpart;
+    f.xm = const_cast<float4 *>(xm);
+    f.vel = vel;
+    f.acc = acc;
+    f.Q = b.Q;
+    f.off = b.off;
+    f.ubase = b.ubase;
+    f.cbase = b.cbase;
+    f.fbase = b.fbase;
+    f.nsys = b.nsys;
+    f.G = G;
+    f.h = 0.5f * dt;
+    f.dt = dt;
+    f.accumulate = (flags & GB_ACCUMULATE) ? 1 : 0;
+    GB_CUDA_TRY(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), s));
+    launch_pass<true>(b.Q, mode == DS_KDK, !(flags & GB_PLAIN_FP32), (unsigned)b.P, (unsigned)b.nfb, a, f, s);
+    GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
 }
 

@@ -117,3 +117,76 @@ def test_batch_bad_arguments(cuda_dev):
         b.set_tiles(3, 4)
     with pytest.raises(ValueError):
         batch.DirectBatch([], device=cuda_dev)
+
+
+# ------------------------------------------------- symmetric batched pass
+def test_batch_sym_acc_matches_oracle(cuda_dev, orc):
+    batch, ic, _ = _mods()
+    sizes = [1, 2, 33, 256, 1000, 1025, 3000, 700, 4096, 17, 512, 513]
+    systems = _systems(ic, sizes)
+    b = batch.DirectBatch(systems, G=1.0, softening=0.02, device=cuda_dev, variant=1)
+    acc = b.a4[:, :3].double().cpu().numpy()
+    assert torch.all(b.a4[:, 3] == 0.0)
+    for s, (p, v, m) in enumerate(systems):
+        o0, o1 = b.offsets[s], b.offsets[s + 1]
+        if sizes[s] == 1:
+            assert np.all(acc[o0:o1] == 0.0)
+            continue
+        rel = _rel(acc[o0:o1], orc.direct_acc(p, m, 1.0, 0.02 ** 2))
+        assert np.sqrt((rel ** 2).mean()) < 1e-5 and rel.max() < 1e-4, (s, rel.max())
+    b.close()
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_batch_sym_kdk_matches_loop_and_repeats(cuda_dev, graph):
+    batch, ic, _ = _mods()
+    sizes = ic.batch_sizes(24, 256, 4096)
+    systems = _systems(ic, sizes)
+    b1 = batch.DirectBatch(systems, G=1.0, softening=0.02, device=cuda_dev, variant=1)
+    b3 = batch.DirectBatch(systems, G=1.0, softening=0.02, device=cuda_dev, variant=1)
+    b2 = batch.DirectBatch(systems, G=1.0, softening=0.02, device=cuda_dev)
+    for b in (b1, b3):
+        b.run(1e-3, 5, graph=graph)
+        b.run(1e-3, 5, graph=graph)
+    b2.run_loop(1e-3, 10)
+    torch.cuda.synchronize()
+    for t1, t3 in zip((b1.xm, b1.v4, b1.a4), (b3.xm, b3.v4, b3.a4)):
+        assert torch.equal(t1, t3)
+    x1 = b1.xm[:, :3].double().cpu().numpy()
+    x2 = b2.xm[:, :3].double().cpu().numpy()
+    assert np.abs(x1 - x2).max() < 1e-5 * np.abs(x2).max()
+    v1 = b1.v4[:, :3].double().cpu().numpy()
+    v2 = b2.v4[:, :3].double().cpu().numpy()
+    assert np.abs(v1 - v2).max() < 1e-4 * np.abs(v2).max()
+    assert b1.launch_count() == 2 * 10 + 2
+    for b in (b1, b2, b3):
+        b.close()
+
+
+def test_batch_sym_graph_equals_direct_launches(cuda_dev):
+    """Switching the variant recaptures the graph; replay and direct launches
+    give the same bits."""
+    batch, ic, _ = _mods()
+    systems = _systems(ic, [900, 2500, 130])
+    out = []
+    for graph in (False, True):
+        b = batch.DirectBatch(systems, G=1.0, softening=0.02, device=cuda_dev)
+        b.run(1e-3, 2, graph=graph)
+        b.set_variant(1)
+        b.run(1e-3, 3, graph=graph)
+        b.set_variant(0)
+        b.run(1e-3, 2, graph=graph)
+        torch.cuda.synchronize()
+        out.append((b.xm.clone(), b.v4.clone(), b.a4.clone()))
+        b.close()
+    for u, w in zip(*out):
+        assert torch.equal(u, w)
+
+
+def test_batch_bad_variant(cuda_dev):
+    batch, ic, _ = _mods()
+    pkg = importlib.import_module(PKG_NAME)
+    b = batch.DirectBatch(_systems(ic, [64, 65]), device=cuda_dev)
+    with pytest.raises(pkg.GravityError):
+        b.set_variant(2)
+    b.close()
