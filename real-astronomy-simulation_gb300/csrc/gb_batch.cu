@@ -203,6 +203,7 @@ struct gb_batch {
     // block bases, nsys + 1 each) and scratch, allocated on first selection.
     int variant;
     int64_t *d_symtab;
+    int *d_fsys;
     float4 *sym;
     SymBatch symb;
 };
@@ -232,22 +233,34 @@ static int batch_sym_plan(gb_batch_t *h) {
         return fail(GB_EINVAL, "symmetric batch pass needs %lld bytes of scratch (limit %lld)",
                     (long long)(need * 16), (long long)SYM_MAX_BYTES);
     if (fb[ns] > INT32_MAX) return fail(GB_EINVAL, "too many particles for the symmetric batch fix-up");
-    if (cudaMalloc(&h->d_symtab, sizeof(int64_t) * tab.size()) != cudaSuccess) {
-        h->d_symtab = nullptr;
-        return fail(GB_ENOMEM, "symmetric batch tables");
-    }
-    if (cudaMalloc(&h->sym, sizeof(float4) * need) != cudaSuccess) {
-        h->sym = nullptr;
+    std::vector<int> fsys(fb[ns]);
+    for (int s = 0; s < ns; ++s)
+        for (int64_t k = fb[s]; k < fb[s + 1]; ++k) fsys[k] = s;
+    auto release = [&]() {
         cudaFree(h->d_symtab);
+        cudaFree(h->d_fsys);
+        cudaFree(h->sym);
         h->d_symtab = nullptr;
-        return fail(GB_ENOMEM, "symmetric batch scratch (%lld bytes)", (long long)(need * 16));
+        h->d_fsys = nullptr;
+        h->sym = nullptr;
+    };
+    if (cudaMalloc(&h->d_symtab, sizeof(int64_t) * tab.size()) != cudaSuccess ||
+        cudaMalloc(&h->d_fsys, sizeof(int) * fsys.size()) != cudaSuccess ||
+        cudaMalloc(&h->sym, sizeof(float4) * need) != cudaSuccess) {
+        release();
+        return fail(GB_ENOMEM, "symmetric batch tables and scratch (%lld bytes)", (long long)(need * 16));
     }
-    GB_CUDA_TRY(cudaMemcpy(h->d_symtab, tab.data(), sizeof(int64_t) * tab.size(), cudaMemcpyHostToDevice));
+    if (cudaMemcpy(h->d_symtab, tab.data(), sizeof(int64_t) * tab.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(h->d_fsys, fsys.data(), sizeof(int) * fsys.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        release();
+        return fail(GB_ECUDA, "symmetric batch tables upload");
+    }
     SymBatch &b = h->symb;
     b.off = h->d_off;
     b.ubase = h->d_symtab;
     b.cbase = h->d_symtab + ns + 1;
     b.fbase = h->d_symtab + 2 * (ns + 1);
+    b.fsys = h->d_fsys;
     b.nsys = ns;
     b.Q = Q;
     b.NU = NU;
@@ -304,6 +317,7 @@ extern "C" int gb_batch_destroy(gb_batch_t *h) {
     cudaFree(h->d_stbase);
     cudaFree(h->part);
     cudaFree(h->d_symtab);
+    cudaFree(h->d_fsys);
     cudaFree(h->sym);
     if (h->loop) gb_direct_destroy(h->loop);
     delete h;

@@ -198,12 +198,13 @@ int reserve_direct_sym(gb_direct *h, int64_t n);
 // The symmetric pass over many systems at once (gb_batch_set_variant 1).
 // Device tables of nsys + 1 entries: particle offsets, unit bases (units of
 // system s: its tile pairs x Q slices), column-slot bases (its tile pairs)
-// and fix-up block bases (ceil(n_s / 32) blocks per system).  scratch holds
-// NU row slots and NPtot column slots of SYM_TILE float4s, then the unit
-// counter.
+// and fix-up block bases (ceil(n_s / 32) blocks per system), and the system
+// of every fix-up block.  scratch holds NU row slots and NPtot column slots
+// of SYM_TILE float4s, then the unit counter.
 constexpr int SYM_TILE = 512;
 struct SymBatch {
     const int64_t *off, *ubase, *cbase, *fbase;
+    const int *fsys;
     int nsys, Q;
     int64_t NU, NPtot, nfb, P;
     float4 *scratch;

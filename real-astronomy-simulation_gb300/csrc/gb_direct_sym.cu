@@ -209,11 +209,13 @@ struct DsFix {
     int64_t n, nt;
     int Q;
     // Many systems (BATCH): as in DsArgs, plus each system's first fix-up
-    // block (blocks of 32 particles never straddle two systems).
+    // block (blocks of 32 particles never straddle two systems) and the
+    // system of every block.
     const int64_t *__restrict__ off;
     const int64_t *__restrict__ ubase;
     const int64_t *__restrict__ cbase;
     const int64_t *__restrict__ fbase;
+    const int *__restrict__ fsys;  // system of each fix-up block
     int nsys;
     float G, h, dt;
     int accumulate;
@@ -233,7 +235,7 @@ __global__ void __launch_bounds__(DS_FIX_WARPS * 32) direct_sym_fixup_kernel(DsF
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int64_t o = 0, n_s = f.n, nt = f.nt, li0 = (int64_t)blockIdx.x * 32, ub = 0, cb = 0;
     if (BATCH) {
-        const int sy = find_base(f.fbase, f.nsys, (int64_t)blockIdx.x);
+        const int sy = __ldg(f.fsys + blockIdx.x);
         o = __ldg(f.off + sy);
         n_s = __ldg(f.off + sy + 1) - o;
         nt = (n_s + DS_T - 1) / DS_T;
@@ -414,6 +416,7 @@ int run_batch_sym(const SymBatch &b, int mode, const float4 *xm, float4 *vel, fl
     f.ubase = b.ubase;
     f.cbase = b.cbase;
     f.fbase = b.fbase;
+    f.fsys = b.fsys;
     f.nsys = b.nsys;
     f.G = G;
     f.h = 0.5f * dt;
