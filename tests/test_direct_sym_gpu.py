@@ -157,3 +157,37 @@ def test_variant_out_of_range_is_rejected(cuda_dev):
     with pytest.raises(pkg.GravityError):
         s.set_tiles(2, 4, 0, 3)
     s.close()
+
+
+def test_kdk_graph_recaptures_after_scratch_regrowth(cuda_dev):
+    """The symmetric force pass and the symmetric adjoint share the handle's
+    tile-pair scratch.  An adjoint step on a larger system regrows it; the
+    next graph-replayed KDK step must capture again (the scratch address is
+    part of the graph key) and match direct launches bit for bit."""
+    grav, ic = _mods()
+    lib = importlib.import_module(PKG_NAME + "._lib")
+    n_small, n_big = 1000, 4096
+    p, v, m = ic.plummer(n_small, seed=21)
+    pb, _, mb = ic.plummer(n_big, seed=22)
+    stream = torch.cuda.current_stream(cuda_dev).cuda_stream
+    out = []
+    for graph in (False, True):
+        s = _sym_solver(grav, n_big, cuda_dev)
+        xm = _xm(p, m, cuda_dev)
+        v4 = torch.zeros_like(xm)
+        v4[:, :3] = torch.tensor(v, dtype=torch.float32, device=cuda_dev)
+        a4 = torch.zeros_like(xm)
+        s.acc(xm, a4, 1.0, 1e-4)
+        s.kdk(xm, v4, a4, 1.0, 1e-4, 1e-3, 3, graph=graph)
+        xb = _xm(pb, mb, cuda_dev)
+        lx, lv, la = (torch.ones_like(xb) for _ in range(3))
+        lm = torch.zeros(n_big, dtype=torch.float32, device=cuda_dev)
+        lib.call("gb_adjoint_set_variant", s.handle, 2)
+        lib.call("gb_adjoint_step", s.handle, xb.data_ptr(), lx.data_ptr(), lv.data_ptr(), la.data_ptr(),
+                 lm.data_ptr(), n_big, 1.0, 1e-4, 1e-3, 0, stream)
+        s.kdk(xm, v4, a4, 1.0, 1e-4, 1e-3, 3, graph=graph)
+        torch.cuda.synchronize()
+        out.append((xm.clone(), v4.clone(), a4.clone(), lx.clone(), lm.clone()))
+        s.close()
+    for u, w in zip(*out):
+        assert torch.equal(u, w)
