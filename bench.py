@@ -373,8 +373,12 @@ def bench_direct(dev, lib_mod, peak_tflops):
     torch.cuda.synchronize()
     t = s.elapsed_time(e) / 1e3
     e1 = eng.energies()
+    gint = n * n * steps / t / 1e9
     out = {"workload": "direct N^2 Plummer N=20000, G=1, eps=0.01, dt=1e-3, 100 KDK steps",
-           "gint_per_s": n * n * steps / t / 1e9, "ms_per_step": t / steps * 1e3,
+           "gint_per_s": gint, "ms_per_step": t / steps * 1e3,
+           # N^2 delivered interactions x 20 flop over the measured FP32 peak;
+           # the symmetric pass evaluates N^2 / 2 pairs to deliver them.
+           "frac_of_fp32_peak_20flop_equivalent": gint * 20 / 1e3 / peak_tflops,
            "energy_drift": abs((e1[2] - e0[2]) / e0[2]), "acc_err_vs_fp64_2048_targets": err}
     kern = {}
     for nk in (20000, 262144):
@@ -406,6 +410,8 @@ def bench_direct(dev, lib_mod, peak_tflops):
         torch.cuda.synchronize()
         ts = s.elapsed_time(e) / reps / 1e3
         kern[str(nk)]["symmetric"] = {"ms": ts * 1e3, "gint_per_s": nk * nk / ts / 1e9,
+                                      "frac_of_fp32_peak_20flop_equivalent":
+                                          20.0 * nk * nk / ts / 1e12 / peak_tflops,
                                       "speedup_vs_per_target": tk / ts}
         g.close()
     out["force_kernel"] = kern
@@ -414,8 +420,9 @@ def bench_direct(dev, lib_mod, peak_tflops):
 
 def bench_merger(dev, drift_steps=1000):
     """Precision: two Plummer spheres (2 x 131,072, G = 1, a = 1, M = 1) 10
-    apart on a parabolic orbit, eps = 0.01.  FP32+Kahan vs plain FP32 vs FP64
-    on 8,192 targets; FP64 energy drift over KDK steps at dt = 5e-4."""
+    apart on a parabolic orbit, eps = 0.01.  FP32+Kahan (per-target and
+    symmetric passes) vs plain FP32 vs FP64 on 8,192 targets; FP64 energy
+    drift over Engine KDK steps (symmetric pass) at dt = 5e-4."""
     pkg = importlib.import_module(PKG)
     ic = importlib.import_module(PKG + ".ic")
     grav = importlib.import_module(PKG + ".solvers.gravity")
@@ -431,6 +438,9 @@ def bench_merger(dev, drift_steps=1000):
     kahan = _rel_stats(acc[:, :3].double().cpu().numpy()[targets], ref)
     g.acc(xm, acc, 1.0, 1e-4, plain=True)
     plain = _rel_stats(acc[:, :3].double().cpu().numpy()[targets], ref)
+    g.set_variant(2)  # the symmetric pass (the Engine's), Kahan-merged slots
+    g.acc(xm, acc, 1.0, 1e-4)
+    sym = _rel_stats(acc[:, :3].double().cpu().numpy()[targets], ref)
     g.close()
     eng = pkg.Engine(softening=0.01, G=1.0, device=dev)
     eng.load_state(pkg.State.from_arrays(pos, vel, mass))
@@ -444,6 +454,7 @@ def bench_merger(dev, drift_steps=1000):
     e1 = eng.energies()
     return {"workload": f"two-Plummer merger 2x131072, eps=0.01, dt=5e-4, {drift_steps} KDK steps",
             "impact_parameter": 2.0, "kahan_vs_fp64": kahan, "plain_fp32_vs_fp64": plain,
+            "symmetric_kahan_vs_fp64": sym,
             "energy_drift": abs((e1[2] - e0[2]) / e0[2]), "E0": e0, "E1": e1,
             "gint_per_s": n * n * drift_steps / t / 1e9}
 
@@ -750,7 +761,8 @@ def bench_snapshot(dev, n=1_000_000, steps=100, every=20):
 def bench_scaling(dev, sizes=(10_000, 100_000, 1_000_000, 4_000_000, 16_000_000)):
     """BH KDK step time and force error against N (exponential disk, theta
     0.5, eps 0.05, 30-bit keys; error against FP64 direct sums on 256 seeded
-    targets), and one direct N^2 force evaluation at N = 1M."""
+    targets), and one direct N^2 force evaluation at N = 1M (per-target and
+    symmetric passes; the symmetric one runs in bands of tile rows)."""
     ic = importlib.import_module(PKG + ".ic")
     bhmod = importlib.import_module(PKG + ".solvers.barnes_hut")
     grav = importlib.import_module(PKG + ".solvers.gravity")
@@ -786,12 +798,15 @@ def bench_scaling(dev, sizes=(10_000, 100_000, 1_000_000, 4_000_000, 16_000_000)
         if n == 1_000_000:
             g = grav.DirectGravity(n, dev)
             acc = torch.zeros_like(xm)
-            g.acc(xm, acc, units.G, BH_EPS * BH_EPS)
-            s.record()
-            g.acc(xm, acc, units.G, BH_EPS * BH_EPS)
-            e.record()
-            torch.cuda.synchronize()
-            direct_ms = s.elapsed_time(e)
+            direct_ms = {}
+            for name, variant in (("per_target", 0), ("symmetric", 2)):
+                g.set_variant(variant)
+                g.acc(xm, acc, units.G, BH_EPS * BH_EPS)
+                s.record()
+                g.acc(xm, acc, units.G, BH_EPS * BH_EPS)
+                e.record()
+                torch.cuda.synchronize()
+                direct_ms[name] = s.elapsed_time(e)
             g.close()
         del xm, v4, a4
         torch.cuda.empty_cache()

@@ -74,11 +74,18 @@ int gb_direct_set_tiles(gb_direct_t *h, int k, int warps, int ctas_per_sm);
 
 /* Inner-loop form: 0 = scalar FP32 (default), 1 = packed .f32x2 FP32, one
  * pass per target; 2 = symmetric packed .f32x2, each unordered pair once,
- * applied to both particles (tile-pair scratch of N^2/32 bytes at large N,
- * up to 5 N^2/64 at small N; where that passes 3 GiB, N above about
- * 310,000, the scalar pass runs).  Same results up to FP32 rounding order;
- * gb_direct_phi always runs the per-target pass. */
+ * applied to both particles.  The symmetric pass keeps 8 KB slots per
+ * 512 x 512 tile pair (N^2/32 bytes in all at large N); above the band
+ * budget (gb_direct_set_sym_band, 1 GiB by default) it runs in bands of tile
+ * rows, two kernels per band, plus 32 bytes per particle of running sums.
+ * Same results up to FP32 rounding order; gb_direct_phi always runs the
+ * per-target pass. */
 int gb_direct_set_variant(gb_direct_t *h, int packed);
+
+/* Tile-pair slot bytes per band of the symmetric pass (at least 40 KB:
+ * one tile pair with four source slices).  Measurement and testing knob; the
+ * default, 1 GiB, keeps a band's slots in a small share of HBM. */
+int gb_direct_set_sym_band(gb_direct_t *h, int64_t bytes);
 
 /* acc_i = G sum_j m_j (x_j - x_i) / (|x_j - x_i|^2 + eps2)^{3/2}, all j
  * (i == j adds zero).  Replaces compute_acc_direct

@@ -76,6 +76,7 @@ SIGNATURES = {
     "gb_direct_destroy": (I32, [P]),
     "gb_direct_set_tiles": (I32, [P, I32, I32, I32]),
     "gb_direct_set_variant": (I32, [P, I32]),
+    "gb_direct_set_sym_band": (I32, [P, I64]),
     "gb_direct_acc": (I32, [P, P, P, I64, F32, F32, I32, P]),
     "gb_direct_kdk": (I32, [P, P, P, P, I64, F32, F32, F32, I64, I32, P]),
     "gb_direct_phi": (I32, [P, P, P, I64, F32, I32, P]),

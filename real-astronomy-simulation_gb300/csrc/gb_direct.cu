@@ -609,6 +609,7 @@ extern "C" int gb_direct_create(gb_direct_t **out, int64_t n_max) {
     h->ctas_per_sm = 0;
     h->packed = 0;
     h->adj_variant = 2;
+    h->sym_band = 1LL << 30;
     int st = ensure_partials(h, max_partials(h, n_max));
     h->st0_cap = h->sms * 64;  // above every plan's CTA count (ctas_per_sm <= 32)
     if (st == GB_OK && cudaMalloc(&h->st0tab, sizeof(int) * h->st0_cap) != cudaSuccess)
@@ -787,8 +788,8 @@ extern "C" int gb_direct_kdk(gb_direct_t *h, float *xm, float *vel, float *acc, 
     // Tile-pair scratch is sized before the capture (no allocation inside
     // it); its address is part of the key, since the adjoint may regrow it.
     if (h->packed == 2) GB_TRY(reserve_direct_sym(h, n));
-    const gb_direct::Key key{xm, vel, acc, h->sym, n, G, eps2, dt, plain, h->np, h->warps, h->ctas_per_sm,
-                             h->packed};
+    const gb_direct::Key key{xm, vel, acc, h->sym, n, h->sym_band, G, eps2, dt, plain, h->np, h->warps,
+                             h->ctas_per_sm, h->packed};
     if (!h->has_graph || !(h->gkey == key)) {
         if (h->has_graph) {
             cudaGraphExecDestroy(h->gexec);
@@ -875,6 +876,16 @@ extern "C" int gb_direct_set_variant(gb_direct_t *h, int packed) {
     if (!h) return fail(GB_EINVAL, "handle is NULL");
     if (packed < 0 || packed > 2) return fail(GB_EINVAL, "variant must be 0, 1 or 2");
     h->packed = packed;
+    return GB_OK;
+}
+
+extern "C" int gb_direct_set_sym_band(gb_direct_t *h, int64_t bytes) {
+    if (!h) return fail(GB_EINVAL, "handle is NULL");
+    // At least one tile pair with its four source slices per band.
+    const int64_t min_bytes = (int64_t)sizeof(float4) * SYM_TILE * 5;
+    if (bytes < min_bytes) return fail(GB_EINVAL, "band budget %lld below %lld bytes", (long long)bytes,
+                                       (long long)min_bytes);
+    h->sym_band = bytes;
     return GB_OK;
 }
 

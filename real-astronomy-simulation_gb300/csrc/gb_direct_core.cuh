@@ -152,6 +152,7 @@ struct gb_direct {
     float4 *sym;        // symmetric adjoint partials (allocated on first use)
     int64_t sym_cap;    // float4 elements
     int adj_variant;    // 2: symmetric packed, 1: symmetric scalar, 0: one pass per target
+    int64_t sym_band;   // symmetric force pass: tile-pair slot bytes per band at most
     // One KDK step captured as a CUDA graph (gb_direct_kdk with
     // GB_USE_GRAPH), replayed per step on the handle's own stream.
     cudaStream_t gstream;
@@ -160,11 +161,11 @@ struct gb_direct {
     bool has_graph;
     struct Key {
         const void *xm, *vel, *acc, *sym;
-        int64_t n;
+        int64_t n, sym_band;
         float G, eps2, dt;
         int plain, np, warps, ctas_per_sm, packed;
         bool operator==(const Key &o) const {
-            return xm == o.xm && vel == o.vel && acc == o.acc && sym == o.sym && n == o.n && G == o.G && eps2 == o.eps2 &&
+            return xm == o.xm && vel == o.vel && acc == o.acc && sym == o.sym && n == o.n && sym_band == o.sym_band && G == o.G && eps2 == o.eps2 &&
                    dt == o.dt && plain == o.plain && np == o.np && warps == o.warps &&
                    ctas_per_sm == o.ctas_per_sm && packed == o.packed;
         }

@@ -21,6 +21,9 @@
 // the closing kick and writes x', v', a').  In the fused KDK form both sides
 // load the leapfrog prediction x' = x + (v + a dt/2) dt with the same FMAs as
 // the per-target kernel, so the two forms see identical positions.
+#include <algorithm>
+#include <vector>
+
 #include "gb_direct_core.cuh"
 
 namespace gb {
@@ -45,6 +48,7 @@ struct DsArgs {
     float4 *__restrict__ colpart;  // tile pairs x DS_T
     unsigned long long *counter;   // zero at launch
     int64_t n, nt, NU;             // one system: particles, tiles; units in all
+    int64_t p0;                    // one system: first tile pair of the band
     // Many systems (BATCH): nsys + 1 particle offsets, unit bases and
     // column-slot bases; units are numbered system after system.
     const int64_t *__restrict__ off;
@@ -148,8 +152,9 @@ __global__ void __launch_bounds__(DS_WARPS * 32, DS_MIN_CTAS) direct_sym_kernel(
             const int64_t lu = BATCH ? s_local : u;
             const int64_t p = lu / Q;
             const int sl = (int)(lu - p * Q);
-            const int64_t I = sym_row(p, nt);
-            const int64_t J = I + (p - sym_base(I, nt));
+            const int64_t pg = BATCH ? p : a.p0 + p;  // pair index in the system's triangle
+            const int64_t I = sym_row(pg, nt);
+            const int64_t J = I + (pg - sym_base(I, nt));
             diag = J == I;
             gbase = sl * G;
 #pragma unroll
@@ -208,6 +213,11 @@ struct DsFix {
     float4 *xm, *vel, *acc;
     int64_t n, nt;
     int Q;
+    // One system, in bands of tile rows [Ib, Ie) whose pairs start at p0;
+    // aux holds the running (sum, compensation) of particles in tiles >= Ie
+    // between bands (two float4 per particle).
+    int64_t Ib, Ie, p0;
+    float4 *aux;
     // Many systems (BATCH): as in DsArgs, plus each system's first fix-up
     // block (blocks of 32 particles never straddle two systems) and the
     // system of every block.
@@ -222,18 +232,24 @@ struct DsFix {
     ExtPot pot;
 };
 
-// Particle i's slots, in a fixed order: its row units (I, J, slice) for
-// J = I .. nt-1, then its column slots (I', I) for I' = 0 .. I.  A CTA of
-// DS_FIX_WARPS warps takes 32 consecutive particles (one tile I); warp w adds
-// slots w, w + DS_FIX_WARPS, ... (coalesced 512-byte rows), and warp 0 adds
-// the warps' sums in warp order.
+// Particle i (in tile T) has, in a fixed order: the running sum left by
+// earlier bands (columns of rows < Ib), its row units (T, J, slice) for
+// J = T .. nt-1 when T is in the band, then its column slots (I', T) for the
+// band's rows I' <= T.  A particle whose tile is in the band is complete
+// (all rows I' <= T are done) and is written out; one past the band keeps
+// its running sum in aux.  A single band (Ib = 0, Ie = nt) is the whole
+// pass, as is a batch system.  A CTA of DS_FIX_WARPS warps takes 32
+// consecutive particles (one tile); warp w adds slots w, w + DS_FIX_WARPS,
+// ... (coalesced 512-byte rows), and warp 0 adds the warps' sums in warp
+// order.
 constexpr int DS_FIX_WARPS = 8;
 
 template <int MODE, bool KAHAN, bool BATCH>
 __global__ void __launch_bounds__(DS_FIX_WARPS * 32) direct_sym_fixup_kernel(DsFix f) {
     __shared__ float3 part[DS_FIX_WARPS][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int64_t o = 0, n_s = f.n, nt = f.nt, li0 = (int64_t)blockIdx.x * 32, ub = 0, cb = 0;
+    int64_t o = 0, n_s = f.n, nt = f.nt, li0 = f.Ib * DS_T + (int64_t)blockIdx.x * 32, ub = 0, cb = 0;
+    int64_t Ib = f.Ib, Ie = f.Ie, p0 = f.p0;
     if (BATCH) {
         const int sy = __ldg(f.fsys + blockIdx.x);
         o = __ldg(f.off + sy);
@@ -242,11 +258,16 @@ __global__ void __launch_bounds__(DS_FIX_WARPS * 32) direct_sym_fixup_kernel(DsF
         li0 = ((int64_t)blockIdx.x - __ldg(f.fbase + sy)) * 32;
         ub = __ldg(f.ubase + sy);
         cb = __ldg(f.cbase + sy);
+        Ib = 0;
+        Ie = nt;
+        p0 = 0;
     }
     const int64_t li = li0 + lane;
-    const int64_t I = li0 / DS_T, r = li - I * DS_T;
-    const int64_t b = sym_base(I, nt);
-    const int64_t R = (nt - I) * f.Q, C = I + 1;
+    const int64_t T = li0 / DS_T, r = li - T * DS_T;
+    const bool in_band = T < Ie;
+    const int64_t R = in_band ? (nt - T) * f.Q : 0;
+    const int64_t C = (in_band ? T : Ie - 1) - Ib + 1;
+    const int64_t rbase = ub + (sym_base(T, nt) - p0) * f.Q;
     float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
     auto add = [&](float4 v) {
         if (KAHAN) {
@@ -259,18 +280,30 @@ __global__ void __launch_bounds__(DS_FIX_WARPS * 32) direct_sym_fixup_kernel(DsF
     };
     // Rows of padded particles (li >= n_s) are zero-mass records: reading
     // them stays inside the scratch; their sums are dropped below.
-    for (int64_t k = w; k < R; k += DS_FIX_WARPS) add(f.rowpart[(ub + b * f.Q + k) * DS_T + r]);
-    for (int64_t k = (R + DS_FIX_WARPS - 1 - w) / DS_FIX_WARPS * DS_FIX_WARPS + w - R; k < C; k += DS_FIX_WARPS)
-        add(f.colpart[(cb + sym_base(k, nt) + (I - k)) * DS_T + r]);
+    for (int64_t k = w; k < R; k += DS_FIX_WARPS) add(f.rowpart[(rbase + k) * DS_T + r]);
+    for (int64_t k = (R + DS_FIX_WARPS - 1 - w) / DS_FIX_WARPS * DS_FIX_WARPS + w - R; k < C; k += DS_FIX_WARPS) {
+        const int64_t I2 = Ib + k;
+        add(f.colpart[(cb + sym_base(I2, nt) + (T - I2) - p0) * DS_T + r]);
+    }
     part[w][lane] = make_float3(sx - cx, sy - cy, sz - cz);
     __syncthreads();
     if (w != 0 || li >= n_s) return;
     const int64_t i = o + li;
     sx = sy = sz = cx = cy = cz = 0.f;
+    if (!BATCH && Ib > 0) {  // the running sum of the earlier bands
+        const float4 s0 = f.aux[2 * i], c0 = f.aux[2 * i + 1];
+        sx = s0.x; sy = s0.y; sz = s0.z;
+        cx = c0.x; cy = c0.y; cz = c0.z;
+    }
 #pragma unroll
     for (int q = 0; q < DS_FIX_WARPS; ++q) {
         const float3 v = part[q][lane];
         add(make_float4(v.x, v.y, v.z, 0.f));
+    }
+    if (!BATCH && !in_band) {
+        f.aux[2 * i] = make_float4(sx, sy, sz, 0.f);
+        f.aux[2 * i + 1] = make_float4(cx, cy, cz, 0.f);
+        return;
     }
     float4 an = make_float4(f.G * (sx - cx), f.G * (sy - cy), f.G * (sz - cz), 0.f);
     if (MODE == DS_ACC) {
@@ -323,20 +356,39 @@ int direct_sym_slices(int64_t pairs, int64_t slots) {
     return Q;
 }
 
+static int64_t host_sym_base(int64_t I, int64_t nt) { return I * nt - I * (I - 1) / 2; }
+
 struct DsPlan {
-    int64_t nt, NP, NU, P, need;  // need: float4s of scratch (+1 for the unit counter)
+    int64_t nt, NP, slots, max_pairs, need;  // need: float4s of scratch
     int Q;
+    std::vector<int64_t> rows;  // band b covers tile rows [rows[b], rows[b + 1])
 };
 
 static DsPlan ds_plan(const gb_direct *h, int64_t n) {
     DsPlan p;
     p.nt = (n + DS_T - 1) / DS_T;
     p.NP = p.nt * (p.nt + 1) / 2;
-    const int64_t slots = direct_sym_slots(h->sms);
-    p.Q = direct_sym_slices(p.NP, slots);
-    p.NU = p.NP * p.Q;
-    p.P = std::min(slots, p.NU);
-    p.need = p.NU * DS_T + p.NP * DS_T + 1;
+    p.slots = direct_sym_slots(h->sms);
+    p.Q = direct_sym_slices(p.NP, p.slots);
+    // Tile pairs per band: the handle's slot budget (larger systems run in
+    // bands of tile rows, so the scratch stays bounded at any N).
+    const int64_t budget = h->sym_band / ((int64_t)sizeof(float4) * DS_T * (p.Q + 1));
+    p.rows.assign(1, 0);
+    p.max_pairs = 0;
+    int64_t pairs = 0;
+    for (int64_t I = 0; I < p.nt; ++I) {
+        if (pairs > 0 && pairs + (p.nt - I) > budget) {
+            p.rows.push_back(I);
+            p.max_pairs = std::max(p.max_pairs, pairs);
+            pairs = 0;
+        }
+        pairs += p.nt - I;
+    }
+    p.rows.push_back(p.nt);
+    p.max_pairs = std::max(p.max_pairs, pairs);
+    // Row slots, column slots, the running sums between bands, the counter.
+    const int64_t aux = p.rows.size() > 2 ? 2 * n : 0;
+    p.need = p.max_pairs * p.Q * DS_T + p.max_pairs * DS_T + aux + 1;
     return p;
 }
 
@@ -357,17 +409,17 @@ int run_direct_sym(gb_direct *h, int mode, const float4 *xm, float4 *vel, float4
     a.vel = vel;
     a.acc = acc;
     a.rowpart = h->sym;
-    a.colpart = h->sym + pl.NU * DS_T;
+    a.colpart = h->sym + pl.max_pairs * pl.Q * DS_T;
     a.counter = (unsigned long long *)(h->sym + pl.need - 1);
     a.n = n;
     a.nt = pl.nt;
-    a.NU = pl.NU;
     a.eps2 = eps2;
     a.h = 0.5f * dt;
     a.dt = dt;
     DsFix f{};
     f.rowpart = a.rowpart;
     f.colpart = a.colpart;
+    f.aux = a.colpart + pl.max_pairs * DS_T;
     f.xm = const_cast<float4 *>(xm);
     f.vel = vel;
     f.acc = acc;
@@ -379,11 +431,20 @@ int run_direct_sym(gb_direct *h, int mode, const float4 *xm, float4 *vel, float4
     f.dt = dt;
     f.accumulate = (flags & GB_ACCUMULATE) ? 1 : 0;
     f.pot = pot;
-    GB_CUDA_TRY(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), s));
-    launch_pass<false>(pl.Q, mode == DS_KDK, !(flags & GB_PLAIN_FP32), (unsigned)pl.P, (unsigned)((n + 31) / 32),
-                       a, f, s);
-    GB_CUDA_TRY(cudaGetLastError());
-    h->launches += 2;
+    const bool kdk = mode == DS_KDK, kahan = !(flags & GB_PLAIN_FP32);
+    for (size_t b = 0; b + 1 < pl.rows.size(); ++b) {
+        const int64_t Ib = pl.rows[b], Ie = pl.rows[b + 1];
+        a.p0 = host_sym_base(Ib, pl.nt);
+        a.NU = (host_sym_base(Ie, pl.nt) - a.p0) * pl.Q;
+        f.Ib = Ib;
+        f.Ie = Ie;
+        f.p0 = a.p0;
+        GB_CUDA_TRY(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), s));
+        launch_pass<false>(pl.Q, kdk, kahan, (unsigned)std::min(pl.slots, a.NU),
+                           (unsigned)((n - Ib * DS_T + 31) / 32), a, f, s);
+        GB_CUDA_TRY(cudaGetLastError());
+        h->launches += 2;
+    }
     *done = true;
     return GB_OK;
 }

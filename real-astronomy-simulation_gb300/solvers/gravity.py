@@ -59,9 +59,14 @@ class DirectGravity:
     def set_variant(self, variant: int):
         """Force-pass form: 0 scalar per target (default), 1 packed per
         target, 2 symmetric (each unordered pair once, both particles
-        updated; needs N^2/32 bytes of scratch at large N, runs the scalar
-        pass where that passes 3 GiB).  The potential pass is per target."""
+        updated; its tile-pair scratch is bounded by running large systems in
+        bands, see set_sym_band).  The potential pass is per target."""
         _lib.call("gb_direct_set_variant", self._h, int(variant))
+
+    def set_sym_band(self, nbytes: int):
+        """Slot bytes per band of the symmetric pass (default 1 GiB); larger
+        systems run in bands of tile rows."""
+        _lib.call("gb_direct_set_sym_band", self._h, int(nbytes))
 
     # -- compute
     def acc(self, xm, acc, G, eps2, accumulate=False, plain=False):

@@ -45,11 +45,13 @@ def _acc(grav, xm, G, eps2, **kw):
     return acc[:, :3].double().cpu().numpy(), solver
 
 
-def test_golden_direct_acc(cuda_dev):
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_golden_direct_acc(cuda_dev, variant):
+    """Every force-pass form against the reference's own accelerations."""
     _, grav, _ = _mods()
     g = load_golden("direct")
     xm = _xm(g["pos"], g["mass"], cuda_dev)
-    a, _ = _acc(grav, xm, float(g["G"]), float(g["eps2"]))
+    a, _ = _acc(grav, xm, float(g["G"]), float(g["eps2"]), tiles=(2, 8, 0, variant))
     rel = _rel(a, g["acc"])
     assert np.sqrt((rel ** 2).mean()) < RMS_TOL and rel.max() < MAX_TOL
 

@@ -191,3 +191,77 @@ def test_kdk_graph_recaptures_after_scratch_regrowth(cuda_dev):
         s.close()
     for u, w in zip(*out):
         assert torch.equal(u, w)
+
+
+BAND_5_PAIRS = 5 * 16 * 512 * 5  # slot bytes for 5 tile pairs with 4 source slices
+
+
+def test_bands_match_oracle_and_single_pass(cuda_dev, orc):
+    """A small band budget splits N = 5,000 into 9 bands of tile rows; the
+    result matches the oracle and the one-band pass up to rounding order."""
+    grav, ic = _mods()
+    n = 5000
+    pos, _, mass = ic.plummer(n, seed=31)
+    pos, mass = _f32(pos), _f32(mass)
+    xm = _xm(pos, mass, cuda_dev)
+    s1 = _sym_solver(grav, n, cuda_dev)
+    s2 = _sym_solver(grav, n, cuda_dev)
+    s2.set_sym_band(BAND_5_PAIRS)
+    a1, a2, a3 = (torch.zeros_like(xm) for _ in range(3))
+    s1.acc(xm, a1, 1.0, 1e-4)
+    s2.acc(xm, a2, 1.0, 1e-4)
+    s2.acc(xm, a3, 1.0, 1e-4)
+    torch.cuda.synchronize()
+    assert torch.equal(a2, a3)
+    assert s2.launch_count() > s1.launch_count()
+    ref = orc.direct_acc(pos, mass, 1.0, 1e-4)
+    rel = _rel(a2[:, :3].double().cpu().numpy(), ref)
+    assert np.sqrt((rel ** 2).mean()) < RMS_TOL and rel.max() < MAX_TOL, rel.max()
+    rel12 = _rel(a2[:, :3].double().cpu().numpy(), a1[:, :3].double().cpu().numpy())
+    assert rel12.max() < 1e-5
+    # acc += form in bands
+    a4 = torch.zeros_like(xm)
+    a4[:, 1] = 2.0
+    s2.acc(xm, a4, 1.0, 1e-4, accumulate=True)
+    ref[:, 1] += 2.0
+    assert _rel(a4[:, :3].double().cpu().numpy(), ref).max() < MAX_TOL
+    s1.close()
+    s2.close()
+
+
+def test_bands_kdk_graph_and_oracle(cuda_dev, orc):
+    grav, ic = _mods()
+    n = 3000
+    pos, vel, mass = ic.plummer(n, seed=32)
+    pos, vel, mass = _f32(pos), _f32(vel), _f32(mass)
+    out = []
+    for graph in (False, True):
+        xm = _xm(pos, mass, cuda_dev)
+        v4 = torch.zeros_like(xm)
+        v4[:, :3] = torch.tensor(vel, dtype=torch.float32, device=cuda_dev)
+        a4 = torch.zeros_like(xm)
+        s = _sym_solver(grav, n, cuda_dev)
+        s.set_sym_band(BAND_5_PAIRS)
+        s.acc(xm, a4, 1.0, 1e-4)
+        s.kdk(xm, v4, a4, 1.0, 1e-4, 1e-3, 4, graph=graph)
+        s.set_sym_band(1 << 30)  # one band from here: the graph is captured again
+        s.kdk(xm, v4, a4, 1.0, 1e-4, 1e-3, 2, graph=graph)
+        torch.cuda.synchronize()
+        out.append((xm.clone(), v4.clone(), a4.clone()))
+        s.close()
+    for u, w in zip(*out):
+        assert torch.equal(u, w)
+    a0 = orc.direct_acc(pos, mass, 1.0, 1e-4)
+    p, v, _ = orc.kdk_direct(pos, vel, a0, mass, 1.0, 1e-4, 1e-3, 6)
+    xm, v4, _ = out[0]
+    assert np.abs(xm[:, :3].double().cpu().numpy() - p).max() < 2e-5 * np.abs(p).max()
+    assert np.abs(v4[:, :3].double().cpu().numpy() - v).max() < 1e-4 * np.abs(v).max()
+
+
+def test_band_budget_validation(cuda_dev):
+    pkg = importlib.import_module(PKG_NAME)
+    grav, _ = _mods()
+    s = grav.DirectGravity(64, cuda_dev)
+    with pytest.raises(pkg.GravityError):
+        s.set_sym_band(1000)
+    s.close()
