@@ -272,12 +272,13 @@ int gb_adjoint_step(gb_direct_t *h, const float *xm, float *lx, float *lv,
 /* Pair evaluation of the adjoint:
  *   2 (default) every unordered pair once, applied to both particles, in
  *     packed FP32x2 arithmetic with CTAs taking tile-pair units from a
- *     counter (scratch about n^2 / 16 bytes, allocated on first use);
+ *     counter (8 KB slots per 512 x 512 tile pair, allocated on first use;
+ *     above the handle's band budget, gb_direct_set_sym_band, it runs in
+ *     bands of tile rows with 16 bytes per particle of running sums);
  *   1 every unordered pair once, scalar FP32, static runs per CTA (scratch
- *     about n^2 / 32 bytes);
+ *     about n^2 / 32 bytes; above 3 GiB of it the call runs form 0);
  *   0 each ordered pair, one pass per target (no extra scratch).
- * A symmetric form whose scratch would pass 3 GiB falls back to 0.  All
- * are deterministic; they differ by FP32 summation order. */
+ * All are deterministic; they differ by FP32 summation order. */
 int gb_adjoint_set_variant(gb_direct_t *h, int variant);
 
 /* ------------------------------------------------- allocation-free call */

@@ -368,10 +368,10 @@ struct Sym2Args {
     const float4 *__restrict__ xm;
     const float4 *__restrict__ lv;
     const float4 *__restrict__ la;
-    float4 *__restrict__ rowpart;  // NP * Q x SYM2_T
-    float4 *__restrict__ colpart;  // NP x SYM2_T
+    float4 *__restrict__ rowpart;  // NU x SYM2_T (one row slot per unit)
+    float4 *__restrict__ colpart;  // band pairs x SYM2_T
     unsigned long long *counter;   // zero at launch
-    int64_t n, nt, NP;
+    int64_t n, nt, NU, p0;         // units of the band, its first tile pair
     float eps2, h;
     int prime;
 };
@@ -460,7 +460,7 @@ __global__ void __launch_bounds__(SYM2_WARPS * 32, 4) adjoint_vjp_sym2_kernel(Sy
     __shared__ float4 sxm[SYM2_T], sw[SYM2_T], sacc[SYM2_T];
     __shared__ long long s_unit;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, tid = threadIdx.x;
-    const int64_t NU = a.NP * Q;
+    const int64_t NU = a.NU;
     const f2 EPS2 = pack2(a.eps2, a.eps2), NEG3 = pack2(-3.f, -3.f);
     for (;;) {
         __syncthreads();  // the previous unit is done with s_unit and shared memory
@@ -476,8 +476,9 @@ __global__ void __launch_bounds__(SYM2_WARPS * 32, 4) adjoint_vjp_sym2_kernel(Sy
         if (u >= NU) break;
         const int64_t p = u / Q;
         const int sl = (int)(u - p * Q);
-        const int64_t I = sym_row(p, a.nt);
-        const int64_t J = I + (p - sym_base(I, a.nt));
+        const int64_t pg = a.p0 + p;  // pair index in the triangle
+        const int64_t I = sym_row(pg, a.nt);
+        const int64_t J = I + (pg - sym_base(I, a.nt));
         diag = J == I;
         gbase = sl * G;
 #pragma unroll
@@ -547,28 +548,46 @@ struct Sym2Fix {
     const float4 *__restrict__ colpart;
     float4 *lx, *lv, *la;
     float *lm;
-    int64_t n, nt;
+    float4 *aux;  // running sums of particles past the band (one float4 each)
+    int64_t n, nt, Ib, Ie, p0;
     int Q;
     float G, h, dt;
     int prime;
 };
 
-// Adds particle i's slots in a fixed order: its row units (I, J, slice) for
-// J = I .. nt-1, then its column slots (I', I) for I' = 0 .. I; then applies
-// the elementwise part of the backward step.
+// Particle i (in tile T, at or after the band's first row Ib) adds, in a
+// fixed order: the running sum left by earlier bands, its row units
+// (T, J, slice) for J = T .. nt-1 when T is in the band, then its column
+// slots (I', T) for the band's rows I' <= T.  A particle of the band is
+// complete and gets the elementwise part of the backward step; one past the
+// band keeps its running sum in aux.  Later bands never read a finished
+// tile, so its adjoint state may change.  One band (Ib = 0, Ie = nt) is the
+// whole pass.
 __global__ void adjoint_sym2_fixup_kernel(Sym2Fix f) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t i = f.Ib * SYM2_T + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= f.n) return;
-    const int64_t I = i / SYM2_T, r = i - I * SYM2_T;
-    const int64_t u0 = sym_base(I, f.nt) * f.Q, u1 = (sym_base(I, f.nt) + (f.nt - I)) * f.Q;
+    const int64_t T = i / SYM2_T, r = i - T * SYM2_T;
+    const bool in_band = T < f.Ie;
     float gx = 0.f, gy = 0.f, gz = 0.f, gm = 0.f;
-    for (int64_t u = u0; u < u1; ++u) {
-        const float4 v = f.rowpart[u * SYM2_T + r];
+    if (f.Ib > 0) {
+        const float4 v = f.aux[i];
+        gx = v.x; gy = v.y; gz = v.z; gm = v.w;
+    }
+    if (in_band) {
+        const int64_t u0 = (sym_base(T, f.nt) - f.p0) * f.Q, u1 = u0 + (f.nt - T) * f.Q;
+        for (int64_t u = u0; u < u1; ++u) {
+            const float4 v = f.rowpart[u * SYM2_T + r];
+            gx += v.x; gy += v.y; gz += v.z; gm += v.w;
+        }
+    }
+    const int64_t last = in_band ? T : f.Ie - 1;
+    for (int64_t I2 = f.Ib; I2 <= last; ++I2) {
+        const float4 v = f.colpart[(sym_base(I2, f.nt) + (T - I2) - f.p0) * SYM2_T + r];
         gx += v.x; gy += v.y; gz += v.z; gm += v.w;
     }
-    for (int64_t I2 = 0; I2 <= I; ++I2) {
-        const float4 v = f.colpart[(sym_base(I2, f.nt) + (I - I2)) * SYM2_T + r];
-        gx += v.x; gy += v.y; gz += v.z; gm += v.w;
+    if (!in_band) {
+        f.aux[i] = make_float4(gx, gy, gz, gm);
+        return;
     }
     gx *= f.G; gy *= f.G; gz *= f.G; gm *= f.G;
     f.lm[i] += gm;
@@ -656,8 +675,13 @@ extern "C" int gb_adjoint_step(gb_direct_t *h, const float *xm, float *lx, float
         // small share of each CTA's work.
         int Q = 1;
         while (Q < 4 && NP * Q < 16 * slots) Q *= 2;
-        const int64_t NU = NP * Q, P = std::min(slots, NU);
-        const int64_t need = NU * SYM2_T + NP * SYM2_T + 1;  // + the unit counter
+        // Bands of tile rows within the handle's slot budget, as for the
+        // symmetric force pass.
+        std::vector<int64_t> rows;
+        const int64_t max_pairs =
+            sym_bands(nt, h->sym_band / ((int64_t)sizeof(float4) * SYM2_T * (Q + 1)), rows);
+        const int64_t aux = rows.size() > 2 ? n : 0;
+        const int64_t need = max_pairs * Q * SYM2_T + max_pairs * SYM2_T + aux + 1;  // + the unit counter
         if (need * (int64_t)sizeof(float4) <= SYM_MAX_BYTES) {
             GB_TRY(ensure_sym(h, need));
             Sym2Args a;
@@ -665,22 +689,17 @@ extern "C" int gb_adjoint_step(gb_direct_t *h, const float *xm, float *lx, float
             a.lv = (const float4 *)lv;
             a.la = (const float4 *)la;
             a.rowpart = h->sym;
-            a.colpart = h->sym + NU * SYM2_T;
+            a.colpart = h->sym + max_pairs * Q * SYM2_T;
             a.counter = (unsigned long long *)(h->sym + need - 1);
             a.n = n;
             a.nt = nt;
-            a.NP = NP;
             a.eps2 = eps2;
             a.h = 0.5f * dt;
             a.prime = prime ? 1 : 0;
-            GB_CUDA_TRY(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), s));
-            if (Q == 1) adjoint_vjp_sym2_kernel<1><<<(unsigned)P, SYM2_WARPS * 32, 0, s>>>(a);
-            else if (Q == 2) adjoint_vjp_sym2_kernel<2><<<(unsigned)P, SYM2_WARPS * 32, 0, s>>>(a);
-            else adjoint_vjp_sym2_kernel<4><<<(unsigned)P, SYM2_WARPS * 32, 0, s>>>(a);
-            GB_CUDA_TRY(cudaGetLastError());
             Sym2Fix f;
             f.rowpart = a.rowpart;
             f.colpart = a.colpart;
+            f.aux = a.colpart + max_pairs * SYM2_T;
             f.lx = (float4 *)lx;
             f.lv = (float4 *)lv;
             f.la = (float4 *)la;
@@ -692,9 +711,22 @@ extern "C" int gb_adjoint_step(gb_direct_t *h, const float *xm, float *lx, float
             f.h = 0.5f * dt;
             f.dt = dt;
             f.prime = a.prime;
-            adjoint_sym2_fixup_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(f);
-            GB_CUDA_TRY(cudaGetLastError());
-            h->launches += 2;
+            for (size_t b = 0; b + 1 < rows.size(); ++b) {
+                a.p0 = host_sym_base(rows[b], nt);
+                a.NU = (host_sym_base(rows[b + 1], nt) - a.p0) * Q;
+                f.Ib = rows[b];
+                f.Ie = rows[b + 1];
+                f.p0 = a.p0;
+                const unsigned P = (unsigned)std::min(slots, a.NU);
+                GB_CUDA_TRY(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), s));
+                if (Q == 1) adjoint_vjp_sym2_kernel<1><<<P, SYM2_WARPS * 32, 0, s>>>(a);
+                else if (Q == 2) adjoint_vjp_sym2_kernel<2><<<P, SYM2_WARPS * 32, 0, s>>>(a);
+                else adjoint_vjp_sym2_kernel<4><<<P, SYM2_WARPS * 32, 0, s>>>(a);
+                GB_CUDA_TRY(cudaGetLastError());
+                adjoint_sym2_fixup_kernel<<<(unsigned)((n - f.Ib * SYM2_T + 255) / 256), 256, 0, s>>>(f);
+                GB_CUDA_TRY(cudaGetLastError());
+                h->launches += 2;
+            }
             return GB_OK;
         }
     }

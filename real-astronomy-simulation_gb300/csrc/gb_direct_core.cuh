@@ -1,6 +1,9 @@
 // Building blocks shared by the single-system and batched direct-sum kernels.
 #pragma once
 
+#include <algorithm>
+#include <vector>
+
 #include "gb_common.cuh"
 
 namespace gb {
@@ -125,6 +128,26 @@ __device__ __forceinline__ void kdk_writeback(float4 *xm, float4 *vel, float4 *a
     vel[i] = make_float4(kick(vhx, an.x, h), kick(vhy, an.y, h), kick(vhz, an.z, h), v.w);
     acc[i] = an;
 }
+
+// Bands of tile rows for the tile-pair passes: band b covers rows
+// [rows[b], rows[b + 1]) and at most `budget` tile pairs (one row more when a
+// single row exceeds it).  Returns the largest band's pair count.
+static inline int64_t sym_bands(int64_t nt, int64_t budget, std::vector<int64_t> &rows) {
+    rows.assign(1, 0);
+    int64_t max_pairs = 0, pairs = 0;
+    for (int64_t I = 0; I < nt; ++I) {
+        if (pairs > 0 && pairs + (nt - I) > budget) {
+            rows.push_back(I);
+            max_pairs = std::max(max_pairs, pairs);
+            pairs = 0;
+        }
+        pairs += nt - I;
+    }
+    rows.push_back(nt);
+    return std::max(max_pairs, pairs);
+}
+
+static inline int64_t host_sym_base(int64_t I, int64_t nt) { return I * nt - I * (I - 1) / 2; }
 
 // Symmetric (tile-pair) scratch above this size is not used: the callers
 // fall back to their per-target forms.

@@ -356,8 +356,6 @@ int direct_sym_slices(int64_t pairs, int64_t slots) {
     return Q;
 }
 
-static int64_t host_sym_base(int64_t I, int64_t nt) { return I * nt - I * (I - 1) / 2; }
-
 struct DsPlan {
     int64_t nt, NP, slots, max_pairs, need;  // need: float4s of scratch
     int Q;
@@ -373,19 +371,7 @@ static DsPlan ds_plan(const gb_direct *h, int64_t n) {
     // Tile pairs per band: the handle's slot budget (larger systems run in
     // bands of tile rows, so the scratch stays bounded at any N).
     const int64_t budget = h->sym_band / ((int64_t)sizeof(float4) * DS_T * (p.Q + 1));
-    p.rows.assign(1, 0);
-    p.max_pairs = 0;
-    int64_t pairs = 0;
-    for (int64_t I = 0; I < p.nt; ++I) {
-        if (pairs > 0 && pairs + (p.nt - I) > budget) {
-            p.rows.push_back(I);
-            p.max_pairs = std::max(p.max_pairs, pairs);
-            pairs = 0;
-        }
-        pairs += p.nt - I;
-    }
-    p.rows.push_back(p.nt);
-    p.max_pairs = std::max(p.max_pairs, pairs);
+    p.max_pairs = sym_bands(p.nt, budget, p.rows);
     // Row slots, column slots, the running sums between bands, the counter.
     const int64_t aux = p.rows.size() > 2 ? 2 * n : 0;
     p.need = p.max_pairs * p.Q * DS_T + p.max_pairs * DS_T + aux + 1;
