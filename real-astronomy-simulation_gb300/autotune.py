@@ -14,6 +14,7 @@ import time
 import torch
 
 from . import _buildlib
+from ._lib import GravityError
 
 CACHE = os.path.join(_buildlib.BUILD, "autotune.json")
 # (k, warps, variant); the symmetric variant 2 has one tile shape of its own.
@@ -94,7 +95,10 @@ def tune_batch(batch, dt=1e-3, reps=2, use_cache=True):
     times = {}
     for k, w, v in BATCH_SHAPES:
         batch.set_tiles(k, w)
-        batch.set_variant(v)
+        try:
+            batch.set_variant(v)
+        except GravityError:  # the symmetric pass's scratch would be too large
+            continue
         times[f"{k},{w},{v}"] = _time(lambda: batch.run(dt, 1, graph=False), reps)
         batch.restore(saved)
     best = min(times, key=times.get)

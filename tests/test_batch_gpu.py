@@ -190,3 +190,20 @@ def test_batch_bad_variant(cuda_dev):
     with pytest.raises(pkg.GravityError):
         b.set_variant(2)
     b.close()
+
+
+def test_batch_sym_scratch_limit_is_an_error_and_autotune_skips_it(cuda_dev):
+    """One 400k-particle system needs about 5 GB of tile-pair slots: selecting
+    the symmetric batch pass fails cleanly and the per-target pass stays."""
+    batch, ic, tune = _mods()
+    pkg = importlib.import_module(PKG_NAME)
+    p, v, m = ic.plummer(400_000, seed=5)
+    b = batch.DirectBatch([(p, v, m)], G=1.0, softening=0.02, device=cuda_dev)
+    with pytest.raises(pkg.GravityError):
+        b.set_variant(1)
+    b.run(1e-3, 1, graph=False)  # still the per-target pass
+    torch.cuda.synchronize()
+    assert torch.isfinite(b.xm).all()
+    shape, times = tune.tune_batch(b, reps=1, use_cache=False)
+    assert shape[2] == 0 and "2,4,1" not in times
+    b.close()
