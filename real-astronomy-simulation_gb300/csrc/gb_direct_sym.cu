@@ -123,6 +123,7 @@ __global__ void __launch_bounds__(DS_WARPS * 32, DS_MIN_CTAS) direct_sym_kernel(
     // The unit and, for a batch, its system's offset, size, local unit and
     // column-slot base (decoded once by thread 0).
     __shared__ long long s_unit, s_off, s_n, s_local, s_cb;
+    __shared__ int s_gend, s_ntgt;  // source groups and targets of the unit that hold particles
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, tid = threadIdx.x;
     const f2 EPS2 = pack2(a.eps2, a.eps2);
     for (;;) {
@@ -157,6 +158,14 @@ __global__ void __launch_bounds__(DS_WARPS * 32, DS_MIN_CTAS) direct_sym_kernel(
             const int64_t J = I + (pg - sym_base(I, nt));
             diag = J == I;
             gbase = sl * G;
+            // Padding of the system's last tile: source groups past the last
+            // particle, and warps whose 128 targets are all past it, hold
+            // zero-mass records only; their rounds would add exact zeros.
+            // The bounds live in shared memory, not in registers.
+            if (tid == 0) {
+                s_gend = (int)((min(n_s - J * DS_T, (int64_t)DS_T) + 31) / 32);
+                s_ntgt = (int)min(n_s - I * DS_T, (int64_t)DS_T);
+            }
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 const float4 x0 = ds_load<MODE>(a, o, n_s, I * DS_T + 128 * wib + 64 * h + lane);
@@ -179,10 +188,12 @@ __global__ void __launch_bounds__(DS_WARPS * 32, DS_MIN_CTAS) direct_sym_kernel(
             // Diagonal tile: targets 128 w .. 128 w + 127 against sources
             // 32 g .. 32 g + 31; no pair has t < s when 4 w > g.
             // Warp-uniform branches; every warp still reaches the barrier.
-            if (!diag)
-                ds_round<false>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX, NY, NZ);
-            else if (4 * wib <= g)
-                ds_round<true>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX, NY, NZ);
+            if (128 * wib < s_ntgt && g < s_gend) {
+                if (!diag)
+                    ds_round<false>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX, NY, NZ);
+                else if (4 * wib <= g)
+                    ds_round<true>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX, NY, NZ);
+            }
             __syncthreads();
         }
         const int64_t u = s_unit;
