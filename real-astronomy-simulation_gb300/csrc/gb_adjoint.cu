@@ -459,6 +459,7 @@ __global__ void __launch_bounds__(SYM2_WARPS * 32, 4) adjoint_vjp_sym2_kernel(Sy
     constexpr int G = 16 / Q, SPAN = G * 32;
     __shared__ float4 sxm[SYM2_T], sw[SYM2_T], sacc[SYM2_T];
     __shared__ long long s_unit;
+    __shared__ int s_gend, s_ntgt;  // source groups and targets of the unit that hold particles
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, tid = threadIdx.x;
     const int64_t NU = a.NU;
     const f2 EPS2 = pack2(a.eps2, a.eps2), NEG3 = pack2(-3.f, -3.f);
@@ -481,6 +482,12 @@ __global__ void __launch_bounds__(SYM2_WARPS * 32, 4) adjoint_vjp_sym2_kernel(Sy
         const int64_t J = I + (pg - sym_base(I, a.nt));
         diag = J == I;
         gbase = sl * G;
+        // Padding of the last tile (zero mass and zero w) adds exact zeros:
+        // its source groups and all-padding target warps are skipped.
+        if (tid == 0) {
+            s_gend = (int)((min(a.n - J * SYM2_T, (int64_t)SYM2_T) + 31) / 32);
+            s_ntgt = (int)min(a.n - I * SYM2_T, (int64_t)SYM2_T);
+        }
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             float4 x[2], w[2];
@@ -514,12 +521,14 @@ __global__ void __launch_bounds__(SYM2_WARPS * 32, 4) adjoint_vjp_sym2_kernel(Sy
             // Diagonal tile: targets 128 w .. 128 w + 127 against sources
             // 32 g .. 32 g + 31; no pair has t < s when 4 w > g.
             // Warp-uniform branches; every warp still reaches the barrier.
-            if (!diag)
-                sym2_round<false>(sxm, sw, sacc, g, lane, wib, EPS2, NEG3, TX, TY, TZ, TNM, TWX, TWY, TWZ, NX, NY,
-                                  NZ, NG);
-            else if (4 * wib <= g)
-                sym2_round<true>(sxm, sw, sacc, g, lane, wib, EPS2, NEG3, TX, TY, TZ, TNM, TWX, TWY, TWZ, NX, NY,
-                                 NZ, NG);
+            if (128 * wib < s_ntgt && g < s_gend) {
+                if (!diag)
+                    sym2_round<false>(sxm, sw, sacc, g, lane, wib, EPS2, NEG3, TX, TY, TZ, TNM, TWX, TWY, TWZ, NX,
+                                      NY, NZ, NG);
+                else if (4 * wib <= g)
+                    sym2_round<true>(sxm, sw, sacc, g, lane, wib, EPS2, NEG3, TX, TY, TZ, TNM, TWX, TWY, TWZ, NX,
+                                     NY, NZ, NG);
+            }
             __syncthreads();
         }
         const int64_t u = s_unit;
