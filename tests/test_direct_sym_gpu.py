@@ -64,7 +64,8 @@ def test_plummer_20k_matches_oracle(cuda_dev, orc, plain):
 
 @pytest.mark.parametrize("n", [1, 2, 3, 33, 511, 512, 513, 1025, 4099, 9000])
 def test_ragged_sizes(cuda_dev, orc, n):
-    """Ragged last tiles, one tile, and the three source-slice counts."""
+    """Ragged last tiles and one tile (all with 4 source slices per tile
+    pair)."""
     grav, ic = _mods()
     pos, _, mass = ic.plummer(max(n, 2), seed=n)
     pos, mass = _f32(pos[:n]), _f32(mass[:n])
@@ -79,6 +80,24 @@ def test_ragged_sizes(cuda_dev, orc, n):
         return
     ref = orc.direct_acc(pos, mass, 2.5, 0.05 ** 2)
     assert _rel(a, ref).max() < MAX_TOL
+    s.close()
+
+
+@pytest.mark.parametrize("n", [70001, 90001])
+def test_fewer_source_slices_match_oracle(cuda_dev, orc, n):
+    """2 source slices per tile pair at N = 70,001 and 1 at N = 90,001 on a
+    152-SM GB300 (the slice count falls as the tile pairs outnumber 16x the
+    resident CTAs), on 2,048 sampled targets."""
+    grav, ic = _mods()
+    pos, _, mass = ic.plummer(n, seed=41)
+    pos, mass = _f32(pos), _f32(mass)
+    xm = _xm(pos, mass, cuda_dev)
+    s = _sym_solver(grav, n, cuda_dev)
+    acc = torch.zeros_like(xm)
+    s.acc(xm, acc, 1.0, 1e-4)
+    targets = np.random.default_rng(2).choice(n, 2048, replace=False)
+    rel = _rel(acc[:, :3].double().cpu().numpy()[targets], orc.direct_acc(pos, mass, 1.0, 1e-4, targets))
+    assert np.sqrt((rel ** 2).mean()) < RMS_TOL and rel.max() < MAX_TOL, rel.max()
     s.close()
 
 
