@@ -193,6 +193,16 @@ class Engine:
         with torch.cuda.device(self.device):
             return self._direct.energies(self.xm, self.v4, self.G, self.eps2)
 
+    def diagnostics(self) -> dict:
+        """The energy / virial record a simulation controller shows
+        (core/sim_controller.py:288-293 builds it from energies() for an
+        engine without its own diagnostics): kinetic, potential, thermal (0:
+        no gas here), total and the virial ratio 2 KE / |PE| (0 when PE is
+        0)."""
+        ke, pe, tot = self.energies()
+        return dict(kinetic=ke, potential=pe, thermal=0.0, total=tot,
+                    virial=(2.0 * ke / abs(pe) if pe else 0.0))
+
     def diag(self) -> dict:
         d = self._direct.diag() if self._direct is not None else {}
         if self._bh is not None:

@@ -222,3 +222,19 @@ def test_kdk_graph_replay_matches_direct_launches(cuda_dev):
         s.close()
     for u, w in zip(*out):
         assert torch.equal(u, w)
+
+
+def test_engine_diagnostics_virial_plummer(cuda_dev):
+    """diagnostics(): the energy/virial record of a simulation controller
+    (core/sim_controller.py:288-293).  A Plummer sphere in equilibrium has
+    2 KE / |PE| near 1; the reference's own check accepts (0.8, 1.2)
+    (verify_phase1.py:30-51)."""
+    pkg, _, ic = _mods()
+    pos, vel, mass = ic.plummer(3000, seed=42)
+    eng = pkg.Engine(softening=0.05, G=1.0, device=cuda_dev)
+    eng.load_state(pkg.State.from_arrays(pos, vel, mass))
+    d = eng.diagnostics()
+    ke, pe, tot = eng.energies()
+    assert d["kinetic"] == ke and d["potential"] == pe and d["total"] == tot and d["thermal"] == 0.0
+    assert d["virial"] == pytest.approx(2.0 * ke / abs(pe), rel=1e-12)
+    assert 0.8 < d["virial"] < 1.2
