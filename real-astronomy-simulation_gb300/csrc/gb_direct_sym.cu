@@ -21,6 +21,11 @@
 // the closing kick and writes x', v', a').  In the fused KDK form both sides
 // load the leapfrog prediction x' = x + (v + a dt/2) dt with the same FMAs as
 // the per-target kernel, so the two forms see identical positions.
+//
+// A system whose slots pass the handle's band budget runs in bands of tile
+// rows (one kernel and one fix-up per band, running sums in between); the
+// BATCH form runs the tile pairs of many systems in one launch.  Rounds over
+// a system's last-tile padding (zero-mass records) are skipped.
 #include <algorithm>
 #include <vector>
 
