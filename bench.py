@@ -71,6 +71,18 @@ def _profiled_traffic(summary: str):
     return int(m.group(1)) if m else None
 
 
+def _profiled_metric(summary: str, metric: str):
+    """One metric's value from the table of the ncu summary in
+    profiles/<summary>; None when absent."""
+    try:
+        with open(os.path.join(ROOT, "profiles", summary)) as f:
+            txt = f.read()
+    except OSError:
+        return None
+    m = re.search(r"`" + re.escape(metric) + r"`\s*\|\s*([0-9.]+)", txt)
+    return float(m.group(1)) if m else None
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle sampling during the timed region."""
 
@@ -264,6 +276,16 @@ def bench_bh(args, dev, rank, world, dist):
         res["roofline"]["traffic"] = traffic
         res["roofline"]["traffic_source"] = ("ncu dram bytes of one launch on this workload "
                                              "(profiles/bh_traverse_1M_disk.md)")
+        # The kernel's actual limit is instruction issue, not HBM: the same
+        # capture's issue-slot and pipe utilisation.
+        res["roofline"]["observed_limit"] = {
+            "issue_active_pct": _profiled_metric("bh_traverse_1M_disk.md",
+                                                 "smsp__issue_active.avg.pct_of_peak_sustained_active"),
+            "alu_pipe_pct": _profiled_metric("bh_traverse_1M_disk.md",
+                                             "sm__pipe_alu_cycles_active.avg.pct_of_peak_sustained_active"),
+            "fma_pipe_pct": _profiled_metric("bh_traverse_1M_disk.md",
+                                             "sm__pipe_fma_cycles_active.avg.pct_of_peak_sustained_active"),
+            "source": "ncu --set full capture of one launch (profiles/bh_traverse_1M_disk.md)"}
     # The same launch seen as FP32 work: 20 flop per monopole term, 10 per
     # acceptance test.
     flops = 20 * per_step["lane_interactions"] + 10 * per_step["lane_tests"]
