@@ -220,8 +220,9 @@ static int batch_sym_plan(gb_batch_t *h) {
         const int64_t n = h->off[s + 1] - h->off[s], nt = (n + SYM_TILE - 1) / SYM_TILE;
         pairs += nt * (nt + 1) / 2;
     }
-    const int64_t slots = direct_sym_slots(h->sms);
-    const int Q = direct_sym_slices(pairs, slots);
+    const SymShape sh = direct_sym_shape(h->sms, pairs);
+    const int64_t slots = sh.slots;
+    const int Q = sh.Q;
     for (int s = 0; s < ns; ++s) {
         const int64_t n = h->off[s + 1] - h->off[s], nt = (n + SYM_TILE - 1) / SYM_TILE;
         ub[s + 1] = ub[s] + nt * (nt + 1) / 2 * Q;
@@ -263,6 +264,7 @@ static int batch_sym_plan(gb_batch_t *h) {
     b.fsys = h->d_fsys;
     b.nsys = ns;
     b.Q = Q;
+    b.H = sh.H;
     b.NU = NU;
     b.NPtot = pairs;
     b.nfb = fb[ns];

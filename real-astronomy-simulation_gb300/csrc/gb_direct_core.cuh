@@ -229,14 +229,19 @@ constexpr int SYM_TILE = 512;
 struct SymBatch {
     const int64_t *off, *ubase, *cbase, *fbase;
     const int *fsys;
-    int nsys, Q;
+    int nsys, Q, H;
     int64_t NU, NPtot, nfb, P;
     float4 *scratch;
 };
-// Resident CTAs of the symmetric kernel on a device with sms SMs, and the
-// source slices per tile pair for a pass of the given tile-pair count.
-int direct_sym_slots(int sms);
+// Source slices per tile pair for a pass of the given tile-pair count over
+// `slots` resident CTAs, and the symmetric force kernel's shape (packed
+// target pairs per lane H, resident CTAs, slices) for such a pass.
 int direct_sym_slices(int64_t pairs, int64_t slots);
+struct SymShape {
+    int H, Q;
+    int64_t slots;
+};
+SymShape direct_sym_shape(int sms, int64_t pairs);
 int run_batch_sym(const SymBatch &b, int mode, const float4 *xm, float4 *vel, float4 *acc, float G, float eps2,
                   float dt, int flags, cudaStream_t s);
 

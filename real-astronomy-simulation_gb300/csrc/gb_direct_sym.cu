@@ -33,17 +33,25 @@
 
 namespace gb {
 
-#ifndef DS_MIN_CTAS
-#define DS_MIN_CTAS 6  // minimum resident CTAs per SM (register budget)
-#endif
 #ifndef DS_UNROLL
 #define DS_UNROLL 4
 #endif
 
 constexpr int DS_T = SYM_TILE;
 constexpr int DS_K_UNROLL = DS_UNROLL;
-constexpr int DS_WARPS = 4;
 constexpr int DS_ACC = 0, DS_KDK = 1;
+
+// CTA shape for H packed target pairs per lane (2H targets): 8/H warps
+// cover one tile of 512 targets.  H = 4 halves the per-source overhead
+// (staging, the shared-memory sum, its 6 scalar adds) per pair but doubles a
+// unit's length, so it is used once there are enough units to keep the CTAs
+// evenly busy; resident-CTA floors give 80 (H = 2) and 128 (H = 4)
+// registers without spills.
+template <int H>
+struct DsShape {
+    static constexpr int WARPS = 8 / H, WT = 64 * H, MIN_CTAS = H == 4 ? 8 : 6;
+    static_assert(WARPS * WT == DS_T, "a CTA's warps cover one tile");
+};
 
 struct DsArgs {
     const float4 *__restrict__ xm;
@@ -72,12 +80,12 @@ __device__ __forceinline__ float4 ds_load(const DsArgs &a, int64_t o, int64_t n_
 }
 
 // One round: lane l at step k takes source jj = 32 g + (l + k) mod 32 of the
-// staged tile against its 4 targets.  DIAG zeroes the pairs with target
+// staged tile against its 2H targets.  DIAG zeroes the pairs with target
 // index >= source index (diagonal tile).
-template <bool DIAG>
+template <bool DIAG, int H>
 __device__ __forceinline__ void ds_round(const float4 *__restrict__ sxm, float4 *sacc, int g, int lane, int wib,
-                                         f2 EPS2, const f2 (&TX)[2], const f2 (&TY)[2], const f2 (&TZ)[2],
-                                         const f2 (&TM)[2], f2 (&NX)[2], f2 (&NY)[2], f2 (&NZ)[2]) {
+                                         f2 EPS2, const f2 (&TX)[H], const f2 (&TY)[H], const f2 (&TZ)[H],
+                                         const f2 (&TM)[H], f2 (&NX)[H], f2 (&NY)[H], f2 (&NZ)[H]) {
 #pragma unroll DS_K_UNROLL
     for (int k = 0; k < 32; ++k) {
         const int jj = g * 32 + ((lane + k) & 31);
@@ -86,7 +94,7 @@ __device__ __forceinline__ void ds_round(const float4 *__restrict__ sxm, float4 
         const f2 sm = pack2(xs.w, xs.w);
         f2 PX = 0ull, PY = 0ull, PZ = 0ull;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
+        for (int h = 0; h < H; ++h) {
             const f2 dx = sub2(sx, TX[h]), dy = sub2(sy, TY[h]), dz = sub2(sz, TZ[h]);
             const f2 r2 = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, EPS2)));
             const f2 inv = rsqrt2(r2);
@@ -94,7 +102,7 @@ __device__ __forceinline__ void ds_round(const float4 *__restrict__ sxm, float4 
             if (DIAG) {
                 float c0, c1;
                 unpack2(c, c0, c1);
-                const int t0 = 128 * wib + 64 * h + lane;
+                const int t0 = DsShape<H>::WT * wib + 64 * h + lane;
                 c0 = t0 < jj ? c0 : 0.f;
                 c1 = t0 + 32 < jj ? c1 : 0.f;
                 c = pack2(c0, c1);
@@ -121,9 +129,11 @@ __device__ __forceinline__ void ds_round(const float4 *__restrict__ sxm, float4 
     }
 }
 
-template <int Q, int MODE, bool BATCH>
-__global__ void __launch_bounds__(DS_WARPS * 32, DS_MIN_CTAS) direct_sym_kernel(DsArgs a) {
+template <int Q, int MODE, bool BATCH, int H>
+__global__ void __launch_bounds__(DsShape<H>::WARPS * 32, DsShape<H>::MIN_CTAS) direct_sym_kernel(DsArgs a) {
     constexpr int G = 16 / Q, SPAN = G * 32;
+    constexpr int WARPS = DsShape<H>::WARPS, WT = DsShape<H>::WT;
+    static_assert(G >= WARPS, "each warp of a round takes its own source group");
     __shared__ float4 sxm[DS_T], sacc[DS_T];
     // The unit and, for a batch, its system's offset, size, local unit and
     // column-slot base (decoded once by thread 0).
@@ -145,7 +155,7 @@ __global__ void __launch_bounds__(DS_WARPS * 32, DS_MIN_CTAS) direct_sym_kernel(
             }
         }
         __syncthreads();
-        f2 TX[2], TY[2], TZ[2], TM[2], NX[2], NY[2], NZ[2];
+        f2 TX[H], TY[H], TZ[H], TM[H], NX[H], NY[H], NZ[H];
         bool diag;
         int gbase;
         {
@@ -172,16 +182,16 @@ __global__ void __launch_bounds__(DS_WARPS * 32, DS_MIN_CTAS) direct_sym_kernel(
                 s_ntgt = (int)min(n_s - I * DS_T, (int64_t)DS_T);
             }
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const float4 x0 = ds_load<MODE>(a, o, n_s, I * DS_T + 128 * wib + 64 * h + lane);
-                const float4 x1 = ds_load<MODE>(a, o, n_s, I * DS_T + 128 * wib + 64 * h + 32 + lane);
+            for (int h = 0; h < H; ++h) {
+                const float4 x0 = ds_load<MODE>(a, o, n_s, I * DS_T + WT * wib + 64 * h + lane);
+                const float4 x1 = ds_load<MODE>(a, o, n_s, I * DS_T + WT * wib + 64 * h + 32 + lane);
                 TX[h] = pack2(x0.x, x1.x);
                 TY[h] = pack2(x0.y, x1.y);
                 TZ[h] = pack2(x0.z, x1.z);
                 TM[h] = pack2(x0.w, x1.w);
                 NX[h] = NY[h] = NZ[h] = 0ull;
             }
-            for (int t = tid; t < SPAN; t += DS_WARPS * 32) {
+            for (int t = tid; t < SPAN; t += WARPS * 32) {
                 const int tt = sl * SPAN + t;
                 sxm[tt] = ds_load<MODE>(a, o, n_s, J * DS_T + tt);
                 sacc[tt] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -189,17 +199,17 @@ __global__ void __launch_bounds__(DS_WARPS * 32, DS_MIN_CTAS) direct_sym_kernel(
         }
         __syncthreads();
         for (int r = 0; r < G; ++r) {
-            const int g = gbase + (((G / 4) * wib + r) & (G - 1));
-            // Diagonal tile: targets 128 w .. 128 w + 127 against sources
-            // 32 g .. 32 g + 31; no pair has t < s when 4 w > g.  (Taking
-            // the unmasked round for g >= 4 w + 4, where every pair has
-            // t < s, measured 2.5% slower on the 512-system batch.)
+            const int g = gbase + (((G / WARPS) * wib + r) & (G - 1));
+            // Diagonal tile: targets WT w .. WT w + WT - 1 against sources
+            // 32 g .. 32 g + 31; no pair has t < s when (WT / 32) w > g.
+            // (Taking the unmasked round where every pair of the group has
+            // t < s measured 2.5% slower on the 512-system batch.)
             // Warp-uniform branches; every warp still reaches the barrier.
-            if (128 * wib < s_ntgt && g < s_gend) {
+            if (WT * wib < s_ntgt && g < s_gend) {
                 if (!diag)
-                    ds_round<false>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX, NY, NZ);
-                else if (4 * wib <= g)
-                    ds_round<true>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX, NY, NZ);
+                    ds_round<false, H>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX, NY, NZ);
+                else if ((WT / 32) * wib <= g)
+                    ds_round<true, H>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX, NY, NZ);
             }
             __syncthreads();
         }
@@ -208,17 +218,17 @@ __global__ void __launch_bounds__(DS_WARPS * 32, DS_MIN_CTAS) direct_sym_kernel(
         const int64_t p = lu / Q;
         const int sl = (int)(lu - p * Q);
         const int64_t col = (BATCH ? s_cb : 0) + p;
-        for (int t = tid; t < SPAN; t += DS_WARPS * 32) {
+        for (int t = tid; t < SPAN; t += WARPS * 32) {
             const int tt = sl * SPAN + t;
             a.colpart[col * DS_T + tt] = sacc[tt];
         }
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
+        for (int h = 0; h < H; ++h) {
             float x0, x1, y0, y1, z0, z1;
             unpack2(NX[h], x0, x1);
             unpack2(NY[h], y0, y1);
             unpack2(NZ[h], z0, z1);
-            float4 *row = a.rowpart + u * DS_T + 128 * wib + 64 * h + lane;
+            float4 *row = a.rowpart + u * DS_T + WT * wib + 64 * h + lane;
             row[0] = make_float4(x0, y0, z0, 0.f);
             row[32] = make_float4(x1, y1, z1, 0.f);
         }
@@ -341,16 +351,23 @@ __global__ void __launch_bounds__(DS_FIX_WARPS * 32) direct_sym_fixup_kernel(DsF
     kdk_writeback(f.xm, f.vel, f.acc, i, an, f.h, f.dt);
 }
 
+template <bool BATCH, int H>
+static void launch_force(int Q, bool kdk, unsigned grid, const DsArgs &a, cudaStream_t s) {
+    const unsigned b = DsShape<H>::WARPS * 32;
+    if (Q == 1) kdk ? direct_sym_kernel<1, DS_KDK, BATCH, H><<<grid, b, 0, s>>>(a)
+                    : direct_sym_kernel<1, DS_ACC, BATCH, H><<<grid, b, 0, s>>>(a);
+    else if (Q == 2) kdk ? direct_sym_kernel<2, DS_KDK, BATCH, H><<<grid, b, 0, s>>>(a)
+                         : direct_sym_kernel<2, DS_ACC, BATCH, H><<<grid, b, 0, s>>>(a);
+    else kdk ? direct_sym_kernel<4, DS_KDK, BATCH, H><<<grid, b, 0, s>>>(a)
+             : direct_sym_kernel<4, DS_ACC, BATCH, H><<<grid, b, 0, s>>>(a);
+}
+
 template <bool BATCH>
-static void launch_pass(int Q, bool kdk, bool kahan, unsigned grid, unsigned fgrid, const DsArgs &a,
+static void launch_pass(int H, int Q, bool kdk, bool kahan, unsigned grid, unsigned fgrid, const DsArgs &a,
                         const DsFix &f, cudaStream_t s) {
-    const unsigned b = DS_WARPS * 32, fb = DS_FIX_WARPS * 32;
-    if (Q == 1) kdk ? direct_sym_kernel<1, DS_KDK, BATCH><<<grid, b, 0, s>>>(a)
-                    : direct_sym_kernel<1, DS_ACC, BATCH><<<grid, b, 0, s>>>(a);
-    else if (Q == 2) kdk ? direct_sym_kernel<2, DS_KDK, BATCH><<<grid, b, 0, s>>>(a)
-                         : direct_sym_kernel<2, DS_ACC, BATCH><<<grid, b, 0, s>>>(a);
-    else kdk ? direct_sym_kernel<4, DS_KDK, BATCH><<<grid, b, 0, s>>>(a)
-             : direct_sym_kernel<4, DS_ACC, BATCH><<<grid, b, 0, s>>>(a);
+    const unsigned fb = DS_FIX_WARPS * 32;
+    if (H == 4) launch_force<BATCH, 4>(Q, kdk, grid, a, s);
+    else launch_force<BATCH, 2>(Q, kdk, grid, a, s);
     if (kdk) {
         if (kahan) direct_sym_fixup_kernel<DS_KDK, true, BATCH><<<fgrid, fb, 0, s>>>(f);
         else direct_sym_fixup_kernel<DS_KDK, false, BATCH><<<fgrid, fb, 0, s>>>(f);
@@ -360,10 +377,28 @@ static void launch_pass(int Q, bool kdk, bool kahan, unsigned grid, unsigned fgr
     }
 }
 
-int direct_sym_slots(int sms) {
+static int sym_slots(int sms, int H) {
     int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, direct_sym_kernel<1, DS_ACC, false>, DS_WARPS * 32, 0);
+    if (H == 4)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, direct_sym_kernel<1, DS_ACC, false, 4>,
+                                                      DsShape<4>::WARPS * 32, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, direct_sym_kernel<1, DS_ACC, false, 2>,
+                                                      DsShape<2>::WARPS * 32, 0);
     return sms * std::max(occ, 1);
+}
+
+SymShape direct_sym_shape(int sms, int64_t pairs) {
+    // The 8-targets-per-lane shape once every CTA gets 8 units or more.
+    SymShape sh;
+    sh.H = 4;
+    sh.slots = sym_slots(sms, 4);
+    sh.Q = direct_sym_slices(pairs, sh.slots);
+    if (pairs * sh.Q >= 8 * sh.slots) return sh;
+    sh.H = 2;
+    sh.slots = sym_slots(sms, 2);
+    sh.Q = direct_sym_slices(pairs, sh.slots);
+    return sh;
 }
 
 int direct_sym_slices(int64_t pairs, int64_t slots) {
@@ -376,7 +411,7 @@ int direct_sym_slices(int64_t pairs, int64_t slots) {
 
 struct DsPlan {
     int64_t nt, NP, slots, max_pairs, need;  // need: float4s of scratch
-    int Q;
+    int Q, H;
     std::vector<int64_t> rows;  // band b covers tile rows [rows[b], rows[b + 1])
 };
 
@@ -384,8 +419,10 @@ static DsPlan ds_plan(const gb_direct *h, int64_t n) {
     DsPlan p;
     p.nt = (n + DS_T - 1) / DS_T;
     p.NP = p.nt * (p.nt + 1) / 2;
-    p.slots = direct_sym_slots(h->sms);
-    p.Q = direct_sym_slices(p.NP, p.slots);
+    const SymShape sh = direct_sym_shape(h->sms, p.NP);
+    p.H = sh.H;
+    p.slots = sh.slots;
+    p.Q = sh.Q;
     // Tile pairs per band: the handle's slot budget (larger systems run in
     // bands of tile rows, so the scratch stays bounded at any N).
     const int64_t budget = h->sym_band / ((int64_t)sizeof(float4) * DS_T * (p.Q + 1));
@@ -444,7 +481,7 @@ int run_direct_sym(gb_direct *h, int mode, const float4 *xm, float4 *vel, float4
         f.Ie = Ie;
         f.p0 = a.p0;
         GB_CUDA_TRY(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), s));
-        launch_pass<false>(pl.Q, kdk, kahan, (unsigned)std::min(pl.slots, a.NU),
+        launch_pass<false>(pl.H, pl.Q, kdk, kahan, (unsigned)std::min(pl.slots, a.NU),
                            (unsigned)((n - Ib * DS_T + 31) / 32), a, f, s);
         GB_CUDA_TRY(cudaGetLastError());
         h->launches += 2;
@@ -488,7 +525,8 @@ int run_batch_sym(const SymBatch &b, int mode, const float4 *xm, float4 *vel, fl
     f.dt = dt;
     f.accumulate = (flags & GB_ACCUMULATE) ? 1 : 0;
     GB_CUDA_TRY(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), s));
-    launch_pass<true>(b.Q, mode == DS_KDK, !(flags & GB_PLAIN_FP32), (unsigned)b.P, (unsigned)b.nfb, a, f, s);
+    launch_pass<true>(b.H, b.Q, mode == DS_KDK, !(flags & GB_PLAIN_FP32), (unsigned)b.P, (unsigned)b.nfb, a, f,
+                      s);
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
 }
