@@ -680,7 +680,7 @@ extern "C" int gb_adjoint_step(gb_direct_t *h, const float *xm, float *lx, float
         int occs = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occs, adjoint_vjp_sym2_kernel<1>, SYM2_WARPS * 32, 0);
         const int64_t slots = (int64_t)h->sms * std::max(occs, 1);
-        const int Q = direct_sym_slices(NP, slots);
+        const int Q = direct_sym_slices(NP, slots, 16 / SYM2_WARPS);
         // Bands of tile rows within the handle's slot budget, as for the
         // symmetric force pass.
         std::vector<int64_t> rows;

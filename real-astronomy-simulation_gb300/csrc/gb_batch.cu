@@ -264,7 +264,6 @@ static int batch_sym_plan(gb_batch_t *h) {
     b.fsys = h->d_fsys;
     b.nsys = ns;
     b.Q = Q;
-    b.H = sh.H;
     b.NU = NU;
     b.NPtot = pairs;
     b.nfb = fb[ns];

@@ -229,16 +229,16 @@ constexpr int SYM_TILE = 512;
 struct SymBatch {
     const int64_t *off, *ubase, *cbase, *fbase;
     const int *fsys;
-    int nsys, Q, H;
+    int nsys, Q;
     int64_t NU, NPtot, nfb, P;
     float4 *scratch;
 };
-// Source slices per tile pair for a pass of the given tile-pair count over
-// `slots` resident CTAs, and the symmetric force kernel's shape (packed
-// target pairs per lane H, resident CTAs, slices) for such a pass.
-int direct_sym_slices(int64_t pairs, int64_t slots);
+// Source slices per tile pair (at most qmax) for a pass of the given
+// tile-pair count over `slots` resident CTAs, and the symmetric force
+// kernel's resident CTAs and slices for such a pass.
+int direct_sym_slices(int64_t pairs, int64_t slots, int qmax);
 struct SymShape {
-    int H, Q;
+    int Q;
     int64_t slots;
 };
 SymShape direct_sym_shape(int sms, int64_t pairs);

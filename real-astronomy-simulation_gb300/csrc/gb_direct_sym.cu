@@ -42,16 +42,18 @@ constexpr int DS_K_UNROLL = DS_UNROLL;
 constexpr int DS_ACC = 0, DS_KDK = 1;
 
 // CTA shape for H packed target pairs per lane (2H targets): 8/H warps
-// cover one tile of 512 targets.  H = 4 halves the per-source overhead
-// (staging, the shared-memory sum, its 6 scalar adds) per pair but doubles a
-// unit's length, so it is used once there are enough units to keep the CTAs
-// evenly busy; resident-CTA floors give 80 (H = 2) and 128 (H = 4)
-// registers without spills.
+// cover one tile of 512 targets.  The pass runs H = 4 (2 warps, 128
+// registers at 8 resident CTAs per SM): against H = 2 (4 warps, 80
+// registers at 6) it halves the per-source overhead per pair (staging, the
+// shared-memory sum and its 6 scalar adds), and with up to 8 source slices
+// per tile pair its units stay short enough for small systems too.
 template <int H>
 struct DsShape {
     static constexpr int WARPS = 8 / H, WT = 64 * H, MIN_CTAS = H == 4 ? 8 : 6;
+    static constexpr int QMAX = 16 / WARPS;  // each warp of a round takes its own source group
     static_assert(WARPS * WT == DS_T, "a CTA's warps cover one tile");
 };
+constexpr int DS_H = 4;
 
 struct DsArgs {
     const float4 *__restrict__ xm;
@@ -358,16 +360,17 @@ static void launch_force(int Q, bool kdk, unsigned grid, const DsArgs &a, cudaSt
                     : direct_sym_kernel<1, DS_ACC, BATCH, H><<<grid, b, 0, s>>>(a);
     else if (Q == 2) kdk ? direct_sym_kernel<2, DS_KDK, BATCH, H><<<grid, b, 0, s>>>(a)
                          : direct_sym_kernel<2, DS_ACC, BATCH, H><<<grid, b, 0, s>>>(a);
-    else kdk ? direct_sym_kernel<4, DS_KDK, BATCH, H><<<grid, b, 0, s>>>(a)
-             : direct_sym_kernel<4, DS_ACC, BATCH, H><<<grid, b, 0, s>>>(a);
+    else if (Q == 4) kdk ? direct_sym_kernel<4, DS_KDK, BATCH, H><<<grid, b, 0, s>>>(a)
+                         : direct_sym_kernel<4, DS_ACC, BATCH, H><<<grid, b, 0, s>>>(a);
+    else kdk ? direct_sym_kernel<8, DS_KDK, BATCH, H><<<grid, b, 0, s>>>(a)
+             : direct_sym_kernel<8, DS_ACC, BATCH, H><<<grid, b, 0, s>>>(a);
 }
 
 template <bool BATCH>
-static void launch_pass(int H, int Q, bool kdk, bool kahan, unsigned grid, unsigned fgrid, const DsArgs &a,
+static void launch_pass(int Q, bool kdk, bool kahan, unsigned grid, unsigned fgrid, const DsArgs &a,
                         const DsFix &f, cudaStream_t s) {
     const unsigned fb = DS_FIX_WARPS * 32;
-    if (H == 4) launch_force<BATCH, 4>(Q, kdk, grid, a, s);
-    else launch_force<BATCH, 2>(Q, kdk, grid, a, s);
+    launch_force<BATCH, DS_H>(Q, kdk, grid, a, s);
     if (kdk) {
         if (kahan) direct_sym_fixup_kernel<DS_KDK, true, BATCH><<<fgrid, fb, 0, s>>>(f);
         else direct_sym_fixup_kernel<DS_KDK, false, BATCH><<<fgrid, fb, 0, s>>>(f);
@@ -377,41 +380,27 @@ static void launch_pass(int H, int Q, bool kdk, bool kahan, unsigned grid, unsig
     }
 }
 
-static int sym_slots(int sms, int H) {
-    int occ = 0;
-    if (H == 4)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, direct_sym_kernel<1, DS_ACC, false, 4>,
-                                                      DsShape<4>::WARPS * 32, 0);
-    else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, direct_sym_kernel<1, DS_ACC, false, 2>,
-                                                      DsShape<2>::WARPS * 32, 0);
-    return sms * std::max(occ, 1);
-}
-
 SymShape direct_sym_shape(int sms, int64_t pairs) {
-    // The 8-targets-per-lane shape once every CTA gets 8 units or more.
     SymShape sh;
-    sh.H = 4;
-    sh.slots = sym_slots(sms, 4);
-    sh.Q = direct_sym_slices(pairs, sh.slots);
-    if (pairs * sh.Q >= 8 * sh.slots) return sh;
-    sh.H = 2;
-    sh.slots = sym_slots(sms, 2);
-    sh.Q = direct_sym_slices(pairs, sh.slots);
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, direct_sym_kernel<1, DS_ACC, false, DS_H>,
+                                                  DsShape<DS_H>::WARPS * 32, 0);
+    sh.slots = (int64_t)sms * std::max(occ, 1);
+    sh.Q = direct_sym_slices(pairs, sh.slots, DsShape<DS_H>::QMAX);
     return sh;
 }
 
-int direct_sym_slices(int64_t pairs, int64_t slots) {
+int direct_sym_slices(int64_t pairs, int64_t slots, int qmax) {
     // Source slices per tile pair: enough units that the last ones are a
     // small share of each CTA's work.
     int Q = 1;
-    while (Q < 4 && pairs * Q < 16 * slots) Q *= 2;
+    while (Q < qmax && pairs * Q < 16 * slots) Q *= 2;
     return Q;
 }
 
 struct DsPlan {
     int64_t nt, NP, slots, max_pairs, need;  // need: float4s of scratch
-    int Q, H;
+    int Q;
     std::vector<int64_t> rows;  // band b covers tile rows [rows[b], rows[b + 1])
 };
 
@@ -420,7 +409,6 @@ static DsPlan ds_plan(const gb_direct *h, int64_t n) {
     p.nt = (n + DS_T - 1) / DS_T;
     p.NP = p.nt * (p.nt + 1) / 2;
     const SymShape sh = direct_sym_shape(h->sms, p.NP);
-    p.H = sh.H;
     p.slots = sh.slots;
     p.Q = sh.Q;
     // Tile pairs per band: the handle's slot budget (larger systems run in
@@ -481,7 +469,7 @@ int run_direct_sym(gb_direct *h, int mode, const float4 *xm, float4 *vel, float4
         f.Ie = Ie;
         f.p0 = a.p0;
         GB_CUDA_TRY(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), s));
-        launch_pass<false>(pl.H, pl.Q, kdk, kahan, (unsigned)std::min(pl.slots, a.NU),
+        launch_pass<false>(pl.Q, kdk, kahan, (unsigned)std::min(pl.slots, a.NU),
                            (unsigned)((n - Ib * DS_T + 31) / 32), a, f, s);
         GB_CUDA_TRY(cudaGetLastError());
         h->launches += 2;
@@ -525,8 +513,7 @@ int run_batch_sym(const SymBatch &b, int mode, const float4 *xm, float4 *vel, fl
     f.dt = dt;
     f.accumulate = (flags & GB_ACCUMULATE) ? 1 : 0;
     GB_CUDA_TRY(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), s));
-    launch_pass<true>(b.H, b.Q, mode == DS_KDK, !(flags & GB_PLAIN_FP32), (unsigned)b.P, (unsigned)b.nfb, a, f,
-                      s);
+    launch_pass<true>(b.Q, mode == DS_KDK, !(flags & GB_PLAIN_FP32), (unsigned)b.P, (unsigned)b.nfb, a, f, s);
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
 }
