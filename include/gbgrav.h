@@ -98,9 +98,10 @@ int gb_direct_acc(gb_direct_t *h, const float *xm, float *acc, int64_t n,
  * acc must hold the accelerations of the current positions on entry.
  * Replaces Engine.step (core/engine.py:108-116) with kick/drift
  * (core/integrators/leapfrog.py:11-22) fused into the force pass.  With
- * GB_USE_GRAPH one step is captured as a CUDA graph (again whenever the
- * pointers, n, a parameter or the tile shape change) and replayed nsteps
- * times: identical results, less launch overhead at small n. */
+ * GB_USE_GRAPH a run of 8 steps and a single step are captured as CUDA graphs
+ * (again whenever the pointers, n, a parameter, the tile shape or the pass
+ * change) and replayed, whole runs first: identical results, less launch
+ * overhead at small n. */
 int gb_direct_kdk(gb_direct_t *h, float *xm, float *vel, float *acc, int64_t n,
                   float G, float eps2, float dt, int64_t nsteps, int flags,
                   void *stream);

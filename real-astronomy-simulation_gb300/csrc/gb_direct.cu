@@ -633,7 +633,8 @@ extern "C" int gb_direct_create(gb_direct_t **out, int64_t n_max) {
 
 extern "C" int gb_direct_destroy(gb_direct_t *h) {
     if (!h) return GB_OK;
-    if (h->has_graph) cudaGraphExecDestroy(h->gexec);
+    for (int g = 0; g < 2; ++g)
+        if (h->gexec[g]) cudaGraphExecDestroy(h->gexec[g]);
     if (h->gev_in) cudaEventDestroy(h->gev_in);
     if (h->gev_out) cudaEventDestroy(h->gev_out);
     if (h->gstream) cudaStreamDestroy(h->gstream);
@@ -784,26 +785,37 @@ extern "C" int gb_direct_kdk(gb_direct_t *h, float *xm, float *vel, float *acc, 
                               dt, plain, s));
         return GB_OK;
     }
-    // One step captured on the handle's stream and replayed nsteps times.
-    // Tile-pair scratch is sized before the capture (no allocation inside
-    // it); its address is part of the key, since the adjoint may regrow it.
+    // One step, and a run of GRAPH_STEPS steps, captured on the handle's
+    // stream and replayed: whole runs first, single steps for the rest (one
+    // graph launch per GRAPH_STEPS steps keeps small systems off the host's
+    // launch rate).  Tile-pair scratch is sized before the capture (no
+    // allocation inside it); its address is part of the key, since the
+    // adjoint may regrow it.
     if (h->packed == 2) GB_TRY(reserve_direct_sym(h, n));
     const gb_direct::Key key{xm, vel, acc, h->sym, n, h->sym_band, G, eps2, dt, plain, h->np, h->warps,
                              h->ctas_per_sm, h->packed};
-    if (!h->has_graph || !(h->gkey == key)) {
-        if (h->has_graph) {
-            cudaGraphExecDestroy(h->gexec);
-            h->has_graph = false;
-        }
-        if (!h->gstream) {
-            GB_CUDA_TRY(cudaStreamCreateWithFlags(&h->gstream, cudaStreamNonBlocking));
-            GB_CUDA_TRY(cudaEventCreateWithFlags(&h->gev_in, cudaEventDisableTiming));
-            GB_CUDA_TRY(cudaEventCreateWithFlags(&h->gev_out, cudaEventDisableTiming));
-        }
+    if (h->has_graph && !(h->gkey == key)) {
+        for (int g = 0; g < 2; ++g)
+            if (h->gexec[g]) cudaGraphExecDestroy(h->gexec[g]);
+        h->gexec[0] = h->gexec[1] = nullptr;
+        h->has_graph = false;
+    }
+    if (!h->gstream) {
+        GB_CUDA_TRY(cudaStreamCreateWithFlags(&h->gstream, cudaStreamNonBlocking));
+        GB_CUDA_TRY(cudaEventCreateWithFlags(&h->gev_in, cudaEventDisableTiming));
+        GB_CUDA_TRY(cudaEventCreateWithFlags(&h->gev_out, cudaEventDisableTiming));
+    }
+    const int64_t runs = nsteps / GRAPH_STEPS, rest = nsteps - runs * GRAPH_STEPS;
+    for (int g = 0; g < 2; ++g) {
+        if (h->gexec[g] || (g == 0 ? rest == 0 : runs == 0)) continue;
+        const int steps = g == 0 ? 1 : GRAPH_STEPS;
         GB_CUDA_TRY(cudaStreamBeginCapture(h->gstream, cudaStreamCaptureModeThreadLocal));
         const uint64_t l0 = h->launches;
-        const int st = run_direct(h, MODE_KDK, (const float4 *)xm, (float4 *)vel, (float4 *)acc, nullptr, n, G,
-                                  eps2, dt, plain, h->gstream);
+        int st = GB_OK;
+        for (int k = 0; k < steps && st == GB_OK; ++k)
+            st = run_direct(h, MODE_KDK, (const float4 *)xm, (float4 *)vel, (float4 *)acc, nullptr, n, G, eps2, dt,
+                            plain, h->gstream);
+        h->glaunches = (h->launches - l0) / steps;
         h->launches = l0;
         cudaGraph_t graph = nullptr;
         const cudaError_t e = cudaStreamEndCapture(h->gstream, &graph);
@@ -812,18 +824,22 @@ extern "C" int gb_direct_kdk(gb_direct_t *h, float *xm, float *vel, float *acc, 
             return st;
         }
         if (e != cudaSuccess) return fail(GB_ECUDA, "graph capture: %s", cudaGetErrorString(e));
-        const cudaError_t ei = cudaGraphInstantiate(&h->gexec, graph, 0);
+        const cudaError_t ei = cudaGraphInstantiate(&h->gexec[g], graph, 0);
         cudaGraphDestroy(graph);
-        if (ei != cudaSuccess) return fail(GB_ECUDA, "graph instantiate: %s", cudaGetErrorString(ei));
+        if (ei != cudaSuccess) {
+            h->gexec[g] = nullptr;
+            return fail(GB_ECUDA, "graph instantiate: %s", cudaGetErrorString(ei));
+        }
         h->has_graph = true;
         h->gkey = key;
     }
     GB_CUDA_TRY(cudaEventRecord(h->gev_in, s));
     GB_CUDA_TRY(cudaStreamWaitEvent(h->gstream, h->gev_in, 0));
-    for (int64_t k = 0; k < nsteps; ++k) GB_CUDA_TRY(cudaGraphLaunch(h->gexec, h->gstream));
+    for (int64_t k = 0; k < runs; ++k) GB_CUDA_TRY(cudaGraphLaunch(h->gexec[1], h->gstream));
+    for (int64_t k = 0; k < rest; ++k) GB_CUDA_TRY(cudaGraphLaunch(h->gexec[0], h->gstream));
     GB_CUDA_TRY(cudaEventRecord(h->gev_out, h->gstream));
     GB_CUDA_TRY(cudaStreamWaitEvent(s, h->gev_out, 0));
-    h->launches += 2 * (uint64_t)nsteps;
+    h->launches += h->glaunches * (uint64_t)nsteps;
     return GB_OK;
 }
 

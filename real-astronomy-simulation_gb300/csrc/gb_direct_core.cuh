@@ -155,6 +155,9 @@ constexpr int64_t SYM_MAX_BYTES = 3LL << 30;
 
 }  // namespace gb
 
+// Steps in the multi-step KDK graph of gb_direct_kdk.
+constexpr int GRAPH_STEPS = 8;
+
 // Direct-sum handle (opaque in the C ABI), shared by the direct-sum and
 // adjoint translation units.
 struct gb_direct {
@@ -176,11 +179,13 @@ struct gb_direct {
     int64_t sym_cap;    // float4 elements
     int adj_variant;    // 2: symmetric packed, 1: symmetric scalar, 0: one pass per target
     int64_t sym_band;   // symmetric force pass: tile-pair slot bytes per band at most
-    // One KDK step captured as a CUDA graph (gb_direct_kdk with
-    // GB_USE_GRAPH), replayed per step on the handle's own stream.
+    // KDK steps captured as CUDA graphs (gb_direct_kdk with GB_USE_GRAPH):
+    // gexec[0] one step, gexec[1] GRAPH_STEPS steps, replayed on the
+    // handle's own stream; glaunches = kernels per captured step.
     cudaStream_t gstream;
     cudaEvent_t gev_in, gev_out;
-    cudaGraphExec_t gexec;
+    cudaGraphExec_t gexec[2];
+    uint64_t glaunches;
     bool has_graph;
     struct Key {
         const void *xm, *vel, *acc, *sym;

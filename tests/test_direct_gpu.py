@@ -199,9 +199,9 @@ def test_bad_arguments_raise(cuda_dev):
 
 
 def test_kdk_graph_replay_matches_direct_launches(cuda_dev):
-    """gb_direct_kdk with GB_USE_GRAPH (one captured step replayed) and with
-    direct launches: identical trajectories, including recaptures when dt
-    and the tile shape change."""
+    """gb_direct_kdk with GB_USE_GRAPH (captured runs of 8 steps and single
+    steps, replayed) and with direct launches: identical trajectories,
+    including recaptures when dt, the tile shape and the pass change."""
     grav = importlib.import_module(PKG_NAME + ".solvers.gravity")
     ic = importlib.import_module(PKG_NAME + ".ic")
     p, v, m = ic.plummer(3000, seed=9)
@@ -217,6 +217,11 @@ def test_kdk_graph_replay_matches_direct_launches(cuda_dev):
         s.kdk(xm, v4, a4, 1.0, 1e-4, 2e-3, 3, graph=graph)
         s.set_tiles(2, 4)
         s.kdk(xm, v4, a4, 1.0, 1e-4, 1e-3, 2, graph=graph)
+        l0 = s.launch_count()
+        s.kdk(xm, v4, a4, 1.0, 1e-4, 1e-3, 19, graph=graph)  # 2 runs of 8 steps + 3 single steps
+        assert s.launch_count() - l0 == 2 * 19
+        s.set_variant(2)  # the symmetric pass: captured again
+        s.kdk(xm, v4, a4, 1.0, 1e-4, 1e-3, 17, graph=graph)
         torch.cuda.synchronize()
         out.append((xm.clone(), v4.clone(), a4.clone()))
         s.close()
