@@ -8,13 +8,14 @@
 // instructions and 2 rsqrt, against 24 FP32 instructions and 2 rsqrt for
 // two ordered pairs of the per-target kernel.
 //
-// Layout and schedule are those of adjoint_vjp_sym2_kernel: tiles of 512
-// particles, 4 warps, 4 targets per lane as two packed pairs (targets
-// q = 0, 1 and 2, 3 of lane l in warp w: 128 w + 32 q + l); CTAs take units
-// (tile pair I <= J, one of Q source slices of tile J) from an atomic
-// counter; in round r warp w takes source group (G/4 w + r) mod G of the
-// slice and at step k lane l source 32 g + (l + k) mod 32, so the per-source
-// shared-memory sums have one writer at a time.  Each unit writes its own
+// The schedule is that of adjoint_vjp_sym2_kernel with a wider CTA shape:
+// tiles of 512 particles, 2 warps, 8 targets per lane as four packed pairs
+// (targets q = 0 .. 7 of lane l in warp w: 256 w + 32 q + l); CTAs take
+// units (tile pair I <= J, one of Q <= 8 source slices of tile J) from an
+// atomic counter; in round r warp w takes source group (G/2 w + r) mod G of
+// the slice (G = 16/Q groups of 32) and at step k lane l source
+// 32 g + (l + k) mod 32, so the per-source shared-memory sums have one
+// writer at a time.  Each unit writes its own
 // row slot (tile I's sums over the slice) and its slice of the pair's column
 // slot; the fix-up adds a particle's slots in a fixed order (Kahan unless
 // GB_PLAIN_FP32), scales by G and writes the result (or, fused KDK, applies
