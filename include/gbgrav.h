@@ -190,13 +190,15 @@ int gb_bh_export(gb_bh_t *h, int what, void *dst, void *stream);
 
 int gb_bh_diag(gb_bh_t *h, gb_diag_t *out, int reset);
 
-/* Traversal shape.  1 (default) and 2: warp-coherent, the warp's 32 (or 64,
- * two per lane) key-consecutive targets walk the tree together, one node
- * record per warp step.  0: per lane, each lane walks its own target with
- * its own stack (max_stack <= 127 and n <= 2^25 + 1; otherwise mode 1
- * runs).  All modes give bit-identical results: each target meets its
- * nodes in the same order.  Mode 1 is fastest on the 1M disk (per-lane
- * record loads diverge). */
+/* Traversal shape.  1 and 2: warp-coherent, the warp's 32 (or 64, two per
+ * lane) key-consecutive targets walk the tree together, one node record per
+ * warp step.  0: per lane, each lane walks its own target with its own
+ * stack (max_stack <= 127 and n <= 2^25 + 1; otherwise mode 1 runs).  -1
+ * (default): 0 below n = 131,072, 1 from there.  All modes give
+ * bit-identical results: each target meets its nodes in the same order.
+ * Mode 1 is fastest on the 1M disk (per-lane record loads diverge); mode 0
+ * on small systems, where a warp-coherent launch has too few warps to hide
+ * each step's latency. */
 int gb_bh_set_traversal(gb_bh_t *h, int targets_per_lane);
 
 /* Stage timing for measurement: with timing enabled, every build/step records

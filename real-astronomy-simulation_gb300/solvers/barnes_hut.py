@@ -132,8 +132,9 @@ class BarnesHut:
         _lib.call("gb_bh_set_graph", self._h, 1 if on else 0)
 
     def set_traversal(self, targets_per_lane: int) -> None:
-        """Traversal shape: 1 (default) or 2 targets per lane, warp-coherent;
-        0 per-lane walks.  Results are bit-identical across shapes."""
+        """Traversal shape: 1 or 2 targets per lane, warp-coherent; 0
+        per-lane walks; -1 (default) per lane below 131,072 particles and
+        warp-coherent from there.  Results are bit-identical across shapes."""
         _lib.call("gb_bh_set_traversal", self._h, int(targets_per_lane))
 
     # -- measurement hooks

@@ -63,7 +63,7 @@ def _run(bhmod, pos, mass, dev, theta=0.5, soft=0.05, bits=21, G=None, max_stack
 
 
 @pytest.mark.parametrize("bits", [21, 10])
-@pytest.mark.parametrize("tpl", [0, 1, 2])
+@pytest.mark.parametrize("tpl", [-1, 0, 1, 2])
 def test_golden_tree_bit_exact(cuda_dev, bits, tpl):
     _, bhmod, _, _ = _mods()
     g = load_golden("bh")
