@@ -142,6 +142,31 @@ def test_small_sizes(cuda_dev, orc, n, tpl):
     _check_acc(a, ref)
 
 
+@pytest.mark.parametrize("n", [2, 4095, 4096, 4097, 32767, 32768, 32769, 40000])
+@pytest.mark.parametrize("bits", [21, 10])
+def test_sort_sizes_at_tile_edges(cuda_dev, orc, n, bits):
+    """Keys, order and topology at the radix sort's tile edges (4,096 keys
+    per CTA) against numpy's stable argsort; duplicate positions exercise
+    the stable order of equal keys."""
+    _, bhmod, ic, _ = _mods()
+    pos, _, mass = ic.exponential_disk(n, seed=7)
+    pos, mass = _f32(pos), _f32(mass)
+    if n > 100:
+        pos[n // 2: n // 2 + 50] = pos[0]  # equal keys
+    b, _ = _run(bhmod, pos, mass, cuda_dev, bits=bits, tpl=-1)
+    t = b.tree_arrays()
+    codes = orc.morton_codes(pos, bits)
+    order = orc.stable_argsort(codes)
+    np.testing.assert_array_equal(t["code"], codes[order])
+    np.testing.assert_array_equal(t["order"], order)
+    if n >= 2:
+        left, right, parent = orc.build_radix(codes[order])
+        np.testing.assert_array_equal(t["left"], left)
+        np.testing.assert_array_equal(t["parent"], parent)
+    assert b.diag()["bad_tree"] == 0
+    b.close()
+
+
 @pytest.mark.parametrize("bits,tpl", [(10, 2), (21, 1), (10, 0)])
 def test_config2_disk_1m(cuda_dev, orc, bits, tpl):
     """N = 1,000,000 exponential disk (M = 5, Rd = 3, z0 = 0.3, galactic G),
