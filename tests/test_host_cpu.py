@@ -126,3 +126,30 @@ def test_state_npz_roundtrip(tmp_path):
         np.testing.assert_array_equal(getattr(t, name), getattr(s, name))
     assert (t.time, t.step, t.seed) == (1.25, 7, 3)
     assert t.meta["level"] == "small" and t.meta["dt"] == 1e-3 and t.temperature is None
+
+
+def test_form_selectors_reject_null_handles_without_gpu(lib):
+    """The force-pass, band and traversal selectors check their handle before
+    any CUDA call."""
+    lib_mod = importlib.import_module(PKG_NAME + "._lib")
+    pkg = importlib.import_module(PKG_NAME)
+    for name, args in (("gb_direct_set_variant", (None, 2)), ("gb_direct_set_sym_band", (None, 1 << 30)),
+                       ("gb_batch_set_variant", (None, 1)), ("gb_bh_set_traversal", (None, -1)),
+                       ("gb_adjoint_set_variant", (None, 2))):
+        with pytest.raises(pkg.GravityError, match="handle is NULL"):
+            lib_mod.call(name, *args)
+
+
+def test_python_surface_of_the_force_forms(pkg):
+    """Engine(symmetric=...) and diagnostics(), the solver and batch form
+    setters, and the autotuner's candidate lists carry the symmetric forms."""
+    import inspect
+    eng = importlib.import_module(PKG_NAME + ".engine")
+    grav = importlib.import_module(PKG_NAME + ".solvers.gravity")
+    batch = importlib.import_module(PKG_NAME + ".batch")
+    tune = importlib.import_module(PKG_NAME + ".autotune")
+    assert inspect.signature(eng.Engine).parameters["symmetric"].default is True
+    assert callable(eng.Engine.diagnostics)
+    assert callable(grav.DirectGravity.set_variant) and callable(grav.DirectGravity.set_sym_band)
+    assert "variant" in inspect.signature(batch.DirectBatch).parameters
+    assert (2, 4, 2) in tune.DIRECT_SHAPES and (2, 4, 1) in tune.BATCH_SHAPES
