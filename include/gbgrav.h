@@ -78,8 +78,9 @@ int gb_direct_set_tiles(gb_direct_t *h, int k, int warps, int ctas_per_sm);
  * 512 x 512 tile pair (N^2/32 bytes in all at large N); above the band
  * budget (gb_direct_set_sym_band, 1 GiB by default) it runs in bands of tile
  * rows, two kernels per band, plus 32 bytes per particle of running sums.
- * Same results up to FP32 rounding order; gb_direct_phi always runs the
- * per-target pass. */
+ * Same results up to FP32 rounding order.  gb_direct_phi (and gb_energy)
+ * follow the variant too: form 2 sums each pair's potential once for both
+ * particles. */
 int gb_direct_set_variant(gb_direct_t *h, int packed);
 
 /* Tile-pair slot bytes per band of the symmetric pass (at least 40 KB:

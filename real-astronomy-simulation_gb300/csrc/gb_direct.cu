@@ -662,9 +662,9 @@ extern "C" int gb_direct_set_tiles(gb_direct_t *h, int k, int warps, int ctas_pe
 static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, float4 *acc, float *phi,
                       int64_t n, float G, float eps2, float dt, int flags, cudaStream_t s,
                       const ExtPot &pot = ExtPot{}) {
-    if (mode != MODE_PHI && h->packed == 2) {
+    if (h->packed == 2) {
         bool done = false;
-        GB_TRY(run_direct_sym(h, mode, xm, vel, acc, n, G, eps2, dt, flags, s, pot, &done));
+        GB_TRY(run_direct_sym(h, mode, xm, vel, acc, phi, n, G, eps2, dt, flags, s, pot, &done));
         if (done) return GB_OK;
     }
     // Variant 2 beyond the tile-pair scratch limit runs the scalar pass.

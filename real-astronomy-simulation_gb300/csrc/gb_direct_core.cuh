@@ -215,11 +215,12 @@ inline int ensure_sym(gb_direct *h, int64_t need) {
     return GB_OK;
 }
 
-// Symmetric direct-sum force pass (gb_direct_sym.cu): mode 0 acceleration,
-// 1 fused KDK.  Returns GB_OK with *done = false when the scratch it needs
-// passes SYM_MAX_BYTES (the caller then runs the per-target pass).
-int run_direct_sym(gb_direct *h, int mode, const float4 *xm, float4 *vel, float4 *acc, int64_t n, float G,
-                   float eps2, float dt, int flags, cudaStream_t s, const ExtPot &pot, bool *done);
+// Symmetric direct-sum pass (gb_direct_sym.cu): mode 0 acceleration, 1
+// fused KDK, 2 the potential sums into phi.  Returns GB_OK with
+// *done = false when the scratch it needs passes SYM_MAX_BYTES (the caller
+// then runs the per-target pass).
+int run_direct_sym(gb_direct *h, int mode, const float4 *xm, float4 *vel, float4 *acc, float *phi, int64_t n,
+                   float G, float eps2, float dt, int flags, cudaStream_t s, const ExtPot &pot, bool *done);
 // Sizes the tile-pair scratch run_direct_sym needs for n particles (nothing
 // when that passes SYM_MAX_BYTES).
 int reserve_direct_sym(gb_direct *h, int64_t n);

@@ -40,7 +40,7 @@ namespace gb {
 
 constexpr int DS_T = SYM_TILE;
 constexpr int DS_K_UNROLL = DS_UNROLL;
-constexpr int DS_ACC = 0, DS_KDK = 1;
+constexpr int DS_ACC = 0, DS_KDK = 1, DS_PHI = 2;
 
 // CTA shape for H packed target pairs per lane (2H targets): 8/H warps
 // cover one tile of 512 targets.  The pass runs H = 4 (2 warps, 128
@@ -132,6 +132,47 @@ __device__ __forceinline__ void ds_round(const float4 *__restrict__ sxm, float4 
     }
 }
 
+// The potential form of a round: phi_t += m_s / |d|, phi_s += m_t / |d|
+// (|d|^2 = d.d + eps2), the sum of potential_energy
+// (core/solvers/gravity.py:47-55); the target sums live in NX, the source
+// sums are added to sacc.x.  DIAG keeps the pairs t < s, so a particle
+// never meets itself (the reference skips j == i).
+template <bool DIAG, int H>
+__device__ __forceinline__ void ds_round_phi(const float4 *__restrict__ sxm, float4 *sacc, int g, int lane, int wib,
+                                             f2 EPS2, const f2 (&TX)[H], const f2 (&TY)[H], const f2 (&TZ)[H],
+                                             const f2 (&TM)[H], f2 (&NX)[H]) {
+#pragma unroll DS_K_UNROLL
+    for (int k = 0; k < 32; ++k) {
+        const int jj = g * 32 + ((lane + k) & 31);
+        const float4 xs = sxm[jj];
+        const f2 sx = pack2(xs.x, xs.x), sy = pack2(xs.y, xs.y), sz = pack2(xs.z, xs.z);
+        const f2 sm = pack2(xs.w, xs.w);
+        f2 PW = 0ull;
+#pragma unroll
+        for (int h = 0; h < H; ++h) {
+            const f2 dx = sub2(sx, TX[h]), dy = sub2(sy, TY[h]), dz = sub2(sz, TZ[h]);
+            const f2 r2 = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, EPS2)));
+            f2 inv = rsqrt2(r2);
+            if (DIAG) {
+                float c0, c1;
+                unpack2(inv, c0, c1);
+                const int t0 = DsShape<H>::WT * wib + 64 * h + lane;
+                c0 = t0 < jj ? c0 : 0.f;
+                c1 = t0 + 32 < jj ? c1 : 0.f;
+                inv = pack2(c0, c1);
+            }
+            NX[h] = fma2(sm, inv, NX[h]);
+            PW = fma2(TM[h], inv, PW);
+        }
+        float4 acc = sacc[jj];
+        float lo, hi;
+        unpack2(PW, lo, hi);
+        acc.x += lo + hi;
+        sacc[jj] = acc;
+        __syncwarp();
+    }
+}
+
 template <int Q, int MODE, bool BATCH, int H>
 __global__ void __launch_bounds__(DsShape<H>::WARPS * 32, DsShape<H>::MIN_CTAS) direct_sym_kernel(DsArgs a) {
     constexpr int G = 16 / Q, SPAN = G * 32;
@@ -209,10 +250,17 @@ __global__ void __launch_bounds__(DsShape<H>::WARPS * 32, DsShape<H>::MIN_CTAS) 
             // t < s measured 2.5% slower on the 512-system batch.)
             // Warp-uniform branches; every warp still reaches the barrier.
             if (WT * wib < s_ntgt && g < s_gend) {
-                if (!diag)
-                    ds_round<false, H>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX, NY, NZ);
-                else if ((WT / 32) * wib <= g)
-                    ds_round<true, H>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX, NY, NZ);
+                if constexpr (MODE == DS_PHI) {
+                    if (!diag)
+                        ds_round_phi<false, H>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX);
+                    else if ((WT / 32) * wib <= g)
+                        ds_round_phi<true, H>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX);
+                } else {
+                    if (!diag)
+                        ds_round<false, H>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX, NY, NZ);
+                    else if ((WT / 32) * wib <= g)
+                        ds_round<true, H>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX, NY, NZ);
+                }
             }
             __syncthreads();
         }
@@ -242,6 +290,7 @@ struct DsFix {
     const float4 *__restrict__ rowpart;
     const float4 *__restrict__ colpart;
     float4 *xm, *vel, *acc;
+    float *phi;  // DS_PHI: the potential sums (in the slots' x)
     int64_t n, nt;
     int Q;
     // One system, in bands of tile rows [Ib, Ie) whose pairs start at p0;
@@ -337,6 +386,10 @@ __global__ void __launch_bounds__(DS_FIX_WARPS * 32) direct_sym_fixup_kernel(DsF
         return;
     }
     float4 an = make_float4(f.G * (sx - cx), f.G * (sy - cy), f.G * (sz - cz), 0.f);
+    if (MODE == DS_PHI) {
+        f.phi[i] = an.x;
+        return;
+    }
     if (MODE == DS_ACC) {
         if (f.pot.on) {
             const float4 x = f.xm[i];
@@ -354,31 +407,30 @@ __global__ void __launch_bounds__(DS_FIX_WARPS * 32) direct_sym_fixup_kernel(DsF
     kdk_writeback(f.xm, f.vel, f.acc, i, an, f.h, f.dt);
 }
 
-template <bool BATCH, int H>
-static void launch_force(int Q, bool kdk, unsigned grid, const DsArgs &a, cudaStream_t s) {
+template <int MODE, bool BATCH, int H>
+static void launch_force(int Q, unsigned grid, const DsArgs &a, cudaStream_t s) {
     const unsigned b = DsShape<H>::WARPS * 32;
-    if (Q == 1) kdk ? direct_sym_kernel<1, DS_KDK, BATCH, H><<<grid, b, 0, s>>>(a)
-                    : direct_sym_kernel<1, DS_ACC, BATCH, H><<<grid, b, 0, s>>>(a);
-    else if (Q == 2) kdk ? direct_sym_kernel<2, DS_KDK, BATCH, H><<<grid, b, 0, s>>>(a)
-                         : direct_sym_kernel<2, DS_ACC, BATCH, H><<<grid, b, 0, s>>>(a);
-    else if (Q == 4) kdk ? direct_sym_kernel<4, DS_KDK, BATCH, H><<<grid, b, 0, s>>>(a)
-                         : direct_sym_kernel<4, DS_ACC, BATCH, H><<<grid, b, 0, s>>>(a);
-    else kdk ? direct_sym_kernel<8, DS_KDK, BATCH, H><<<grid, b, 0, s>>>(a)
-             : direct_sym_kernel<8, DS_ACC, BATCH, H><<<grid, b, 0, s>>>(a);
+    if (Q == 1) direct_sym_kernel<1, MODE, BATCH, H><<<grid, b, 0, s>>>(a);
+    else if (Q == 2) direct_sym_kernel<2, MODE, BATCH, H><<<grid, b, 0, s>>>(a);
+    else if (Q == 4) direct_sym_kernel<4, MODE, BATCH, H><<<grid, b, 0, s>>>(a);
+    else direct_sym_kernel<8, MODE, BATCH, H><<<grid, b, 0, s>>>(a);
 }
 
+template <int MODE, bool BATCH>
+static void launch_mode(int Q, bool kahan, unsigned grid, unsigned fgrid, const DsArgs &a, const DsFix &f,
+                        cudaStream_t s) {
+    launch_force<MODE, BATCH, DS_H>(Q, grid, a, s);
+    if (kahan) direct_sym_fixup_kernel<MODE, true, BATCH><<<fgrid, DS_FIX_WARPS * 32, 0, s>>>(f);
+    else direct_sym_fixup_kernel<MODE, false, BATCH><<<fgrid, DS_FIX_WARPS * 32, 0, s>>>(f);
+}
+
+// mode: DS_ACC, DS_KDK or (one system) DS_PHI.
 template <bool BATCH>
-static void launch_pass(int Q, bool kdk, bool kahan, unsigned grid, unsigned fgrid, const DsArgs &a,
+static void launch_pass(int mode, int Q, bool kahan, unsigned grid, unsigned fgrid, const DsArgs &a,
                         const DsFix &f, cudaStream_t s) {
-    const unsigned fb = DS_FIX_WARPS * 32;
-    launch_force<BATCH, DS_H>(Q, kdk, grid, a, s);
-    if (kdk) {
-        if (kahan) direct_sym_fixup_kernel<DS_KDK, true, BATCH><<<fgrid, fb, 0, s>>>(f);
-        else direct_sym_fixup_kernel<DS_KDK, false, BATCH><<<fgrid, fb, 0, s>>>(f);
-    } else {
-        if (kahan) direct_sym_fixup_kernel<DS_ACC, true, BATCH><<<fgrid, fb, 0, s>>>(f);
-        else direct_sym_fixup_kernel<DS_ACC, false, BATCH><<<fgrid, fb, 0, s>>>(f);
-    }
+    if (mode == DS_KDK) launch_mode<DS_KDK, BATCH>(Q, kahan, grid, fgrid, a, f, s);
+    else if (mode == DS_ACC) launch_mode<DS_ACC, BATCH>(Q, kahan, grid, fgrid, a, f, s);
+    else if constexpr (!BATCH) launch_mode<DS_PHI, BATCH>(Q, kahan, grid, fgrid, a, f, s);
 }
 
 SymShape direct_sym_shape(int sms, int64_t pairs) {
@@ -428,8 +480,8 @@ int reserve_direct_sym(gb_direct *h, int64_t n) {
     return ensure_sym(h, p.need);
 }
 
-int run_direct_sym(gb_direct *h, int mode, const float4 *xm, float4 *vel, float4 *acc, int64_t n, float G,
-                   float eps2, float dt, int flags, cudaStream_t s, const ExtPot &pot, bool *done) {
+int run_direct_sym(gb_direct *h, int mode, const float4 *xm, float4 *vel, float4 *acc, float *phi, int64_t n,
+                   float G, float eps2, float dt, int flags, cudaStream_t s, const ExtPot &pot, bool *done) {
     *done = false;
     const DsPlan pl = ds_plan(h, n);
     if (pl.need * (int64_t)sizeof(float4) > SYM_MAX_BYTES) return GB_OK;
@@ -459,9 +511,10 @@ int run_direct_sym(gb_direct *h, int mode, const float4 *xm, float4 *vel, float4
     f.G = G;
     f.h = 0.5f * dt;
     f.dt = dt;
+    f.phi = phi;
     f.accumulate = (flags & GB_ACCUMULATE) ? 1 : 0;
     f.pot = pot;
-    const bool kdk = mode == DS_KDK, kahan = !(flags & GB_PLAIN_FP32);
+    const bool kahan = !(flags & GB_PLAIN_FP32);
     for (size_t b = 0; b + 1 < pl.rows.size(); ++b) {
         const int64_t Ib = pl.rows[b], Ie = pl.rows[b + 1];
         a.p0 = host_sym_base(Ib, pl.nt);
@@ -470,7 +523,7 @@ int run_direct_sym(gb_direct *h, int mode, const float4 *xm, float4 *vel, float4
         f.Ie = Ie;
         f.p0 = a.p0;
         GB_CUDA_TRY(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), s));
-        launch_pass<false>(pl.Q, kdk, kahan, (unsigned)std::min(pl.slots, a.NU),
+        launch_pass<false>(mode, pl.Q, kahan, (unsigned)std::min(pl.slots, a.NU),
                            (unsigned)((n - Ib * DS_T + 31) / 32), a, f, s);
         GB_CUDA_TRY(cudaGetLastError());
         h->launches += 2;
@@ -514,7 +567,7 @@ int run_batch_sym(const SymBatch &b, int mode, const float4 *xm, float4 *vel, fl
     f.dt = dt;
     f.accumulate = (flags & GB_ACCUMULATE) ? 1 : 0;
     GB_CUDA_TRY(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), s));
-    launch_pass<true>(b.Q, mode == DS_KDK, !(flags & GB_PLAIN_FP32), (unsigned)b.P, (unsigned)b.nfb, a, f, s);
+    launch_pass<true>(mode, b.Q, !(flags & GB_PLAIN_FP32), (unsigned)b.P, (unsigned)b.nfb, a, f, s);
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
 }

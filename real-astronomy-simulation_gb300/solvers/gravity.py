@@ -60,7 +60,7 @@ class DirectGravity:
         """Force-pass form: 0 scalar per target (default), 1 packed per
         target, 2 symmetric (each unordered pair once, both particles
         updated; its tile-pair scratch is bounded by running large systems in
-        bands, see set_sym_band).  The potential pass is per target."""
+        bands, see set_sym_band).  phi() and energies() follow the variant."""
         _lib.call("gb_direct_set_variant", self._h, int(variant))
 
     def set_sym_band(self, nbytes: int):

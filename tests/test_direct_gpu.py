@@ -162,16 +162,45 @@ def test_energies_golden(cuda_dev):
     assert tot == pytest.approx(ke + pe, rel=1e-12)
 
 
-def test_phi_matches_oracle(cuda_dev, orc):
+@pytest.mark.parametrize("variant", [0, 2])
+@pytest.mark.parametrize("n", [5000, 70001])
+def test_phi_matches_oracle(cuda_dev, orc, variant, n):
+    """The potential sums (j != i) of the per-target pass and of the
+    symmetric pass (each pair once, both particles; 8 and 4 source slices
+    at these sizes) against the oracle."""
     _, grav, ic = _mods()
-    pos, _, mass = ic.plummer(5000, seed=8)
+    pos, _, mass = ic.plummer(n, seed=8)
     pos, mass = _f32(pos), _f32(mass)
     xm = _xm(pos, mass, cuda_dev)
-    s = grav.DirectGravity(5000, cuda_dev)
+    s = grav.DirectGravity(n, cuda_dev)
+    s.set_variant(variant)
     phi = s.phi(xm, 1e-4).double().cpu().numpy()
-    t = np.arange(0, 5000, 7)
+    t = np.arange(0, n, 7 if n < 10000 else 97)
     ref = orc.phi_targets(pos, mass, 1e-4, t)
     assert np.abs(phi[t] - ref).max() / np.abs(ref).max() < 1e-5
+
+
+def test_symmetric_phi_in_bands_and_energies(cuda_dev):
+    """The potential in bands of tile rows equals the one-band sums to FP32
+    rounding, and the energies of both passes agree."""
+    _, grav, ic = _mods()
+    pos, vel, mass = ic.plummer(5000, seed=9)
+    xm = _xm(pos, mass, cuda_dev)
+    v4 = torch.zeros_like(xm)
+    v4[:, :3] = torch.tensor(vel, dtype=torch.float32, device=cuda_dev)
+    s0, s2, s2b = (grav.DirectGravity(5000, cuda_dev) for _ in range(3))
+    s2.set_variant(2)
+    s2b.set_variant(2)
+    s2b.set_sym_band(5 * 16 * 512 * 9)  # 5 tile pairs with 8 source slices: several bands
+    p2 = s2.phi(xm, 1e-4).double().cpu().numpy()
+    p2b = s2b.phi(xm, 1e-4).double().cpu().numpy()
+    assert np.abs(p2b - p2).max() / np.abs(p2).max() < 1e-6
+    e0 = s0.energies(xm, v4, 1.0, 1e-4)
+    e2 = s2.energies(xm, v4, 1.0, 1e-4)
+    assert e2[0] == e0[0]
+    assert e2[1] == pytest.approx(e0[1], rel=1e-6)
+    for s in (s0, s2, s2b):
+        s.close()
 
 
 def test_fp64_targets_match_oracle(cuda_dev, orc):
