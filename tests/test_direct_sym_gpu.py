@@ -83,11 +83,11 @@ def test_ragged_sizes(cuda_dev, orc, n):
     s.close()
 
 
-@pytest.mark.parametrize("n", [70001, 90001])
+@pytest.mark.parametrize("n", [70001, 90001, 110001])
 def test_fewer_source_slices_match_oracle(cuda_dev, orc, n):
-    """2 source slices per tile pair at N = 70,001 and 1 at N = 90,001 on a
-    152-SM GB300 (the slice count falls as the tile pairs outnumber 16x the
-    resident CTAs), on 2,048 sampled targets."""
+    """4, 2 and 1 source slices per tile pair at N = 70,001, 90,001 and
+    110,001 on a 152-SM GB300 (the slice count falls as the tile pairs
+    outnumber 16x the resident CTAs), on 2,048 sampled targets."""
     grav, ic = _mods()
     pos, _, mass = ic.plummer(n, seed=41)
     pos, mass = _f32(pos), _f32(mass)
