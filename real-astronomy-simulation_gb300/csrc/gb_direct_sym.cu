@@ -34,12 +34,8 @@
 
 namespace gb {
 
-#ifndef DS_UNROLL
-#define DS_UNROLL 4
-#endif
-
 constexpr int DS_T = SYM_TILE;
-constexpr int DS_K_UNROLL = DS_UNROLL;
+constexpr int DS_K_UNROLL = 4;  // steps of a round unrolled (1-4 measured within 3%)
 constexpr int DS_ACC = 0, DS_KDK = 1, DS_PHI = 2;
 
 // CTA shape for H packed target pairs per lane (2H targets): 8/H warps
