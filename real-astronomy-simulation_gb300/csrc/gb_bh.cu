@@ -292,6 +292,16 @@ __device__ __forceinline__ unsigned arrive(unsigned *p) {
     return old;
 }
 
+// True for the second child to arrive.  A sibling that already arrived is
+// seen by an acquire load, which synchronises with its release and needs no
+// fence of the caller's own stores: those are released by the atomic at the
+// first node where the caller arrives first, the only place it stops.
+__device__ __forceinline__ bool second_arrival(unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v != 0u || arrive(p) != 0u;
+}
+
 // Summarises every internal node k once both children are done and writes
 // the traversal record of its two children as (left, right) pairs:
 //   inode[3k] = {x_L, x_R, y_L, y_R}, inode[3k+1] = {z_L, z_R, m_L, m_R},
@@ -311,7 +321,7 @@ __global__ void bh_bottomup_kernel(const float4 *__restrict__ leaf, const int2 *
             return;
         }
         const int k = node - n;
-        if (arrive(arrivals + k) == 0u) return;  // the sibling subtree is still running
+        if (!second_arrival(arrivals + k)) return;  // the sibling subtree is still running
         const int2 c = __ldg(child + k);
         if ((unsigned)c.x >= (unsigned)(2 * n - 1) || (unsigned)c.y >= (unsigned)(2 * n - 1)) {
             atomicAdd(diag + DIAG_BAD_TREE, 1ull);
