@@ -167,6 +167,43 @@ def test_sort_sizes_at_tile_edges(cuda_dev, orc, n, bits):
     b.close()
 
 
+def _boundary_positions(n, bits, seed):
+    """Coordinates within a few ulps of a key-cell boundary of the FP64
+    quantisation: the box is pinned by two anchor particles, the scale is the
+    one the reference derives from it (core/solvers/barnes_hut.py:37-45), and
+    each coordinate sits at lo + (cell + tiny offset) / scale."""
+    rng = np.random.default_rng(seed)
+    lo32 = float(np.float32(-3.7))
+    hi32 = float(np.float32(-3.7 + 41.3))
+    qmax = float((1 << bits) - 1)
+    scale = qmax / ((hi32 - lo32) * 1.0000001)
+    cell = rng.integers(0, 1 << bits, (n, 3)).astype(np.float64)
+    off = rng.normal(0.0, 1e-6, (n, 3)) * rng.choice([1e-2, 1.0, 30.0, 3e3], (n, 3))
+    pos = _f32(np.clip(lo32 + (cell + off) / scale, lo32, hi32))
+    pos[0], pos[1] = lo32, hi32
+    return pos
+
+
+@pytest.mark.parametrize("bits", [10, 21])
+def test_keys_at_quantisation_boundaries(cuda_dev, orc, bits):
+    """Keys and order bit-exact against the reference's Morton codes for
+    coordinates on key-cell boundaries, where an FP32 evaluation of the
+    quantisation would put 24% (10 bits) to 49% (21 bits) of the coordinates
+    in the wrong cell."""
+    _, bhmod, _, _ = _mods()
+    n = 200_000
+    pos = _boundary_positions(n, bits, 11 + bits)
+    mass = np.full(n, 1.0 / n)
+    b, _ = _run(bhmod, pos, mass, cuda_dev, bits=bits, tpl=-1)
+    t = b.tree_arrays()
+    codes = orc.morton_codes(pos, bits)
+    order = orc.stable_argsort(codes)
+    np.testing.assert_array_equal(t["code"], codes[order])
+    np.testing.assert_array_equal(t["order"], order)
+    assert b.diag()["bad_tree"] == 0
+    b.close()
+
+
 @pytest.mark.parametrize("bits,tpl", [(10, 2), (21, 1), (10, 0)])
 def test_config2_disk_1m(cuda_dev, orc, bits, tpl):
     """N = 1,000,000 exponential disk (M = 5, Rd = 3, z0 = 0.3, galactic G),
