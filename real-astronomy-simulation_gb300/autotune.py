@@ -62,7 +62,7 @@ def tune_direct(solver, xm, G=1.0, eps2=1e-4, reps=3, use_cache=True):
     bucket = 1 << max(0, (n - 1).bit_length())
     key = _key("direct", bucket)
     cache = _load() if use_cache else {}
-    if key in cache:
+    if key in cache and len(cache[key]["best"]) == 3:
         shape = tuple(cache[key]["best"])
         solver.set_tiles(shape[0], shape[1], 0, shape[2])
         return shape, cache[key]["ms"]
