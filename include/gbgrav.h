@@ -123,7 +123,8 @@ int gb_direct_phi(gb_direct_t *h, const float *xm, float *phi, int64_t n,
 /* FP64 energies into out3 (device, 3 doubles): kinetic, potential, total.
  * KE = 1/2 sum m v^2 (core/solvers/gravity.py:29-36); PE = -1/2 G sum m_i
  * phi_i (core/solvers/gravity.py:39-57) with phi from gb_direct_phi; the
- * reductions run in FP64 in a fixed order. */
+ * reductions run in FP64 in a fixed order.  n = 0 writes zeros (xm and vel
+ * may then be NULL). */
 int gb_energy(gb_direct_t *h, const float *xm, const float *vel, int64_t n,
               float G, float eps2, double *out3, void *stream);
 

@@ -857,8 +857,10 @@ extern "C" int gb_direct_phi(gb_direct_t *h, const float *xm, float *phi, int64_
 extern "C" int gb_energy(gb_direct_t *h, const float *xm, const float *vel, int64_t n, float G, float eps2,
                          double *out3, void *stream) {
     GB_TRY(check_n(h, n));
-    GB_TRY(check_xm(xm, "xm"));
-    GB_TRY(check_xm(vel, "vel"));
+    if (n > 0) {  // an empty system reads neither buffer and gets zeros
+        GB_TRY(check_xm(xm, "xm"));
+        GB_TRY(check_xm(vel, "vel"));
+    }
     if (!out3) return fail(GB_EINVAL, "out3 is NULL");
     cudaStream_t s = (cudaStream_t)stream;
     if (n > 0) GB_TRY(gb_direct_phi(h, xm, h->phi, n, eps2, 0, stream));

@@ -272,3 +272,32 @@ def test_engine_diagnostics_virial_plummer(cuda_dev):
     assert d["kinetic"] == ke and d["potential"] == pe and d["total"] == tot and d["thermal"] == 0.0
     assert d["virial"] == pytest.approx(2.0 * ke / abs(pe), rel=1e-12)
     assert 0.8 < d["virial"] < 1.2
+
+
+@pytest.mark.parametrize("mode", ["direct", "bh"])
+def test_empty_system(cuda_dev, mode):
+    """No particles: the Engine loads, steps and reports zero energies, the
+    solver calls are no-ops returning zeros, and the same Engine then takes a
+    real system."""
+    pkg, grav, ic = _mods()
+    state_mod = importlib.import_module(PKG_NAME + ".state")
+    eng = pkg.Engine(softening=0.05, gravity_mode=mode, device=cuda_dev)
+    empty = state_mod.State.from_arrays(np.zeros((0, 3)), np.zeros((0, 3)), np.zeros(0))
+    eng.load_state(empty)
+    eng.step(1e-3)
+    eng.run(1e-3, 3)
+    assert eng.energies() == (0.0, 0.0, 0.0)
+    assert eng.diagnostics()["virial"] == 0.0
+    out = eng.to_state()
+    assert out.n == 0 and out.step == 4 and abs(out.time - 4e-3) < 1e-15
+    g = grav.DirectGravity(16, cuda_dev)
+    xm = torch.zeros((0, 4), dtype=torch.float32, device=cuda_dev)
+    g.acc(xm, torch.zeros_like(xm), 1.0, 1e-4)
+    g.kdk(xm, torch.zeros_like(xm), torch.zeros_like(xm), 1.0, 1e-4, 1e-3, 2)
+    assert g.energies(xm, torch.zeros_like(xm), 1.0, 1e-4) == (0.0, 0.0, 0.0)
+    p, v, m = ic.plummer(300, seed=1)
+    eng.load_state(state_mod.State.from_arrays(p, v, m))
+    eng.step(1e-3)
+    ke, pe, tot = eng.energies()
+    assert ke > 0.0 and pe < 0.0 and np.isfinite(tot)
+    assert torch.isfinite(eng.a4).all()
