@@ -42,6 +42,7 @@ extern "C" {
 #define GB_PLAIN_FP32 0x2  /* plain FP32 accumulation (no Kahan compensation) */
 #define GB_COUNT_WORK 0x4  /* tree traversal also counts its work (gb_diag_t) */
 #define GB_USE_GRAPH 0x8   /* KDK calls: replay captured steps as a CUDA graph */
+#define GB_CHECK 0x10      /* tree calls: wait for the call and fail on counted failures */
 
 /* Device diagnostic counters, read back by gb_*_diag (synchronising). */
 typedef struct gb_diag {
@@ -128,6 +129,30 @@ int gb_direct_phi(gb_direct_t *h, const float *xm, float *phi, int64_t n,
 int gb_energy(gb_direct_t *h, const float *xm, const float *vel, int64_t n,
               float G, float eps2, double *out3, void *stream);
 
+/* The potential as an epilogue of the force pass: gb_direct_acc /
+ * gb_direct_kdk that also write phi (n floats, device) with the same sums
+ * gb_direct_phi returns, phi_i = sum_{j != i} m_j / sqrt(|x_j - x_i|^2 +
+ * eps2) (no G), of the positions the pass evaluated (for the KDK call: the
+ * positions after its last step; earlier steps run without it).  The pair
+ * loop forms m_j / |d| for the force anyway: the potential costs one FMA per
+ * pair side in the symmetric form and one add per pair in the per-target
+ * forms, plus the particle's own term, which the per-target fix-up
+ * subtracts.  Replaces the separate O(N^2) potential_energy pass
+ * (core/solvers/gravity.py:39-57) that the reference's callers run at every
+ * print (core/simulation.py:112-114, core/sim_controller.py:287-293). */
+int gb_direct_acc_phi(gb_direct_t *h, const float *xm, float *acc, float *phi,
+                      int64_t n, float G, float eps2, int flags, void *stream);
+int gb_direct_kdk_phi(gb_direct_t *h, float *xm, float *vel, float *acc,
+                      float *phi, int64_t n, float G, float eps2, float dt,
+                      int64_t nsteps, int flags, void *stream);
+
+/* gb_energy with phi given (from an epilogue above, or gb_bh_accel_phi):
+ * only the O(n) FP64 reductions run, KE = 1/2 sum m v^2, PE = -1/2 G sum m
+ * phi (core/solvers/gravity.py:29-57). */
+int gb_energy_phi(gb_direct_t *h, const float *xm, const float *vel,
+                  const float *phi, int64_t n, float G, double *out3,
+                  void *stream);
+
 /* FP64 oracle on the device for sampled targets: acc_out (nt x 3 doubles)
  * = compute_acc_direct (core/solvers/gravity.py:13-26) in float64 for the
  * particles listed in targets. */
@@ -159,9 +184,25 @@ int gb_bh_build(gb_bh_t *h, const float *xm, int64_t n, void *stream);
 
 /* Accelerations from the last build: _traverse (core/solvers/barnes_hut.py:
  * 180-217) with the same acceptance test and max_stack rule; pushes that the
- * rule skips are counted in gb_diag_t.stack_drops. */
+ * rule skips are counted in gb_diag_t.stack_drops (the reference drops them
+ * silently, :212).  With GB_CHECK in flags (or gb_bh_set_check on) the call
+ * waits for its stream and fails when failure counters grew since the last
+ * checked call on the handle (or the last diag reset): GB_ESTACK for pushes
+ * dropped by the max_stack rule or lost to the traversal stack's capacity,
+ * GB_EINVAL for non-finite positions or an inconsistent tree.  The results
+ * are written either way. */
 int gb_bh_accel(gb_bh_t *h, float *acc, float theta, float eps2, float G,
                 int max_stack, int flags, void *stream);
+
+/* gb_bh_accel that also writes the tree potential of every particle into
+ * phi (n floats, device, no G): the monopole terms m / sqrt(|d|^2 + eps2) of
+ * the nodes the traversal accepts for the force, the particle's own leaf
+ * excluded.  It approximates the potential_energy sum
+ * (core/solvers/gravity.py:47-55) within the tree's own error (the
+ * reference has no tree potential and always runs the O(N^2) sum). */
+int gb_bh_accel_phi(gb_bh_t *h, float *acc, float *phi, float theta,
+                    float eps2, float G, int max_stack, int flags,
+                    void *stream);
 
 /* build + accel: BarnesHut.compute (core/solvers/barnes_hut.py:242-259). */
 int gb_bh_compute(gb_bh_t *h, const float *xm, float *acc, int64_t n,
@@ -170,10 +211,25 @@ int gb_bh_compute(gb_bh_t *h, const float *xm, float *acc, int64_t n,
 
 /* nsteps KDK steps with tree forces, in place (Engine.step with the BH
  * solver, core/engine.py:101-116); kick and drift are fused into the first
- * tree stage and the closing kick into the traversal. */
+ * tree stage and the closing kick into the traversal.  With
+ * gb_bh_set_check on, the call waits for the steps and reports failures
+ * counted during them as gb_bh_accel does with GB_CHECK. */
 int gb_bh_kdk(gb_bh_t *h, float *xm, float *vel, float *acc, int64_t n,
               float theta, float eps2, float G, float dt, int64_t nsteps,
               int max_stack, void *stream);
+
+/* gb_bh_kdk whose last step also writes the tree potential of the final
+ * positions into phi (as gb_bh_accel_phi); the earlier steps run without
+ * it.  The step with the potential is captured as a graph of its own. */
+int gb_bh_kdk_phi(gb_bh_t *h, float *xm, float *vel, float *acc, float *phi,
+                  int64_t n, float theta, float eps2, float G, float dt,
+                  int64_t nsteps, int max_stack, void *stream);
+
+/* FP64 energies from a tree potential (gb_energy_phi on the tree handle's
+ * scratch): KE, PE = -1/2 G sum m phi, total into out3 (3 doubles). */
+int gb_bh_energy(gb_bh_t *h, const float *xm, const float *vel,
+                 const float *phi, int64_t n, float G, double *out3,
+                 void *stream);
 
 /* gb_bh_kdk replays one captured step as a CUDA graph (on = 1, default)
  * instead of launching its kernels one by one (on = 0).  The graph is
@@ -182,6 +238,14 @@ int gb_bh_kdk(gb_bh_t *h, float *xm, float *vel, float *acc, int64_t n,
  * at N = 3,000, 6% at 100,000, 1% at 1,000,000).  While stage timing
  * (gb_bh_timing) is on, the kernels are launched directly. */
 int gb_bh_set_graph(gb_bh_t *h, int on);
+
+/* Failure checks on every tree call of the handle (on = 1), as the GB_CHECK
+ * flag gives one call: gb_bh_accel, gb_bh_accel_ext, gb_bh_compute and
+ * gb_bh_kdk wait for their stream and return GB_ESTACK / GB_EINVAL when
+ * failure counters grew.  Off (0) by default: the calls stay asynchronous.
+ * No reference counterpart (its stack rule drops work silently,
+ * core/solvers/barnes_hut.py:212). */
+int gb_bh_set_check(gb_bh_t *h, int on);
 
 /* Copies one array of the last build, in the reference's layout, to device
  * memory dst: 0 codes (uint64[n], key order), 1 order (int32[n]), 2 left,
@@ -292,15 +356,18 @@ int gb_adjoint_set_variant(gb_direct_t *h, int variant);
  * an application whose memory pool owns the whole GPU, a plug-in running in
  * another framework's memory arena, or a loop that must never block
  * (cudaMalloc/cudaFree can synchronise the device).  Same arguments and
- * result as gb_direct_acc (flags GB_ACCUMULATE, GB_PLAIN_FP32); the caller
+ * result as gb_direct_acc; only the flags GB_ACCUMULATE and GB_PLAIN_FP32
+ * apply, and any other flag bit is rejected with GB_EINVAL.  The caller
  * still passes xm and acc.  Scratch is a 4 MiB file-scope device array that
  * every GPU loading the library keeps until the process exits; it holds the
  * partial sums of systems of at most GB_NOALLOC_MAX_N particles, and larger
  * n is rejected with GB_EINVAL.  The first call on each device looks up the
- * array's device address (with that device current); make that first call
- * before any stream capture.  All calls on a device share the array: calls
- * whose kernels overlap on the GPU (other streams or host threads) race and
- * must be ordered by the caller. */
+ * array's device address (with that device current) and caches it; make
+ * that first call before any stream capture.  A cudaDeviceReset of a device
+ * invalidates the cached address: do not call this entry point on a device
+ * after resetting it.  All calls on a device share the array: calls whose
+ * kernels overlap on the GPU (other streams or host threads) race and must
+ * be ordered by the caller. */
 #define GB_NOALLOC_MAX_N 65536
 #define GB_NOALLOC_MAX_DEVICES 64
 int gb_direct_acc_noalloc(const float *xm, float *acc, int64_t n, float G,

@@ -390,9 +390,10 @@ static int64_t traverse_one(const double *pos, const int32_t *order,
                             const double *nmin, const double *nmax,
                             const int32_t *left, const int32_t *right, int n,
                             int root, double theta2, double eps2, int max_stack,
-                            double G, int p, int32_t *stack, double *out) {
+                            double G, int p, int32_t *stack, double *out,
+                            double *phi_out) {
     const double px = pos[3 * p], py = pos[3 * p + 1], pz = pos[3 * p + 2];
-    double ax = 0.0, ay = 0.0, az = 0.0;
+    double ax = 0.0, ay = 0.0, az = 0.0, w = 0.0;
     int64_t dropped = 0;
     int sp = 0;
     stack[sp++] = root;
@@ -409,6 +410,7 @@ static int64_t traverse_one(const double *pos, const int32_t *order,
                 ax += s * dx;
                 ay += s * dy;
                 az += s * dz;
+                w += nmass[node] * inv;
             }
         } else {
             const int ii = node - n;
@@ -427,6 +429,7 @@ static int64_t traverse_one(const double *pos, const int32_t *order,
                 ax += s * dx;
                 ay += s * dy;
                 az += s * dz;
+                w += nmass[node] * inv;
             } else if (sp + 2 <= max_stack) {
                 stack[sp++] = left[ii];
                 stack[sp++] = right[ii];
@@ -438,17 +441,39 @@ static int64_t traverse_one(const double *pos, const int32_t *order,
     out[0] = ax;
     out[1] = ay;
     out[2] = az;
+    if (phi_out) *phi_out = w;
     return dropped;
 }
 
 /* Evaluate the traversal for the given particles (all when targets == NULL).
  * acc is indexed like targets (or by particle when targets == NULL). */
+/* phi (optional): the tree potential sum of each target, sum m / sqrt(r2)
+ * over the nodes the walk above accepts (the own leaf skipped, no G): the
+ * potential_energy sum (core/solvers/gravity.py:47-55) evaluated on the
+ * reference traversal's node set, the check for a device tree potential. */
+int64_t orc_traverse_phi(const double *pos, const int32_t *order, const double *com,
+                         const double *nmass, const double *nmin,
+                         const double *nmax, const int32_t *left,
+                         const int32_t *right, int n, double theta2, double eps2,
+                         int max_stack, double G, const int64_t *targets,
+                         int64_t nt, double *acc, double *phi);
+
 int64_t orc_traverse(const double *pos, const int32_t *order, const double *com,
                      const double *nmass, const double *nmin,
                      const double *nmax, const int32_t *left,
                      const int32_t *right, int n, double theta2, double eps2,
                      int max_stack, double G, const int64_t *targets,
                      int64_t nt, double *acc) {
+    return orc_traverse_phi(pos, order, com, nmass, nmin, nmax, left, right, n, theta2, eps2,
+                            max_stack, G, targets, nt, acc, NULL);
+}
+
+int64_t orc_traverse_phi(const double *pos, const int32_t *order, const double *com,
+                         const double *nmass, const double *nmin,
+                         const double *nmax, const int32_t *left,
+                         const int32_t *right, int n, double theta2, double eps2,
+                         int max_stack, double G, const int64_t *targets,
+                         int64_t nt, double *acc, double *phi) {
     int64_t dropped = 0;
     const int64_t count = targets ? nt : n;
 #pragma omp parallel reduction(+ : dropped)
@@ -459,7 +484,7 @@ int64_t orc_traverse(const double *pos, const int32_t *order, const double *com,
             const int p = targets ? (int)targets[t] : (int)t;
             dropped += traverse_one(pos, order, com, nmass, nmin, nmax, left,
                                     right, n, n, theta2, eps2, max_stack, G, p,
-                                    stack, acc + 3 * t);
+                                    stack, acc + 3 * t, phi ? phi + t : NULL);
         }
         free(stack);
     }

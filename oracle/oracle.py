@@ -18,6 +18,7 @@ Every function follows a reference function line by line:
 * ``build_radix``         core/solvers/barnes_hut.py:50-121
 * ``summaries``           core/solvers/barnes_hut.py:124-177
 * ``traverse``            core/solvers/barnes_hut.py:180-217
+* ``traverse_phi``        the same walk's monopole potential (gravity.py:47-55 on its node set)
 * ``bh_compute``          core/solvers/barnes_hut.py:242-259
 * ``analytic_acc``        core/living_galaxy_engine.py:124-151, core/gas_disk_engine.py:54-81
 * ``grav_ext_acc``        core/gas_disk_engine.py:20-51
@@ -88,6 +89,9 @@ def _declare(L):
     L.orc_traverse.argtypes = [P, P, P, P, P, P, P, P, I32, D, D, I32, D, P,
                                I64, P]
     L.orc_traverse.restype = I64
+    L.orc_traverse_phi.argtypes = [P, P, P, P, P, P, P, P, I32, D, D, I32, D, P,
+                                   I64, P, P]
+    L.orc_traverse_phi.restype = I64
 
 
 def _p(a: np.ndarray):
@@ -280,6 +284,31 @@ def traverse(pos, order, com, nmass, nmin, nmax, left, right, theta, eps2, G,
                                  float(theta) ** 2, eps2, max_stack, G,
                                  _p(t) if t is not None else None, nt, _p(acc))
     return acc, dropped
+
+
+def traverse_phi(pos, order, com, nmass, nmin, nmax, left, right, theta, eps2,
+                 max_stack=64, targets=None):
+    """The tree potential of the same walk as ``traverse``: for each target
+    sum m / sqrt(|d|^2 + eps2) over the accepted nodes and other leaves (no
+    G).  Returns (phi, dropped_pushes)."""
+    pos = _f64(pos, (-1, 3))
+    n = pos.shape[0]
+    args = [np.ascontiguousarray(order, dtype=np.int32), _f64(com, (-1, 3)),
+            _f64(nmass, (-1,)), _f64(nmin, (-1, 3)), _f64(nmax, (-1, 3)),
+            np.ascontiguousarray(left, dtype=np.int32),
+            np.ascontiguousarray(right, dtype=np.int32)]
+    if targets is None:
+        t, nt = None, n
+    else:
+        t = np.ascontiguousarray(targets, dtype=np.int64)
+        nt = t.size
+    acc = np.zeros((nt, 3))
+    phi = np.zeros(nt)
+    dropped = lib().orc_traverse_phi(_p(pos), *[_p(a) for a in args], n,
+                                     float(theta) ** 2, eps2, max_stack, 1.0,
+                                     _p(t) if t is not None else None, nt,
+                                     _p(acc), _p(phi))
+    return phi, dropped
 
 
 def bh_tree(pos, mass, bits=21):

@@ -62,11 +62,17 @@ def empty4(n: int, device) -> torch.Tensor:
 
 class FieldView:
     """Reference-style field access (``to_numpy`` / ``from_numpy``) over a
-    column slice of a float4 device buffer."""
+    column slice of a float4 device buffer; ``on_write`` (optional) is
+    called after every write through the view."""
 
-    def __init__(self, buf: torch.Tensor, cols):
+    def __init__(self, buf: torch.Tensor, cols, on_write=None):
         self._buf = buf
         self._cols = cols
+        self._on_write = on_write
+
+    def _written(self) -> None:
+        if self._on_write is not None:
+            self._on_write()
 
     @property
     def tensor(self) -> torch.Tensor:
@@ -82,6 +88,7 @@ class FieldView:
     def from_numpy(self, arr) -> None:
         src = torch.as_tensor(np.asarray(arr, dtype=np.float32)).reshape(self.shape)
         self._buf[:, self._cols] = src.to(self._buf.device)
+        self._written()
 
     def __array__(self, dtype=None, copy=None):
         a = self.to_numpy()
@@ -109,6 +116,7 @@ def write_rows(dst, values: torch.Tensor) -> None:
     n = values.shape[0]
     if isinstance(dst, FieldView):
         dst._buf[:n, dst._cols] = values.to(dst._buf.dtype)
+        dst._written()
     elif isinstance(dst, torch.Tensor):
         dst[:n] = values.to(device=dst.device, dtype=dst.dtype)
     elif isinstance(dst, np.ndarray):

@@ -29,6 +29,7 @@ GB_ACCUMULATE = 0x1
 GB_PLAIN_FP32 = 0x2
 GB_COUNT_WORK = 0x4
 GB_USE_GRAPH = 0x8
+GB_CHECK = 0x10
 
 _STATUS = {GB_EINVAL: "GB_EINVAL", GB_ENOMEM: "GB_ENOMEM", GB_ESTACK: "GB_ESTACK",
            GB_ETIMEOUT: "GB_ETIMEOUT", GB_ECUDA: "GB_ECUDA",
@@ -81,6 +82,9 @@ SIGNATURES = {
     "gb_direct_kdk": (I32, [P, P, P, P, I64, F32, F32, F32, I64, I32, P]),
     "gb_direct_phi": (I32, [P, P, P, I64, F32, I32, P]),
     "gb_energy": (I32, [P, P, P, I64, F32, F32, P, P]),
+    "gb_direct_acc_phi": (I32, [P, P, P, P, I64, F32, F32, I32, P]),
+    "gb_direct_kdk_phi": (I32, [P, P, P, P, P, I64, F32, F32, F32, I64, I32, P]),
+    "gb_energy_phi": (I32, [P, P, P, P, I64, F32, P, P]),
     "gb_direct_acc_fp64": (I32, [P, I64, P, I64, F64, F64, P, P]),
     "gb_direct_diag": (I32, [P, ctypes.POINTER(Diag), I32]),
     "gb_direct_launch_count": (ctypes.c_uint64, [P]),
@@ -92,6 +96,9 @@ SIGNATURES = {
     "gb_bh_accel": (I32, [P, P, F32, F32, F32, I32, I32, P]),
     "gb_bh_compute": (I32, [P, P, P, I64, F32, F32, F32, I32, I32, P]),
     "gb_bh_kdk": (I32, [P, P, P, P, I64, F32, F32, F32, F32, I64, I32, P]),
+    "gb_bh_accel_phi": (I32, [P, P, P, F32, F32, F32, I32, I32, P]),
+    "gb_bh_kdk_phi": (I32, [P, P, P, P, P, I64, F32, F32, F32, F32, I64, I32, P]),
+    "gb_bh_energy": (I32, [P, P, P, P, I64, F32, P, P]),
     "gb_bh_export": (I32, [P, I32, P, P]),
     "gb_bh_diag": (I32, [P, ctypes.POINTER(Diag), I32]),
     "gb_bh_timing": (I32, [P, I32]),
@@ -113,6 +120,7 @@ SIGNATURES = {
     "gb_direct_acc_ext": (I32, [P, P, P, I64, F32, F32, P, I32, P]),
     "gb_bh_accel_ext": (I32, [P, P, F32, F32, F32, I32, P, I32, P]),
     "gb_bh_set_graph": (I32, [P, I32]),
+    "gb_bh_set_check": (I32, [P, I32]),
     "gb_kick": (I32, [P, P, I64, F32, P]),
     "gb_drift": (I32, [P, P, I64, F32, P]),
     "gb_grid_create": (I32, [ctypes.POINTER(P), I64, F64]),

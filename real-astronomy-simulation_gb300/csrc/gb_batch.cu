@@ -82,10 +82,10 @@ batch_force_kernel(BatchArgs a) {
             __syncthreads();
             src[threadIdx.x] = s4;
             __syncthreads();
-            float AX[K], AY[K], AZ[K];
+            float AX[K], AY[K], AZ[K], PW[K];
 #pragma unroll
-            for (int q = 0; q < K; ++q) AX[q] = AY[q] = AZ[q] = 0.f;
-            interact_chunk<K, JU>(src, X, Y, Z, AX, AY, AZ, a.eps2);
+            for (int q = 0; q < K; ++q) AX[q] = AY[q] = AZ[q] = PW[q] = 0.f;
+            interact_chunk<K, JU>(src, X, Y, Z, AX, AY, AZ, PW, a.eps2);
 #pragma unroll
             for (int q = 0; q < K; ++q) {
                 if (KAHAN) {

@@ -361,6 +361,7 @@ struct TravArgs {
     const uint32_t *__restrict__ order;
     float4 *acc;
     float4 *vel;
+    float *phi;  // PHI kernels: the tree potential sum of every particle (no G)
     int n;
     float theta2, eps2, G, h;
     int max_stack;
@@ -370,9 +371,9 @@ struct TravArgs {
 };
 
 struct Lane {
-    float px, py, pz, ax, ay, az;
-    f2 PX, PY, PZ;  // (p, p) pairs
-    f2 AX, AY, AZ;  // accumulators for (left, right) children
+    float px, py, pz, ax, ay, az, pw;
+    f2 PX, PY, PZ;      // (p, p) pairs
+    f2 AX, AY, AZ, PW;  // accumulators for (left, right) children
     unsigned n_int, n_test, drops;
 };
 
@@ -382,8 +383,10 @@ struct Lane {
 // internal nodes.  An accepted child adds its monopole; the lane's own leaf
 // (which the reference skips, :198) sits exactly at the lane's position, so
 // its term is d * (...) = +0 and needs no test.  A rejected (internal) child
-// is opened.  Returns "open".
-template <bool COUNT>
+// is opened.  Returns "open".  PHI: an accepted child other than the lane's
+// own leaf also adds its monopole potential m / |d| (|d|^2 = d.d + eps^2),
+// the tree form of the potential_energy sum (core/solvers/gravity.py:47-55).
+template <bool COUNT, bool PHI>
 __device__ __forceinline__ bool visit_child(Lane &L, const TravArgs &a, float4 q, float size2, int id, int s,
                                             bool in) {
     const float dx = q.x - L.px, dy = q.y - L.py, dz = q.z - L.pz;
@@ -395,6 +398,7 @@ __device__ __forceinline__ bool visit_child(Lane &L, const TravArgs &a, float4 q
     L.ax = __fmaf_rn(sc, dx, L.ax);
     L.ay = __fmaf_rn(sc, dy, L.ay);
     L.az = __fmaf_rn(sc, dz, L.az);
+    if (PHI) L.pw += (add && id != s) ? q.w * inv : 0.f;
     if (COUNT) {
         L.n_int += (add && id != s) ? 1u : 0u;
         L.n_test += (in && size2 >= 0.f) ? 1u : 0u;
@@ -404,8 +408,8 @@ __device__ __forceinline__ bool visit_child(Lane &L, const TravArgs &a, float4 q
 
 // Both children of an expanded node for one lane, on packed (left, right)
 // pairs: the same test and monopole as visit_child, two children per
-// instruction.  Sets openL / openR.
-template <bool COUNT>
+// instruction.  Sets openL / openR.  PHI as in visit_child.
+template <bool COUNT, bool PHI>
 __device__ __forceinline__ void visit_pair(Lane &L, const TravArgs &a, ulonglong2 A, ulonglong2 B, float4 C, int s,
                                            bool in, f2 E2, f2 TH2, bool &openL, bool &openR) {
     const f2 dx = sub2(A.x, L.PX), dy = sub2(A.y, L.PY), dz = sub2(B.x, L.PZ);
@@ -418,13 +422,20 @@ __device__ __forceinline__ void visit_pair(Lane &L, const TravArgs &a, ulonglong
     unpack2(t, tL, tR);
     const bool accL = C.x < tL, accR = C.y < tR;
     const f2 inv = pack2(rsqrt_approx(r2L), rsqrt_approx(r2R));
-    const f2 sc = mul2(mul2(B.y, inv), mul2(inv, inv));
+    const f2 mi = mul2(B.y, inv);
+    const f2 sc = mul2(mi, mul2(inv, inv));
     float scL, scR;
     unpack2(sc, scL, scR);
     const f2 scm = pack2((in && accL) ? scL : 0.f, (in && accR) ? scR : 0.f);
     L.AX = fma2(scm, dx, L.AX);
     L.AY = fma2(scm, dy, L.AY);
     L.AZ = fma2(scm, dz, L.AZ);
+    if (PHI) {
+        float miL, miR;
+        unpack2(mi, miL, miR);
+        L.PW = add2(L.PW, pack2((in && accL && __float_as_int(C.z) != s) ? miL : 0.f,
+                                (in && accR && __float_as_int(C.w) != s) ? miR : 0.f));
+    }
     if (COUNT) {
         L.n_int += (in && accL && __float_as_int(C.z) != s) ? 1u : 0u;
         L.n_int += (in && accR && __float_as_int(C.w) != s) ? 1u : 0u;
@@ -455,7 +466,7 @@ __device__ __forceinline__ bool apply_room(Lane &L, bool open, int sp, int max_s
 // reference's per-particle stack when a node is popped, depends only on the
 // node's path (one pending left sibling per right turn), so it travels with
 // the node.
-template <bool KDK, bool COUNT, int TPL>
+template <bool KDK, bool COUNT, int TPL, bool PHI>
 __global__ void __launch_bounds__(TRAV_WARPS * 32)
 bh_traverse_kernel(TravArgs a) {
     __shared__ int4 stk[TRAV_WARPS][TRAV_STACK];
@@ -475,11 +486,11 @@ bh_traverse_kernel(TravArgs a) {
             const float4 p = __ldg(a.leaf + s[q]);
             L[q].px = p.x; L[q].py = p.y; L[q].pz = p.z;
         }
-        L[q].ax = L[q].ay = L[q].az = 0.f;
+        L[q].ax = L[q].ay = L[q].az = L[q].pw = 0.f;
         L[q].PX = pack2(L[q].px, L[q].px);
         L[q].PY = pack2(L[q].py, L[q].py);
         L[q].PZ = pack2(L[q].pz, L[q].pz);
-        L[q].AX = L[q].AY = L[q].AZ = 0ull;
+        L[q].AX = L[q].AY = L[q].AZ = L[q].PW = 0ull;
         L[q].n_int = L[q].n_test = L[q].drops = 0;
     }
     const f2 E2 = pack2(a.eps2, a.eps2), TH2 = pack2(a.theta2, a.theta2);
@@ -495,7 +506,7 @@ bh_traverse_kernel(TravArgs a) {
         const float4 R0 = __ldg(a.root), R1 = __ldg(a.root + 1);
 #pragma unroll
         for (int q = 0; q < TPL; ++q) {
-            const bool want = apply_room(L[q], visit_child<COUNT>(L[q], a, R0, R1.x, n, s[q], valid[q]), 0,
+            const bool want = apply_room(L[q], visit_child<COUNT, PHI>(L[q], a, R0, R1.x, n, s[q], valid[q]), 0,
                                          a.max_stack);
             m[q] = __ballot_sync(0xffffffffu, want);
             any |= m[q];
@@ -521,7 +532,7 @@ bh_traverse_kernel(TravArgs a) {
             for (int q = 0; q < TPL; ++q) {
                 const bool in = (m[q] >> lane) & 1u;
                 bool wantR, wantL;
-                visit_pair<COUNT>(L[q], a, A, B, C, s[q], in, E2, TH2, wantL, wantR);
+                visit_pair<COUNT, PHI>(L[q], a, A, B, C, s[q], in, E2, TH2, wantL, wantR);
                 if (!room2) {
                     wantR = apply_room(L[q], wantR, sp + 1, a.max_stack);
                     wantL = apply_room(L[q], wantL, sp, a.max_stack);
@@ -614,6 +625,11 @@ bh_traverse_kernel(TravArgs a) {
         float gx = a.G * (L[q].ax + (xl + xr)), gy = a.G * (L[q].ay + (yl + yr)),
               gz = a.G * (L[q].az + (zl + zr));
         if (a.pot.on) ext_acc_add(a.pot, L[q].px, L[q].py, L[q].pz, gx, gy, gz);
+        if (PHI) {
+            float wl, wr;
+            unpack2(L[q].PW, wl, wr);
+            a.phi[p] = L[q].pw + (wl + wr);
+        }
         if (KDK) {
             const float4 vh = a.vel[p];
             a.vel[p] = make_float4(kick(vh.x, gx, a.h), kick(vh.y, gy, a.h), kick(vh.z, gz, a.h), vh.w);
@@ -648,7 +664,7 @@ constexpr int LANE_MAX_STACK = 127;
 // between 100k and 300k particles on a disk).
 constexpr int64_t LANE_AUTO_N = 131072;
 
-template <bool KDK, bool COUNT>
+template <bool KDK, bool COUNT, bool PHI>
 __global__ void __launch_bounds__(LANE_THREADS)
 bh_traverse_lane_kernel(TravArgs a) {
     extern __shared__ int lstk[];  // [max_stack][LANE_THREADS]
@@ -662,11 +678,11 @@ bh_traverse_lane_kernel(TravArgs a) {
         const float4 p = __ldg(a.leaf + s);
         L.px = p.x; L.py = p.y; L.pz = p.z;
     }
-    L.ax = L.ay = L.az = 0.f;
+    L.ax = L.ay = L.az = L.pw = 0.f;
     L.PX = pack2(L.px, L.px);
     L.PY = pack2(L.py, L.py);
     L.PZ = pack2(L.pz, L.pz);
-    L.AX = L.AY = L.AZ = 0ull;
+    L.AX = L.AY = L.AZ = L.PW = 0ull;
     L.n_int = L.n_test = L.drops = 0;
     const f2 E2 = pack2(a.eps2, a.eps2), TH2 = pack2(a.theta2, a.theta2);
     unsigned overflow = 0, bad = 0, reads = 0;
@@ -675,7 +691,7 @@ bh_traverse_lane_kernel(TravArgs a) {
     if (valid && n >= 2) {
         // The root is popped first, with an empty stack (d = 0).
         const float4 R0 = __ldg(a.root), R1 = __ldg(a.root + 1);
-        active = apply_room(L, visit_child<COUNT>(L, a, R0, R1.x, n, s, true), 0, a.max_stack);
+        active = apply_room(L, visit_child<COUNT, PHI>(L, a, R0, R1.x, n, s, true), 0, a.max_stack);
     }
     for (;;) {
         if (!active) {
@@ -694,7 +710,7 @@ bh_traverse_lane_kernel(TravArgs a) {
         const float4 C = __ldg(a.inode + 3 * k + 2);
         if (COUNT) ++reads;
         bool wantL, wantR;
-        visit_pair<COUNT>(L, a, A, B, C, s, true, E2, TH2, wantL, wantR);
+        visit_pair<COUNT, PHI>(L, a, A, B, C, s, true, E2, TH2, wantL, wantR);
         if (d + 3 > a.max_stack) {  // the rule only bites near max_stack
             wantR = apply_room(L, wantR, d + 1, a.max_stack);
             wantL = apply_room(L, wantL, d, a.max_stack);
@@ -755,6 +771,11 @@ bh_traverse_lane_kernel(TravArgs a) {
     unpack2(L.AZ, zl, zr);
     float gx = a.G * (L.ax + (xl + xr)), gy = a.G * (L.ay + (yl + yr)), gz = a.G * (L.az + (zl + zr));
     if (a.pot.on) ext_acc_add(a.pot, L.px, L.py, L.pz, gx, gy, gz);
+    if (PHI) {
+        float wl, wr;
+        unpack2(L.PW, wl, wr);
+        a.phi[p] = L.pw + (wl + wr);
+    }
     if (KDK) {
         const float4 vh = a.vel[p];
         a.vel[p] = make_float4(kick(vh.x, gx, a.h), kick(vh.y, gy, a.h), kick(vh.z, gz, a.h), vh.w);
@@ -874,22 +895,29 @@ struct gb_bh {
     int tpl;            // traversal shape: -1 by n (default), 0 per lane, 1 or 2 targets per lane
     // One KDK step captured as a CUDA graph (gb_bh_kdk), replayed per step
     // on the handle's own stream and joined to the caller's by events.
+    // gexec[0]: a plain step; gexec[1]: a step that also writes the tree
+    // potential (gb_bh_kdk_phi); each captured again when its key changes.
     int use_graph;
     cudaStream_t gstream;
     cudaEvent_t gev_in, gev_out;
-    cudaGraphExec_t gexec;
-    bool has_graph;
+    cudaGraphExec_t gexec[2];
     struct Key {
-        const void *xm, *vel, *acc;
+        const void *xm, *vel, *acc, *phi;
         int64_t n;
         float theta, eps2, G, dt;
         int max_stack, tpl;
         bool operator==(const Key &o) const {
-            return xm == o.xm && vel == o.vel && acc == o.acc && n == o.n && theta == o.theta && eps2 == o.eps2 &&
-                   G == o.G && dt == o.dt && max_stack == o.max_stack && tpl == o.tpl;
+            return xm == o.xm && vel == o.vel && acc == o.acc && phi == o.phi && n == o.n && theta == o.theta &&
+                   eps2 == o.eps2 && G == o.G && dt == o.dt && max_stack == o.max_stack && tpl == o.tpl;
         }
-    } gkey;
-    uint64_t graph_launches;  // kernels in the captured step
+    } gkey[2];
+    uint64_t graph_launches[2];  // kernels in each captured step
+    double2 *epart;              // energy block partials (gb_bh_energy)
+    int epart_cap;
+    // Failure checks (GB_CHECK, gb_bh_set_check): the failure counters as
+    // read by the last checked call (or zero after a diag reset).
+    int check;
+    unsigned long long seen[4];
 };
 
 static void mark(gb_bh_t *h, int step_slot, int stage, cudaStream_t s) {
@@ -903,10 +931,11 @@ extern "C" int gb_bh_destroy(gb_bh_t *h) {
     if (!h) return GB_OK;
     void *ptrs[] = {h->keys[0], h->keys[1], h->vals[0], h->vals[1], h->hist, h->bbox_part, h->ticket,
                     h->prm, h->leaf, h->child, h->parent, h->arrivals, h->sums, h->bmin, h->bmax,
-                    h->inode, h->root, h->totals, h->diag};
+                    h->inode, h->root, h->totals, h->diag, h->epart};
     for (void *p : ptrs)
         if (p) cudaFree(p);
-    if (h->has_graph) cudaGraphExecDestroy(h->gexec);
+    for (auto &g : h->gexec)
+        if (g) cudaGraphExecDestroy(g);
     if (h->gev_in) cudaEventDestroy(h->gev_in);
     if (h->gev_out) cudaEventDestroy(h->gev_out);
     if (h->gstream) cudaStreamDestroy(h->gstream);
@@ -930,10 +959,14 @@ extern "C" int gb_bh_create(gb_bh_t **out, int64_t n_max, int key_bits) {
     h->use_graph = 1;
     {
         const int smem_max = (int)sizeof(int) * LANE_MAX_STACK * LANE_THREADS;
-        const void *lk[] = {(const void *)bh_traverse_lane_kernel<false, false>,
-                            (const void *)bh_traverse_lane_kernel<false, true>,
-                            (const void *)bh_traverse_lane_kernel<true, false>,
-                            (const void *)bh_traverse_lane_kernel<true, true>};
+        const void *lk[] = {(const void *)bh_traverse_lane_kernel<false, false, false>,
+                            (const void *)bh_traverse_lane_kernel<false, true, false>,
+                            (const void *)bh_traverse_lane_kernel<true, false, false>,
+                            (const void *)bh_traverse_lane_kernel<true, true, false>,
+                            (const void *)bh_traverse_lane_kernel<false, false, true>,
+                            (const void *)bh_traverse_lane_kernel<false, true, true>,
+                            (const void *)bh_traverse_lane_kernel<true, false, true>,
+                            (const void *)bh_traverse_lane_kernel<true, true, true>};
         for (const void *f : lk) {
             if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max) != cudaSuccess) {
                 delete h;
@@ -970,6 +1003,8 @@ extern "C" int gb_bh_create(gb_bh_t **out, int64_t n_max, int key_bits) {
     A((void **)&h->root, sizeof(float4) * 2);
     A((void **)&h->totals, sizeof(uint32_t) * RS_BINS);
     A((void **)&h->diag, sizeof(unsigned long long) * DIAG_COUNT);
+    h->epart_cap = 4 * h->sms;
+    A((void **)&h->epart, sizeof(double2) * h->epart_cap);
     if (!ok) {
         gb_bh_destroy(h);
         return fail(GB_ENOMEM, "gb_bh_create: device allocation failed for n_max=%lld", (long long)n_max);
@@ -1047,8 +1082,50 @@ static int check_ptr(const void *p, const char *name) {
     return GB_OK;
 }
 
-static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float theta, float eps2, float G, float dt, int max_stack,
-                    int flags, bool kdk, cudaStream_t s, int slot, const ExtPot &pot = ExtPot{}) {
+template <bool KDK, bool COUNT, bool PHI>
+static void launch_lane(unsigned grid, size_t smem, const TravArgs &a, cudaStream_t s) {
+    bh_traverse_lane_kernel<KDK, COUNT, PHI><<<grid, LANE_THREADS, smem, s>>>(a);
+}
+
+template <bool KDK, bool COUNT, bool PHI>
+static void launch_warp(int tpl, unsigned grid, const TravArgs &a, cudaStream_t s) {
+    if (tpl == 2) bh_traverse_kernel<KDK, COUNT, 2, PHI><<<grid, TRAV_WARPS * 32, 0, s>>>(a);
+    else bh_traverse_kernel<KDK, COUNT, 1, PHI><<<grid, TRAV_WARPS * 32, 0, s>>>(a);
+}
+
+// Dispatches L<KDK, COUNT, PHI>::go(args...) on run-time flags.
+template <template <bool, bool, bool> class L, typename... Args>
+static void dispatch3(bool kdk, bool count, bool phi, Args... args) {
+    const int sel = (kdk ? 4 : 0) + (count ? 2 : 0) + (phi ? 1 : 0);
+    switch (sel) {
+        case 0: L<false, false, false>::go(args...); break;
+        case 1: L<false, false, true>::go(args...); break;
+        case 2: L<false, true, false>::go(args...); break;
+        case 3: L<false, true, true>::go(args...); break;
+        case 4: L<true, false, false>::go(args...); break;
+        case 5: L<true, false, true>::go(args...); break;
+        case 6: L<true, true, false>::go(args...); break;
+        default: L<true, true, true>::go(args...); break;
+    }
+}
+template <bool KDK, bool COUNT, bool PHI>
+struct LaneLaunch {
+    static void go(unsigned grid, size_t smem, const TravArgs *a, cudaStream_t s) {
+        launch_lane<KDK, COUNT, PHI>(grid, smem, *a, s);
+    }
+};
+template <bool KDK, bool COUNT, bool PHI>
+struct WarpLaunch {
+    static void go(int tpl, unsigned grid, const TravArgs *a, cudaStream_t s) {
+        launch_warp<KDK, COUNT, PHI>(tpl, grid, *a, s);
+    }
+};
+
+// The traversal of the last build: accelerations into acc (KDK: the
+// closing kick into vel too) and, when phi is not NULL, the tree potential
+// sums into phi.
+static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float *phi, float theta, float eps2, float G, float dt,
+                    int max_stack, int flags, bool kdk, cudaStream_t s, int slot, const ExtPot &pot = ExtPot{}) {
     const int64_t n = h->n;
     if (n <= 0) return GB_OK;
     TravArgs a;
@@ -1058,6 +1135,7 @@ static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float theta, float eps
     a.order = h->vals[h->cur];
     a.acc = acc;
     a.vel = vel;
+    a.phi = phi;
     a.n = (int)n;
     a.theta2 = theta * theta;
     a.eps2 = eps2;
@@ -1075,35 +1153,39 @@ static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float theta, float eps
     if (shape == 0 && max_stack <= LANE_MAX_STACK && n - 1 <= ((int64_t)1 << LANE_KBITS)) {
         const unsigned grid = (unsigned)((n + LANE_THREADS - 1) / LANE_THREADS);
         const size_t smem = sizeof(int) * (size_t)std::max(max_stack, 1) * LANE_THREADS;
-        const int sel = (kdk ? 2 : 0) + (count ? 1 : 0);
-        switch (sel) {
-            case 0: bh_traverse_lane_kernel<false, false><<<grid, LANE_THREADS, smem, s>>>(a); break;
-            case 1: bh_traverse_lane_kernel<false, true><<<grid, LANE_THREADS, smem, s>>>(a); break;
-            case 2: bh_traverse_lane_kernel<true, false><<<grid, LANE_THREADS, smem, s>>>(a); break;
-            default: bh_traverse_lane_kernel<true, true><<<grid, LANE_THREADS, smem, s>>>(a); break;
-        }
-        GB_CUDA_TRY(cudaGetLastError());
-        mark(h, slot, 5, s);
-        h->launches += 1;
-        return GB_OK;
-    }
-    const int tpl = shape == 2 ? 2 : 1;
-    const int64_t warps = (n + 32 * tpl - 1) / (32 * tpl);
-    const unsigned grid = (unsigned)((warps + TRAV_WARPS - 1) / TRAV_WARPS);
-    const int sel = (kdk ? 4 : 0) + (count ? 2 : 0) + (tpl == 2 ? 1 : 0);
-    switch (sel) {
-        case 0: bh_traverse_kernel<false, false, 1><<<grid, TRAV_WARPS * 32, 0, s>>>(a); break;
-        case 1: bh_traverse_kernel<false, false, 2><<<grid, TRAV_WARPS * 32, 0, s>>>(a); break;
-        case 2: bh_traverse_kernel<false, true, 1><<<grid, TRAV_WARPS * 32, 0, s>>>(a); break;
-        case 3: bh_traverse_kernel<false, true, 2><<<grid, TRAV_WARPS * 32, 0, s>>>(a); break;
-        case 4: bh_traverse_kernel<true, false, 1><<<grid, TRAV_WARPS * 32, 0, s>>>(a); break;
-        case 5: bh_traverse_kernel<true, false, 2><<<grid, TRAV_WARPS * 32, 0, s>>>(a); break;
-        case 6: bh_traverse_kernel<true, true, 1><<<grid, TRAV_WARPS * 32, 0, s>>>(a); break;
-        default: bh_traverse_kernel<true, true, 2><<<grid, TRAV_WARPS * 32, 0, s>>>(a); break;
+        dispatch3<LaneLaunch>(kdk, count, phi != nullptr, grid, smem, &a, s);
+    } else {
+        const int tpl = shape == 2 ? 2 : 1;
+        const int64_t warps = (n + 32 * tpl - 1) / (32 * tpl);
+        const unsigned grid = (unsigned)((warps + TRAV_WARPS - 1) / TRAV_WARPS);
+        dispatch3<WarpLaunch>(kdk, count, phi != nullptr, tpl, grid, &a, s);
     }
     GB_CUDA_TRY(cudaGetLastError());
     mark(h, slot, 5, s);
     h->launches += 1;
+    return GB_OK;
+}
+
+// Synchronises `s` and compares the failure counters (stack drops, stack
+// overflow, non-finite positions, bad tree) with the values the last check
+// saw: anything counted since then fails the call.  Non-finite positions
+// and index guards give GB_EINVAL, dropped or overflowed pushes GB_ESTACK.
+static int check_failures(gb_bh_t *h, cudaStream_t s, const char *call) {
+    unsigned long long d[4];
+    GB_CUDA_TRY(cudaMemcpyAsync(d, h->diag, sizeof(d), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    unsigned long long inc[4];
+    for (int k = 0; k < 4; ++k) {
+        inc[k] = d[k] - h->seen[k];
+        h->seen[k] = d[k];
+    }
+    if (inc[DIAG_NONFINITE])
+        return fail(GB_EINVAL, "%s: %llu non-finite particle positions", call, inc[DIAG_NONFINITE]);
+    if (inc[DIAG_BAD_TREE])
+        return fail(GB_EINVAL, "%s: inconsistent tree (%llu index guards taken)", call, inc[DIAG_BAD_TREE]);
+    if (inc[DIAG_STACK_DROPS] || inc[DIAG_STACK_OVERFLOW])
+        return fail(GB_ESTACK, "%s: the max_stack rule dropped %llu pushes; %llu overflowed the traversal stack",
+                    call, inc[DIAG_STACK_DROPS], inc[DIAG_STACK_OVERFLOW]);
     return GB_OK;
 }
 
@@ -1132,8 +1214,24 @@ extern "C" int gb_bh_accel(gb_bh_t *h, float *acc, float theta, float eps2, floa
     if (h->n == 0) return GB_OK;
     GB_TRY(check_ptr(acc, "acc"));
     GB_TRY(check_params(theta, eps2, max_stack));
-    return traverse(h, (float4 *)acc, nullptr, theta, eps2, G, 0.f, max_stack, flags, false, (cudaStream_t)stream,
-                    h->pending_slot);
+    GB_TRY(traverse(h, (float4 *)acc, nullptr, nullptr, theta, eps2, G, 0.f, max_stack, flags, false,
+                    (cudaStream_t)stream, h->pending_slot));
+    if ((flags & GB_CHECK) || h->check) return check_failures(h, (cudaStream_t)stream, "gb_bh_accel");
+    return GB_OK;
+}
+
+extern "C" int gb_bh_accel_phi(gb_bh_t *h, float *acc, float *phi, float theta, float eps2, float G, int max_stack,
+                               int flags, void *stream) {
+    if (!h) return fail(GB_EINVAL, "handle is NULL");
+    if (h->n < 0) return fail(GB_ENOTREADY, "gb_bh_accel_phi before gb_bh_build");
+    if (h->n == 0) return GB_OK;
+    GB_TRY(check_ptr(acc, "acc"));
+    if (!phi) return fail(GB_EINVAL, "phi is NULL");
+    GB_TRY(check_params(theta, eps2, max_stack));
+    GB_TRY(traverse(h, (float4 *)acc, nullptr, phi, theta, eps2, G, 0.f, max_stack, flags, false,
+                    (cudaStream_t)stream, h->pending_slot));
+    if ((flags & GB_CHECK) || h->check) return check_failures(h, (cudaStream_t)stream, "gb_bh_accel_phi");
+    return GB_OK;
 }
 
 extern "C" int gb_bh_accel_ext(gb_bh_t *h, float *acc, float theta, float eps2, float G, int max_stack,
@@ -1145,8 +1243,10 @@ extern "C" int gb_bh_accel_ext(gb_bh_t *h, float *acc, float theta, float eps2, 
     if (h->n == 0) return GB_OK;
     GB_TRY(check_ptr(acc, "acc"));
     GB_TRY(check_params(theta, eps2, max_stack));
-    return traverse(h, (float4 *)acc, nullptr, theta, eps2, G, 0.f, max_stack, flags, false, (cudaStream_t)stream,
-                    h->pending_slot, ep);
+    GB_TRY(traverse(h, (float4 *)acc, nullptr, nullptr, theta, eps2, G, 0.f, max_stack, flags, false,
+                    (cudaStream_t)stream, h->pending_slot, ep));
+    if ((flags & GB_CHECK) || h->check) return check_failures(h, (cudaStream_t)stream, "gb_bh_accel_ext");
+    return GB_OK;
 }
 
 extern "C" int gb_bh_compute(gb_bh_t *h, const float *xm, float *acc, int64_t n, float theta, float eps2, float G,
@@ -1161,16 +1261,47 @@ extern "C" int gb_bh_compute(gb_bh_t *h, const float *xm, float *acc, int64_t n,
 }
 
 // One KDK step: tree build with the fused kick and drift, then the traversal
-// with the closing kick.
-static int kdk_step(gb_bh_t *h, float4 *xm, float4 *vel, float4 *acc, int64_t n, float theta, float eps2, float G,
-                    float dt, int max_stack, cudaStream_t s) {
+// with the closing kick (and the tree potential of the new positions when
+// phi is not NULL).
+static int kdk_step(gb_bh_t *h, float4 *xm, float4 *vel, float4 *acc, float *phi, int64_t n, float theta,
+                    float eps2, float G, float dt, int max_stack, cudaStream_t s) {
     const int slot = next_slot(h);
     GB_TRY(build_any(h, xm, vel, acc, n, dt, true, s, slot));
-    return traverse(h, acc, vel, theta, eps2, G, dt, max_stack, 0, true, s, slot);
+    return traverse(h, acc, vel, phi, theta, eps2, G, dt, max_stack, 0, true, s, slot);
 }
 
-extern "C" int gb_bh_kdk(gb_bh_t *h, float *xm, float *vel, float *acc, int64_t n, float theta, float eps2, float G,
-                         float dt, int64_t nsteps, int max_stack, void *stream) {
+// Graph slot g (0 plain, 1 with the potential) holds one captured step with
+// this key, captured again when the key changed.
+static int ensure_graph(gb_bh_t *h, int g, const gb_bh::Key &key, float4 *x, float4 *v, float4 *a, float *phi,
+                        int64_t n, float theta, float eps2, float G, float dt, int max_stack) {
+    if (h->gexec[g] && h->gkey[g] == key) return GB_OK;
+    if (h->gexec[g]) cudaGraphExecDestroy(h->gexec[g]);
+    h->gexec[g] = nullptr;
+    GB_CUDA_TRY(cudaStreamBeginCapture(h->gstream, cudaStreamCaptureModeThreadLocal));
+    const uint64_t l0 = h->launches;
+    const int st = kdk_step(h, x, v, a, phi, n, theta, eps2, G, dt, max_stack, h->gstream);
+    h->graph_launches[g] = h->launches - l0;
+    h->launches = l0;
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(h->gstream, &graph);
+    if (st != GB_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return st;
+    }
+    if (e != cudaSuccess) return fail(GB_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+    const cudaError_t ei = cudaGraphInstantiate(&h->gexec[g], graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+        h->gexec[g] = nullptr;
+        return fail(GB_ECUDA, "graph instantiate: %s", cudaGetErrorString(ei));
+    }
+    h->gkey[g] = key;
+    return GB_OK;
+}
+
+// nsteps KDK steps; with phi, the last step also writes the tree potential.
+static int bh_kdk_impl(gb_bh_t *h, float *xm, float *vel, float *acc, float *phi, int64_t n, float theta, float eps2,
+                       float G, float dt, int64_t nsteps, int max_stack, void *stream, const char *call) {
     GB_TRY(check_bh(h, n));
     if (nsteps < 0) return fail(GB_EINVAL, "nsteps < 0");
     if (n == 0 || nsteps == 0) return GB_OK;
@@ -1181,45 +1312,62 @@ extern "C" int gb_bh_kdk(gb_bh_t *h, float *xm, float *vel, float *acc, int64_t 
     cudaStream_t s = (cudaStream_t)stream;
     float4 *x = (float4 *)xm, *v = (float4 *)vel, *a = (float4 *)acc;
     if (!h->use_graph || h->timing) {
-        for (int64_t k = 0; k < nsteps; ++k) GB_TRY(kdk_step(h, x, v, a, n, theta, eps2, G, dt, max_stack, s));
-        return GB_OK;
+        for (int64_t k = 0; k < nsteps; ++k)
+            GB_TRY(kdk_step(h, x, v, a, k == nsteps - 1 ? phi : nullptr, n, theta, eps2, G, dt, max_stack, s));
+        return h->check ? check_failures(h, s, call) : GB_OK;
     }
-    const gb_bh::Key key{xm, vel, acc, n, theta, eps2, G, dt, max_stack, h->tpl};
-    if (!h->has_graph || !(h->gkey == key)) {
-        if (h->has_graph) {
-            cudaGraphExecDestroy(h->gexec);
-            h->has_graph = false;
-        }
-        if (!h->gstream) {
-            GB_CUDA_TRY(cudaStreamCreateWithFlags(&h->gstream, cudaStreamNonBlocking));
-            GB_CUDA_TRY(cudaEventCreateWithFlags(&h->gev_in, cudaEventDisableTiming));
-            GB_CUDA_TRY(cudaEventCreateWithFlags(&h->gev_out, cudaEventDisableTiming));
-        }
-        GB_CUDA_TRY(cudaStreamBeginCapture(h->gstream, cudaStreamCaptureModeThreadLocal));
-        const uint64_t l0 = h->launches;
-        const int st = kdk_step(h, x, v, a, n, theta, eps2, G, dt, max_stack, h->gstream);
-        h->graph_launches = h->launches - l0;
-        h->launches = l0;
-        cudaGraph_t graph = nullptr;
-        const cudaError_t e = cudaStreamEndCapture(h->gstream, &graph);
-        if (st != GB_OK) {
-            if (graph) cudaGraphDestroy(graph);
-            return st;
-        }
-        if (e != cudaSuccess) return fail(GB_ECUDA, "graph capture: %s", cudaGetErrorString(e));
-        const cudaError_t ei = cudaGraphInstantiate(&h->gexec, graph, 0);
-        cudaGraphDestroy(graph);
-        if (ei != cudaSuccess) return fail(GB_ECUDA, "graph instantiate: %s", cudaGetErrorString(ei));
-        h->has_graph = true;
-        h->gkey = key;
+    if (!h->gstream) {
+        GB_CUDA_TRY(cudaStreamCreateWithFlags(&h->gstream, cudaStreamNonBlocking));
+        GB_CUDA_TRY(cudaEventCreateWithFlags(&h->gev_in, cudaEventDisableTiming));
+        GB_CUDA_TRY(cudaEventCreateWithFlags(&h->gev_out, cudaEventDisableTiming));
+    }
+    const int64_t plain_steps = phi ? nsteps - 1 : nsteps;
+    gb_bh::Key key{xm, vel, acc, nullptr, n, theta, eps2, G, dt, max_stack, h->tpl};
+    if (plain_steps) GB_TRY(ensure_graph(h, 0, key, x, v, a, nullptr, n, theta, eps2, G, dt, max_stack));
+    if (phi) {
+        key.phi = phi;
+        GB_TRY(ensure_graph(h, 1, key, x, v, a, phi, n, theta, eps2, G, dt, max_stack));
     }
     GB_CUDA_TRY(cudaEventRecord(h->gev_in, s));
     GB_CUDA_TRY(cudaStreamWaitEvent(h->gstream, h->gev_in, 0));
-    for (int64_t k = 0; k < nsteps; ++k) GB_CUDA_TRY(cudaGraphLaunch(h->gexec, h->gstream));
+    for (int64_t k = 0; k < plain_steps; ++k) GB_CUDA_TRY(cudaGraphLaunch(h->gexec[0], h->gstream));
+    if (phi) GB_CUDA_TRY(cudaGraphLaunch(h->gexec[1], h->gstream));
     GB_CUDA_TRY(cudaEventRecord(h->gev_out, h->gstream));
     GB_CUDA_TRY(cudaStreamWaitEvent(s, h->gev_out, 0));
-    h->launches += h->graph_launches * (uint64_t)nsteps;
+    h->launches += h->graph_launches[0] * (uint64_t)plain_steps + (phi ? h->graph_launches[1] : 0);
     h->n = n;
+    return h->check ? check_failures(h, s, call) : GB_OK;
+}
+
+extern "C" int gb_bh_kdk(gb_bh_t *h, float *xm, float *vel, float *acc, int64_t n, float theta, float eps2, float G,
+                         float dt, int64_t nsteps, int max_stack, void *stream) {
+    return bh_kdk_impl(h, xm, vel, acc, nullptr, n, theta, eps2, G, dt, nsteps, max_stack, stream, "gb_bh_kdk");
+}
+
+extern "C" int gb_bh_kdk_phi(gb_bh_t *h, float *xm, float *vel, float *acc, float *phi, int64_t n, float theta,
+                             float eps2, float G, float dt, int64_t nsteps, int max_stack, void *stream) {
+    if (!phi && n > 0 && nsteps > 0) return fail(GB_EINVAL, "phi is NULL");
+    return bh_kdk_impl(h, xm, vel, acc, phi, n, theta, eps2, G, dt, nsteps, max_stack, stream, "gb_bh_kdk_phi");
+}
+
+extern "C" int gb_bh_energy(gb_bh_t *h, const float *xm, const float *vel, const float *phi, int64_t n, float G,
+                            double *out3, void *stream) {
+    GB_TRY(check_bh(h, n));
+    if (n > 0) {
+        GB_TRY(check_ptr(xm, "xm"));
+        GB_TRY(check_ptr(vel, "vel"));
+        if (!phi) return fail(GB_EINVAL, "phi is NULL");
+    }
+    if (!out3) return fail(GB_EINVAL, "out3 is NULL");
+    GB_TRY(launch_energy((const float4 *)xm, (const float4 *)vel, phi, n, G, h->epart, h->epart_cap, out3,
+                         (cudaStream_t)stream));
+    h->launches += 2;
+    return GB_OK;
+}
+
+extern "C" int gb_bh_set_check(gb_bh_t *h, int on) {
+    if (!h) return fail(GB_EINVAL, "handle is NULL");
+    h->check = on ? 1 : 0;
     return GB_OK;
 }
 
@@ -1249,7 +1397,10 @@ extern "C" int gb_bh_export(gb_bh_t *h, int what, void *dst, void *stream) {
 
 extern "C" int gb_bh_diag(gb_bh_t *h, gb_diag_t *out, int reset) {
     if (!h || !out) return fail(GB_EINVAL, "NULL argument");
-    return read_diag(h->diag, out, reset);
+    GB_TRY(read_diag(h->diag, out, reset));
+    if (reset)
+        for (auto &v : h->seen) v = 0;
+    return GB_OK;
 }
 
 extern "C" int gb_bh_timing(gb_bh_t *h, int enable) {

@@ -48,6 +48,12 @@ int num_sms();
 // Copies the device counters into the C-ABI struct (synchronising).
 int read_diag(unsigned long long *dev, gb_diag_t *out, int reset);
 
+// FP64 energies into out3 (KE, PE = -1/2 G sum m phi, total) from n float4
+// records and the potential sums phi: per-block partials into epart (at most
+// epart_cap blocks), then one block adds them in block order (two launches).
+int launch_energy(const float4 *xm, const float4 *vel, const float *phi, int64_t n, float G, double2 *epart,
+                  int epart_cap, double *out3, cudaStream_t s);
+
 // ------------------------------------------------------- packed FP32 pairs
 // Blackwell executes two FP32 operations per lane per instruction with the
 // .f32x2 forms; a pair lives in one 64-bit register.

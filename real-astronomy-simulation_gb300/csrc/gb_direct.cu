@@ -21,7 +21,9 @@
 // predict x' = x + (v + a dt/2) dt on the fly from the stored state, and the
 // fix-up applies v' = v + a dt/2 + a' dt/2, writing x', v', a' in place.
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
+#include <mutex>
 
 #include "gb_direct_core.cuh"
 
@@ -56,7 +58,7 @@ __device__ __forceinline__ float4 load_particle(const DirectArgs &a, int64_t i) 
 // live in shared memory between source chunks, which keeps registers for
 // the interleave.  One pair per lane (NP = 1) fits 64 registers: 32
 // resident warps/SM.
-template <int NP, int WARPS, int MODE, bool KAHAN>
+template <int NP, int WARPS, int MODE, bool KAHAN, bool PHI>
 __global__ void __launch_bounds__(WARPS * 32, NP == 1 ? 1024 / (WARPS * 32) : 1)
 direct_force_kernel(DirectArgs a) {
     constexpr int K = 2 * NP;
@@ -64,8 +66,9 @@ direct_force_kernel(DirectArgs a) {
     constexpr int ST = WARPS * TILE;
     constexpr int JU = WARPS * 32;
     constexpr int T = WARPS * 32;
+    constexpr int NV = PHI ? 8 : 6;  // per pair: S{x,y,z}, C{x,y,z} (+ S, C of the potential)
     __shared__ ulonglong2 src[2 * JU];
-    __shared__ f2 kah[6 * NP][T];  // per thread: S{x,y,z}, C{x,y,z} per pair
+    __shared__ f2 kah[NV * NP][T];
 
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
@@ -94,7 +97,7 @@ direct_force_kernel(DirectArgs a) {
             Z[p] = pack2(t0.z, t1.z);
         }
 #pragma unroll
-        for (int v = 0; v < 6 * NP; ++v) kah[v][tid] = 0ull;
+        for (int v = 0; v < NV * NP; ++v) kah[v][tid] = 0ull;
 
         for (; u < run_end; ++u) {
             const int64_t ju = u - st * a.num_ju;
@@ -104,9 +107,10 @@ direct_force_kernel(DirectArgs a) {
             src[2 * threadIdx.x + 1] = make_ulonglong2(pack2(s4.z, s4.z), pack2(s4.w, s4.w));
             __syncthreads();
 
-            f2 AX[2][NP], AY[2][NP], AZ[2][NP];
+            f2 AX[2][NP], AY[2][NP], AZ[2][NP], AW[2][NP];
 #pragma unroll
-            for (int p = 0; p < NP; ++p) AX[0][p] = AY[0][p] = AZ[0][p] = AX[1][p] = AY[1][p] = AZ[1][p] = 0ull;
+            for (int p = 0; p < NP; ++p)
+                AX[0][p] = AY[0][p] = AZ[0][p] = AX[1][p] = AY[1][p] = AZ[1][p] = AW[0][p] = AW[1][p] = 0ull;
 #pragma unroll 2
             for (int jj = 0; jj < JU; jj += 2) {
 #pragma unroll
@@ -123,10 +127,12 @@ direct_force_kernel(DirectArgs a) {
                         r2 = fma2(dz, dz, r2);
                         const f2 inv = rsqrt2(r2);
                         const f2 inv2 = mul2(inv, inv);
-                        const f2 sc = mul2(mul2(B.y, inv), inv2);
+                        const f2 mi = mul2(B.y, inv);
+                        const f2 sc = mul2(mi, inv2);
                         AX[h][p] = fma2(sc, dx, AX[h][p]);
                         AY[h][p] = fma2(sc, dy, AY[h][p]);
                         AZ[h][p] = fma2(sc, dz, AZ[h][p]);
+                        if (PHI) AW[h][p] = add2(AW[h][p], mi);
                     }
                 }
             }
@@ -152,6 +158,14 @@ direct_force_kernel(DirectArgs a) {
                 kah[6 * p][tid] = sx;
                 kah[6 * p + 1][tid] = sy;
                 kah[6 * p + 2][tid] = sz;
+                if (PHI) {
+                    const f2 aw = add2(AW[0][p], AW[1][p]);
+                    f2 sw = kah[6 * NP + 2 * p][tid], cw = kah[6 * NP + 2 * p + 1][tid];
+                    if (KAHAN) kahan_add2(sw, cw, aw);
+                    else sw = add2(sw, aw);
+                    kah[6 * NP + 2 * p][tid] = sw;
+                    kah[6 * NP + 2 * p + 1][tid] = cw;
+                }
             }
         }
         // Flush the compensated partial: estimate = hi + lo with lo = -c.
@@ -165,11 +179,16 @@ direct_force_kernel(DirectArgs a) {
             unpack2(kah[6 * p + 3][tid], cx0, cx1);
             unpack2(kah[6 * p + 4][tid], cy0, cy1);
             unpack2(kah[6 * p + 5][tid], cz0, cz1);
+            float hw0 = 0.f, hw1 = 0.f, cw0 = 0.f, cw1 = 0.f;
+            if (PHI) {
+                unpack2(kah[6 * NP + 2 * p][tid], hw0, hw1);
+                unpack2(kah[6 * NP + 2 * p + 1][tid], cw0, cw1);
+            }
             const int64_t s0 = slot + (2 * p) * 32, s1 = s0 + 32;
-            a.part[2 * s0] = make_float4(hx0, hy0, hz0, 0.f);
-            a.part[2 * s0 + 1] = make_float4(-cx0, -cy0, -cz0, 0.f);
-            a.part[2 * s1] = make_float4(hx1, hy1, hz1, 0.f);
-            a.part[2 * s1 + 1] = make_float4(-cx1, -cy1, -cz1, 0.f);
+            a.part[2 * s0] = make_float4(hx0, hy0, hz0, hw0);
+            a.part[2 * s0 + 1] = make_float4(-cx0, -cy0, -cz0, -cw0);
+            a.part[2 * s1] = make_float4(hx1, hy1, hz1, hw1);
+            a.part[2 * s1 + 1] = make_float4(-cx1, -cy1, -cz1, -cw1);
         }
     }
 }
@@ -180,7 +199,7 @@ direct_force_kernel(DirectArgs a) {
 // FINE: units of SCALAR_UNIT sources (up to WARPS of them staged per
 // shared-memory batch) instead of WARPS * 32, so short CTA runs split the
 // work evenly; the host picks it when the coarse split leaves a tail.
-template <int NP, int WARPS, int MODE, bool KAHAN, bool FINE>
+template <int NP, int WARPS, int MODE, bool KAHAN, bool FINE, bool PHI>
 __global__ void __launch_bounds__(WARPS * 32, NP == 1 ? 1024 / (WARPS * 32) : 1)
 direct_force_scalar_kernel(DirectArgs a) {
     constexpr int K = 2 * NP;
@@ -203,12 +222,12 @@ direct_force_scalar_kernel(DirectArgs a) {
         const int64_t st = u / a.num_ju;
         const int64_t run_end = min(u_end, (st + 1) * a.num_ju);
         const int64_t tbase = st * ST + wib * TILE + lane;
-        float X[K], Y[K], Z[K], SX[K], SY[K], SZ[K], CX[K], CY[K], CZ[K];
+        float X[K], Y[K], Z[K], SX[K], SY[K], SZ[K], CX[K], CY[K], CZ[K], SW[K], CW[K];
 #pragma unroll
         for (int q = 0; q < K; ++q) {
             const float4 t = load_particle<MODE>(a, tbase + q * 32);
             X[q] = t.x; Y[q] = t.y; Z[q] = t.z;
-            SX[q] = SY[q] = SZ[q] = CX[q] = CY[q] = CZ[q] = 0.f;
+            SX[q] = SY[q] = SZ[q] = CX[q] = CY[q] = CZ[q] = SW[q] = CW[q] = 0.f;
         }
         while (u < run_end) {
             const int64_t jc = u - st * a.num_ju;
@@ -226,14 +245,14 @@ direct_force_scalar_kernel(DirectArgs a) {
             src[threadIdx.x] = s4;
             __syncthreads();
             u += cnt;
-            float AX[K], AY[K], AZ[K];
+            float AX[K], AY[K], AZ[K], PW[K];
 #pragma unroll
-            for (int q = 0; q < K; ++q) AX[q] = AY[q] = AZ[q] = 0.f;
+            for (int q = 0; q < K; ++q) AX[q] = AY[q] = AZ[q] = PW[q] = 0.f;
             if (FINE) {
                 for (int b = 0; b < cnt; ++b)
-                    interact_chunk<K, SCALAR_UNIT>(src + b * SCALAR_UNIT, X, Y, Z, AX, AY, AZ, a.eps2);
+                    interact_chunk<K, SCALAR_UNIT, PHI>(src + b * SCALAR_UNIT, X, Y, Z, AX, AY, AZ, PW, a.eps2);
             } else {
-                interact_chunk<K, JU>(src, X, Y, Z, AX, AY, AZ, a.eps2);
+                interact_chunk<K, JU, PHI>(src, X, Y, Z, AX, AY, AZ, PW, a.eps2);
             }
 #pragma unroll
             for (int q = 0; q < K; ++q) {
@@ -241,8 +260,10 @@ direct_force_scalar_kernel(DirectArgs a) {
                     kahan_add(SX[q], CX[q], AX[q]);
                     kahan_add(SY[q], CY[q], AY[q]);
                     kahan_add(SZ[q], CZ[q], AZ[q]);
+                    if (PHI) kahan_add(SW[q], CW[q], PW[q]);
                 } else {
                     SX[q] += AX[q]; SY[q] += AY[q]; SZ[q] += AZ[q];
+                    if (PHI) SW[q] += PW[q];
                 }
             }
         }
@@ -250,8 +271,8 @@ direct_force_scalar_kernel(DirectArgs a) {
 #pragma unroll
         for (int q = 0; q < K; ++q) {
             const int64_t sq = slot + q * 32;
-            a.part[2 * sq] = make_float4(SX[q], SY[q], SZ[q], 0.f);
-            a.part[2 * sq + 1] = make_float4(-CX[q], -CY[q], -CZ[q], 0.f);
+            a.part[2 * sq] = make_float4(SX[q], SY[q], SZ[q], SW[q]);
+            a.part[2 * sq + 1] = make_float4(-CX[q], -CY[q], -CZ[q], -CW[q]);
         }
     }
 }
@@ -333,15 +354,17 @@ struct FixArgs {
     float4 *xm;   // KDK: in/out positions
     float4 *vel;  // KDK: in/out velocities
     float4 *acc;  // ACC/KDK: output accelerations (KDK: in = previous)
-    float *phi;   // PHI: output
+    float *phi;   // MODE_PHI, or a force pass with the potential: output
     int64_t n, num_ju, U, P, st_size;
     int smax;
-    float G, h, dt;
+    float G, h, dt, eps2;
     int accumulate;
     ExtPot pot;  // ACC: analytic potential added to the result (pot.on)
 };
 
-template <int MODE>
+// MODE_ACC / MODE_KDK with PHI: the partials also carry the potential sums
+// in .w, whose sum less the particle's own term is written to phi.
+template <int MODE, bool PHI = false>
 __global__ void direct_fixup_kernel(FixArgs f) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= f.n) return;
@@ -349,7 +372,7 @@ __global__ void direct_fixup_kernel(FixArgs f) {
     const int64_t off = i - st * f.st_size;
     const int64_t c_lo = unit_owner(f.U, f.P, st * f.num_ju);
     const int64_t c_hi = unit_owner(f.U, f.P, (st + 1) * f.num_ju - 1);
-    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f, sw = 0.f, cw = 0.f;
     for (int64_t c = c_lo; c <= c_hi; ++c) {
         const int64_t st0c = __ldg(f.st0tab + c);
         const int64_t slot = (c * f.smax + (st - st0c)) * f.st_size + off;
@@ -363,11 +386,19 @@ __global__ void direct_fixup_kernel(FixArgs f) {
             kahan_add(sz, cz, hi.z);
             kahan_add(sz, cz, lo.z);
         }
+        if (PHI) {
+            kahan_add(sw, cw, hi.w);
+            kahan_add(sw, cw, lo.w);
+        }
     }
     const float tx = sx - cx, ty = sy - cy, tz = sz - cz;
     if (MODE == MODE_PHI) {
         f.phi[i] = tx;
         return;
+    }
+    if (PHI) {
+        kahan_add(sw, cw, -self_phi_term(f.xm[i].w, f.eps2));
+        f.phi[i] = sw - cw;
     }
     float4 an = make_float4(f.G * tx, f.G * ty, f.G * tz, 0.f);
     if (MODE == MODE_ACC) {
@@ -441,6 +472,15 @@ __global__ void energy_final_kernel(const double2 *__restrict__ part, int nb, do
     }
 }
 
+int launch_energy(const float4 *xm, const float4 *vel, const float *phi, int64_t n, float G, double2 *epart,
+                  int epart_cap, double *out3, cudaStream_t s) {
+    const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(epart_cap, (n + 255) / 256));
+    energy_partial_kernel<<<nb, 256, 0, s>>>(xm, vel, phi, n, epart);
+    energy_final_kernel<<<1, 32, 0, s>>>(epart, nb, (double)G, out3);
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+}
+
 // ------------------------------------------------- FP64 sampled oracle
 // One CTA per sampled target; threads stride the sources; FP64 arithmetic in
 // the order of core/solvers/gravity.py:22-25; fixed-order block reduction.
@@ -489,33 +529,47 @@ __global__ void direct_fp64_kernel(const float4 *__restrict__ xm, int64_t n,
 
 // ------------------------------------------------------------------ host
 
-template <int NP, int WARPS, bool FINE>
-static void launch_scalar(int mode, bool kahan, dim3 grid, const DirectArgs &a, cudaStream_t s) {
+template <int NP, int WARPS, int MODE, bool FINE, bool PHI>
+static void launch_scalar_m(bool kahan, dim3 grid, const DirectArgs &a, cudaStream_t s) {
     const dim3 block(WARPS * 32);
+    if (kahan) direct_force_scalar_kernel<NP, WARPS, MODE, true, FINE, PHI><<<grid, block, 0, s>>>(a);
+    else direct_force_scalar_kernel<NP, WARPS, MODE, false, FINE, PHI><<<grid, block, 0, s>>>(a);
+}
+
+template <int NP, int WARPS, bool FINE>
+static void launch_scalar(int mode, bool kahan, bool phi, dim3 grid, const DirectArgs &a, cudaStream_t s) {
     if (mode == MODE_ACC) {
-        if (kahan) direct_force_scalar_kernel<NP, WARPS, MODE_ACC, true, FINE><<<grid, block, 0, s>>>(a);
-        else direct_force_scalar_kernel<NP, WARPS, MODE_ACC, false, FINE><<<grid, block, 0, s>>>(a);
+        if (phi) launch_scalar_m<NP, WARPS, MODE_ACC, FINE, true>(kahan, grid, a, s);
+        else launch_scalar_m<NP, WARPS, MODE_ACC, FINE, false>(kahan, grid, a, s);
     } else {
-        if (kahan) direct_force_scalar_kernel<NP, WARPS, MODE_KDK, true, FINE><<<grid, block, 0, s>>>(a);
-        else direct_force_scalar_kernel<NP, WARPS, MODE_KDK, false, FINE><<<grid, block, 0, s>>>(a);
+        if (phi) launch_scalar_m<NP, WARPS, MODE_KDK, FINE, true>(kahan, grid, a, s);
+        else launch_scalar_m<NP, WARPS, MODE_KDK, FINE, false>(kahan, grid, a, s);
     }
 }
 
+template <int NP, int WARPS, int MODE, bool PHI>
+static void launch_packed_m(bool kahan, dim3 grid, const DirectArgs &a, cudaStream_t s) {
+    const dim3 block(WARPS * 32);
+    if (kahan) direct_force_kernel<NP, WARPS, MODE, true, PHI><<<grid, block, 0, s>>>(a);
+    else direct_force_kernel<NP, WARPS, MODE, false, PHI><<<grid, block, 0, s>>>(a);
+}
+
+// phi: the pass also sums the potential (PHI kernels).
 template <int NP, int WARPS>
-static cudaError_t launch_force(int mode, bool kahan, const DirectPlan &pl, const DirectArgs &a,
+static cudaError_t launch_force(int mode, bool kahan, bool phi, const DirectPlan &pl, const DirectArgs &a,
                                 cudaStream_t s, int packed, bool fine) {
-    const dim3 grid((unsigned)pl.P), block(WARPS * 32);
+    const dim3 grid((unsigned)pl.P);
     if (!packed) {
-        if (fine) launch_scalar<NP, WARPS, true>(mode, kahan, grid, a, s);
-        else launch_scalar<NP, WARPS, false>(mode, kahan, grid, a, s);
+        if (fine) launch_scalar<NP, WARPS, true>(mode, kahan, phi, grid, a, s);
+        else launch_scalar<NP, WARPS, false>(mode, kahan, phi, grid, a, s);
         return cudaGetLastError();
     }
     if (mode == MODE_ACC) {
-        if (kahan) direct_force_kernel<NP, WARPS, MODE_ACC, true><<<grid, block, 0, s>>>(a);
-        else direct_force_kernel<NP, WARPS, MODE_ACC, false><<<grid, block, 0, s>>>(a);
+        if (phi) launch_packed_m<NP, WARPS, MODE_ACC, true>(kahan, grid, a, s);
+        else launch_packed_m<NP, WARPS, MODE_ACC, false>(kahan, grid, a, s);
     } else {
-        if (kahan) direct_force_kernel<NP, WARPS, MODE_KDK, true><<<grid, block, 0, s>>>(a);
-        else direct_force_kernel<NP, WARPS, MODE_KDK, false><<<grid, block, 0, s>>>(a);
+        if (phi) launch_packed_m<NP, WARPS, MODE_KDK, true>(kahan, grid, a, s);
+        else launch_packed_m<NP, WARPS, MODE_KDK, false>(kahan, grid, a, s);
     }
     return cudaGetLastError();
 }
@@ -524,15 +578,15 @@ typedef const void *KernelPtr;
 
 static KernelPtr force_kernel_ptr(int np, int warps, int packed) {
     if (!packed) {
-        if (np == 1 && warps == 4) return (KernelPtr)direct_force_scalar_kernel<1, 4, MODE_KDK, true, false>;
-        if (np == 1 && warps == 8) return (KernelPtr)direct_force_scalar_kernel<1, 8, MODE_KDK, true, false>;
-        if (np == 2 && warps == 4) return (KernelPtr)direct_force_scalar_kernel<2, 4, MODE_KDK, true, false>;
-        return (KernelPtr)direct_force_scalar_kernel<2, 8, MODE_KDK, true, false>;
+        if (np == 1 && warps == 4) return (KernelPtr)direct_force_scalar_kernel<1, 4, MODE_KDK, true, false, false>;
+        if (np == 1 && warps == 8) return (KernelPtr)direct_force_scalar_kernel<1, 8, MODE_KDK, true, false, false>;
+        if (np == 2 && warps == 4) return (KernelPtr)direct_force_scalar_kernel<2, 4, MODE_KDK, true, false, false>;
+        return (KernelPtr)direct_force_scalar_kernel<2, 8, MODE_KDK, true, false, false>;
     }
-    if (np == 1 && warps == 4) return (KernelPtr)direct_force_kernel<1, 4, MODE_KDK, true>;
-    if (np == 1 && warps == 8) return (KernelPtr)direct_force_kernel<1, 8, MODE_KDK, true>;
-    if (np == 2 && warps == 4) return (KernelPtr)direct_force_kernel<2, 4, MODE_KDK, true>;
-    return (KernelPtr)direct_force_kernel<2, 8, MODE_KDK, true>;
+    if (np == 1 && warps == 4) return (KernelPtr)direct_force_kernel<1, 4, MODE_KDK, true, false>;
+    if (np == 1 && warps == 8) return (KernelPtr)direct_force_kernel<1, 8, MODE_KDK, true, false>;
+    if (np == 2 && warps == 4) return (KernelPtr)direct_force_kernel<2, 4, MODE_KDK, true, false>;
+    return (KernelPtr)direct_force_kernel<2, 8, MODE_KDK, true, false>;
 }
 
 }  // namespace gb
@@ -633,8 +687,8 @@ extern "C" int gb_direct_create(gb_direct_t **out, int64_t n_max) {
 
 extern "C" int gb_direct_destroy(gb_direct_t *h) {
     if (!h) return GB_OK;
-    for (int g = 0; g < 2; ++g)
-        if (h->gexec[g]) cudaGraphExecDestroy(h->gexec[g]);
+    for (auto &g : h->gexec)
+        if (g) cudaGraphExecDestroy(g);
     if (h->gev_in) cudaEventDestroy(h->gev_in);
     if (h->gev_out) cudaEventDestroy(h->gev_out);
     if (h->gstream) cudaStreamDestroy(h->gstream);
@@ -659,6 +713,9 @@ extern "C" int gb_direct_set_tiles(gb_direct_t *h, int k, int warps, int ctas_pe
     return GB_OK;
 }
 
+// mode MODE_ACC / MODE_KDK: accelerations (or one KDK step), and, when phi
+// is not NULL, the potential sums of the same positions in the same pass;
+// MODE_PHI: the potential sums alone.
 static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, float4 *acc, float *phi,
                       int64_t n, float G, float eps2, float dt, int flags, cudaStream_t s,
                       const ExtPot &pot = ExtPot{}) {
@@ -691,6 +748,7 @@ static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, f
     a.h = 0.5f * dt;
     a.dt = dt;
     const bool kahan = !(flags & GB_PLAIN_FP32);
+    const bool with_phi = mode != MODE_PHI && phi != nullptr;
     cudaError_t e;
     if (mode == MODE_PHI) {
         const dim3 grid((unsigned)pl.P), block(h->warps * 32);
@@ -703,11 +761,11 @@ static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, f
         }
         e = cudaGetLastError();
     } else if (pl.np == 1) {
-        e = pl.warps == 4 ? launch_force<1, 4>(mode, kahan, pl, a, s, packed, fine)
-                          : launch_force<1, 8>(mode, kahan, pl, a, s, packed, fine);
+        e = pl.warps == 4 ? launch_force<1, 4>(mode, kahan, with_phi, pl, a, s, packed, fine)
+                          : launch_force<1, 8>(mode, kahan, with_phi, pl, a, s, packed, fine);
     } else {
-        e = pl.warps == 4 ? launch_force<2, 4>(mode, kahan, pl, a, s, packed, fine)
-                          : launch_force<2, 8>(mode, kahan, pl, a, s, packed, fine);
+        e = pl.warps == 4 ? launch_force<2, 4>(mode, kahan, with_phi, pl, a, s, packed, fine)
+                          : launch_force<2, 8>(mode, kahan, with_phi, pl, a, s, packed, fine);
     }
     if (e != cudaSuccess) return fail(GB_ECUDA, "force launch: %s", cudaGetErrorString(e));
     FixArgs f;
@@ -726,12 +784,19 @@ static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, f
     f.G = G;
     f.h = 0.5f * dt;
     f.dt = dt;
+    f.eps2 = eps2;
     f.accumulate = (flags & GB_ACCUMULATE) ? 1 : 0;
     f.pot = pot;
     const unsigned fb = 256, fg = (unsigned)((n + fb - 1) / fb);
-    if (mode == MODE_ACC) direct_fixup_kernel<MODE_ACC><<<fg, fb, 0, s>>>(f);
-    else if (mode == MODE_KDK) direct_fixup_kernel<MODE_KDK><<<fg, fb, 0, s>>>(f);
-    else direct_fixup_kernel<MODE_PHI><<<fg, fb, 0, s>>>(f);
+    if (mode == MODE_ACC) {
+        if (with_phi) direct_fixup_kernel<MODE_ACC, true><<<fg, fb, 0, s>>>(f);
+        else direct_fixup_kernel<MODE_ACC><<<fg, fb, 0, s>>>(f);
+    } else if (mode == MODE_KDK) {
+        if (with_phi) direct_fixup_kernel<MODE_KDK, true><<<fg, fb, 0, s>>>(f);
+        else direct_fixup_kernel<MODE_KDK><<<fg, fb, 0, s>>>(f);
+    } else {
+        direct_fixup_kernel<MODE_PHI><<<fg, fb, 0, s>>>(f);
+    }
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(GB_ECUDA, "fix-up launch: %s", cudaGetErrorString(e));
     h->launches += 2;
@@ -768,8 +833,43 @@ extern "C" int gb_direct_acc_ext(gb_direct_t *h, const float *xm, float *acc, in
                       flags, (cudaStream_t)stream, ep);
 }
 
-extern "C" int gb_direct_kdk(gb_direct_t *h, float *xm, float *vel, float *acc, int64_t n, float G, float eps2,
-                             float dt, int64_t nsteps, int flags, void *stream) {
+// Graph slot g holds `steps` captured KDK steps (the last one also writing
+// the potential into phi when phi is not NULL); captured again when the key
+// of the slot changed.
+static int ensure_graph(gb_direct_t *h, int g, int steps, const gb_direct::Key &key, float *xm, float *vel,
+                        float *acc, float *phi, int64_t n, float G, float eps2, float dt, int plain) {
+    if (h->gexec[g] && h->gkey[g] == key) return GB_OK;
+    if (h->gexec[g]) cudaGraphExecDestroy(h->gexec[g]);
+    h->gexec[g] = nullptr;
+    GB_CUDA_TRY(cudaStreamBeginCapture(h->gstream, cudaStreamCaptureModeThreadLocal));
+    const uint64_t l0 = h->launches;
+    int st = GB_OK;
+    for (int k = 0; k < steps && st == GB_OK; ++k)
+        st = run_direct(h, MODE_KDK, (const float4 *)xm, (float4 *)vel, (float4 *)acc, k == steps - 1 ? phi : nullptr,
+                        n, G, eps2, dt, plain, h->gstream);
+    h->glaunches[g] = h->launches - l0;
+    h->launches = l0;
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(h->gstream, &graph);
+    if (st != GB_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return st;
+    }
+    if (e != cudaSuccess) return fail(GB_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+    const cudaError_t ei = cudaGraphInstantiate(&h->gexec[g], graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+        h->gexec[g] = nullptr;
+        return fail(GB_ECUDA, "graph instantiate: %s", cudaGetErrorString(ei));
+    }
+    h->gkey[g] = key;
+    return GB_OK;
+}
+
+// nsteps fused KDK steps; with phi, the last step's force pass also writes
+// the potential sums of the final positions.
+static int kdk_impl(gb_direct_t *h, float *xm, float *vel, float *acc, float *phi, int64_t n, float G, float eps2,
+                    float dt, int64_t nsteps, int flags, void *stream) {
     GB_TRY(check_n(h, n));
     if (n == 0 || nsteps == 0) return GB_OK;
     if (nsteps < 0) return fail(GB_EINVAL, "nsteps < 0");
@@ -781,66 +881,64 @@ extern "C" int gb_direct_kdk(gb_direct_t *h, float *xm, float *vel, float *acc, 
     const int plain = flags & GB_PLAIN_FP32;
     if (!(flags & GB_USE_GRAPH)) {
         for (int64_t k = 0; k < nsteps; ++k)
-            GB_TRY(run_direct(h, MODE_KDK, (const float4 *)xm, (float4 *)vel, (float4 *)acc, nullptr, n, G, eps2,
-                              dt, plain, s));
+            GB_TRY(run_direct(h, MODE_KDK, (const float4 *)xm, (float4 *)vel, (float4 *)acc,
+                              k == nsteps - 1 ? phi : nullptr, n, G, eps2, dt, plain, s));
         return GB_OK;
     }
-    // One step, and a run of GRAPH_STEPS steps, captured on the handle's
-    // stream and replayed: whole runs first, single steps for the rest (one
-    // graph launch per GRAPH_STEPS steps keeps small systems off the host's
-    // launch rate).  Tile-pair scratch is sized before the capture (no
-    // allocation inside it); its address is part of the key, since the
-    // adjoint may regrow it.
+    // Steps captured on the handle's stream and replayed: runs of
+    // GRAPH_STEPS steps first, single steps for the rest (one graph launch
+    // per GRAPH_STEPS steps keeps small systems off the host's launch rate),
+    // and the potential step last.  Tile-pair scratch is sized before the
+    // capture (no allocation inside it); its address is part of the key,
+    // since the adjoint may regrow it.
     if (h->packed == 2) GB_TRY(reserve_direct_sym(h, n));
-    const gb_direct::Key key{xm, vel, acc, h->sym, n, h->sym_band, G, eps2, dt, plain, h->np, h->warps,
-                             h->ctas_per_sm, h->packed};
-    if (h->has_graph && !(h->gkey == key)) {
-        for (int g = 0; g < 2; ++g)
-            if (h->gexec[g]) cudaGraphExecDestroy(h->gexec[g]);
-        h->gexec[0] = h->gexec[1] = nullptr;
-        h->has_graph = false;
-    }
+    gb_direct::Key key{xm, vel, acc, h->sym, nullptr, n, h->sym_band, G, eps2, dt, plain, h->np, h->warps,
+                       h->ctas_per_sm, h->packed};
     if (!h->gstream) {
         GB_CUDA_TRY(cudaStreamCreateWithFlags(&h->gstream, cudaStreamNonBlocking));
         GB_CUDA_TRY(cudaEventCreateWithFlags(&h->gev_in, cudaEventDisableTiming));
         GB_CUDA_TRY(cudaEventCreateWithFlags(&h->gev_out, cudaEventDisableTiming));
     }
-    const int64_t runs = nsteps / GRAPH_STEPS, rest = nsteps - runs * GRAPH_STEPS;
-    for (int g = 0; g < 2; ++g) {
-        if (h->gexec[g] || (g == 0 ? rest == 0 : runs == 0)) continue;
-        const int steps = g == 0 ? 1 : GRAPH_STEPS;
-        GB_CUDA_TRY(cudaStreamBeginCapture(h->gstream, cudaStreamCaptureModeThreadLocal));
-        const uint64_t l0 = h->launches;
-        int st = GB_OK;
-        for (int k = 0; k < steps && st == GB_OK; ++k)
-            st = run_direct(h, MODE_KDK, (const float4 *)xm, (float4 *)vel, (float4 *)acc, nullptr, n, G, eps2, dt,
-                            plain, h->gstream);
-        h->glaunches = (h->launches - l0) / steps;
-        h->launches = l0;
-        cudaGraph_t graph = nullptr;
-        const cudaError_t e = cudaStreamEndCapture(h->gstream, &graph);
-        if (st != GB_OK) {
-            if (graph) cudaGraphDestroy(graph);
-            return st;
-        }
-        if (e != cudaSuccess) return fail(GB_ECUDA, "graph capture: %s", cudaGetErrorString(e));
-        const cudaError_t ei = cudaGraphInstantiate(&h->gexec[g], graph, 0);
-        cudaGraphDestroy(graph);
-        if (ei != cudaSuccess) {
-            h->gexec[g] = nullptr;
-            return fail(GB_ECUDA, "graph instantiate: %s", cudaGetErrorString(ei));
-        }
-        h->has_graph = true;
-        h->gkey = key;
+    const int64_t plain_steps = phi ? nsteps - 1 : nsteps;
+    const int64_t runs = plain_steps / GRAPH_STEPS, rest = plain_steps - runs * GRAPH_STEPS;
+    if (runs) GB_TRY(ensure_graph(h, 1, GRAPH_STEPS, key, xm, vel, acc, nullptr, n, G, eps2, dt, plain));
+    if (rest) GB_TRY(ensure_graph(h, 0, 1, key, xm, vel, acc, nullptr, n, G, eps2, dt, plain));
+    if (phi) {
+        key.phi = phi;
+        GB_TRY(ensure_graph(h, 2, 1, key, xm, vel, acc, phi, n, G, eps2, dt, plain));
     }
     GB_CUDA_TRY(cudaEventRecord(h->gev_in, s));
     GB_CUDA_TRY(cudaStreamWaitEvent(h->gstream, h->gev_in, 0));
     for (int64_t k = 0; k < runs; ++k) GB_CUDA_TRY(cudaGraphLaunch(h->gexec[1], h->gstream));
     for (int64_t k = 0; k < rest; ++k) GB_CUDA_TRY(cudaGraphLaunch(h->gexec[0], h->gstream));
+    if (phi) GB_CUDA_TRY(cudaGraphLaunch(h->gexec[2], h->gstream));
     GB_CUDA_TRY(cudaEventRecord(h->gev_out, h->gstream));
     GB_CUDA_TRY(cudaStreamWaitEvent(s, h->gev_out, 0));
-    h->launches += h->glaunches * (uint64_t)nsteps;
+    h->launches += h->glaunches[1] * (uint64_t)runs + h->glaunches[0] * (uint64_t)rest + (phi ? h->glaunches[2] : 0);
     return GB_OK;
+}
+
+extern "C" int gb_direct_kdk(gb_direct_t *h, float *xm, float *vel, float *acc, int64_t n, float G, float eps2,
+                             float dt, int64_t nsteps, int flags, void *stream) {
+    return kdk_impl(h, xm, vel, acc, nullptr, n, G, eps2, dt, nsteps, flags, stream);
+}
+
+extern "C" int gb_direct_kdk_phi(gb_direct_t *h, float *xm, float *vel, float *acc, float *phi, int64_t n, float G,
+                                 float eps2, float dt, int64_t nsteps, int flags, void *stream) {
+    if (!phi && n > 0 && nsteps > 0) return fail(GB_EINVAL, "phi is NULL");
+    return kdk_impl(h, xm, vel, acc, phi, n, G, eps2, dt, nsteps, flags, stream);
+}
+
+extern "C" int gb_direct_acc_phi(gb_direct_t *h, const float *xm, float *acc, float *phi, int64_t n, float G,
+                                 float eps2, int flags, void *stream) {
+    GB_TRY(check_n(h, n));
+    if (n == 0) return GB_OK;
+    GB_TRY(check_xm(xm, "xm"));
+    GB_TRY(check_xm(acc, "acc"));
+    if (!phi) return fail(GB_EINVAL, "phi is NULL");
+    if (!(eps2 > 0.f)) return fail(GB_EINVAL, "eps2 must be > 0");
+    return run_direct(h, MODE_ACC, (const float4 *)xm, nullptr, (float4 *)acc, phi, n, G, eps2, 0.f, flags,
+                      (cudaStream_t)stream);
 }
 
 extern "C" int gb_direct_phi(gb_direct_t *h, const float *xm, float *phi, int64_t n, float eps2, int flags,
@@ -862,12 +960,24 @@ extern "C" int gb_energy(gb_direct_t *h, const float *xm, const float *vel, int6
         GB_TRY(check_xm(vel, "vel"));
     }
     if (!out3) return fail(GB_EINVAL, "out3 is NULL");
-    cudaStream_t s = (cudaStream_t)stream;
     if (n > 0) GB_TRY(gb_direct_phi(h, xm, h->phi, n, eps2, 0, stream));
-    const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(h->epart_cap, (n + 255) / 256));
-    energy_partial_kernel<<<nb, 256, 0, s>>>((const float4 *)xm, (const float4 *)vel, h->phi, n, h->epart);
-    energy_final_kernel<<<1, 32, 0, s>>>(h->epart, nb, (double)G, out3);
-    GB_CUDA_TRY(cudaGetLastError());
+    GB_TRY(launch_energy((const float4 *)xm, (const float4 *)vel, h->phi, n, G, h->epart, h->epart_cap, out3,
+                         (cudaStream_t)stream));
+    h->launches += 2;
+    return GB_OK;
+}
+
+extern "C" int gb_energy_phi(gb_direct_t *h, const float *xm, const float *vel, const float *phi, int64_t n,
+                             float G, double *out3, void *stream) {
+    GB_TRY(check_n(h, n));
+    if (n > 0) {
+        GB_TRY(check_xm(xm, "xm"));
+        GB_TRY(check_xm(vel, "vel"));
+        if (!phi) return fail(GB_EINVAL, "phi is NULL");
+    }
+    if (!out3) return fail(GB_EINVAL, "out3 is NULL");
+    GB_TRY(launch_energy((const float4 *)xm, (const float4 *)vel, phi, n, G, h->epart, h->epart_cap, out3,
+                         (cudaStream_t)stream));
     h->launches += 2;
     return GB_OK;
 }
@@ -934,15 +1044,43 @@ static __device__ int g_noalloc_tab[NOALLOC_CTAS];  // first supertile per CTA
 
 // Device addresses of g_noalloc_part and g_noalloc_tab per device: in host
 // code the symbol names are only host-side stand-ins, so the addresses are
-// looked up once per device (with that device current) and cached.
-static void *g_noalloc_addr[GB_NOALLOC_MAX_DEVICES];
-static void *g_noalloc_tab_addr[GB_NOALLOC_MAX_DEVICES];
+// looked up once per device (with that device current) and cached.  The
+// cache is read without a lock (acquire loads); the first lookup on a
+// device runs under a mutex, so concurrent first calls from several host
+// threads look it up once.  A cudaDeviceReset of that device unloads the
+// module and moves the array: the cached address is then stale (as is every
+// device buffer the caller held), so the entry point must not be used on a
+// device after it was reset.
+static std::atomic<void *> g_noalloc_addr[GB_NOALLOC_MAX_DEVICES];
+static std::atomic<void *> g_noalloc_tab_addr[GB_NOALLOC_MAX_DEVICES];
+static std::mutex g_noalloc_mu;
+
+static int noalloc_addresses(int dev, void **part, void **tab) {
+    *part = g_noalloc_addr[dev].load(std::memory_order_acquire);
+    *tab = g_noalloc_tab_addr[dev].load(std::memory_order_acquire);
+    if (*part && *tab) return GB_OK;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    *part = g_noalloc_addr[dev].load(std::memory_order_acquire);
+    *tab = g_noalloc_tab_addr[dev].load(std::memory_order_acquire);
+    if (*part && *tab) return GB_OK;
+    void *p = nullptr, *t = nullptr;
+    GB_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_part));
+    GB_CUDA_TRY(cudaGetSymbolAddress(&t, g_noalloc_tab));
+    g_noalloc_tab_addr[dev].store(t, std::memory_order_release);
+    g_noalloc_addr[dev].store(p, std::memory_order_release);
+    *part = p;
+    *tab = t;
+    return GB_OK;
+}
 
 extern "C" int gb_direct_acc_noalloc(const float *xm, float *acc, int64_t n, float G, float eps2, int flags,
                                      void *stream) {
     if (n < 0 || n > GB_NOALLOC_MAX_N)
         return fail(GB_EINVAL, "gb_direct_acc_noalloc: n=%lld outside [0, %d]; use gb_direct_acc for larger systems",
                     (long long)n, GB_NOALLOC_MAX_N);
+    if (flags & ~(GB_ACCUMULATE | GB_PLAIN_FP32))
+        return fail(GB_EINVAL, "gb_direct_acc_noalloc: flags 0x%x: only GB_ACCUMULATE and GB_PLAIN_FP32 apply",
+                    flags);
     if (n == 0) return GB_OK;
     GB_TRY(check_xm(xm, "xm"));
     GB_TRY(check_xm(acc, "acc"));
@@ -950,13 +1088,8 @@ extern "C" int gb_direct_acc_noalloc(const float *xm, float *acc, int64_t n, flo
     int dev = 0;
     GB_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= GB_NOALLOC_MAX_DEVICES) return fail(GB_EINVAL, "device index %d not supported", dev);
-    if (!g_noalloc_addr[dev]) {
-        void *p = nullptr, *t = nullptr;
-        GB_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_part));
-        GB_CUDA_TRY(cudaGetSymbolAddress(&t, g_noalloc_tab));
-        g_noalloc_tab_addr[dev] = t;
-        g_noalloc_addr[dev] = p;
-    }
+    void *part_addr = nullptr, *tab_addr = nullptr;
+    GB_TRY(noalloc_addresses(dev, &part_addr, &tab_addr));
     DirectPlan pl;
     const bool fine = use_fine_units(n, NOALLOC_NP, NOALLOC_WARPS, NOALLOC_CTAS);
     make_plan(n, NOALLOC_NP, NOALLOC_WARPS, NOALLOC_CTAS, &pl, fine ? SCALAR_UNIT : 0);
@@ -966,8 +1099,8 @@ extern "C" int gb_direct_acc_noalloc(const float *xm, float *acc, int64_t n, flo
     a.xm = (const float4 *)xm;
     a.vel = nullptr;
     a.acc = nullptr;
-    a.part = (float4 *)g_noalloc_addr[dev];
-    a.st0tab = (int *)g_noalloc_tab_addr[dev];
+    a.part = (float4 *)part_addr;
+    a.st0tab = (int *)tab_addr;
     a.n = n;
     a.num_ju = pl.num_ju;
     a.U = pl.U;
@@ -979,8 +1112,8 @@ extern "C" int gb_direct_acc_noalloc(const float *xm, float *acc, int64_t n, flo
     cudaStream_t s = (cudaStream_t)stream;
     const dim3 grid((unsigned)pl.P);
     const bool kahan = !(flags & GB_PLAIN_FP32);
-    if (fine) launch_scalar<NOALLOC_NP, NOALLOC_WARPS, true>(MODE_ACC, kahan, grid, a, s);
-    else launch_scalar<NOALLOC_NP, NOALLOC_WARPS, false>(MODE_ACC, kahan, grid, a, s);
+    if (fine) launch_scalar<NOALLOC_NP, NOALLOC_WARPS, true>(MODE_ACC, kahan, false, grid, a, s);
+    else launch_scalar<NOALLOC_NP, NOALLOC_WARPS, false>(MODE_ACC, kahan, false, grid, a, s);
     GB_CUDA_TRY(cudaGetLastError());
     FixArgs f;
     f.part = a.part;
@@ -998,6 +1131,7 @@ extern "C" int gb_direct_acc_noalloc(const float *xm, float *acc, int64_t n, flo
     f.G = G;
     f.h = 0.f;
     f.dt = 0.f;
+    f.eps2 = eps2;
     f.accumulate = (flags & GB_ACCUMULATE) ? 1 : 0;
     f.pot = ExtPot{};
     direct_fixup_kernel<MODE_ACC><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(f);

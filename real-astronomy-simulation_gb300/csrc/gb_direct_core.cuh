@@ -47,10 +47,12 @@ static inline int64_t plan_partials(const DirectPlan &p) { return 2 * p.P * p.sm
 // targets per lane into AX/AY/AZ (FP32; G applied later):
 //   d = x_j - x_i, r2 = d.d + eps2, a += m_j rsqrt(r2)^3 d
 // (core/solvers/gravity.py:22-25).  Zero-mass padding sources add zero.
-template <int K, int JU>
+// PHI also adds the potential terms m_j rsqrt(r2) into PW (the product the
+// force term starts from), the self pair included (the caller removes it).
+template <int K, int JU, bool PHI = false>
 __device__ __forceinline__ void interact_chunk(const float4 *src, const float (&X)[K], const float (&Y)[K],
                                                const float (&Z)[K], float (&AX)[K], float (&AY)[K],
-                                               float (&AZ)[K], float eps2) {
+                                               float (&AZ)[K], float (&PW)[K], float eps2) {
 #pragma unroll 4
     for (int jj = 0; jj < JU; ++jj) {
         const float4 sj = src[jj];
@@ -59,13 +61,21 @@ __device__ __forceinline__ void interact_chunk(const float4 *src, const float (&
             const float dx = sj.x - X[q], dy = sj.y - Y[q], dz = sj.z - Z[q];
             const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, eps2)));
             const float inv = rsqrt_approx(r2);
-            const float sc = (sj.w * inv) * (inv * inv);
+            const float mi = sj.w * inv;
+            const float sc = mi * (inv * inv);
             AX[q] = __fmaf_rn(sc, dx, AX[q]);
             AY[q] = __fmaf_rn(sc, dy, AY[q]);
             AZ[q] = __fmaf_rn(sc, dz, AZ[q]);
+            if (PHI) PW[q] += mi;
         }
     }
 }
+
+// The potential term a particle adds to its own sum in the per-target
+// passes: d = 0 gives r2 = eps2 exactly, so the term is m * rsqrt(eps2)
+// rounded as the pair loop rounds it.  The fix-up subtracts it, which gives
+// the j != i sum of potential_energy (core/solvers/gravity.py:51-52).
+__device__ __forceinline__ float self_phi_term(float m, float eps2) { return m * rsqrt_approx(eps2); }
 
 // Sources per stream-K unit of the scalar force kernel: one warp-width
 // sub-chunk, so CTA runs split the work evenly even at small N.
@@ -180,24 +190,25 @@ struct gb_direct {
     int adj_variant;    // 2: symmetric packed, 1: symmetric scalar, 0: one pass per target
     int64_t sym_band;   // symmetric force pass: tile-pair slot bytes per band at most
     // KDK steps captured as CUDA graphs (gb_direct_kdk with GB_USE_GRAPH):
-    // gexec[0] one step, gexec[1] GRAPH_STEPS steps, replayed on the
-    // handle's own stream; glaunches = kernels per captured step.
+    // gexec[0] one step, gexec[1] GRAPH_STEPS steps, gexec[2] one step that
+    // also writes the potential (gb_direct_kdk_phi), replayed on the
+    // handle's own stream; glaunches[g] = kernels per replay of slot g; a
+    // slot is captured again when its key changes.
     cudaStream_t gstream;
     cudaEvent_t gev_in, gev_out;
-    cudaGraphExec_t gexec[2];
-    uint64_t glaunches;
-    bool has_graph;
+    cudaGraphExec_t gexec[3];
+    uint64_t glaunches[3];
     struct Key {
-        const void *xm, *vel, *acc, *sym;
+        const void *xm, *vel, *acc, *sym, *phi;
         int64_t n, sym_band;
         float G, eps2, dt;
         int plain, np, warps, ctas_per_sm, packed;
         bool operator==(const Key &o) const {
-            return xm == o.xm && vel == o.vel && acc == o.acc && sym == o.sym && n == o.n && sym_band == o.sym_band && G == o.G && eps2 == o.eps2 &&
-                   dt == o.dt && plain == o.plain && np == o.np && warps == o.warps &&
-                   ctas_per_sm == o.ctas_per_sm && packed == o.packed;
+            return xm == o.xm && vel == o.vel && acc == o.acc && sym == o.sym && phi == o.phi && n == o.n &&
+                   sym_band == o.sym_band && G == o.G && eps2 == o.eps2 && dt == o.dt && plain == o.plain &&
+                   np == o.np && warps == o.warps && ctas_per_sm == o.ctas_per_sm && packed == o.packed;
         }
-    } gkey;
+    } gkey[3];
 };
 
 namespace gb {

@@ -80,32 +80,36 @@ __device__ __forceinline__ float4 ds_load(const DsArgs &a, int64_t o, int64_t n_
 
 // One round: lane l at step k takes source jj = 32 g + (l + k) mod 32 of the
 // staged tile against its 2H targets.  DIAG zeroes the pairs with target
-// index >= source index (diagonal tile).
-template <bool DIAG, int H>
+// index >= source index (diagonal tile).  PHI also sums the pair's
+// potential terms, phi_t += m_s / |d| into NW and phi_s += m_t / |d| into
+// sacc.w (one packed FMA per side), the sums of potential_energy
+// (core/solvers/gravity.py:47-55) taken from the same pass.
+template <bool DIAG, int H, bool PHI>
 __device__ __forceinline__ void ds_round(const float4 *__restrict__ sxm, float4 *sacc, int g, int lane, int wib,
                                          f2 EPS2, const f2 (&TX)[H], const f2 (&TY)[H], const f2 (&TZ)[H],
-                                         const f2 (&TM)[H], f2 (&NX)[H], f2 (&NY)[H], f2 (&NZ)[H]) {
+                                         const f2 (&TM)[H], f2 (&NX)[H], f2 (&NY)[H], f2 (&NZ)[H],
+                                         f2 (&NW)[H]) {
 #pragma unroll DS_K_UNROLL
     for (int k = 0; k < 32; ++k) {
         const int jj = g * 32 + ((lane + k) & 31);
         const float4 xs = sxm[jj];
         const f2 sx = pack2(xs.x, xs.x), sy = pack2(xs.y, xs.y), sz = pack2(xs.z, xs.z);
         const f2 sm = pack2(xs.w, xs.w);
-        f2 PX = 0ull, PY = 0ull, PZ = 0ull;
+        f2 PX = 0ull, PY = 0ull, PZ = 0ull, PW = 0ull;
 #pragma unroll
         for (int h = 0; h < H; ++h) {
             const f2 dx = sub2(sx, TX[h]), dy = sub2(sy, TY[h]), dz = sub2(sz, TZ[h]);
             const f2 r2 = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, EPS2)));
-            const f2 inv = rsqrt2(r2);
-            f2 c = mul2(inv, mul2(inv, inv));
-            if (DIAG) {
+            f2 inv = rsqrt2(r2);
+            if (DIAG) {  // a zero inv zeroes the pair's force and potential terms
                 float c0, c1;
-                unpack2(c, c0, c1);
+                unpack2(inv, c0, c1);
                 const int t0 = DsShape<H>::WT * wib + 64 * h + lane;
                 c0 = t0 < jj ? c0 : 0.f;
                 c1 = t0 + 32 < jj ? c1 : 0.f;
-                c = pack2(c0, c1);
+                inv = pack2(c0, c1);
             }
+            const f2 c = mul2(inv, mul2(inv, inv));
             const f2 ct = mul2(sm, c);     // m_s c: the targets' side
             const f2 cs = mul2(TM[h], c);  // m_t c: the source's side (subtracted)
             NX[h] = fma2(ct, dx, NX[h]);
@@ -114,6 +118,10 @@ __device__ __forceinline__ void ds_round(const float4 *__restrict__ sxm, float4 
             PX = fma2(cs, dx, PX);
             PY = fma2(cs, dy, PY);
             PZ = fma2(cs, dz, PZ);
+            if (PHI) {
+                NW[h] = fma2(sm, inv, NW[h]);
+                PW = fma2(TM[h], inv, PW);
+            }
         }
         float4 acc = sacc[jj];
         float lo, hi;
@@ -123,6 +131,10 @@ __device__ __forceinline__ void ds_round(const float4 *__restrict__ sxm, float4 
         acc.y -= lo + hi;
         unpack2(PZ, lo, hi);
         acc.z -= lo + hi;
+        if (PHI) {
+            unpack2(PW, lo, hi);
+            acc.w += lo + hi;
+        }
         sacc[jj] = acc;
         __syncwarp();
     }
@@ -169,7 +181,9 @@ __device__ __forceinline__ void ds_round_phi(const float4 *__restrict__ sxm, flo
     }
 }
 
-template <int Q, int MODE, bool BATCH, int H>
+// PHI (one system, MODE DS_ACC or DS_KDK): the pass also returns the
+// potential sums of its positions, in the slots' .w.
+template <int Q, int MODE, bool BATCH, int H, bool PHI>
 __global__ void __launch_bounds__(DsShape<H>::WARPS * 32, DsShape<H>::MIN_CTAS) direct_sym_kernel(DsArgs a) {
     constexpr int G = 16 / Q, SPAN = G * 32;
     constexpr int WARPS = DsShape<H>::WARPS, WT = DsShape<H>::WT;
@@ -195,7 +209,7 @@ __global__ void __launch_bounds__(DsShape<H>::WARPS * 32, DsShape<H>::MIN_CTAS) 
             }
         }
         __syncthreads();
-        f2 TX[H], TY[H], TZ[H], TM[H], NX[H], NY[H], NZ[H];
+        f2 TX[H], TY[H], TZ[H], TM[H], NX[H], NY[H], NZ[H], NW[H];
         bool diag;
         int gbase;
         {
@@ -229,7 +243,7 @@ __global__ void __launch_bounds__(DsShape<H>::WARPS * 32, DsShape<H>::MIN_CTAS) 
                 TY[h] = pack2(x0.y, x1.y);
                 TZ[h] = pack2(x0.z, x1.z);
                 TM[h] = pack2(x0.w, x1.w);
-                NX[h] = NY[h] = NZ[h] = 0ull;
+                NX[h] = NY[h] = NZ[h] = NW[h] = 0ull;
             }
             for (int t = tid; t < SPAN; t += WARPS * 32) {
                 const int tt = sl * SPAN + t;
@@ -253,9 +267,9 @@ __global__ void __launch_bounds__(DsShape<H>::WARPS * 32, DsShape<H>::MIN_CTAS) 
                         ds_round_phi<true, H>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX);
                 } else {
                     if (!diag)
-                        ds_round<false, H>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX, NY, NZ);
+                        ds_round<false, H, PHI>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX, NY, NZ, NW);
                     else if ((WT / 32) * wib <= g)
-                        ds_round<true, H>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX, NY, NZ);
+                        ds_round<true, H, PHI>(sxm, sacc, g, lane, wib, EPS2, TX, TY, TZ, TM, NX, NY, NZ, NW);
                 }
             }
             __syncthreads();
@@ -271,13 +285,14 @@ __global__ void __launch_bounds__(DsShape<H>::WARPS * 32, DsShape<H>::MIN_CTAS) 
         }
 #pragma unroll
         for (int h = 0; h < H; ++h) {
-            float x0, x1, y0, y1, z0, z1;
+            float x0, x1, y0, y1, z0, z1, w0 = 0.f, w1 = 0.f;
             unpack2(NX[h], x0, x1);
             unpack2(NY[h], y0, y1);
             unpack2(NZ[h], z0, z1);
+            if (PHI) unpack2(NW[h], w0, w1);
             float4 *row = a.rowpart + u * DS_T + WT * wib + 64 * h + lane;
-            row[0] = make_float4(x0, y0, z0, 0.f);
-            row[32] = make_float4(x1, y1, z1, 0.f);
+            row[0] = make_float4(x0, y0, z0, w0);
+            row[32] = make_float4(x1, y1, z1, w1);
         }
     }
 }
@@ -320,9 +335,12 @@ struct DsFix {
 // order.
 constexpr int DS_FIX_WARPS = 8;
 
-template <int MODE, bool KAHAN, bool BATCH>
+// PHI: the slots also carry potential sums in .w (force pass with the
+// potential); the particle's sum is written to phi (without G) beside its
+// acceleration.
+template <int MODE, bool KAHAN, bool BATCH, bool PHI>
 __global__ void __launch_bounds__(DS_FIX_WARPS * 32) direct_sym_fixup_kernel(DsFix f) {
-    __shared__ float3 part[DS_FIX_WARPS][32];
+    __shared__ float4 part[DS_FIX_WARPS][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int64_t o = 0, n_s = f.n, nt = f.nt, li0 = f.Ib * DS_T + (int64_t)blockIdx.x * 32, ub = 0, cb = 0;
     int64_t Ib = f.Ib, Ie = f.Ie, p0 = f.p0;
@@ -344,14 +362,16 @@ __global__ void __launch_bounds__(DS_FIX_WARPS * 32) direct_sym_fixup_kernel(DsF
     const int64_t R = in_band ? (nt - T) * f.Q : 0;
     const int64_t C = (in_band ? T : Ie - 1) - Ib + 1;
     const int64_t rbase = ub + (sym_base(T, nt) - p0) * f.Q;
-    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f, sw = 0.f, cw = 0.f;
     auto add = [&](float4 v) {
         if (KAHAN) {
             kahan_add(sx, cx, v.x);
             kahan_add(sy, cy, v.y);
             kahan_add(sz, cz, v.z);
+            if (PHI) kahan_add(sw, cw, v.w);
         } else {
             sx += v.x; sy += v.y; sz += v.z;
+            if (PHI) sw += v.w;
         }
     };
     // Rows of padded particles (li >= n_s) are zero-mass records: reading
@@ -361,26 +381,24 @@ __global__ void __launch_bounds__(DS_FIX_WARPS * 32) direct_sym_fixup_kernel(DsF
         const int64_t I2 = Ib + k;
         add(f.colpart[(cb + sym_base(I2, nt) + (T - I2) - p0) * DS_T + r]);
     }
-    part[w][lane] = make_float3(sx - cx, sy - cy, sz - cz);
+    part[w][lane] = make_float4(sx - cx, sy - cy, sz - cz, sw - cw);
     __syncthreads();
     if (w != 0 || li >= n_s) return;
     const int64_t i = o + li;
-    sx = sy = sz = cx = cy = cz = 0.f;
+    sx = sy = sz = cx = cy = cz = sw = cw = 0.f;
     if (!BATCH && Ib > 0) {  // the running sum of the earlier bands
         const float4 s0 = f.aux[2 * i], c0 = f.aux[2 * i + 1];
-        sx = s0.x; sy = s0.y; sz = s0.z;
-        cx = c0.x; cy = c0.y; cz = c0.z;
+        sx = s0.x; sy = s0.y; sz = s0.z; sw = s0.w;
+        cx = c0.x; cy = c0.y; cz = c0.z; cw = c0.w;
     }
 #pragma unroll
-    for (int q = 0; q < DS_FIX_WARPS; ++q) {
-        const float3 v = part[q][lane];
-        add(make_float4(v.x, v.y, v.z, 0.f));
-    }
+    for (int q = 0; q < DS_FIX_WARPS; ++q) add(part[q][lane]);
     if (!BATCH && !in_band) {
-        f.aux[2 * i] = make_float4(sx, sy, sz, 0.f);
-        f.aux[2 * i + 1] = make_float4(cx, cy, cz, 0.f);
+        f.aux[2 * i] = make_float4(sx, sy, sz, sw);
+        f.aux[2 * i + 1] = make_float4(cx, cy, cz, cw);
         return;
     }
+    if (PHI) f.phi[i] = sw - cw;
     float4 an = make_float4(f.G * (sx - cx), f.G * (sy - cy), f.G * (sz - cz), 0.f);
     if (MODE == DS_PHI) {
         f.phi[i] = an.x;
@@ -403,36 +421,41 @@ __global__ void __launch_bounds__(DS_FIX_WARPS * 32) direct_sym_fixup_kernel(DsF
     kdk_writeback(f.xm, f.vel, f.acc, i, an, f.h, f.dt);
 }
 
-template <int MODE, bool BATCH, int H>
+template <int MODE, bool BATCH, int H, bool PHI>
 static void launch_force(int Q, unsigned grid, const DsArgs &a, cudaStream_t s) {
     const unsigned b = DsShape<H>::WARPS * 32;
-    if (Q == 1) direct_sym_kernel<1, MODE, BATCH, H><<<grid, b, 0, s>>>(a);
-    else if (Q == 2) direct_sym_kernel<2, MODE, BATCH, H><<<grid, b, 0, s>>>(a);
-    else if (Q == 4) direct_sym_kernel<4, MODE, BATCH, H><<<grid, b, 0, s>>>(a);
-    else direct_sym_kernel<8, MODE, BATCH, H><<<grid, b, 0, s>>>(a);
+    if (Q == 1) direct_sym_kernel<1, MODE, BATCH, H, PHI><<<grid, b, 0, s>>>(a);
+    else if (Q == 2) direct_sym_kernel<2, MODE, BATCH, H, PHI><<<grid, b, 0, s>>>(a);
+    else if (Q == 4) direct_sym_kernel<4, MODE, BATCH, H, PHI><<<grid, b, 0, s>>>(a);
+    else direct_sym_kernel<8, MODE, BATCH, H, PHI><<<grid, b, 0, s>>>(a);
 }
 
-template <int MODE, bool BATCH>
+template <int MODE, bool BATCH, bool PHI>
 static void launch_mode(int Q, bool kahan, unsigned grid, unsigned fgrid, const DsArgs &a, const DsFix &f,
                         cudaStream_t s) {
-    launch_force<MODE, BATCH, DS_H>(Q, grid, a, s);
-    if (kahan) direct_sym_fixup_kernel<MODE, true, BATCH><<<fgrid, DS_FIX_WARPS * 32, 0, s>>>(f);
-    else direct_sym_fixup_kernel<MODE, false, BATCH><<<fgrid, DS_FIX_WARPS * 32, 0, s>>>(f);
+    launch_force<MODE, BATCH, DS_H, PHI>(Q, grid, a, s);
+    if (kahan) direct_sym_fixup_kernel<MODE, true, BATCH, PHI><<<fgrid, DS_FIX_WARPS * 32, 0, s>>>(f);
+    else direct_sym_fixup_kernel<MODE, false, BATCH, PHI><<<fgrid, DS_FIX_WARPS * 32, 0, s>>>(f);
 }
 
-// mode: DS_ACC, DS_KDK or (one system) DS_PHI.
+// mode: DS_ACC, DS_KDK or (one system) DS_PHI; phi (one system, DS_ACC or
+// DS_KDK): the force pass also writes the potential sums.
 template <bool BATCH>
-static void launch_pass(int mode, int Q, bool kahan, unsigned grid, unsigned fgrid, const DsArgs &a,
+static void launch_pass(int mode, bool phi, int Q, bool kahan, unsigned grid, unsigned fgrid, const DsArgs &a,
                         const DsFix &f, cudaStream_t s) {
-    if (mode == DS_KDK) launch_mode<DS_KDK, BATCH>(Q, kahan, grid, fgrid, a, f, s);
-    else if (mode == DS_ACC) launch_mode<DS_ACC, BATCH>(Q, kahan, grid, fgrid, a, f, s);
-    else if constexpr (!BATCH) launch_mode<DS_PHI, BATCH>(Q, kahan, grid, fgrid, a, f, s);
+    if constexpr (!BATCH) {
+        if (phi && mode == DS_KDK) return launch_mode<DS_KDK, false, true>(Q, kahan, grid, fgrid, a, f, s);
+        if (phi && mode == DS_ACC) return launch_mode<DS_ACC, false, true>(Q, kahan, grid, fgrid, a, f, s);
+    }
+    if (mode == DS_KDK) launch_mode<DS_KDK, BATCH, false>(Q, kahan, grid, fgrid, a, f, s);
+    else if (mode == DS_ACC) launch_mode<DS_ACC, BATCH, false>(Q, kahan, grid, fgrid, a, f, s);
+    else if constexpr (!BATCH) launch_mode<DS_PHI, BATCH, false>(Q, kahan, grid, fgrid, a, f, s);
 }
 
 SymShape direct_sym_shape(int sms, int64_t pairs) {
     SymShape sh;
     int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, direct_sym_kernel<1, DS_ACC, false, DS_H>,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, direct_sym_kernel<1, DS_ACC, false, DS_H, false>,
                                                   DsShape<DS_H>::WARPS * 32, 0);
     sh.slots = (int64_t)sms * std::max(occ, 1);
     sh.Q = direct_sym_slices(pairs, sh.slots, DsShape<DS_H>::QMAX);
@@ -519,8 +542,8 @@ int run_direct_sym(gb_direct *h, int mode, const float4 *xm, float4 *vel, float4
         f.Ie = Ie;
         f.p0 = a.p0;
         GB_CUDA_TRY(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), s));
-        launch_pass<false>(mode, pl.Q, kahan, (unsigned)std::min(pl.slots, a.NU),
-                           (unsigned)((n - Ib * DS_T + 31) / 32), a, f, s);
+        launch_pass<false>(mode, phi != nullptr && mode != DS_PHI, pl.Q, kahan,
+                           (unsigned)std::min(pl.slots, a.NU), (unsigned)((n - Ib * DS_T + 31) / 32), a, f, s);
         GB_CUDA_TRY(cudaGetLastError());
         h->launches += 2;
     }
@@ -563,7 +586,7 @@ int run_batch_sym(const SymBatch &b, int mode, const float4 *xm, float4 *vel, fl
     f.dt = dt;
     f.accumulate = (flags & GB_ACCUMULATE) ? 1 : 0;
     GB_CUDA_TRY(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), s));
-    launch_pass<true>(mode, b.Q, !(flags & GB_PLAIN_FP32), (unsigned)b.P, (unsigned)b.nfb, a, f, s);
+    launch_pass<true>(mode, false, b.Q, !(flags & GB_PLAIN_FP32), (unsigned)b.P, (unsigned)b.nfb, a, f, s);
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
 }

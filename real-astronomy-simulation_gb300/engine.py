@@ -9,7 +9,20 @@ library.  Extra keyword arguments: ``G`` (default core/units.py:21),
 ``max_stack`` (traversal stack rule, reference default 64), ``plain_fp32``
 (disable Kahan accumulation), ``symmetric`` (direct sum: evaluate each
 unordered pair once and update both particles, default; False runs one pass
-per target), ``device``.
+per target), ``check`` (tree mode: every step waits for the device and
+raises GravityError when the traversal's max_stack rule dropped work or a
+position is not finite; the reference drops such work silently),
+``fused_potential`` (default True: the force pass of the last step of every
+``step``/``run`` call, and of the priming in ``load_state``, also writes the
+potential of its positions, so ``energies()`` afterwards runs only the O(N)
+FP64 reductions instead of an O(N^2) potential pass), ``device``.
+
+Energies (core/engine.py:119-124): the direct mode's potential is the
+potential_energy sum (core/solvers/gravity.py:39-57); the tree mode's is the
+tree potential of the traversal (monopole terms of the accepted nodes),
+which agrees with that sum within the tree's own error.
+``energies(exact=True)`` runs the O(N^2) sum in either mode, as the
+reference does at every call.
 
 As in the reference (core/engine.py:75-80), gravity_mode="bh" uses the tree
 only for n >= 256; smaller systems use the direct sum.
@@ -37,7 +50,7 @@ class Engine:
     def __init__(self, softening: float = 0.05, gravity_mode: str = "direct",
                  theta: float = 0.6, *, G: float = units.G, key_bits: int = 21,
                  max_stack: int = 64, plain_fp32: bool = False, symmetric: bool = True,
-                 device=None):
+                 check: bool = False, fused_potential: bool = True, device=None):
         if gravity_mode not in ("direct", "bh"):
             raise ValueError(f"gravity_mode must be 'direct' or 'bh', got {gravity_mode!r}")
         self.softening = float(softening)
@@ -48,6 +61,10 @@ class Engine:
         self.max_stack = int(max_stack)
         self.plain_fp32 = bool(plain_fp32)
         self.symmetric = bool(symmetric)
+        self.check = bool(check)
+        self.fused_potential = bool(fused_potential)
+        self.phi = None          # potential sums (no G) of the current positions, when valid
+        self._phi_valid = False
         self.device = require_cuda(device)
         self._bh = None
         self._direct = None
@@ -63,11 +80,15 @@ class Engine:
     # ---------------------------------------------------------------- fields
     @property
     def pos(self):
-        return None if self.xm is None else FieldView(self.xm, slice(0, 3))
+        return None if self.xm is None else FieldView(self.xm, slice(0, 3), self._invalidate_phi)
 
     @property
     def mass(self):
-        return None if self.xm is None else FieldView(self.xm, 3)
+        return None if self.xm is None else FieldView(self.xm, 3, self._invalidate_phi)
+
+    def _invalidate_phi(self) -> None:
+        """Positions or masses were written: the stored potential is stale."""
+        self._phi_valid = False
 
     @property
     def vel(self):
@@ -98,20 +119,28 @@ class Engine:
             self.xm = pack_xm(state.pos, state.mass, self.device)
             self.v4 = pack_vec(state.vel, self.device)
             self.a4 = empty4(self.n, self.device)
+            self.phi = torch.zeros(self.n, dtype=torch.float32, device=self.device)
             self._make_solvers()
             self._compute_acc()
 
     def _make_solvers(self) -> None:
-        if self._direct is None or self._direct.n_max < max(self.n, 1):
-            self._direct = DirectGravity(max(self.n, 1), self.device)
-            self._direct.set_variant(2 if self.symmetric else 0)
         if self.gravity_mode == "bh" and self.n >= BH_MIN_N:
             from .solvers.barnes_hut import BarnesHut
             self._bh = BarnesHut(self.n, theta=self.theta, softening=self.softening,
                                  max_stack=self.max_stack, key_bits=self.key_bits,
-                                 G=self.G, device=self.device)
+                                 G=self.G, check=self.check, device=self.device)
         else:
             self._bh = None
+            self._direct_solver()
+
+    def _direct_solver(self) -> DirectGravity:
+        """The direct-sum solver, made on first use: the direct mode steps with
+        it; the tree mode needs it only for a potential its steps did not
+        provide."""
+        if self._direct is None or self._direct.n_max < max(self.n, 1):
+            self._direct = DirectGravity(max(self.n, 1), self.device)
+            self._direct.set_variant(2 if self.symmetric else 0)
+        return self._direct
 
     def to_state(self) -> State:
         """Download the state into a host State (core/engine.py:83-98)."""
@@ -151,19 +180,26 @@ class Engine:
             self.v4 = empty4(n, self.device)
             self.v4[:, :3] = vel.to(self.device, torch.float32)
             self.a4 = empty4(n, self.device)
+            self.phi = torch.zeros(n, dtype=torch.float32, device=self.device)
             self._make_solvers()
             self._compute_acc()
 
     # -------------------------------------------------------------- stepping
     def _compute_acc(self) -> None:
-        """core/engine.py:101-106."""
+        """core/engine.py:101-106 (with fused_potential the same pass also
+        writes the potential)."""
+        self._phi_valid = False
         if self.n == 0:
             return
+        phi = self.phi if self.fused_potential else None
         with torch.cuda.device(self.device):
             if self._bh is not None:
-                self._bh.compute(self.xm, self.a4)
+                self._bh.compute(self.xm, self.a4, phi=phi)
+            elif phi is not None:
+                self._direct.acc_phi(self.xm, self.a4, phi, self.G, self.eps2, plain=self.plain_fp32)
             else:
                 self._direct.acc(self.xm, self.a4, self.G, self.eps2, plain=self.plain_fp32)
+        self._phi_valid = phi is not None
 
     def step(self, dt: float) -> None:
         """One KDK step (core/engine.py:108-116); kick and drift are fused
@@ -175,23 +211,39 @@ class Engine:
         if nsteps <= 0:
             return
         if self.n > 0:
+            self._phi_valid = False
+            phi = self.phi if self.fused_potential else None
             with torch.cuda.device(self.device):
                 if self._bh is not None:
-                    self._bh.kdk(self.xm, self.v4, self.a4, dt, nsteps)
+                    self._bh.kdk(self.xm, self.v4, self.a4, dt, nsteps, phi=phi)
                 else:
                     self._direct.kdk(self.xm, self.v4, self.a4, self.G, self.eps2, dt, nsteps,
-                                     plain=self.plain_fp32, graph=True)
+                                     plain=self.plain_fp32, graph=True, phi=phi)
+            self._phi_valid = phi is not None
         self.time += dt * nsteps
         self.step_count += nsteps
 
     # ----------------------------------------------------------- diagnostics
-    def energies(self) -> tuple[float, float, float]:
-        """(kinetic, potential, total) in code units (core/engine.py:119-124);
-        FP64 reductions over FP32-Kahan pair sums."""
+    def energies(self, exact: bool = False) -> tuple[float, float, float]:
+        """(kinetic, potential, total) in code units (core/engine.py:119-124),
+        FP64 reductions.  The potential is the one the last force pass wrote
+        (fused_potential) when it is current, else a pass of its own: the
+        tree potential in tree mode, the FP32-Kahan pair sum otherwise.
+        exact=True always runs the O(N^2) pair sum, as the reference does."""
         if self.n == 0:
             return 0.0, 0.0, 0.0
         with torch.cuda.device(self.device):
-            return self._direct.energies(self.xm, self.v4, self.G, self.eps2)
+            if exact:
+                return self._direct_solver().energies(self.xm, self.v4, self.G, self.eps2)
+            if not self._phi_valid:
+                if self._bh is not None:
+                    self._bh.compute(self.xm, torch.empty_like(self.a4), phi=self.phi)
+                else:
+                    self._direct.phi(self.xm, self.eps2, out=self.phi, plain=self.plain_fp32)
+                self._phi_valid = True
+            if self._bh is not None:
+                return self._bh.energies_from_phi(self.xm, self.v4, self.phi)
+            return self._direct.energies_from_phi(self.xm, self.v4, self.phi, self.G)
 
     def diagnostics(self) -> dict:
         """The energy / virial record a simulation controller shows

@@ -5,8 +5,11 @@ Mirrors ``BarnesHut(n, theta, softening, max_stack).compute(pos, mass, acc)``
 sort, Karras build, node summaries, traversal) runs on the device; keys,
 order and topology are bit-identical to the reference's and each particle
 accepts the same node set.  Extra keyword arguments: ``key_bits`` (21 = the
-reference's 63-bit keys, 10 = 30-bit keys) and ``G`` (the reference compiles
-core/units.py:21 into its traversal).
+reference's 63-bit keys, 10 = 30-bit keys), ``G`` (the reference compiles
+core/units.py:21 into its traversal) and ``check``: every call waits for the
+device and raises GravityError (GB_ESTACK) when the max_stack rule dropped
+work, or (GB_EINVAL) on non-finite positions, where the reference drops
+subtrees silently (core/solvers/barnes_hut.py:212).
 """
 from __future__ import annotations
 
@@ -29,7 +32,7 @@ _TORCH = {np.uint64: torch.int64, np.int32: torch.int32, np.float64: torch.float
 class BarnesHut:
     def __init__(self, n: int, theta: float = 0.6, softening: float = 0.1,
                  max_stack: int = 64, *, key_bits: int = 21, G: float = units.G,
-                 device=None):
+                 check: bool = False, device=None):
         self.device = require_cuda(device)
         self.n = int(n)
         self.theta = float(theta)
@@ -44,6 +47,10 @@ class BarnesHut:
             _lib.call("gb_bh_create", ctypes.byref(h), max(self.n, 1), self.key_bits)
         self._h = h
         self._last_n = 0
+        self._out3 = None
+        self.check = bool(check)
+        if self.check:
+            _lib.call("gb_bh_set_check", h, 1)
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
@@ -70,19 +77,30 @@ class BarnesHut:
         self._last_n = self._n(xm)
         _lib.call("gb_bh_build", self._h, ptr(xm, "xm"), self._last_n, stream_handle(self.device))
 
-    def accel(self, acc: torch.Tensor, accumulate: bool = False) -> torch.Tensor:
-        _lib.call("gb_bh_accel", self._h, ptr(acc, "acc"), self.theta, self.eps2, self.G,
-                  self.max_stack, _lib.GB_ACCUMULATE if accumulate else 0,
-                  stream_handle(self.device))
+    def accel(self, acc: torch.Tensor, accumulate: bool = False, phi=None) -> torch.Tensor:
+        """Tree accelerations of the last build; with phi ((n,) float32
+        device tensor) the traversal also writes the tree potential (the
+        monopole terms of the accepted nodes, without G)."""
+        flags = _lib.GB_ACCUMULATE if accumulate else 0
+        if phi is None:
+            _lib.call("gb_bh_accel", self._h, ptr(acc, "acc"), self.theta, self.eps2, self.G,
+                      self.max_stack, flags, stream_handle(self.device))
+        else:
+            _lib.call("gb_bh_accel_phi", self._h, ptr(acc, "acc"), ptr(phi, "phi", rows4=False),
+                      self.theta, self.eps2, self.G, self.max_stack, flags, stream_handle(self.device))
         return acc
 
-    def compute(self, *args, accumulate: bool = False, count_work: bool = False):
+    def compute(self, *args, accumulate: bool = False, count_work: bool = False,
+                check: bool = False, phi=None):
         """acc <- tree accelerations (core/solvers/barnes_hut.py:242-259).
         Call forms: ``compute(pos_field, mass_field, acc_field)``, the
         reference's (fields, numpy arrays or tensors; acc filled in place),
         or ``compute(xm, acc)`` on (n, 4) float32 device records.
         count_work adds the traversal work counters to diag() (a slightly
-        slower kernel variant)."""
+        slower kernel variant); check waits for the call and raises
+        GravityError on failures counted since the last checked call (see
+        the ``check`` constructor argument); phi ((n,) float32 device
+        tensor, record form only) receives the tree potential."""
         if len(args) == 3:
             pos, mass, acc_out = args
             dev = pick_device(pos, mass, acc_out)
@@ -92,25 +110,48 @@ class BarnesHut:
             acc = empty4(self.n, dev)
             if accumulate:
                 acc[:, :3] = field_values(acc_out, dev)[: self.n].reshape(self.n, 3)
-            self._compute(xm, acc, accumulate, count_work)
+            self._compute(xm, acc, accumulate, count_work, check)
             write_rows(acc_out, acc[:, :3])
             return acc_out
         xm, acc = args
-        return self._compute(xm, acc, accumulate, count_work)
+        return self._compute(xm, acc, accumulate, count_work, check, phi)
 
-    def _compute(self, xm, acc, accumulate, count_work):
+    def _compute(self, xm, acc, accumulate, count_work, check=False, phi=None):
         self._last_n = self._n(xm)
-        flags = (_lib.GB_ACCUMULATE if accumulate else 0) | (_lib.GB_COUNT_WORK if count_work else 0)
+        flags = ((_lib.GB_ACCUMULATE if accumulate else 0) | (_lib.GB_COUNT_WORK if count_work else 0)
+                 | (_lib.GB_CHECK if check else 0))
+        if phi is not None:
+            _lib.call("gb_bh_build", self._h, ptr(xm, "xm"), self._last_n, stream_handle(self.device))
+            _lib.call("gb_bh_accel_phi", self._h, ptr(acc, "acc"), ptr(phi, "phi", rows4=False),
+                      self.theta, self.eps2, self.G, self.max_stack, flags, stream_handle(self.device))
+            return acc
         _lib.call("gb_bh_compute", self._h, ptr(xm, "xm"), ptr(acc, "acc"), self._last_n,
                   self.theta, self.eps2, self.G, self.max_stack, flags, stream_handle(self.device))
         return acc
 
-    def kdk(self, xm, vel, acc, dt: float, nsteps: int = 1) -> None:
-        """nsteps KDK leapfrog steps with tree forces, in place."""
+    def kdk(self, xm, vel, acc, dt: float, nsteps: int = 1, phi=None) -> None:
+        """nsteps KDK leapfrog steps with tree forces, in place; with phi
+        the last step also writes the tree potential of the final
+        positions."""
         self._last_n = self._n(xm)
-        _lib.call("gb_bh_kdk", self._h, ptr(xm, "xm"), ptr(vel, "vel"), ptr(acc, "acc"),
-                  self._n(xm), self.theta, self.eps2, self.G, float(dt), int(nsteps),
-                  self.max_stack, stream_handle(self.device))
+        if phi is None:
+            _lib.call("gb_bh_kdk", self._h, ptr(xm, "xm"), ptr(vel, "vel"), ptr(acc, "acc"),
+                      self._n(xm), self.theta, self.eps2, self.G, float(dt), int(nsteps),
+                      self.max_stack, stream_handle(self.device))
+        else:
+            _lib.call("gb_bh_kdk_phi", self._h, ptr(xm, "xm"), ptr(vel, "vel"), ptr(acc, "acc"),
+                      ptr(phi, "phi", rows4=False), self._n(xm), self.theta, self.eps2, self.G,
+                      float(dt), int(nsteps), self.max_stack, stream_handle(self.device))
+
+    def energies_from_phi(self, xm, vel, phi) -> tuple[float, float, float]:
+        """(KE, PE, KE+PE) in FP64 from a tree potential phi."""
+        if self._out3 is None:
+            self._out3 = torch.zeros(3, dtype=torch.float64, device=self.device)
+        _lib.call("gb_bh_energy", self._h, ptr(xm, "xm"), ptr(vel, "vel"),
+                  ptr(phi, "phi", rows4=False), xm.shape[0], self.G,
+                  ptr(self._out3, "out3", torch.float64, rows4=False), stream_handle(self.device))
+        e = self._out3.cpu().numpy()
+        return float(e[0]), float(e[1]), float(e[2])
 
     def export(self, name: str) -> np.ndarray:
         """One array of the last build in the reference's layout."""

@@ -76,13 +76,29 @@ class DirectGravity:
                   float(G), float(eps2), flags, stream_handle(self.device))
         return acc
 
-    def kdk(self, xm, vel, acc, G, eps2, dt, nsteps=1, plain=False, graph=False):
-        """nsteps fused KDK steps in place; graph=True replays one captured
-        step as a CUDA graph (identical results, fewer launches)."""
+    def acc_phi(self, xm, acc, phi, G, eps2, plain=False):
+        """acc() that also writes the potential sums of the same positions
+        into phi ((n,) float32 device tensor, without G) from the same pass."""
+        n = xm.shape[0]
+        _lib.call("gb_direct_acc_phi", self._h, ptr(xm, "xm"), ptr(acc, "acc"),
+                  ptr(phi, "phi", rows4=False), n, float(G), float(eps2),
+                  _lib.GB_PLAIN_FP32 if plain else 0, stream_handle(self.device))
+        return acc
+
+    def kdk(self, xm, vel, acc, G, eps2, dt, nsteps=1, plain=False, graph=False, phi=None):
+        """nsteps fused KDK steps in place; graph=True replays captured
+        steps as CUDA graphs (identical results, fewer launches).  With phi
+        ((n,) float32 device tensor) the last step's force pass also writes
+        the potential sums of the final positions."""
         n = xm.shape[0]
         flags = (_lib.GB_PLAIN_FP32 if plain else 0) | (_lib.GB_USE_GRAPH if graph else 0)
-        _lib.call("gb_direct_kdk", self._h, ptr(xm, "xm"), ptr(vel, "vel"), ptr(acc, "acc"),
-                  n, float(G), float(eps2), float(dt), int(nsteps), flags, stream_handle(self.device))
+        if phi is None:
+            _lib.call("gb_direct_kdk", self._h, ptr(xm, "xm"), ptr(vel, "vel"), ptr(acc, "acc"),
+                      n, float(G), float(eps2), float(dt), int(nsteps), flags, stream_handle(self.device))
+        else:
+            _lib.call("gb_direct_kdk_phi", self._h, ptr(xm, "xm"), ptr(vel, "vel"), ptr(acc, "acc"),
+                      ptr(phi, "phi", rows4=False), n, float(G), float(eps2), float(dt), int(nsteps),
+                      flags, stream_handle(self.device))
 
     def phi(self, xm, eps2, out=None, plain=False):
         n = xm.shape[0]
@@ -101,6 +117,15 @@ class DirectGravity:
 
     def energies(self, xm, vel, G, eps2):
         e = self.energies_async(xm, vel, G, eps2).cpu().numpy()
+        return float(e[0]), float(e[1]), float(e[2])
+
+    def energies_from_phi(self, xm, vel, phi, G):
+        """(KE, PE, KE+PE) from potential sums phi the force pass already
+        produced: only the O(n) FP64 reductions run."""
+        _lib.call("gb_energy_phi", self._h, ptr(xm, "xm"), ptr(vel, "vel"),
+                  ptr(phi, "phi", rows4=False), xm.shape[0], float(G),
+                  ptr(self._out3, "out3", torch.float64, rows4=False), stream_handle(self.device))
+        e = self._out3.cpu().numpy()
         return float(e[0]), float(e[1]), float(e[2])
 
     def launch_count(self) -> int:

@@ -7,9 +7,10 @@ source change is ``rewrite_atomics`` applied to ``_accumulate``
 (core/solvers/barnes_hut.py:143-166), turning ``ti.atomic_add/min/max`` on a
 field element into the equivalent in-place update.
 
-Run from the repository root, in a container where the reference is mounted:
+Run from the repository root, in a container where the reference is mounted,
+with the reference's root directory as the first argument:
 
-    python tests/golden/gen_golden.py /root/reference
+    python tests/golden/gen_golden.py <reference root> [generator names...]
 
 Inputs are rounded to float32 first (the GPU engine stores float32), then
 passed to the reference as float64, so the fixtures describe the reference's
@@ -342,7 +343,9 @@ GENERATORS = (gen_plummer_ic, gen_direct, gen_engine_direct, gen_morton,
 def main(argv):
     """argv: [script, reference root, generator names...]; no names runs
     every generator."""
-    ref_root = argv[1] if len(argv) > 1 else "/root/reference"
+    if len(argv) < 2:
+        sys.exit("usage: gen_golden.py <reference root> [generator names...]")
+    ref_root = argv[1]
     R = _load_reference(ref_root)
     out = {}
     wanted = set(argv[2:])

@@ -324,3 +324,82 @@ def test_graph_replay_matches_direct_launches(cuda_dev):
         b.close()
     for u, w in zip(*out):
         assert torch.equal(u, w)
+
+
+def test_engine_bh_gate_at_256(cuda_dev, orc):
+    """Engine(gravity_mode="bh") uses the tree only for n >= 256
+    (core/engine.py:75): at n = 255 the accelerations are the direct sum's,
+    at n = 256 the tree's (the two differ by the monopole error, about 1e-2
+    at theta = 0.6, so each is told apart from the other)."""
+    pkg, _, ic, _ = _mods()
+    for n in (255, 256):
+        pos, vel, mass = ic.exponential_disk(n, seed=21)
+        pos, vel, mass = _f32(pos), _f32(vel), _f32(mass)
+        eng = pkg.Engine(softening=0.05, gravity_mode="bh", theta=0.6, device=cuda_dev)
+        eng.load_state(pkg.State.from_arrays(pos, vel, mass))
+        a = eng.acc.to_numpy()
+        direct = orc.direct_acc(pos, mass, eng.G, 0.0025)
+        tree, _, _ = orc.bh_compute(pos, mass, 0.6, 0.05, eng.G)
+        err_direct, err_tree = np.median(_rel(a, direct)), np.median(_rel(a, tree))
+        if n == 255:
+            assert eng._bh is None
+            assert err_direct < 1e-5 and err_tree > 1e-4, (err_direct, err_tree)
+        else:
+            assert eng._bh is not None
+            assert err_tree < 1e-5 and err_direct > 1e-4, (err_direct, err_tree)
+
+
+def test_nonfinite_positions_are_counted_and_reported(cuda_dev):
+    """NaN and infinite positions: the keying pass counts them (key 0), the
+    call finishes, and a checked call reports them as GB_EINVAL."""
+    pkg, bhmod, ic, _ = _mods()
+    lib_mod = importlib.import_module(PKG_NAME + "._lib")
+    n = 5000
+    pos, _, mass = ic.exponential_disk(n, seed=31)
+    pos = _f32(pos)
+    bad = [7, 100, 2500, 4999]
+    pos[bad[0], 0] = np.nan
+    pos[bad[1], 2] = np.inf
+    pos[bad[2]] = np.nan
+    pos[bad[3], 1] = -np.inf
+    b = bhmod.BarnesHut(n, theta=0.5, softening=0.05, device=cuda_dev)
+    xm = _xm(pos, mass, cuda_dev)
+    acc = torch.zeros_like(xm)
+    b.compute(xm, acc)
+    torch.cuda.synchronize()
+    assert b.diag(reset=True)["nonfinite"] == len(bad)
+    with pytest.raises(pkg.GravityError, match="non-finite") as e:
+        b.compute(xm, acc, check=True)
+    assert e.value.status == lib_mod.GB_EINVAL
+    # A finite system on the same handle passes the check afterwards.
+    pos2, _, mass2 = ic.exponential_disk(n, seed=32)
+    b.compute(_xm(pos2, mass2, cuda_dev), acc, check=True)
+    assert torch.isfinite(acc).all()
+
+
+@pytest.mark.parametrize("tpl", [0, 1])
+def test_checked_calls_report_stack_drops(cuda_dev, orc, tpl):
+    """With the check on, a call whose traversal dropped pushes under the
+    max_stack rule returns GB_ESTACK (the reference drops them silently,
+    core/solvers/barnes_hut.py:212); accelerations are still written, equal to
+    the unchecked call's.  An Engine with check=True raises from step()."""
+    pkg, bhmod, ic, _ = _mods()
+    lib_mod = importlib.import_module(PKG_NAME + "._lib")
+    g = load_golden("bh")
+    pos, mass = g["pos"][:400], g["mass"][:400]
+    b, a_plain = _run(bhmod, pos, mass, cuda_dev, bits=21, G=float(g["G"]), max_stack=6, tpl=tpl)
+    xm = _xm(pos, mass, cuda_dev)
+    acc = torch.zeros_like(xm)
+    with pytest.raises(pkg.GravityError, match="max_stack") as e:
+        b.compute(xm, acc, check=True)
+    assert e.value.status == lib_mod.GB_ESTACK
+    assert np.array_equal(acc[:, :3].double().cpu().numpy(), a_plain)
+    # The default max_stack drops nothing here: the check passes.
+    b2 = bhmod.BarnesHut(400, theta=0.5, softening=0.05, G=float(g["G"]), check=True, device=cuda_dev)
+    b2.compute(xm, acc)
+    eng = pkg.Engine(softening=0.05, gravity_mode="bh", theta=0.5, max_stack=6, G=float(g["G"]),
+                     check=True, device=cuda_dev)
+    with pytest.raises(pkg.GravityError, match="max_stack"):
+        eng.load_state(pkg.State.from_arrays(pos, np.zeros_like(pos), mass))
+    with pytest.raises(pkg.GravityError, match="max_stack"):
+        eng.step(1e-4)

@@ -153,3 +153,19 @@ def test_python_surface_of_the_force_forms(pkg):
     assert callable(grav.DirectGravity.set_variant) and callable(grav.DirectGravity.set_sym_band)
     assert "variant" in inspect.signature(batch.DirectBatch).parameters
     assert (2, 4, 2) in tune.DIRECT_SHAPES and (2, 4, 1) in tune.BATCH_SHAPES
+
+
+def test_noalloc_rejects_bad_arguments_without_gpu(lib):
+    """gb_direct_acc_noalloc refuses flag bits other than GB_ACCUMULATE and
+    GB_PLAIN_FP32, and sizes above its static scratch, before any CUDA call
+    (the pointers below are never dereferenced)."""
+    lib_mod = importlib.import_module(PKG_NAME + "._lib")
+    pkg = importlib.import_module(PKG_NAME)
+    fake = 1 << 12  # aligned, never read
+    for bad in (lib_mod.GB_USE_GRAPH, lib_mod.GB_COUNT_WORK, 0x100):
+        with pytest.raises(pkg.GravityError, match="flags") as e:
+            lib_mod.call("gb_direct_acc_noalloc", fake, fake, 10, 1.0, 1e-4, bad, None)
+        assert e.value.status == lib_mod.GB_EINVAL
+    with pytest.raises(pkg.GravityError, match="outside") as e:
+        lib_mod.call("gb_direct_acc_noalloc", fake, fake, 65537, 1.0, 1e-4, 0, None)
+    assert e.value.status == lib_mod.GB_EINVAL
