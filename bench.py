@@ -21,6 +21,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes
+import hashlib
 import importlib
 import json
 import os
@@ -56,6 +57,26 @@ def _peaks():
         return float(p["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def _git_blob(path: str) -> str:
+    """git's blob hash of a file (sha1 of "blob <size>\\0" + content), so a
+    profile note can name the exact kernel source it measured."""
+    with open(path, "rb") as f:
+        data = f.read()
+    return hashlib.sha1(b"blob %d\0" % len(data) + data).hexdigest()
+
+
+def _profile_current(summary: str, source: str) -> bool:
+    """True when profiles/<summary> records the git blob hash of the kernel
+    source it measured and that hash is the current file's."""
+    try:
+        with open(os.path.join(ROOT, "profiles", summary)) as f:
+            txt = f.read()
+    except OSError:
+        return False
+    m = re.search(r"git blob `([0-9a-f]{40})`", txt)
+    return bool(m) and m.group(1) == _git_blob(os.path.join(ROOT, PKG, "csrc", source))
 
 
 def _profiled_traffic(summary: str):
@@ -272,6 +293,12 @@ def bench_bh(args, dev, rank, world, dist):
                        "algorithmic_bytes_per_launch": bytes_launch,
                        "launch_ms": trav_ms}
     traffic = _profiled_traffic("bh_traverse_1M_disk.md")
+    if traffic is not None and not _profile_current("bh_traverse_1M_disk.md", "gb_bh.cu"):
+        # The capture measured another revision of the kernel source: its
+        # figures are not this kernel's.
+        res["roofline"]["traffic_source"] = ("none: profiles/bh_traverse_1M_disk.md was captured on "
+                                             "another revision of csrc/gb_bh.cu")
+        traffic = None
     if traffic is not None and BH_N == 1_000_000 and BH_BITS == 10:
         res["roofline"]["traffic"] = traffic
         res["roofline"]["traffic_source"] = ("ncu dram bytes of one launch on this workload "
@@ -317,8 +344,125 @@ def bench_bh(args, dev, rank, world, dist):
                   "unit": "particle-steps/s", "h2d_bytes_per_step": nbytes,
                   "d2h_bytes_per_step": nbytes,
                   "path": "gb_bh_kdk via the C ABI, pinned host state copied in/out each step"}
+
+    # energies() right after a step (untimed for the headline): wall clock of
+    # one step, of one step whose traversal also writes the tree potential,
+    # and of that step plus the FP64 energy reductions read back to the host.
+    phi = torch.zeros(BH_N, dtype=torch.float32, device=dev)
+
+    def wall(fn, reps=20):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps * 1e3
+
+    t_step = wall(lambda: bh.kdk(xm, v4, a4, BH_DT, 1))
+    t_phi = wall(lambda: bh.kdk(xm, v4, a4, BH_DT, 1, phi=phi))
+    t_e = wall(lambda: (bh.kdk(xm, v4, a4, BH_DT, 1, phi=phi), bh.energies_from_phi(xm, v4, phi)))
+    res["energies_after_step"] = {"step_ms": t_step, "step_with_tree_potential_ms": t_phi,
+                                  "energies_ms": t_e - t_phi, "energies_over_step": (t_e - t_step) / t_step,
+                                  "note": "wall clock per call at N=1M: gb_bh_kdk, gb_bh_kdk_phi, "
+                                          "gb_bh_kdk_phi + gb_bh_energy read back"}
     bh.close()
+    if not args.no_secondary:
+        res["group_walk"] = bench_group_walk(args, dev, rank, world, dist, flush, hbm, src)
     return res
+
+
+def bench_group_walk(args, dev, rank, world, dist, flush, hbm, src):
+    """The opt-in group walk (traversal shape 3) on the same workload and
+    initial state as the headline: KDK step throughput (device and e2e),
+    stage split, traversal roofline and force error against FP64 direct sums
+    on the same 4,096 seeded targets at its own final state."""
+    ic = importlib.import_module(PKG + ".ic")
+    bhmod = importlib.import_module(PKG + ".solvers.barnes_hut")
+    units = importlib.import_module(PKG + ".units")
+    grav = importlib.import_module(PKG + ".solvers.gravity")
+    pos, vel, mass = ic.exponential_disk(BH_N, seed=rank)
+    xm, v4 = _xm(pos, mass, dev), _v4(vel, dev)
+    a4 = torch.zeros_like(xm)
+    bh = bhmod.BarnesHut(BH_N, theta=BH_THETA, softening=BH_EPS, key_bits=BH_BITS,
+                         G=units.G, device=dev)
+    bh.set_traversal(3)
+    bh.compute(xm, a4)
+    for _ in range(args.warmup):
+        bh.kdk(xm, v4, a4, BH_DT, 1)
+    starts, ends = _events(args.steps)
+    torch.cuda.synchronize()
+    bh.diag(reset=True)
+    bh.timing(True)
+    bh.stage_times()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        flush.zero_()
+        starts[k].record()
+        bh.kdk(xm, v4, a4, BH_DT, 1)
+        ends[k].record()
+    torch.cuda.synchronize()
+    total_ms = max_over_ranks(float(sum(s.elapsed_time(e) for s, e in zip(starts, ends))), dist, dev)
+    stages, nst = bh.stage_times()
+    bh.timing(False)
+    diag = bh.diag(reset=True)
+    out = {"traversal": 3, "value": world * BH_N * args.steps / (total_ms / 1e3),
+           "unit": "particle-steps/s", "ms_per_step": total_ms / args.steps,
+           "stages_ms_per_step": {k: v / max(nst, 1) for k, v in stages.items()},
+           "diag": {k: diag[k] for k in ("stack_overflow", "nonfinite", "bad_tree")}}
+    targets = np.random.default_rng(1234).choice(BH_N, 4096, replace=False)
+    ref = grav.acc_fp64_targets(xm, targets, units.G, BH_EPS * BH_EPS)
+    got = a4[torch.as_tensor(targets, device=dev), :3].double().cpu().numpy()
+    rel = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    out["force_error_vs_fp64_direct"] = {"targets": 4096, "median": float(np.median(rel)),
+                                         "p99": float(np.percentile(rel, 99)), "max": float(rel.max()),
+                                         "rms": float(np.sqrt((rel ** 2).mean()))}
+    # Traversal roofline: node records read (48 B each, one per lane per
+    # popped internal node; 32 B root record per group) + per particle own
+    # leaf 16 B, order 4 B, group size 4 B, velocity 16 B read + 16 B write,
+    # acceleration 16 B write.
+    tmp = torch.zeros_like(a4)
+    bh.compute(xm, tmp, count_work=True)
+    work = bh.diag(reset=True)
+    del tmp
+    trav_ms = out["stages_ms_per_step"]["traverse"]
+    bytes_launch = (48 * work["warp_node_reads"] + 32 * work["warp_root_reads"]
+                    + BH_N * (16 + 4 + 4 + 16 + 16 + 16))
+    achieved = bytes_launch / (trav_ms / 1e3) / 1e9
+    out["roofline"] = {"kernel": "bh_group_kernel", "bound": "hbm", "achieved": achieved, "peak": hbm,
+                       "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured"
+                       else "fallback 6800 GB/s", "unit": "GB/s", "frac": achieved / hbm,
+                       "algorithmic_bytes_per_launch": bytes_launch, "launch_ms": trav_ms}
+    # FP32 work: 20 flop per monopole term (list entry x target), 10 per
+    # box-acceptance test (two per record).
+    out["work_per_step"] = {"node_reads": work["warp_node_reads"], "groups": work["warp_root_reads"],
+                            "interactions": work["lane_interactions"], "tests": work["lane_tests"]}
+    out["traverse_fp32_tflops"] = (20 * work["lane_interactions"] + 10 * work["lane_tests"]) / (trav_ms / 1e3) / 1e12
+    # e2e through the C ABI with host buffers, as the headline's.
+    hx, hv, ha = (t_.detach().cpu().pin_memory() for t_ in (xm, v4, a4))
+    e_s, e_e = _events(args.steps)
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        flush.zero_()
+        e_s[k].record()
+        xm.copy_(hx, non_blocking=True)
+        v4.copy_(hv, non_blocking=True)
+        a4.copy_(ha, non_blocking=True)
+        bh.kdk(xm, v4, a4, BH_DT, 1)
+        hx.copy_(xm, non_blocking=True)
+        hv.copy_(v4, non_blocking=True)
+        ha.copy_(a4, non_blocking=True)
+        e_e[k].record()
+    torch.cuda.synchronize()
+    e2e_ms = max_over_ranks(float(sum(s.elapsed_time(e) for s, e in zip(e_s, e_e))), dist, dev)
+    nbytes = 3 * BH_N * 16
+    out["e2e"] = {"value": world * BH_N * args.steps / (e2e_ms / 1e3), "unit": "particle-steps/s",
+                  "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                  "path": "gb_bh_kdk (traversal 3) via the C ABI, pinned host state copied in/out each step"}
+    bh.close()
+    return out
 
 
 # ------------------------------------------------------------ CPU oracle
@@ -367,11 +511,51 @@ def cpu_bh_step(budget_s: float = 20.0):
 
 
 # ------------------------------------------------------------- secondary
-def bench_direct(dev, lib_mod, peak_tflops):
+# FP32 work of one unordered pair in the symmetric pass, FMA = 2 flop: 3 sub,
+# 3 FMA for |d|^2 + eps^2, 2 mul for rsqrt^3, 2 mul for the two mass
+# factors, 6 FMA for the two sides' sums (the rsqrt is on the MUFU pipe).
+SYM_PAIR_FLOP = 3 + 6 + 2 + 2 + 12
+
+
+def cpu_direct_step(n=20000, budget_s=10.0):
+    """One direct-sum KDK step of the Plummer workload (N = 20,000, G = 1,
+    eps = 0.01) with the float64 oracle (OpenMP over all host threads): the
+    force sum of a seeded target sample sized to the budget, scaled to all
+    N targets; the kick/drift halves are O(N) and timed on all particles."""
+    from oracle import oracle
+
+    ic = importlib.import_module(PKG + ".ic")
+    pos, vel, mass = ic.plummer(n, seed=0)
+    pos, vel, mass = _f32(pos), _f32(vel), _f32(mass)
+    oracle.build()
+    rng = np.random.default_rng(0)
+    probe = rng.choice(n, 500, replace=False)
+    t0 = time.perf_counter()
+    oracle.direct_acc(pos, mass, 1.0, 1e-4, probe)
+    per_target = (time.perf_counter() - t0) / probe.size
+    sample = int(min(n, max(500, budget_s / max(per_target, 1e-9))))
+    targets = np.sort(rng.choice(n, sample, replace=False))
+    acc = np.zeros_like(pos)
+    t0 = time.perf_counter()
+    vh = vel + acc * 5e-4
+    p1 = pos + vh * 1e-3
+    t_kick = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    oracle.direct_acc(p1, mass, 1.0, 1e-4, targets)
+    t_force = time.perf_counter() - t0
+    t_step = 2 * t_kick + t_force * n / sample
+    return {"value": n * n / t_step / 1e9, "unit": "G interactions/s", "cores": oracle.max_threads(),
+            "kind": "port", "ms_per_step": t_step * 1e3,
+            "sample": (f"one KDK step of the N={n} Plummer workload: kick/drift over all particles, "
+                       f"force sum of {sample} seeded targets over all {n} sources scaled to {n} targets")}
+
+
+def bench_direct(dev, lib_mod, peak_tflops, cpu=True):
     """Direct N^2 Plummer, N = 20,000, G = 1, eps = 0.01, dt = 1e-3, 100 KDK
-    steps through the Engine (symmetric pass); plus the per-target force
-    kernel's own FP32 fraction at N = 20k and 262k, and the symmetric pass
-    at the same sizes."""
+    steps through the Engine (symmetric pass); the same step through the C
+    ABI with host buffers (e2e); energies() right after a step; the CPU
+    baseline; plus the per-target force kernel's own FP32 fraction at
+    N = 20k and 262k, and the symmetric pass at the same sizes."""
     pkg = importlib.import_module(PKG)
     ic = importlib.import_module(PKG + ".ic")
     grav = importlib.import_module(PKG + ".solvers.gravity")
@@ -383,7 +567,6 @@ def bench_direct(dev, lib_mod, peak_tflops):
     targets = np.random.default_rng(0).choice(n, 2048, replace=False)
     ref = grav.acc_fp64_targets(eng.xm, targets, 1.0, 1e-4)
     err = _rel_stats(eng.acc.to_numpy()[targets], ref)
-    e0 = eng.energies()
     eng.run(1e-3, 3)
     eng.load_state(pkg.State.from_arrays(pos, vel, mass))
     e0 = eng.energies()
@@ -398,10 +581,70 @@ def bench_direct(dev, lib_mod, peak_tflops):
     gint = n * n * steps / t / 1e9
     out = {"workload": "direct N^2 Plummer N=20000, G=1, eps=0.01, dt=1e-3, 100 KDK steps",
            "gint_per_s": gint, "ms_per_step": t / steps * 1e3,
-           # N^2 delivered interactions x 20 flop over the measured FP32 peak;
-           # the symmetric pass evaluates N^2 / 2 pairs to deliver them.
-           "frac_of_fp32_peak_20flop_equivalent": gint * 20 / 1e3 / peak_tflops,
+           # Delivered interactions (N^2 per step) x 20 flop over the
+           # measured FP32 peak: a throughput; the symmetric pass evaluates
+           # N^2 / 2 pairs to deliver them.
+           "delivered_20flop_rate_over_fp32_peak": gint * 20 / 1e3 / peak_tflops,
            "energy_drift": abs((e1[2] - e0[2]) / e0[2]), "acc_err_vs_fp64_2048_targets": err}
+
+    # energies() right after a step (the reference's print cadence), wall
+    # clock: the step alone, the step plus energies() from the potential the
+    # step wrote, and the step plus an exact O(N^2) potential pass.
+    def wall(fn, reps=50):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps * 1e3
+
+    t_step = wall(lambda: eng.step(1e-3))
+    t_step_e = wall(lambda: (eng.step(1e-3), eng.energies()))
+    t_step_x = wall(lambda: (eng.step(1e-3), eng.energies(exact=True)))
+    eng_nf = pkg.Engine(softening=0.01, G=1.0, fused_potential=False, device=dev)
+    eng_nf.load_state(pkg.State.from_arrays(pos, vel, mass))
+    t_step_nf = wall(lambda: eng_nf.step(1e-3))
+    out["energies_after_step"] = {
+        "step_ms": t_step, "step_without_potential_ms": t_step_nf,
+        "energies_ms": t_step_e - t_step, "energies_exact_pass_ms": t_step_x - t_step,
+        "energies_over_step": (t_step_e - t_step) / t_step,
+        "note": "wall clock per Engine.step(dt) call at N=20000, with and without energies() after it"}
+
+    # e2e: the KDK step through the C ABI with host buffers: pinned host
+    # state copied in before and read back after every step.
+    g = grav.DirectGravity(n, dev)
+    g.set_variant(2)
+    xm, v4 = _xm(pos, mass, dev), _v4(vel, dev)
+    a4 = torch.zeros_like(xm)
+    g.acc(xm, a4, 1.0, 1e-4)
+    hx, hv, ha = (t_.detach().cpu().pin_memory() for t_ in (xm, v4, a4))
+    reps = 50
+    for _ in range(3):
+        g.kdk(xm, v4, a4, 1.0, 1e-4, 1e-3, 1, graph=True)
+    torch.cuda.synchronize()
+    s.record()
+    for _ in range(reps):
+        xm.copy_(hx, non_blocking=True)
+        v4.copy_(hv, non_blocking=True)
+        a4.copy_(ha, non_blocking=True)
+        g.kdk(xm, v4, a4, 1.0, 1e-4, 1e-3, 1, graph=True)
+        hx.copy_(xm, non_blocking=True)
+        hv.copy_(v4, non_blocking=True)
+        ha.copy_(a4, non_blocking=True)
+    e.record()
+    torch.cuda.synchronize()
+    te = s.elapsed_time(e) / reps / 1e3
+    out["e2e"] = {"value": n * n / te / 1e9, "unit": "G interactions/s", "h2d_bytes_per_step": 3 * n * 16,
+                  "d2h_bytes_per_step": 3 * n * 16, "ms_per_step": te * 1e3,
+                  "path": "gb_direct_kdk (symmetric pass, graph replay) via the C ABI, pinned host state "
+                          "copied in/out each step"}
+    g.close()
+    if cpu:
+        out["cpu_baseline"] = cpu_direct_step(n)
+        out["gpu_over_cpu"] = gint / out["cpu_baseline"]["value"]
+        out["e2e_over_cpu"] = out["e2e"]["value"] / out["cpu_baseline"]["value"]
+
     kern = {}
     for nk in (20000, 262144):
         p2, _, m2 = ic.plummer(nk, seed=1)
@@ -420,8 +663,9 @@ def bench_direct(dev, lib_mod, peak_tflops):
         tf = 20.0 * nk * nk / tk / 1e12
         kern[str(nk)] = {"ms": tk * 1e3, "gint_per_s": nk * nk / tk / 1e9, "tflops_20flop": tf,
                          "frac_of_fp32_peak": tf / peak_tflops}
-        # Symmetric variant (the Engine's default): n^2/2 pair evaluations;
-        # gint_per_s counts the n^2 ordered interactions it delivers.
+        # Symmetric variant (the Engine's default): N^2 / 2 pair evaluations.
+        # gint_per_s counts the N^2 ordered interactions it delivers; the
+        # achieved FLOP/s counts the FP32 work it executes per pair.
         g.set_variant(2)
         for _ in range(3):
             g.acc(xm, acc, 1.0, 1e-4)
@@ -431,9 +675,12 @@ def bench_direct(dev, lib_mod, peak_tflops):
         e.record()
         torch.cuda.synchronize()
         ts = s.elapsed_time(e) / reps / 1e3
+        achieved = SYM_PAIR_FLOP * nk * nk / 2 / ts / 1e12
         kern[str(nk)]["symmetric"] = {"ms": ts * 1e3, "gint_per_s": nk * nk / ts / 1e9,
-                                      "frac_of_fp32_peak_20flop_equivalent":
+                                      "delivered_20flop_rate_over_fp32_peak":
                                           20.0 * nk * nk / ts / 1e12 / peak_tflops,
+                                      "achieved_fp32_tflops": achieved,
+                                      "achieved_frac_of_fp32_peak": achieved / peak_tflops,
                                       "speedup_vs_per_target": tk / ts}
         g.close()
     out["force_kernel"] = kern
@@ -927,8 +1174,11 @@ def main(argv=None):
             "traverse_work_per_step": res["work_per_step"],
             "traverse_fp32_tflops": res["traverse_fp32_tflops"],
             "force_error_vs_fp64_direct": res["force_error_vs_fp64_direct"],
+            "energies_after_step": res["energies_after_step"],
             "diag": {k: res["diag"][k] for k in ("stack_drops", "stack_overflow", "nonfinite",
                                                   "bad_tree")}}
+    if "group_walk" in res:
+        line["group_walk"] = res["group_walk"]
     if rank == 0 and world == 1:
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_bh_step()

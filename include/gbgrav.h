@@ -264,7 +264,19 @@ int gb_bh_diag(gb_bh_t *h, gb_diag_t *out, int reset);
  * bit-identical results: each target meets its nodes in the same order.
  * Mode 1 is fastest on the 1M disk (per-lane record loads diverge); mode 0
  * on small systems, where a warp-coherent launch has too few warps to hide
- * each step's latency. */
+ * each step's latency.
+ * 3 (opt-in): group walk.  The targets are cut into groups, the largest
+ * subtrees with at most 32 leaves; a group accepts a node when
+ * size^2 < theta^2 (dmin^2 + eps^2), dmin the distance from the node's
+ * centre of mass to the group's bounding box, so every target of the group
+ * passes the reference's own test (core/solvers/barnes_hut.py:204-210) on
+ * every accepted node: each target sums a refinement of its per-particle
+ * node set, with force errors no larger on the 1M disk (median 0.84 %
+ * against 0.94 %) in about a third of the traversal time.  The node sets
+ * differ from the per-particle walk's, so results are not bit-identical to
+ * modes -1..2; the max_stack rule does not apply (a full group stack takes
+ * the child as a monopole and counts it in stack_overflow).  Keys, order and
+ * topology are the same in every mode. */
 int gb_bh_set_traversal(gb_bh_t *h, int targets_per_lane);
 
 /* Stage timing for measurement: with timing enabled, every build/step records

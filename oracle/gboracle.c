@@ -491,6 +491,122 @@ int64_t orc_traverse_phi(const double *pos, const int32_t *order, const double *
     return dropped;
 }
 
+/* Group walk: the targets are cut into groups, the maximal subtrees with at
+ * most `group` leaves (consecutive ranges of the key order, each inside one
+ * node's box); a group accepts a node when size^2 < theta2 (dmin^2 + eps2),
+ * dmin the distance from the node's centre of mass to the group's bounding
+ * box, and every leaf (its own included) is accepted.  Each target of the
+ * group sums the accepted nodes' monopoles (acc with G, phi without G, its
+ * own leaf skipped): the FP64 restatement of the device's group traversal,
+ * with the reference's acceptance test (core/solvers/barnes_hut.py:204-210)
+ * applied to a box instead of a point.  acc / phi are indexed by particle. */
+static void group_walk_one(const double *pos, const int32_t *order, const double *com,
+                           const double *nmass, const double *nmin, const double *nmax,
+                           const int32_t *left, const int32_t *right, int n, int b0, int b1,
+                           double theta2, double eps2, double G, int32_t *stack, int32_t *list,
+                           double *acc, double *phi) {
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int i = b0; i < b1; ++i)
+        for (int a = 0; a < 3; ++a) {
+            const double x = pos[3 * order[i] + a];
+            if (x < lo[a]) lo[a] = x;
+            if (x > hi[a]) hi[a] = x;
+        }
+    int sp = 0, nl = 0;
+    if (n >= 2) stack[sp++] = n; else list[nl++] = 0;
+    while (sp > 0) {
+        const int node = stack[--sp];
+        if (node < n) {
+            list[nl++] = node;
+            continue;
+        }
+        double d2 = 0.0, size = 0.0;
+        for (int a = 0; a < 3; ++a) {
+            const double c = com[3 * node + a];
+            double d = lo[a] - c > c - hi[a] ? lo[a] - c : c - hi[a];
+            d = d > 0.0 ? d : 0.0;
+            d2 += d * d;
+            const double e = nmax[3 * node + a] - nmin[3 * node + a];
+            if (e > size) size = e;
+        }
+        if (size * size < theta2 * (d2 + eps2)) {
+            list[nl++] = node;
+        } else {
+            stack[sp++] = left[node - n];
+            stack[sp++] = right[node - n];
+        }
+    }
+    for (int i = b0; i < b1; ++i) {
+        const int p = order[i];
+        const double px = pos[3 * p], py = pos[3 * p + 1], pz = pos[3 * p + 2];
+        double ax = 0.0, ay = 0.0, az = 0.0, w = 0.0;
+        for (int t = 0; t < nl; ++t) {
+            const int node = list[t];
+            if (node < n && order[node] == p) continue;
+            const double dx = com[3 * node] - px;
+            const double dy = com[3 * node + 1] - py;
+            const double dz = com[3 * node + 2] - pz;
+            const double r2 = dx * dx + dy * dy + dz * dz + eps2;
+            const double inv = 1.0 / sqrt(r2);
+            const double sc = G * nmass[node] * inv * inv * inv;
+            ax += sc * dx;
+            ay += sc * dy;
+            az += sc * dz;
+            w += nmass[node] * inv;
+        }
+        acc[3 * p] = ax;
+        acc[3 * p + 1] = ay;
+        acc[3 * p + 2] = az;
+        if (phi) phi[p] = w;
+    }
+}
+
+void orc_group_walk(const double *pos, const int32_t *order, const double *com,
+                    const double *nmass, const double *nmin, const double *nmax,
+                    const int32_t *left, const int32_t *right, int n, int group,
+                    double theta2, double eps2, double G, double *acc,
+                    double *phi) {
+    /* The groups: descend from the root until a node has at most `group`
+     * leaves (its leaves are its leftmost to its rightmost leaf). */
+    int32_t *g0 = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n + 1));
+    int32_t *g1 = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n + 1));
+    int32_t *st = (int32_t *)malloc(sizeof(int32_t) * (size_t)(2 * n + 2));
+    int ng = 0, sp = 0;
+    st[sp++] = n >= 2 ? n : 0;
+    while (sp > 0) {
+        const int v = st[--sp];
+        int lo = v, hi = v;
+        if (v >= n) {
+            lo = v;
+            while (lo >= n) lo = left[lo - n];
+            hi = v;
+            while (hi >= n) hi = right[hi - n];
+        }
+        if (hi - lo + 1 <= group) {
+            g0[ng] = lo;
+            g1[ng] = hi + 1;
+            ++ng;
+        } else {
+            st[sp++] = right[v - n];
+            st[sp++] = left[v - n];
+        }
+    }
+    free(st);
+#pragma omp parallel
+    {
+        int32_t *stack = (int32_t *)malloc(sizeof(int32_t) * (size_t)(2 * n + 2));
+        int32_t *list = (int32_t *)malloc(sizeof(int32_t) * (size_t)(2 * n + 2));
+#pragma omp for schedule(dynamic, 4)
+        for (int g = 0; g < ng; ++g)
+            group_walk_one(pos, order, com, nmass, nmin, nmax, left, right, n, g0[g], g1[g], theta2,
+                           eps2, G, stack, list, acc, phi);
+        free(stack);
+        free(list);
+    }
+    free(g0);
+    free(g1);
+}
+
 /* ------------------------------------------------------- neighbour grid
  * NeighborGrid.rebuild / rebuild_all (core/solvers/neighbor_grid.py:49-136):
  * gas = particles with is_star == 0 (all when is_star is NULL), in index

@@ -19,6 +19,7 @@ Every function follows a reference function line by line:
 * ``summaries``           core/solvers/barnes_hut.py:124-177
 * ``traverse``            core/solvers/barnes_hut.py:180-217
 * ``traverse_phi``        the same walk's monopole potential (gravity.py:47-55 on its node set)
+* ``group_walk``          the walk with the acceptance test applied to a group's box (:204-210)
 * ``bh_compute``          core/solvers/barnes_hut.py:242-259
 * ``analytic_acc``        core/living_galaxy_engine.py:124-151, core/gas_disk_engine.py:54-81
 * ``grav_ext_acc``        core/gas_disk_engine.py:20-51
@@ -92,6 +93,7 @@ def _declare(L):
     L.orc_traverse_phi.argtypes = [P, P, P, P, P, P, P, P, I32, D, D, I32, D, P,
                                    I64, P, P]
     L.orc_traverse_phi.restype = I64
+    L.orc_group_walk.argtypes = [P, P, P, P, P, P, P, P, I32, I32, D, D, D, P, P]
 
 
 def _p(a: np.ndarray):
@@ -309,6 +311,24 @@ def traverse_phi(pos, order, com, nmass, nmin, nmax, left, right, theta, eps2,
                                      _p(t) if t is not None else None, nt,
                                      _p(acc), _p(phi))
     return phi, dropped
+
+
+def group_walk(pos, tree, theta, eps2, G, group=32):
+    """Accelerations and potentials (no G) of every particle from the group
+    walk over ``tree`` (``bh_tree``'s dict): the maximal subtrees with at
+    most ``group`` leaves share the node set their bounding box accepts.
+    Returns (acc, phi) indexed by particle."""
+    pos = _f64(pos, (-1, 3))
+    n = pos.shape[0]
+    acc = np.zeros((n, 3))
+    phi = np.zeros(n)
+    args = [np.ascontiguousarray(tree["order"], dtype=np.int32), _f64(tree["com"], (-1, 3)),
+            _f64(tree["nmass"], (-1,)), _f64(tree["nmin"], (-1, 3)), _f64(tree["nmax"], (-1, 3)),
+            np.ascontiguousarray(tree["left"], dtype=np.int32),
+            np.ascontiguousarray(tree["right"], dtype=np.int32)]
+    lib().orc_group_walk(_p(pos), *[_p(a) for a in args], n, group, float(theta) ** 2, eps2, G,
+                         _p(acc), _p(phi))
+    return acc, phi
 
 
 def bh_tree(pos, mass, bits=21):

@@ -209,9 +209,17 @@ __device__ __forceinline__ int kdelta(const KeyT *__restrict__ k, int n, int i, 
     return clz63(x);
 }
 
+// Leaves per group of the group walk (traversal shape 3).
+constexpr int GW_GROUP = 32;
+
+// gsize (when not NULL, zeroed before the launch): the group walk's groups,
+// the maximal subtrees with at most GW_GROUP leaves; gsize[first leaf] =
+// its leaf count.  They partition the leaves into key-order ranges, each
+// inside one node's box (32 key-consecutive leaves can straddle a jump of
+// the Morton curve and span most of the system).
 template <typename KeyT>
 __global__ void bh_karras_kernel(const KeyT *__restrict__ k, int n, int2 *__restrict__ child,
-                                 int *__restrict__ parent) {
+                                 int *__restrict__ parent, int *__restrict__ gsize) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) parent[n] = -1;  // the root (internal node 0 = id n)
     if (i >= n - 1) return;
@@ -237,6 +245,15 @@ __global__ void bh_karras_kernel(const KeyT *__restrict__ k, int n, int2 *__rest
     child[i] = make_int2(lc, rc);
     parent[lc] = i + n;
     parent[rc] = i + n;
+    if (gsize) {
+        const int cnt = hi - lo + 1, cl = gamma - lo + 1, cr = hi - gamma;
+        if (cnt > GW_GROUP) {
+            if (cl <= GW_GROUP) gsize[lo] = cl;
+            if (cr <= GW_GROUP) gsize[gamma + 1] = cr;
+        } else if (i == 0) {
+            gsize[0] = cnt;  // the whole system is one group
+        }
+    }
 }
 
 // -------------------------------------------------------------- bottom-up
@@ -361,7 +378,6 @@ struct TravArgs {
     const uint32_t *__restrict__ order;
     float4 *acc;
     float4 *vel;
-    float *phi;  // PHI kernels: the tree potential sum of every particle (no G)
     int n;
     float theta2, eps2, G, h;
     int max_stack;
@@ -371,10 +387,17 @@ struct TravArgs {
 };
 
 struct Lane {
-    float px, py, pz, ax, ay, az, pw;
-    f2 PX, PY, PZ;      // (p, p) pairs
-    f2 AX, AY, AZ, PW;  // accumulators for (left, right) children
+    float px, py, pz, ax, ay, az;
+    f2 PX, PY, PZ;  // (p, p) pairs
+    f2 AX, AY, AZ;  // accumulators for (left, right) children
     unsigned n_int, n_test, drops;
+};
+
+// Tree-potential sums of a lane (PHI kernels only): pw for the root,
+// PW for the (left, right) children.
+struct LanePhi {
+    float pw;
+    f2 PW;
 };
 
 // One child for one lane of the expanding mask (branch-free).  Leaves carry
@@ -387,8 +410,8 @@ struct Lane {
 // own leaf also adds its monopole potential m / |d| (|d|^2 = d.d + eps^2),
 // the tree form of the potential_energy sum (core/solvers/gravity.py:47-55).
 template <bool COUNT, bool PHI>
-__device__ __forceinline__ bool visit_child(Lane &L, const TravArgs &a, float4 q, float size2, int id, int s,
-                                            bool in) {
+__device__ __forceinline__ bool visit_child(Lane &L, LanePhi &W, const TravArgs &a, float4 q, float size2, int id,
+                                            int s, bool in) {
     const float dx = q.x - L.px, dy = q.y - L.py, dz = q.z - L.pz;
     const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, a.eps2)));
     const bool accept = size2 < a.theta2 * r2;
@@ -398,7 +421,7 @@ __device__ __forceinline__ bool visit_child(Lane &L, const TravArgs &a, float4 q
     L.ax = __fmaf_rn(sc, dx, L.ax);
     L.ay = __fmaf_rn(sc, dy, L.ay);
     L.az = __fmaf_rn(sc, dz, L.az);
-    if (PHI) L.pw += (add && id != s) ? q.w * inv : 0.f;
+    if (PHI) W.pw += (add && id != s) ? q.w * inv : 0.f;
     if (COUNT) {
         L.n_int += (add && id != s) ? 1u : 0u;
         L.n_test += (in && size2 >= 0.f) ? 1u : 0u;
@@ -410,8 +433,8 @@ __device__ __forceinline__ bool visit_child(Lane &L, const TravArgs &a, float4 q
 // pairs: the same test and monopole as visit_child, two children per
 // instruction.  Sets openL / openR.  PHI as in visit_child.
 template <bool COUNT, bool PHI>
-__device__ __forceinline__ void visit_pair(Lane &L, const TravArgs &a, ulonglong2 A, ulonglong2 B, float4 C, int s,
-                                           bool in, f2 E2, f2 TH2, bool &openL, bool &openR) {
+__device__ __forceinline__ void visit_pair(Lane &L, LanePhi &W, const TravArgs &a, ulonglong2 A, ulonglong2 B,
+                                           float4 C, int s, bool in, f2 E2, f2 TH2, bool &openL, bool &openR) {
     const f2 dx = sub2(A.x, L.PX), dy = sub2(A.y, L.PY), dz = sub2(B.x, L.PZ);
     f2 r2 = fma2(dx, dx, E2);
     r2 = fma2(dy, dy, r2);
@@ -422,8 +445,7 @@ __device__ __forceinline__ void visit_pair(Lane &L, const TravArgs &a, ulonglong
     unpack2(t, tL, tR);
     const bool accL = C.x < tL, accR = C.y < tR;
     const f2 inv = pack2(rsqrt_approx(r2L), rsqrt_approx(r2R));
-    const f2 mi = mul2(B.y, inv);
-    const f2 sc = mul2(mi, mul2(inv, inv));
+    const f2 sc = mul2(mul2(B.y, inv), mul2(inv, inv));
     float scL, scR;
     unpack2(sc, scL, scR);
     const f2 scm = pack2((in && accL) ? scL : 0.f, (in && accR) ? scR : 0.f);
@@ -432,8 +454,8 @@ __device__ __forceinline__ void visit_pair(Lane &L, const TravArgs &a, ulonglong
     L.AZ = fma2(scm, dz, L.AZ);
     if (PHI) {
         float miL, miR;
-        unpack2(mi, miL, miR);
-        L.PW = add2(L.PW, pack2((in && accL && __float_as_int(C.z) != s) ? miL : 0.f,
+        unpack2(mul2(B.y, inv), miL, miR);
+        W.PW = add2(W.PW, pack2((in && accL && __float_as_int(C.z) != s) ? miL : 0.f,
                                 (in && accR && __float_as_int(C.w) != s) ? miR : 0.f));
     }
     if (COUNT) {
@@ -466,9 +488,13 @@ __device__ __forceinline__ bool apply_room(Lane &L, bool open, int sp, int max_s
 // reference's per-particle stack when a node is popped, depends only on the
 // node's path (one pending left sibling per right turn), so it travels with
 // the node.
+// PHI: phi receives the tree potential sum of every particle (no G).  It is
+// a kernel argument of its own: inside TravArgs it changed the register
+// allocation of the kernels without it (46 against 48 registers, 13% more
+// instructions per node expansion, measured).
 template <bool KDK, bool COUNT, int TPL, bool PHI>
 __global__ void __launch_bounds__(TRAV_WARPS * 32)
-bh_traverse_kernel(TravArgs a) {
+bh_traverse_kernel(TravArgs a, float *__restrict__ phi) {
     __shared__ int4 stk[TRAV_WARPS][TRAV_STACK];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int wbase = (blockIdx.x * TRAV_WARPS + wid) * (32 * TPL);
@@ -477,6 +503,7 @@ bh_traverse_kernel(TravArgs a) {
     int s[TPL];
     bool valid[TPL];
     Lane L[TPL];
+    LanePhi W[TPL];
 #pragma unroll
     for (int q = 0; q < TPL; ++q) {
         s[q] = wbase + 32 * q + lane;
@@ -486,11 +513,13 @@ bh_traverse_kernel(TravArgs a) {
             const float4 p = __ldg(a.leaf + s[q]);
             L[q].px = p.x; L[q].py = p.y; L[q].pz = p.z;
         }
-        L[q].ax = L[q].ay = L[q].az = L[q].pw = 0.f;
+        L[q].ax = L[q].ay = L[q].az = 0.f;
         L[q].PX = pack2(L[q].px, L[q].px);
         L[q].PY = pack2(L[q].py, L[q].py);
         L[q].PZ = pack2(L[q].pz, L[q].pz);
-        L[q].AX = L[q].AY = L[q].AZ = L[q].PW = 0ull;
+        L[q].AX = L[q].AY = L[q].AZ = 0ull;
+        W[q].pw = 0.f;
+        W[q].PW = 0ull;
         L[q].n_int = L[q].n_test = L[q].drops = 0;
     }
     const f2 E2 = pack2(a.eps2, a.eps2), TH2 = pack2(a.theta2, a.theta2);
@@ -506,8 +535,8 @@ bh_traverse_kernel(TravArgs a) {
         const float4 R0 = __ldg(a.root), R1 = __ldg(a.root + 1);
 #pragma unroll
         for (int q = 0; q < TPL; ++q) {
-            const bool want = apply_room(L[q], visit_child<COUNT, PHI>(L[q], a, R0, R1.x, n, s[q], valid[q]), 0,
-                                         a.max_stack);
+            const bool want = apply_room(L[q], visit_child<COUNT, PHI>(L[q], W[q], a, R0, R1.x, n, s[q], valid[q]),
+                                         0, a.max_stack);
             m[q] = __ballot_sync(0xffffffffu, want);
             any |= m[q];
         }
@@ -532,7 +561,7 @@ bh_traverse_kernel(TravArgs a) {
             for (int q = 0; q < TPL; ++q) {
                 const bool in = (m[q] >> lane) & 1u;
                 bool wantR, wantL;
-                visit_pair<COUNT, PHI>(L[q], a, A, B, C, s[q], in, E2, TH2, wantL, wantR);
+                visit_pair<COUNT, PHI>(L[q], W[q], a, A, B, C, s[q], in, E2, TH2, wantL, wantR);
                 if (!room2) {
                     wantR = apply_room(L[q], wantR, sp + 1, a.max_stack);
                     wantL = apply_room(L[q], wantL, sp, a.max_stack);
@@ -627,8 +656,8 @@ bh_traverse_kernel(TravArgs a) {
         if (a.pot.on) ext_acc_add(a.pot, L[q].px, L[q].py, L[q].pz, gx, gy, gz);
         if (PHI) {
             float wl, wr;
-            unpack2(L[q].PW, wl, wr);
-            a.phi[p] = L[q].pw + (wl + wr);
+            unpack2(W[q].PW, wl, wr);
+            phi[p] = W[q].pw + (wl + wr);
         }
         if (KDK) {
             const float4 vh = a.vel[p];
@@ -666,23 +695,26 @@ constexpr int64_t LANE_AUTO_N = 131072;
 
 template <bool KDK, bool COUNT, bool PHI>
 __global__ void __launch_bounds__(LANE_THREADS)
-bh_traverse_lane_kernel(TravArgs a) {
+bh_traverse_lane_kernel(TravArgs a, float *__restrict__ phi) {
     extern __shared__ int lstk[];  // [max_stack][LANE_THREADS]
     const int tid = threadIdx.x;
     const int n = a.n;
     const int s = blockIdx.x * LANE_THREADS + tid;
     const bool valid = s < n;
     Lane L;
+    LanePhi W;
+    W.pw = 0.f;
+    W.PW = 0ull;
     L.px = L.py = L.pz = 0.f;
     if (valid) {
         const float4 p = __ldg(a.leaf + s);
         L.px = p.x; L.py = p.y; L.pz = p.z;
     }
-    L.ax = L.ay = L.az = L.pw = 0.f;
+    L.ax = L.ay = L.az = 0.f;
     L.PX = pack2(L.px, L.px);
     L.PY = pack2(L.py, L.py);
     L.PZ = pack2(L.pz, L.pz);
-    L.AX = L.AY = L.AZ = L.PW = 0ull;
+    L.AX = L.AY = L.AZ = 0ull;
     L.n_int = L.n_test = L.drops = 0;
     const f2 E2 = pack2(a.eps2, a.eps2), TH2 = pack2(a.theta2, a.theta2);
     unsigned overflow = 0, bad = 0, reads = 0;
@@ -691,7 +723,7 @@ bh_traverse_lane_kernel(TravArgs a) {
     if (valid && n >= 2) {
         // The root is popped first, with an empty stack (d = 0).
         const float4 R0 = __ldg(a.root), R1 = __ldg(a.root + 1);
-        active = apply_room(L, visit_child<COUNT, PHI>(L, a, R0, R1.x, n, s, true), 0, a.max_stack);
+        active = apply_room(L, visit_child<COUNT, PHI>(L, W, a, R0, R1.x, n, s, true), 0, a.max_stack);
     }
     for (;;) {
         if (!active) {
@@ -710,7 +742,7 @@ bh_traverse_lane_kernel(TravArgs a) {
         const float4 C = __ldg(a.inode + 3 * k + 2);
         if (COUNT) ++reads;
         bool wantL, wantR;
-        visit_pair<COUNT, PHI>(L, a, A, B, C, s, true, E2, TH2, wantL, wantR);
+        visit_pair<COUNT, PHI>(L, W, a, A, B, C, s, true, E2, TH2, wantL, wantR);
         if (d + 3 > a.max_stack) {  // the rule only bites near max_stack
             wantR = apply_room(L, wantR, d + 1, a.max_stack);
             wantL = apply_room(L, wantL, d, a.max_stack);
@@ -773,8 +805,8 @@ bh_traverse_lane_kernel(TravArgs a) {
     if (a.pot.on) ext_acc_add(a.pot, L.px, L.py, L.pz, gx, gy, gz);
     if (PHI) {
         float wl, wr;
-        unpack2(L.PW, wl, wr);
-        a.phi[p] = L.pw + (wl + wr);
+        unpack2(W.PW, wl, wr);
+        phi[p] = W.pw + (wl + wr);
     }
     if (KDK) {
         const float4 vh = a.vel[p];
@@ -786,6 +818,255 @@ bh_traverse_lane_kernel(TravArgs a) {
         a.acc[p] = o;
     } else {
         a.acc[p] = make_float4(gx, gy, gz, 0.f);
+    }
+}
+
+// ------------------------------------------------------------- group walk
+// Group walk (gb_bh_set_traversal 3): the warp's 32 key-consecutive targets
+// share one walk and one interaction list.  A node is accepted for the whole
+// group when size^2 < theta^2 (dmin^2 + eps^2), dmin the distance from its
+// centre of mass to the group's bounding box; since every target is at
+// least dmin away, each target then also passes the reference's own test
+// (core/solvers/barnes_hut.py:204-210), so the group accepts a refinement of
+// every target's node set: more, smaller nodes, never a coarser one.  Leaves
+// are always accepted.  The walk keeps a stack of internal nodes in shared
+// memory; each iteration pops up to 32 of them, one per lane, loads their
+// two-children records and tests both children: accepted children go to the
+// interaction list (compacted by ballots), opened ones are pushed.  The list
+// is evaluated by every lane for its own target, two entries per packed
+// .f32x2 instruction, whenever it fills and at the end.  Deterministic (no
+// atomics); not the reference's per-particle node set, so its results are
+// not bit-identical to the other shapes; the max_stack rule does not apply.
+// A push that would overflow the warp's stack takes the child as a monopole
+// instead and counts it in stack_overflow.
+constexpr int GW_WARPS = 4;
+constexpr int GW_STACK = 1024;           // internal nodes per warp (the 1M disk peaks near 310)
+constexpr int GW_LIST = 256;             // list entries per warp
+constexpr int GW_FLUSH = GW_LIST - 64;   // an iteration appends at most 64
+
+struct GwWarp {
+    int stk[GW_STACK];
+    float4 lst[GW_LIST / 2][2];  // entry pairs {x0, x1, y0, y1}, {z0, z1, m0, m1}
+};
+
+__device__ __forceinline__ void gw_put(GwWarp &w, int j, float x, float y, float z, float m) {
+    float *a = reinterpret_cast<float *>(&w.lst[j >> 1][0]);
+    float *b = reinterpret_cast<float *>(&w.lst[j >> 1][1]);
+    const int h = j & 1;
+    a[h] = x;
+    a[2 + h] = y;
+    b[h] = z;
+    b[2 + h] = m;
+}
+
+// Squared distance from (x, y, z) to the box [lo, hi].
+__device__ __forceinline__ float box_dist2(float x, float y, float z, float lx, float ly, float lz, float hx, float hy,
+                                           float hz) {
+    const float dx = fmaxf(fmaxf(lx - x, x - hx), 0.f);
+    const float dy = fmaxf(fmaxf(ly - y, y - hy), 0.f);
+    const float dz = fmaxf(fmaxf(lz - z, z - hz), 0.f);
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));
+}
+
+// Adds entries [0, cnt) of the list (cnt even) to the lane's target.
+template <bool PHI>
+__device__ __forceinline__ void gw_eval(const GwWarp &w, int cnt, f2 PX, f2 PY, f2 PZ, f2 E2, f2 &AX, f2 &AY,
+                                        f2 &AZ, f2 &PW) {
+    const ulonglong2 *L = reinterpret_cast<const ulonglong2 *>(&w.lst[0][0]);
+#pragma unroll 4
+    for (int q = 0; q < (cnt >> 1); ++q) {
+        const ulonglong2 A = L[2 * q], B = L[2 * q + 1];
+        const f2 dx = sub2(A.x, PX), dy = sub2(A.y, PY), dz = sub2(B.x, PZ);
+        f2 r2 = fma2(dx, dx, E2);
+        r2 = fma2(dy, dy, r2);
+        r2 = fma2(dz, dz, r2);
+        const f2 inv = rsqrt2(r2);
+        const f2 mi = mul2(B.y, inv);
+        const f2 sc = mul2(mi, mul2(inv, inv));
+        AX = fma2(sc, dx, AX);
+        AY = fma2(sc, dy, AY);
+        AZ = fma2(sc, dz, AZ);
+        if (PHI) PW = add2(PW, mi);
+    }
+}
+
+// One group: leaves [g0, g0 + size) (size <= 32), lane l walks with target
+// g0 + l.
+template <bool KDK, bool COUNT, bool PHI>
+__device__ __forceinline__ void gw_group(GwWarp &w, const TravArgs &a, float *__restrict__ phi, int g0, int size,
+                                         int lane, unsigned &reads, unsigned &evals, unsigned &overflow,
+                                         unsigned &bad) {
+    const int n = a.n;
+    const int s = g0 + lane;
+    const bool valid = lane < size;
+    float px = 0.f, py = 0.f, pz = 0.f, pm = 0.f;
+    if (valid) {
+        const float4 p = __ldg(a.leaf + s);
+        px = p.x; py = p.y; pz = p.z; pm = p.w;
+    }
+    // The group's bounding box.
+    float lx = valid ? px : INFINITY, ly = valid ? py : INFINITY, lz = valid ? pz : INFINITY;
+    float hx = valid ? px : -INFINITY, hy = valid ? py : -INFINITY, hz = valid ? pz : -INFINITY;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lx = fminf(lx, __shfl_xor_sync(0xffffffffu, lx, o));
+        ly = fminf(ly, __shfl_xor_sync(0xffffffffu, ly, o));
+        lz = fminf(lz, __shfl_xor_sync(0xffffffffu, lz, o));
+        hx = fmaxf(hx, __shfl_xor_sync(0xffffffffu, hx, o));
+        hy = fmaxf(hy, __shfl_xor_sync(0xffffffffu, hy, o));
+        hz = fmaxf(hz, __shfl_xor_sync(0xffffffffu, hz, o));
+    }
+    const f2 PX = pack2(px, px), PY = pack2(py, py), PZ = pack2(pz, pz), E2 = pack2(a.eps2, a.eps2);
+    f2 AX = 0ull, AY = 0ull, AZ = 0ull, PW = 0ull;
+    const unsigned lt = (1u << lane) - 1u;
+    unsigned selfbits = 0;
+    int cnt = 0, top = 0;
+    if (n >= 2) {
+        // The root, tested for the whole group: a monopole, or its children.
+        const float4 R0 = __ldg(a.root), R1 = __ldg(a.root + 1);
+        const float d2 = box_dist2(R0.x, R0.y, R0.z, lx, ly, lz, hx, hy, hz);
+        if (R1.x < a.theta2 * (d2 + a.eps2)) {
+            if (lane == 0) gw_put(w, 0, R0.x, R0.y, R0.z, R0.w);
+            cnt = 1;
+        } else {
+            if (lane == 0) w.stk[0] = 0;
+            top = 1;
+        }
+        __syncwarp();
+    }
+    // A consistent tree expands each internal node at most once per group,
+    // so more than n - 1 iterations means a corrupted tree: stop.
+    for (int iter = 0; top > 0; ++iter) {
+        if (iter >= n) {
+            bad += lane == 0 ? 1u : 0u;
+            break;
+        }
+        const int take = min(top, 32);
+        top -= take;
+        bool act = lane < take;
+        const int k = act ? w.stk[top + lane] : 0;
+        __syncwarp();  // the popped entries are read before pushes reuse them
+        if (act && (unsigned)k >= (unsigned)(n - 1)) {  // never for a consistent tree
+            ++bad;
+            act = false;
+        }
+        float4 A = make_float4(0.f, 0.f, 0.f, 0.f), B = A, C = A;
+        if (act) {
+            A = __ldg(a.inode + 3 * k);      // {x_L, x_R, y_L, y_R}
+            B = __ldg(a.inode + 3 * k + 1);  // {z_L, z_R, m_L, m_R}
+            C = __ldg(a.inode + 3 * k + 2);  // {size2_L, size2_R, id_L, id_R}
+        }
+        if (COUNT) reads += __popc(__ballot_sync(0xffffffffu, act));
+        // A leaf child carries size2 = -1 and is always accepted.
+        const bool accL = act && C.x < a.theta2 * (box_dist2(A.x, A.z, B.x, lx, ly, lz, hx, hy, hz) + a.eps2);
+        const bool accR = act && C.y < a.theta2 * (box_dist2(A.y, A.w, B.y, lx, ly, lz, hx, hy, hz) + a.eps2);
+        const bool openL = act && !accL, openR = act && !accR;
+        const int idL = __float_as_int(C.z), idR = __float_as_int(C.w);
+        const unsigned bL = __ballot_sync(0xffffffffu, accL), bR = __ballot_sync(0xffffffffu, accR);
+        if (accL) gw_put(w, cnt + __popc(bL & lt), A.x, A.z, B.x, B.z);
+        if (accR) gw_put(w, cnt + __popc(bL) + __popc(bR & lt), A.y, A.w, B.y, B.w);
+        cnt += __popc(bL) + __popc(bR);
+        if (PHI) {
+            // Own leaves of the group's targets in the list: their terms are
+            // removed from the potential at the end.
+            unsigned bit = 0;
+            if (accL && (unsigned)(idL - g0) < (unsigned)size) bit |= 1u << (idL - g0);
+            if (accR && (unsigned)(idR - g0) < (unsigned)size) bit |= 1u << (idR - g0);
+            selfbits |= __reduce_or_sync(0xffffffffu, bit);
+        }
+        const unsigned cL = __ballot_sync(0xffffffffu, openL), cR = __ballot_sync(0xffffffffu, openR);
+        const int np = __popc(cL) + __popc(cR);
+        if (top + np <= GW_STACK) {
+            if (openL) w.stk[top + __popc(cL & lt)] = idL - n;
+            if (openR) w.stk[top + __popc(cL) + __popc(cR & lt)] = idR - n;
+            top += np;
+        } else {  // no room: the opened children enter the list as monopoles
+            if (openL) gw_put(w, cnt + __popc(cL & lt), A.x, A.z, B.x, B.z);
+            if (openR) gw_put(w, cnt + __popc(cL) + __popc(cR & lt), A.y, A.w, B.y, B.w);
+            cnt += np;
+            overflow += np;
+        }
+        __syncwarp();
+        if (cnt > GW_FLUSH) {
+            if ((cnt & 1) && lane == 0) gw_put(w, cnt, 0.f, 0.f, 0.f, 0.f);
+            __syncwarp();
+            gw_eval<PHI>(w, cnt + (cnt & 1), PX, PY, PZ, E2, AX, AY, AZ, PW);
+            if (COUNT) evals += cnt * size;
+            cnt = 0;
+            __syncwarp();  // the list is read before the next appends
+        }
+    }
+    if (cnt > 0) {
+        if ((cnt & 1) && lane == 0) gw_put(w, cnt, 0.f, 0.f, 0.f, 0.f);
+        __syncwarp();
+        gw_eval<PHI>(w, cnt + (cnt & 1), PX, PY, PZ, E2, AX, AY, AZ, PW);
+        if (COUNT) evals += cnt * size;
+    }
+    __syncwarp();  // the next group reuses the stack and the list
+    if (!valid) return;
+    const uint32_t p = __ldg(a.order + s);
+    if (p >= (uint32_t)n) {
+        ++bad;
+        return;
+    }
+    float xl, xr, yl, yr, zl, zr;
+    unpack2(AX, xl, xr);
+    unpack2(AY, yl, yr);
+    unpack2(AZ, zl, zr);
+    float gx = a.G * (xl + xr), gy = a.G * (yl + yr), gz = a.G * (zl + zr);
+    if (a.pot.on) ext_acc_add(a.pot, px, py, pz, gx, gy, gz);
+    if (PHI) {
+        float wl, wr;
+        unpack2(PW, wl, wr);
+        float pw = wl + wr;
+        if ((selfbits >> lane) & 1u) pw -= pm * rsqrt_approx(a.eps2);  // the term the list added
+        phi[p] = pw;
+    }
+    if (KDK) {
+        const float4 vh = a.vel[p];
+        a.vel[p] = make_float4(kick(vh.x, gx, a.h), kick(vh.y, gy, a.h), kick(vh.z, gz, a.h), vh.w);
+        a.acc[p] = make_float4(gx, gy, gz, 0.f);
+    } else if (a.accumulate) {
+        float4 o = a.acc[p];
+        o.x += gx; o.y += gy; o.z += gz;
+        a.acc[p] = o;
+    } else {
+        a.acc[p] = make_float4(gx, gy, gz, 0.f);
+    }
+}
+
+// Warp w walks the groups whose first leaf lies in [32 w, 32 w + 32) (gsize
+// from the Karras kernel), one after the other.
+template <bool KDK, bool COUNT, bool PHI>
+__global__ void __launch_bounds__(GW_WARPS * 32)
+bh_group_kernel(TravArgs a, const int *__restrict__ gsize, float *__restrict__ phi) {
+    __shared__ GwWarp sw[GW_WARPS];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    GwWarp &w = sw[wid];
+    const int c0 = (blockIdx.x * GW_WARPS + wid) * 32;
+    if (c0 >= a.n) return;  // whole warp out of range
+    const int n = a.n;
+    int gs = (c0 + lane < n) ? __ldg(gsize + c0 + lane) : 0;
+    if (n == 1 && lane == 0) gs = 1;  // a single particle: no internal node, one group
+    unsigned starts = __ballot_sync(0xffffffffu, gs > 0 && gs <= GW_GROUP);
+    unsigned reads = 0, evals = 0, overflow = 0, bad = 0, ngroups = 0;
+    while (starts) {
+        const int j = __ffs(starts) - 1;
+        starts &= starts - 1u;
+        const int size = min(__shfl_sync(0xffffffffu, gs, j), n - (c0 + j));
+        gw_group<KDK, COUNT, PHI>(w, a, phi, c0 + j, size, lane, reads, evals, overflow, bad);
+        ++ngroups;
+    }
+    const unsigned bsum = __reduce_add_sync(0xffffffffu, bad);
+    if (lane == 0) {
+        if (overflow) atomicAdd(a.diag + DIAG_STACK_OVERFLOW, (unsigned long long)overflow);
+        if (bsum) atomicAdd(a.diag + DIAG_BAD_TREE, (unsigned long long)bsum);
+        if (COUNT) {
+            atomicAdd(a.diag + DIAG_NODE_READS, (unsigned long long)reads);
+            atomicAdd(a.diag + DIAG_ROOT_READS, (unsigned long long)ngroups);
+            atomicAdd(a.diag + DIAG_INTERACTIONS, (unsigned long long)evals);
+            atomicAdd(a.diag + DIAG_TESTS, 2ull * reads + ngroups);
+        }
     }
 }
 
@@ -914,6 +1195,8 @@ struct gb_bh {
     uint64_t graph_launches[2];  // kernels in each captured step
     double2 *epart;              // energy block partials (gb_bh_energy)
     int epart_cap;
+    int *gsize;                  // group-walk groups of the last build (mode 3)
+    int64_t groups_n;            // n of the build that marked them (-1: none)
     // Failure checks (GB_CHECK, gb_bh_set_check): the failure counters as
     // read by the last checked call (or zero after a diag reset).
     int check;
@@ -931,7 +1214,7 @@ extern "C" int gb_bh_destroy(gb_bh_t *h) {
     if (!h) return GB_OK;
     void *ptrs[] = {h->keys[0], h->keys[1], h->vals[0], h->vals[1], h->hist, h->bbox_part, h->ticket,
                     h->prm, h->leaf, h->child, h->parent, h->arrivals, h->sums, h->bmin, h->bmax,
-                    h->inode, h->root, h->totals, h->diag, h->epart};
+                    h->inode, h->root, h->totals, h->diag, h->epart, h->gsize};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &g : h->gexec)
@@ -1005,6 +1288,8 @@ extern "C" int gb_bh_create(gb_bh_t **out, int64_t n_max, int key_bits) {
     A((void **)&h->diag, sizeof(unsigned long long) * DIAG_COUNT);
     h->epart_cap = 4 * h->sms;
     A((void **)&h->epart, sizeof(double2) * h->epart_cap);
+    A((void **)&h->gsize, sizeof(int) * nn);
+    h->groups_n = -1;
     if (!ok) {
         gb_bh_destroy(h);
         return fail(GB_ENOMEM, "gb_bh_create: device allocation failed for n_max=%lld", (long long)n_max);
@@ -1043,7 +1328,11 @@ static int build_impl(gb_bh_t *h, float4 *xm, float4 *vel, const float4 *acc, in
     mark(h, slot, 2, s);
     bh_gather_kernel<<<g256, 256, 0, s>>>(xm, v0, n, h->leaf, h->diag);
     const int ni = (int)std::max<int64_t>(n - 1, 1);
-    bh_karras_kernel<KeyT><<<(ni + 255) / 256, 256, 0, s>>>(k0, (int)n, h->child, h->parent);
+    // The group walk's groups are marked when the handle walks groups.
+    int *gsize = h->tpl == 3 ? h->gsize : nullptr;
+    if (gsize) GB_CUDA_TRY(cudaMemsetAsync(gsize, 0, sizeof(int) * n, s));
+    bh_karras_kernel<KeyT><<<(ni + 255) / 256, 256, 0, s>>>(k0, (int)n, h->child, h->parent, gsize);
+    h->groups_n = gsize ? n : -1;
     mark(h, slot, 3, s);
     if (n >= 2) {
         GB_CUDA_TRY(cudaMemsetAsync(h->arrivals, 0, sizeof(unsigned) * (n - 1), s));
@@ -1083,14 +1372,14 @@ static int check_ptr(const void *p, const char *name) {
 }
 
 template <bool KDK, bool COUNT, bool PHI>
-static void launch_lane(unsigned grid, size_t smem, const TravArgs &a, cudaStream_t s) {
-    bh_traverse_lane_kernel<KDK, COUNT, PHI><<<grid, LANE_THREADS, smem, s>>>(a);
+static void launch_lane(unsigned grid, size_t smem, const TravArgs &a, float *phi, cudaStream_t s) {
+    bh_traverse_lane_kernel<KDK, COUNT, PHI><<<grid, LANE_THREADS, smem, s>>>(a, phi);
 }
 
 template <bool KDK, bool COUNT, bool PHI>
-static void launch_warp(int tpl, unsigned grid, const TravArgs &a, cudaStream_t s) {
-    if (tpl == 2) bh_traverse_kernel<KDK, COUNT, 2, PHI><<<grid, TRAV_WARPS * 32, 0, s>>>(a);
-    else bh_traverse_kernel<KDK, COUNT, 1, PHI><<<grid, TRAV_WARPS * 32, 0, s>>>(a);
+static void launch_warp(int tpl, unsigned grid, const TravArgs &a, float *phi, cudaStream_t s) {
+    if (tpl == 2) bh_traverse_kernel<KDK, COUNT, 2, PHI><<<grid, TRAV_WARPS * 32, 0, s>>>(a, phi);
+    else bh_traverse_kernel<KDK, COUNT, 1, PHI><<<grid, TRAV_WARPS * 32, 0, s>>>(a, phi);
 }
 
 // Dispatches L<KDK, COUNT, PHI>::go(args...) on run-time flags.
@@ -1110,14 +1399,20 @@ static void dispatch3(bool kdk, bool count, bool phi, Args... args) {
 }
 template <bool KDK, bool COUNT, bool PHI>
 struct LaneLaunch {
-    static void go(unsigned grid, size_t smem, const TravArgs *a, cudaStream_t s) {
-        launch_lane<KDK, COUNT, PHI>(grid, smem, *a, s);
+    static void go(unsigned grid, size_t smem, const TravArgs *a, float *phi, cudaStream_t s) {
+        launch_lane<KDK, COUNT, PHI>(grid, smem, *a, phi, s);
+    }
+};
+template <bool KDK, bool COUNT, bool PHI>
+struct GroupLaunch {
+    static void go(unsigned grid, const TravArgs *a, const int *gsize, float *phi, cudaStream_t s) {
+        bh_group_kernel<KDK, COUNT, PHI><<<grid, GW_WARPS * 32, 0, s>>>(*a, gsize, phi);
     }
 };
 template <bool KDK, bool COUNT, bool PHI>
 struct WarpLaunch {
-    static void go(int tpl, unsigned grid, const TravArgs *a, cudaStream_t s) {
-        launch_warp<KDK, COUNT, PHI>(tpl, grid, *a, s);
+    static void go(int tpl, unsigned grid, const TravArgs *a, float *phi, cudaStream_t s) {
+        launch_warp<KDK, COUNT, PHI>(tpl, grid, *a, phi, s);
     }
 };
 
@@ -1135,7 +1430,6 @@ static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float *phi, float thet
     a.order = h->vals[h->cur];
     a.acc = acc;
     a.vel = vel;
-    a.phi = phi;
     a.n = (int)n;
     a.theta2 = theta * theta;
     a.eps2 = eps2;
@@ -1150,15 +1444,36 @@ static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float *phi, float thet
     // has too few warps to hide each step's latency (1M disk: 3.44 ms
     // warp-coherent against 5.84 ms per lane; 10k: 0.24 against 0.18 ms).
     const int shape = h->tpl >= 0 ? h->tpl : (n < LANE_AUTO_N ? 0 : 1);
-    if (shape == 0 && max_stack <= LANE_MAX_STACK && n - 1 <= ((int64_t)1 << LANE_KBITS)) {
+    if (shape == 3) {
+        const int64_t warps = (n + 31) / 32;
+        const unsigned grid = (unsigned)((warps + GW_WARPS - 1) / GW_WARPS);
+        if (h->groups_n != n) {
+            // Built in another traversal mode: mark the groups from the
+            // sorted keys of the same build (the topology is rewritten with
+            // identical values).
+            int *gsize = h->gsize;
+            GB_CUDA_TRY(cudaMemsetAsync(gsize, 0, sizeof(int) * n, s));
+            const int ni = (int)std::max<int64_t>(n - 1, 1);
+            if (h->key_bits == 10)
+                bh_karras_kernel<uint32_t><<<(ni + 255) / 256, 256, 0, s>>>(
+                    (const uint32_t *)h->keys[h->cur], (int)n, h->child, h->parent, gsize);
+            else
+                bh_karras_kernel<uint64_t><<<(ni + 255) / 256, 256, 0, s>>>(
+                    (const uint64_t *)h->keys[h->cur], (int)n, h->child, h->parent, gsize);
+            GB_CUDA_TRY(cudaGetLastError());
+            h->launches += 1;
+            h->groups_n = n;
+        }
+        dispatch3<GroupLaunch>(kdk, count, phi != nullptr, grid, &a, (const int *)h->gsize, phi, s);
+    } else if (shape == 0 && max_stack <= LANE_MAX_STACK && n - 1 <= ((int64_t)1 << LANE_KBITS)) {
         const unsigned grid = (unsigned)((n + LANE_THREADS - 1) / LANE_THREADS);
         const size_t smem = sizeof(int) * (size_t)std::max(max_stack, 1) * LANE_THREADS;
-        dispatch3<LaneLaunch>(kdk, count, phi != nullptr, grid, smem, &a, s);
+        dispatch3<LaneLaunch>(kdk, count, phi != nullptr, grid, smem, &a, phi, s);
     } else {
         const int tpl = shape == 2 ? 2 : 1;
         const int64_t warps = (n + 32 * tpl - 1) / (32 * tpl);
         const unsigned grid = (unsigned)((warps + TRAV_WARPS - 1) / TRAV_WARPS);
-        dispatch3<WarpLaunch>(kdk, count, phi != nullptr, tpl, grid, &a, s);
+        dispatch3<WarpLaunch>(kdk, count, phi != nullptr, tpl, grid, &a, phi, s);
     }
     GB_CUDA_TRY(cudaGetLastError());
     mark(h, slot, 5, s);
@@ -1434,8 +1749,8 @@ extern "C" uint64_t gb_bh_launch_count(gb_bh_t *h) { return h ? h->launches : 0;
 
 extern "C" int gb_bh_set_traversal(gb_bh_t *h, int targets_per_lane) {
     if (!h) return fail(GB_EINVAL, "handle is NULL");
-    if (targets_per_lane < -1 || targets_per_lane > 2)
-        return fail(GB_EINVAL, "traversal mode must be -1, 0, 1 or 2 (got %d)", targets_per_lane);
+    if (targets_per_lane < -1 || targets_per_lane > 3)
+        return fail(GB_EINVAL, "traversal mode must be -1, 0, 1, 2 or 3 (got %d)", targets_per_lane);
     h->tpl = targets_per_lane;
     return GB_OK;
 }

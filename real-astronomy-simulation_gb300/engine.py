@@ -12,7 +12,10 @@ unordered pair once and update both particles, default; False runs one pass
 per target), ``check`` (tree mode: every step waits for the device and
 raises GravityError when the traversal's max_stack rule dropped work or a
 position is not finite; the reference drops such work silently),
-``fused_potential`` (default True: the force pass of the last step of every
+``bh_traversal`` (tree mode: traversal shape, default -1, the per-particle
+walk of the reference; 3 selects the group walk, see
+BarnesHut.set_traversal), ``fused_potential`` (default True: the force
+pass of the last step of every
 ``step``/``run`` call, and of the priming in ``load_state``, also writes the
 potential of its positions, so ``energies()`` afterwards runs only the O(N)
 FP64 reductions instead of an O(N^2) potential pass), ``device``.
@@ -50,7 +53,8 @@ class Engine:
     def __init__(self, softening: float = 0.05, gravity_mode: str = "direct",
                  theta: float = 0.6, *, G: float = units.G, key_bits: int = 21,
                  max_stack: int = 64, plain_fp32: bool = False, symmetric: bool = True,
-                 check: bool = False, fused_potential: bool = True, device=None):
+                 check: bool = False, fused_potential: bool = True, bh_traversal: int = -1,
+                 device=None):
         if gravity_mode not in ("direct", "bh"):
             raise ValueError(f"gravity_mode must be 'direct' or 'bh', got {gravity_mode!r}")
         self.softening = float(softening)
@@ -63,6 +67,7 @@ class Engine:
         self.symmetric = bool(symmetric)
         self.check = bool(check)
         self.fused_potential = bool(fused_potential)
+        self.bh_traversal = int(bh_traversal)
         self.phi = None          # potential sums (no G) of the current positions, when valid
         self._phi_valid = False
         self.device = require_cuda(device)
@@ -129,6 +134,8 @@ class Engine:
             self._bh = BarnesHut(self.n, theta=self.theta, softening=self.softening,
                                  max_stack=self.max_stack, key_bits=self.key_bits,
                                  G=self.G, check=self.check, device=self.device)
+            if self.bh_traversal != -1:
+                self._bh.set_traversal(self.bh_traversal)
         else:
             self._bh = None
             self._direct_solver()

@@ -175,7 +175,13 @@ class BarnesHut:
     def set_traversal(self, targets_per_lane: int) -> None:
         """Traversal shape: 1 or 2 targets per lane, warp-coherent; 0
         per-lane walks; -1 (default) per lane below 131,072 particles and
-        warp-coherent from there.  Results are bit-identical across shapes."""
+        warp-coherent from there.  Results are bit-identical across these
+        shapes.  3 (opt-in): group walk, each group of up to 32
+        key-consecutive targets (one subtree) shares the node set its
+        bounding box accepts under the reference's test: every target sums
+        a refinement of its own node set, so the error is no larger, but
+        the results are not bit-identical to the per-particle shapes and
+        the max_stack rule does not apply."""
         _lib.call("gb_bh_set_traversal", self._h, int(targets_per_lane))
 
     # -- measurement hooks

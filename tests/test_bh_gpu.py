@@ -403,3 +403,84 @@ def test_checked_calls_report_stack_drops(cuda_dev, orc, tpl):
         eng.load_state(pkg.State.from_arrays(pos, np.zeros_like(pos), mass))
     with pytest.raises(pkg.GravityError, match="max_stack"):
         eng.step(1e-4)
+
+
+# ------------------------------------------------------------- group walk
+@pytest.mark.parametrize("n", [2, 3, 33, 1000, 50000])
+def test_group_walk_matches_oracle(cuda_dev, orc, n):
+    """Traversal shape 3 (group walk): accelerations and tree potentials
+    against the oracle's FP64 group walk (the same per-group node sets), with
+    the tolerances of the per-particle traversal; repeat calls are
+    bit-identical."""
+    _, bhmod, ic, _ = _mods()
+    pos, _, mass = ic.exponential_disk(n, seed=40 + n)
+    pos, mass = _f32(pos), _f32(mass)
+    b = bhmod.BarnesHut(n, theta=0.5, softening=0.05, key_bits=10, device=cuda_dev)
+    b.set_traversal(3)
+    xm = _xm(pos, mass, cuda_dev)
+    acc = torch.zeros_like(xm)
+    phi = torch.zeros(n, device=cuda_dev)
+    b.compute(xm, acc, phi=phi)
+    acc2 = torch.zeros_like(xm)
+    b.compute(xm, acc2)
+    torch.cuda.synchronize()
+    assert torch.equal(acc, acc2)
+    t = orc.bh_tree(pos, mass, bits=10)
+    ref_acc, ref_phi = orc.group_walk(pos, t, 0.5, 0.0025, b.G)
+    _check_acc(acc[:, :3].double().cpu().numpy(), ref_acc)
+    got = phi.double().cpu().numpy()
+    rel = np.abs(got - ref_phi) / np.maximum(np.abs(ref_phi), 1e-300)
+    assert np.median(rel) < 1e-5 and np.percentile(rel, 99) < 1e-4 and rel.max() < 1e-2, rel.max()
+    d = b.diag()
+    assert d["stack_overflow"] == 0 and d["bad_tree"] == 0
+    b.close()
+
+
+def test_group_walk_error_budget_1m(cuda_dev, orc):
+    """On the 1M disk workload the group walk's force errors against FP64
+    direct sums (4,096 seeded targets) are no worse than the exact
+    per-particle traversal's in median and 99th percentile: each group
+    accepts a refinement of its targets' node sets."""
+    _, bhmod, ic, grav = _mods()
+    n = 1_000_000
+    pos, _, mass = ic.exponential_disk(n, seed=0)
+    pos, mass = _f32(pos), _f32(mass)
+    xm = _xm(pos, mass, cuda_dev)
+    targets = np.random.default_rng(0).choice(n, 4096, replace=False)
+    b = bhmod.BarnesHut(n, theta=0.5, softening=0.05, key_bits=10, device=cuda_dev)
+    direct = grav.acc_fp64_targets(xm, targets, b.G, 0.0025)
+    err = {}
+    for tpl in (1, 3):
+        b.set_traversal(tpl)
+        acc = torch.zeros_like(xm)
+        b.compute(xm, acc)
+        err[tpl] = _rel(acc[:, :3].double().cpu().numpy()[targets], direct)
+    assert np.median(err[3]) <= np.median(err[1]), (np.median(err[3]), np.median(err[1]))
+    assert np.percentile(err[3], 99) <= np.percentile(err[1], 99)
+    assert b.diag()["stack_overflow"] == 0
+    b.close()
+
+
+def test_group_walk_kdk_matches_oracle(cuda_dev, orc):
+    _, bhmod, ic, _ = _mods()
+    n = 3000
+    pos, vel, mass = ic.exponential_disk(n, seed=17)
+    pos, vel, mass = _f32(pos), _f32(vel), _f32(mass)
+    b = bhmod.BarnesHut(n, theta=0.5, softening=0.05, key_bits=10, device=cuda_dev)
+    b.set_traversal(3)
+    xm = _xm(pos, mass, cuda_dev)
+    v4 = torch.zeros_like(xm)
+    v4[:, :3] = torch.tensor(vel, dtype=torch.float32)
+    acc = torch.zeros_like(xm)
+    b.compute(xm, acc)
+    dt = 1e-4
+    b.kdk(xm, v4, acc, dt, 3)
+    p, v = pos.copy(), vel.copy()
+    a, _ = orc.group_walk(p, orc.bh_tree(p, mass, bits=10), 0.5, 0.0025, b.G)
+    for _ in range(3):
+        v = v + a * (0.5 * dt)
+        p = p + v * dt
+        a, _ = orc.group_walk(p, orc.bh_tree(p, mass, bits=10), 0.5, 0.0025, b.G)
+        v = v + a * (0.5 * dt)
+    assert np.abs(xm[:, :3].double().cpu().numpy() - p).max() < 1e-5 * np.abs(p).max()
+    assert np.abs(v4[:, :3].double().cpu().numpy() - v).max() < 1e-3 * np.abs(v).max()
