@@ -225,6 +225,7 @@ def bench_bh(args, dev, rank, world, dist):
     a4 = torch.zeros_like(xm)
     bh = bhmod.BarnesHut(BH_N, theta=BH_THETA, softening=BH_EPS, key_bits=BH_BITS,
                          G=units.G, device=dev)
+    bh.set_traversal(args.bh_traversal)
     bh.compute(xm, a4)
     for _ in range(args.warmup):
         bh.kdk(xm, v4, a4, BH_DT, 1)
@@ -282,8 +283,9 @@ def bench_bh(args, dev, rank, world, dist):
     # 32 B root record) + per particle: own leaf 16 B, order 4 B, velocity
     # 16 B read + 16 B write, acceleration 16 B write.
     trav_ms = res["stages_ms_per_step"]["traverse"]
+    # The group walk (shape 3) also reads a 4 B group size per particle.
     bytes_launch = (48 * per_step["warp_node_reads"] + 32 * per_step["warp_root_reads"]
-                    + BH_N * (16 + 4 + 16 + 16 + 16))
+                    + BH_N * (16 + 4 + 16 + 16 + 16 + (4 if args.bh_traversal == 3 else 0)))
     hbm, src = _peaks()
     achieved = bytes_launch / (trav_ms / 1e3) / 1e9
     res["roofline"] = {"kernel": "bh_traverse_kernel", "bound": "hbm", "achieved": achieved,
@@ -367,7 +369,11 @@ def bench_bh(args, dev, rank, world, dist):
                                   "note": "wall clock per call at N=1M: gb_bh_kdk, gb_bh_kdk_phi, "
                                           "gb_bh_kdk_phi + gb_bh_energy read back"}
     bh.close()
-    if not args.no_secondary:
+    if args.bh_traversal == 3:
+        res["roofline"].update(kernel="bh_group_kernel", traffic=None,
+                               traffic_source="none: the headline ran the group walk")
+        res["roofline"].pop("observed_limit", None)
+    if not args.no_secondary and args.bh_traversal != 3:
         res["group_walk"] = bench_group_walk(args, dev, rank, world, dist, flush, hbm, src)
     return res
 
@@ -1129,6 +1135,8 @@ def main(argv=None):
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--drift-steps", type=int, default=1000)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
+    ap.add_argument("--bh-traversal", type=int, default=-1, choices=(-1, 0, 1, 2, 3),
+                    help="traversal shape of the headline step (default -1: the per-particle walk)")
     ap.add_argument("--only", choices=("direct", "merger", "batch", "adjoint", "grid", "snapshot", "scaling"),
                     help="run one secondary workload alone (profiling runs)")
     args = ap.parse_args(argv)

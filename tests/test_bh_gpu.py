@@ -484,3 +484,29 @@ def test_group_walk_kdk_matches_oracle(cuda_dev, orc):
         v = v + a * (0.5 * dt)
     assert np.abs(xm[:, :3].double().cpu().numpy() - p).max() < 1e-5 * np.abs(p).max()
     assert np.abs(v4[:, :3].double().cpu().numpy() - v).max() < 1e-3 * np.abs(v).max()
+
+
+def test_engine_group_walk_option(cuda_dev, orc):
+    """Engine(gravity_mode="bh", bh_traversal=3) primes and steps with the
+    group walk: its accelerations equal the oracle's group walk within the
+    traversal tolerances, and one step matches a BarnesHut handle in shape 3
+    bit for bit."""
+    pkg, bhmod, ic, _ = _mods()
+    n = 5000
+    pos, vel, mass = ic.exponential_disk(n, seed=5)
+    pos, vel, mass = _f32(pos), _f32(vel), _f32(mass)
+    eng = pkg.Engine(softening=0.05, gravity_mode="bh", theta=0.5, key_bits=10, bh_traversal=3,
+                     device=cuda_dev)
+    eng.load_state(pkg.State.from_arrays(pos, vel, mass))
+    ref, _ = orc.group_walk(pos, orc.bh_tree(pos, mass, bits=10), 0.5, 0.0025, eng.G)
+    _check_acc(eng.acc.to_numpy(), ref)
+    b = bhmod.BarnesHut(n, theta=0.5, softening=0.05, key_bits=10, device=cuda_dev)
+    b.set_traversal(3)
+    xm = eng.xm.clone()
+    v4 = eng.v4.clone()
+    a4 = eng.a4.clone()
+    eng.step(1e-4)
+    b.kdk(xm, v4, a4, 1e-4, 1)
+    torch.cuda.synchronize()
+    assert torch.equal(eng.xm, xm) and torch.equal(eng.v4, v4) and torch.equal(eng.a4, a4)
+    b.close()
