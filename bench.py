@@ -517,6 +517,36 @@ def cpu_bh_step(budget_s: float = 20.0):
 
 
 # ------------------------------------------------------------- secondary
+def bench_sharded_direct(args, dev, rank, world, dist, n=262_144, dt=5e-4):
+    """Direct N^2 with the targets split across the ranks (ShardedDirect):
+    one Plummer sphere of n = 262,144 (G = 1, eps = 0.01), each step one
+    all-gather of the 16 B position records and a range force pass per
+    rank.  Total work is fixed as ranks are added (strong scaling)."""
+    sh = importlib.import_module(PKG + ".sharded")
+    ic = importlib.import_module(PKG + ".ic")
+    pos, vel, mass = ic.plummer(n, seed=0)
+    s = sh.ShardedDirect(pos, vel, mass, G=1.0, softening=0.01, device=dev)
+    s.run(dt, args.warmup)
+    steps = max(1, args.steps)
+    st, en = _events(1)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    st[0].record()
+    s.run(dt, steps)
+    en[0].record()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = max_over_ranks(st[0].elapsed_time(en[0]), dist, dev)
+    s.close()
+    return {"workload": f"direct N^2 Plummer N={n}, G=1, eps=0.01, dt={dt}, targets split over {world} rank(s)",
+            "value": n * n * steps / (ms / 1e3) / 1e9, "unit": "G interactions/s", "n_ranks": world,
+            "scaling": "strong", "ms_per_step": ms / steps, "steps": steps,
+            "allgather_bytes_per_step": 16 * n,
+            "path": "ShardedDirect: gb_kick/gb_drift on the own slice, all-gather, gb_direct_acc_range"}
+
+
 # FP32 work of one unordered pair in the symmetric pass, FMA = 2 flop: 3 sub,
 # 3 FMA for |d|^2 + eps^2, 2 mul for rsqrt^3, 2 mul for the two mass
 # factors, 6 FMA for the two sides' sums (the rsqrt is on the MUFU pipe).
@@ -1153,6 +1183,7 @@ def main(argv=None):
     dist = None
     if world > 1:
         import torch.distributed as dist
+        os.environ.setdefault("NCCL_NVLS_ENABLE", "0")
         dist.init_process_group("nccl", device_id=dev)
     pkg = importlib.import_module(PKG)
     pkg.load_library()
@@ -1187,6 +1218,8 @@ def main(argv=None):
                                                   "bad_tree")}}
     if "group_walk" in res:
         line["group_walk"] = res["group_walk"]
+    if not args.no_secondary:
+        line["sharded_direct"] = bench_sharded_direct(args, dev, rank, world, dist)
     if rank == 0 and world == 1:
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_bh_step()

@@ -146,6 +146,20 @@ int gb_direct_kdk_phi(gb_direct_t *h, float *xm, float *vel, float *acc,
                       float *phi, int64_t n, float G, float eps2, float dt,
                       int64_t nsteps, int flags, void *stream);
 
+/* Accelerations of the targets t0 .. t0 + nt - 1 from all n sources of xm
+ * into acc[0 .. nt) (nt float4 records), and, when phi is not NULL, their
+ * potential sums into phi[0 .. nt): one slice of the target loop
+ * `for i in range(n)` of compute_acc_direct (core/solvers/gravity.py:18-26),
+ * the unit a rank computes when the targets are split across GPUs (each
+ * rank holds all n positions, gathered once per step).  Runs the handle's
+ * per-target pass (the scalar pass when the variant is 2); flags
+ * GB_ACCUMULATE and GB_PLAIN_FP32.  Each target sums the same terms as in
+ * gb_direct_acc; the stream-K split of the work differs, so results agree
+ * with a whole-system call to FP32 rounding of the Kahan-compensated sums. */
+int gb_direct_acc_range(gb_direct_t *h, const float *xm, int64_t n,
+                        int64_t t0, int64_t nt, float *acc, float *phi,
+                        float G, float eps2, int flags, void *stream);
+
 /* gb_energy with phi given (from an epilogue above, or gb_bh_accel_phi):
  * only the O(n) FP64 reductions run, KE = 1/2 sum m v^2, PE = -1/2 G sum m
  * phi (core/solvers/gravity.py:29-57). */

@@ -83,6 +83,7 @@ SIGNATURES = {
     "gb_direct_phi": (I32, [P, P, P, I64, F32, I32, P]),
     "gb_energy": (I32, [P, P, P, I64, F32, F32, P, P]),
     "gb_direct_acc_phi": (I32, [P, P, P, P, I64, F32, F32, I32, P]),
+    "gb_direct_acc_range": (I32, [P, P, I64, I64, I64, P, P, F32, F32, I32, P]),
     "gb_direct_kdk_phi": (I32, [P, P, P, P, P, I64, F32, F32, F32, I64, I32, P]),
     "gb_energy_phi": (I32, [P, P, P, P, I64, F32, P, P]),
     "gb_direct_acc_fp64": (I32, [P, I64, P, I64, F64, F64, P, P]),

@@ -31,6 +31,8 @@ namespace gb {
 
 enum DirectMode { MODE_ACC = 0, MODE_KDK = 1, MODE_PHI = 2 };
 
+// Targets are particles t0 .. t0 + nt - 1 (all n in every call but
+// gb_direct_acc_range); sources are particles 0 .. n - 1.
 struct DirectArgs {
     const float4 *__restrict__ xm;
     const float4 *__restrict__ vel;
@@ -39,6 +41,7 @@ struct DirectArgs {
     int *st0tab;  // per CTA: its first supertile (read by the fix-up)
     int64_t n, num_ju, U;
     int64_t P;
+    int64_t t0, nt;
     int smax;
     float eps2, h, dt;
 };
@@ -50,6 +53,13 @@ __device__ __forceinline__ float4 load_particle(const DirectArgs &a, int64_t i) 
     float4 x = ldg4(a.xm + i);
     if (MODE == MODE_KDK) x = predict_xm(x, ldg4(a.vel + i), ldg4(a.acc + i), a.h, a.dt);
     return x;
+}
+
+// Target i of the call's range (zeros past its end).
+template <int MODE>
+__device__ __forceinline__ float4 load_target(const DirectArgs &a, int64_t i) {
+    if (i >= a.nt) return make_float4(0.f, 0.f, 0.f, 0.f);
+    return load_particle<MODE>(a, a.t0 + i);
 }
 
 // Force kernel for MODE_ACC / MODE_KDK.  NP packed target pairs per lane.
@@ -90,8 +100,8 @@ direct_force_kernel(DirectArgs a) {
         f2 X[NP], Y[NP], Z[NP];
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
-            const float4 t0 = load_particle<MODE>(a, tbase + (2 * p) * 32);
-            const float4 t1 = load_particle<MODE>(a, tbase + (2 * p + 1) * 32);
+            const float4 t0 = load_target<MODE>(a, tbase + (2 * p) * 32);
+            const float4 t1 = load_target<MODE>(a, tbase + (2 * p + 1) * 32);
             X[p] = pack2(t0.x, t1.x);
             Y[p] = pack2(t0.y, t1.y);
             Z[p] = pack2(t0.z, t1.z);
@@ -225,7 +235,7 @@ direct_force_scalar_kernel(DirectArgs a) {
         float X[K], Y[K], Z[K], SX[K], SY[K], SZ[K], CX[K], CY[K], CZ[K], SW[K], CW[K];
 #pragma unroll
         for (int q = 0; q < K; ++q) {
-            const float4 t = load_particle<MODE>(a, tbase + q * 32);
+            const float4 t = load_target<MODE>(a, tbase + q * 32);
             X[q] = t.x; Y[q] = t.y; Z[q] = t.z;
             SX[q] = SY[q] = SZ[q] = CX[q] = CY[q] = CZ[q] = SW[q] = CW[q] = 0.f;
         }
@@ -355,7 +365,9 @@ struct FixArgs {
     float4 *vel;  // KDK: in/out velocities
     float4 *acc;  // ACC/KDK: output accelerations (KDK: in = previous)
     float *phi;   // MODE_PHI, or a force pass with the potential: output
-    int64_t n, num_ju, U, P, st_size;
+    int64_t n;    // targets (the range's nt; outputs acc[i], phi[i], i < n)
+    int64_t t0;   // first target's particle index (xm[t0 + i]; 0 but for ranges)
+    int64_t num_ju, U, P, st_size;
     int smax;
     float G, h, dt, eps2;
     int accumulate;
@@ -397,13 +409,13 @@ __global__ void direct_fixup_kernel(FixArgs f) {
         return;
     }
     if (PHI) {
-        kahan_add(sw, cw, -self_phi_term(f.xm[i].w, f.eps2));
+        kahan_add(sw, cw, -self_phi_term(f.xm[f.t0 + i].w, f.eps2));
         f.phi[i] = sw - cw;
     }
     float4 an = make_float4(f.G * tx, f.G * ty, f.G * tz, 0.f);
     if (MODE == MODE_ACC) {
         if (f.pot.on) {
-            const float4 x = f.xm[i];
+            const float4 x = f.xm[f.t0 + i];
             ext_acc_add(f.pot, x.x, x.y, x.z, an.x, an.y, an.z);
         }
         if (f.accumulate) {
@@ -618,10 +630,10 @@ static int ensure_partials(gb_direct_t *h, int64_t need) {
 // the longest CTA run over the mean run (the tail the last CTAs add) of the
 // coarse split against that of the fine split, which costs about 1.6% more
 // per interaction (measured at N = 65,536 and 262,144).
-static bool use_fine_units(int64_t n, int np, int warps, int64_t P) {
+static bool use_fine_units(int64_t n, int np, int warps, int64_t P, int64_t nt = -1) {
     DirectPlan c, f;
-    make_plan(n, np, warps, P, &c);
-    make_plan(n, np, warps, P, &f, SCALAR_UNIT);
+    make_plan(n, np, warps, P, &c, 0, nt);
+    make_plan(n, np, warps, P, &f, SCALAR_UNIT, nt);
     const double tail_c = (double)((c.U + c.P - 1) / c.P) * (double)c.P / (double)c.U;
     const double tail_f = (double)((f.U + f.P - 1) / f.P) * (double)f.P / (double)f.U * 1.016;
     return tail_f < tail_c;
@@ -715,11 +727,15 @@ extern "C" int gb_direct_set_tiles(gb_direct_t *h, int k, int warps, int ctas_pe
 
 // mode MODE_ACC / MODE_KDK: accelerations (or one KDK step), and, when phi
 // is not NULL, the potential sums of the same positions in the same pass;
-// MODE_PHI: the potential sums alone.
+// MODE_PHI: the potential sums alone.  nt >= 0 (MODE_ACC only): the targets
+// are particles t0 .. t0 + nt - 1, written to acc[0 .. nt) and phi[0 .. nt),
+// on the per-target pass of the handle's variant (the scalar pass for 2).
 static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, float4 *acc, float *phi,
                       int64_t n, float G, float eps2, float dt, int flags, cudaStream_t s,
-                      const ExtPot &pot = ExtPot{}) {
-    if (h->packed == 2) {
+                      const ExtPot &pot = ExtPot{}, int64_t t0 = 0, int64_t nt = -1) {
+    const bool range = nt >= 0;
+    if (!range) nt = n;
+    if (h->packed == 2 && !range) {
         bool done = false;
         GB_TRY(run_direct_sym(h, mode, xm, vel, acc, phi, n, G, eps2, dt, flags, s, pot, &done));
         if (done) return GB_OK;
@@ -729,8 +745,8 @@ static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, f
     DirectPlan pl;
     const int np = mode == MODE_PHI ? 1 : h->np;
     const int64_t ctas = grid_ctas(h, h->np, h->warps, packed);
-    const bool fine = mode != MODE_PHI && !packed && use_fine_units(n, np, h->warps, ctas);
-    make_plan(n, np, h->warps, ctas, &pl, fine ? SCALAR_UNIT : 0);
+    const bool fine = mode != MODE_PHI && !packed && use_fine_units(n, np, h->warps, ctas, nt);
+    make_plan(n, np, h->warps, ctas, &pl, fine ? SCALAR_UNIT : 0, nt);
     if (plan_partials(pl) > h->part_cap) return fail(GB_EINVAL, "scratch too small for n=%lld", (long long)n);
     if (pl.P > h->st0_cap) return fail(GB_EINVAL, "%lld CTAs exceed the handle's table", (long long)pl.P);
     DirectArgs a;
@@ -743,6 +759,8 @@ static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, f
     a.num_ju = pl.num_ju;
     a.U = pl.U;
     a.P = pl.P;
+    a.t0 = t0;
+    a.nt = nt;
     a.smax = pl.smax;
     a.eps2 = eps2;
     a.h = 0.5f * dt;
@@ -775,7 +793,8 @@ static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, f
     f.vel = vel;
     f.acc = acc;
     f.phi = phi;
-    f.n = n;
+    f.n = nt;
+    f.t0 = t0;
     f.num_ju = pl.num_ju;
     f.U = pl.U;
     f.P = pl.P;
@@ -787,7 +806,7 @@ static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, f
     f.eps2 = eps2;
     f.accumulate = (flags & GB_ACCUMULATE) ? 1 : 0;
     f.pot = pot;
-    const unsigned fb = 256, fg = (unsigned)((n + fb - 1) / fb);
+    const unsigned fb = 256, fg = (unsigned)((nt + fb - 1) / fb);
     if (mode == MODE_ACC) {
         if (with_phi) direct_fixup_kernel<MODE_ACC, true><<<fg, fb, 0, s>>>(f);
         else direct_fixup_kernel<MODE_ACC><<<fg, fb, 0, s>>>(f);
@@ -939,6 +958,23 @@ extern "C" int gb_direct_acc_phi(gb_direct_t *h, const float *xm, float *acc, fl
     if (!(eps2 > 0.f)) return fail(GB_EINVAL, "eps2 must be > 0");
     return run_direct(h, MODE_ACC, (const float4 *)xm, nullptr, (float4 *)acc, phi, n, G, eps2, 0.f, flags,
                       (cudaStream_t)stream);
+}
+
+extern "C" int gb_direct_acc_range(gb_direct_t *h, const float *xm, int64_t n, int64_t t0, int64_t nt, float *acc,
+                                   float *phi, float G, float eps2, int flags, void *stream) {
+    GB_TRY(check_n(h, n));
+    if (t0 < 0 || nt < 0 || t0 > n || nt > n - t0)
+        return fail(GB_EINVAL, "target range [%lld, %lld) outside [0, n=%lld)", (long long)t0,
+                    (long long)(t0 + nt), (long long)n);
+    if (flags & ~(GB_ACCUMULATE | GB_PLAIN_FP32))
+        return fail(GB_EINVAL, "gb_direct_acc_range: flags 0x%x: only GB_ACCUMULATE and GB_PLAIN_FP32 apply",
+                    flags);
+    if (nt == 0) return GB_OK;
+    GB_TRY(check_xm(xm, "xm"));
+    GB_TRY(check_xm(acc, "acc"));
+    if (!(eps2 > 0.f)) return fail(GB_EINVAL, "eps2 must be > 0");
+    return run_direct(h, MODE_ACC, (const float4 *)xm, nullptr, (float4 *)acc, phi, n, G, eps2, 0.f, flags,
+                      (cudaStream_t)stream, ExtPot{}, t0, nt);
 }
 
 extern "C" int gb_direct_phi(gb_direct_t *h, const float *xm, float *phi, int64_t n, float eps2, int flags,
@@ -1105,6 +1141,8 @@ extern "C" int gb_direct_acc_noalloc(const float *xm, float *acc, int64_t n, flo
     a.num_ju = pl.num_ju;
     a.U = pl.U;
     a.P = pl.P;
+    a.t0 = 0;
+    a.nt = n;
     a.smax = pl.smax;
     a.eps2 = eps2;
     a.h = 0.f;
@@ -1123,6 +1161,7 @@ extern "C" int gb_direct_acc_noalloc(const float *xm, float *acc, int64_t n, flo
     f.acc = (float4 *)acc;
     f.phi = nullptr;
     f.n = n;
+    f.t0 = 0;
     f.num_ju = pl.num_ju;
     f.U = pl.U;
     f.P = pl.P;

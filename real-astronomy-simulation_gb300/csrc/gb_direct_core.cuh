@@ -19,18 +19,21 @@ __device__ __forceinline__ int64_t unit_owner(int64_t U, int64_t P, int64_t u) {
 // Units are (target supertile of warps*32*2*np targets) x (source chunk of
 // unit_src sources), supertile-major; smax bounds the supertiles one CTA run
 // touches, so a CTA's partials fit smax slots.
+// nt >= 0: only the targets of a range of nt particles (sources: all n).
 struct DirectPlan {
     int np, warps;
-    int64_t n, st_size, num_st, num_ju, U, P;
+    int64_t n, nt, st_size, num_st, num_ju, U, P;
     int smax;
 };
 
-static inline void make_plan(int64_t n, int np, int warps, int64_t P, DirectPlan *p, int unit_src = 0) {
+static inline void make_plan(int64_t n, int np, int warps, int64_t P, DirectPlan *p, int unit_src = 0,
+                             int64_t nt = -1) {
     p->np = np;
     p->warps = warps;
     p->n = n;
+    p->nt = nt >= 0 ? nt : n;
     p->st_size = (int64_t)warps * 32 * 2 * np;
-    p->num_st = (n + p->st_size - 1) / p->st_size;
+    p->num_st = (p->nt + p->st_size - 1) / p->st_size;
     const int64_t ju = unit_src > 0 ? unit_src : (int64_t)warps * 32;
     p->num_ju = (n + ju - 1) / ju;
     p->U = p->num_st * p->num_ju;

@@ -85,6 +85,18 @@ class DirectGravity:
                   _lib.GB_PLAIN_FP32 if plain else 0, stream_handle(self.device))
         return acc
 
+    def acc_range(self, xm, n, t0, nt, acc, G, eps2, phi=None, accumulate=False, plain=False):
+        """Accelerations of targets t0 .. t0 + nt - 1 from the first n
+        records of xm into acc[:nt] (and their potential sums into phi[:nt]
+        when phi is given): one rank's slice of the target loop."""
+        if xm.shape[0] < n or acc.shape[0] < nt or (phi is not None and phi.shape[0] < nt):
+            raise ValueError("acc_range: buffers shorter than n / nt")
+        flags = (_lib.GB_ACCUMULATE if accumulate else 0) | (_lib.GB_PLAIN_FP32 if plain else 0)
+        _lib.call("gb_direct_acc_range", self._h, ptr(xm, "xm"), int(n), int(t0), int(nt),
+                  ptr(acc, "acc"), None if phi is None else ptr(phi, "phi", rows4=False),
+                  float(G), float(eps2), flags, stream_handle(self.device))
+        return acc
+
     def kdk(self, xm, vel, acc, G, eps2, dt, nsteps=1, plain=False, graph=False, phi=None):
         """nsteps fused KDK steps in place; graph=True replays captured
         steps as CUDA graphs (identical results, fewer launches).  With phi
