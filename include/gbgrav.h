@@ -121,11 +121,15 @@ int gb_drift(float *xm, const float *vel, int64_t n, float dt, void *stream);
 int gb_direct_phi(gb_direct_t *h, const float *xm, float *phi, int64_t n,
                   float eps2, int flags, void *stream);
 
-/* FP64 energies into out3 (device, 3 doubles): kinetic, potential, total.
+/* FP64 energies into out3 (3 doubles): kinetic, potential, total.
  * KE = 1/2 sum m v^2 (core/solvers/gravity.py:29-36); PE = -1/2 G sum m_i
  * phi_i (core/solvers/gravity.py:39-57) with phi from gb_direct_phi; the
- * reductions run in FP64 in a fixed order.  n = 0 writes zeros (xm and vel
- * may then be NULL). */
+ * reductions run in FP64 in a fixed order, in one launch.  n = 0 writes
+ * zeros (xm and vel may then be NULL).  out3 in device memory: the call is
+ * asynchronous.  out3 in host memory (pinned, or pageable): the call copies
+ * the three sums there and waits for the stream before it returns (the
+ * energy calls' synchronous form, for a caller that reads them at once;
+ * not for use while the stream is being captured). */
 int gb_energy(gb_direct_t *h, const float *xm, const float *vel, int64_t n,
               float G, float eps2, double *out3, void *stream);
 
@@ -162,7 +166,8 @@ int gb_direct_acc_range(gb_direct_t *h, const float *xm, int64_t n,
 
 /* gb_energy with phi given (from an epilogue above, or gb_bh_accel_phi):
  * only the O(n) FP64 reductions run, KE = 1/2 sum m v^2, PE = -1/2 G sum m
- * phi (core/solvers/gravity.py:29-57). */
+ * phi (core/solvers/gravity.py:29-57).  out3 as in gb_energy (device:
+ * asynchronous; host: copied there, the call waits). */
 int gb_energy_phi(gb_direct_t *h, const float *xm, const float *vel,
                   const float *phi, int64_t n, float G, double *out3,
                   void *stream);
@@ -240,7 +245,8 @@ int gb_bh_kdk_phi(gb_bh_t *h, float *xm, float *vel, float *acc, float *phi,
                   int64_t nsteps, int max_stack, void *stream);
 
 /* FP64 energies from a tree potential (gb_energy_phi on the tree handle's
- * scratch): KE, PE = -1/2 G sum m phi, total into out3 (3 doubles). */
+ * scratch): KE, PE = -1/2 G sum m phi, total into out3 (3 doubles; device:
+ * asynchronous; host: copied there, the call waits). */
 int gb_bh_energy(gb_bh_t *h, const float *xm, const float *vel,
                  const float *phi, int64_t n, float G, double *out3,
                  void *stream);

@@ -393,12 +393,28 @@ struct Lane {
     unsigned n_int, n_test, drops;
 };
 
-// Tree-potential sums of a lane (PHI kernels only): pw for the root,
-// PW for the (left, right) children.
+// Tree-potential sums of a lane (PHI kernels only): pw for the root, PW for
+// the (left, right) children.  The children's terms are added as sc * r2
+// (= m / |d| up to rsqrt rounding) from the masked force factor, the lane's
+// own leaf included; self records whether the walk reached it (its parent,
+// internal node kp, was expanded for the lane), and the epilogue then
+// removes its term m rsqrt(eps^2)^3 eps^2.
 struct LanePhi {
-    float pw;
+    float pw, pm;
     f2 PW;
+    int kp;
+    bool self;
 };
+
+// The lane's potential sum without its own leaf's term.
+__device__ __forceinline__ float lane_phi(const LanePhi &W, float eps2) {
+    float wl, wr;
+    unpack2(W.PW, wl, wr);
+    const float pw = W.pw + (wl + wr);
+    if (!W.self) return pw;
+    const float inv = rsqrt_approx(eps2);
+    return __fmaf_rn(-((W.pm * inv) * (inv * inv)), eps2, pw);
+}
 
 // One child for one lane of the expanding mask (branch-free).  Leaves carry
 // size2 = -1 in the record, so the one comparison size2 < theta^2 (|d|^2 +
@@ -421,7 +437,7 @@ __device__ __forceinline__ bool visit_child(Lane &L, LanePhi &W, const TravArgs 
     L.ax = __fmaf_rn(sc, dx, L.ax);
     L.ay = __fmaf_rn(sc, dy, L.ay);
     L.az = __fmaf_rn(sc, dz, L.az);
-    if (PHI) W.pw += (add && id != s) ? q.w * inv : 0.f;
+    if (PHI) W.pw += (add && id != s) ? q.w * inv : 0.f;  // the root: never the own leaf
     if (COUNT) {
         L.n_int += (add && id != s) ? 1u : 0u;
         L.n_test += (in && size2 >= 0.f) ? 1u : 0u;
@@ -452,12 +468,7 @@ __device__ __forceinline__ void visit_pair(Lane &L, LanePhi &W, const TravArgs &
     L.AX = fma2(scm, dx, L.AX);
     L.AY = fma2(scm, dy, L.AY);
     L.AZ = fma2(scm, dz, L.AZ);
-    if (PHI) {
-        float miL, miR;
-        unpack2(mul2(B.y, inv), miL, miR);
-        W.PW = add2(W.PW, pack2((in && accL && __float_as_int(C.z) != s) ? miL : 0.f,
-                                (in && accR && __float_as_int(C.w) != s) ? miR : 0.f));
-    }
+    if (PHI) W.PW = fma2(scm, r2, W.PW);
     if (COUNT) {
         L.n_int += (in && accL && __float_as_int(C.z) != s) ? 1u : 0u;
         L.n_int += (in && accR && __float_as_int(C.w) != s) ? 1u : 0u;
@@ -494,7 +505,7 @@ __device__ __forceinline__ bool apply_room(Lane &L, bool open, int sp, int max_s
 // instructions per node expansion, measured).
 template <bool KDK, bool COUNT, int TPL, bool PHI>
 __global__ void __launch_bounds__(TRAV_WARPS * 32)
-bh_traverse_kernel(TravArgs a, float *__restrict__ phi) {
+bh_traverse_kernel(TravArgs a, float *__restrict__ phi, const int *__restrict__ parent) {
     __shared__ int4 stk[TRAV_WARPS][TRAV_STACK];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int wbase = (blockIdx.x * TRAV_WARPS + wid) * (32 * TPL);
@@ -509,9 +520,11 @@ bh_traverse_kernel(TravArgs a, float *__restrict__ phi) {
         s[q] = wbase + 32 * q + lane;
         valid[q] = s[q] < n;
         L[q].px = L[q].py = L[q].pz = 0.f;
+        W[q].pm = 0.f;
         if (valid[q]) {
             const float4 p = __ldg(a.leaf + s[q]);
             L[q].px = p.x; L[q].py = p.y; L[q].pz = p.z;
+            W[q].pm = p.w;
         }
         L[q].ax = L[q].ay = L[q].az = 0.f;
         L[q].PX = pack2(L[q].px, L[q].px);
@@ -520,6 +533,8 @@ bh_traverse_kernel(TravArgs a, float *__restrict__ phi) {
         L[q].AX = L[q].AY = L[q].AZ = 0ull;
         W[q].pw = 0.f;
         W[q].PW = 0ull;
+        W[q].self = false;
+        W[q].kp = (PHI && valid[q] && n >= 2) ? __ldg(parent + s[q]) - n : -1;
         L[q].n_int = L[q].n_test = L[q].drops = 0;
     }
     const f2 E2 = pack2(a.eps2, a.eps2), TH2 = pack2(a.theta2, a.theta2);
@@ -562,6 +577,7 @@ bh_traverse_kernel(TravArgs a, float *__restrict__ phi) {
                 const bool in = (m[q] >> lane) & 1u;
                 bool wantR, wantL;
                 visit_pair<COUNT, PHI>(L[q], W[q], a, A, B, C, s[q], in, E2, TH2, wantL, wantR);
+                if (PHI) W[q].self |= in && k == W[q].kp;
                 if (!room2) {
                     wantR = apply_room(L[q], wantR, sp + 1, a.max_stack);
                     wantL = apply_room(L[q], wantL, sp, a.max_stack);
@@ -654,11 +670,7 @@ bh_traverse_kernel(TravArgs a, float *__restrict__ phi) {
         float gx = a.G * (L[q].ax + (xl + xr)), gy = a.G * (L[q].ay + (yl + yr)),
               gz = a.G * (L[q].az + (zl + zr));
         if (a.pot.on) ext_acc_add(a.pot, L[q].px, L[q].py, L[q].pz, gx, gy, gz);
-        if (PHI) {
-            float wl, wr;
-            unpack2(W[q].PW, wl, wr);
-            phi[p] = W[q].pw + (wl + wr);
-        }
+        if (PHI) phi[p] = lane_phi(W[q], a.eps2);
         if (KDK) {
             const float4 vh = a.vel[p];
             a.vel[p] = make_float4(kick(vh.x, gx, a.h), kick(vh.y, gy, a.h), kick(vh.z, gz, a.h), vh.w);
@@ -695,7 +707,7 @@ constexpr int64_t LANE_AUTO_N = 131072;
 
 template <bool KDK, bool COUNT, bool PHI>
 __global__ void __launch_bounds__(LANE_THREADS)
-bh_traverse_lane_kernel(TravArgs a, float *__restrict__ phi) {
+bh_traverse_lane_kernel(TravArgs a, float *__restrict__ phi, const int *__restrict__ parent) {
     extern __shared__ int lstk[];  // [max_stack][LANE_THREADS]
     const int tid = threadIdx.x;
     const int n = a.n;
@@ -705,10 +717,14 @@ bh_traverse_lane_kernel(TravArgs a, float *__restrict__ phi) {
     LanePhi W;
     W.pw = 0.f;
     W.PW = 0ull;
+    W.pm = 0.f;
+    W.self = false;
+    W.kp = (PHI && valid && n >= 2) ? __ldg(parent + s) - n : -1;
     L.px = L.py = L.pz = 0.f;
     if (valid) {
         const float4 p = __ldg(a.leaf + s);
         L.px = p.x; L.py = p.y; L.pz = p.z;
+        W.pm = p.w;
     }
     L.ax = L.ay = L.az = 0.f;
     L.PX = pack2(L.px, L.px);
@@ -743,6 +759,7 @@ bh_traverse_lane_kernel(TravArgs a, float *__restrict__ phi) {
         if (COUNT) ++reads;
         bool wantL, wantR;
         visit_pair<COUNT, PHI>(L, W, a, A, B, C, s, true, E2, TH2, wantL, wantR);
+        if (PHI) W.self |= k == W.kp;
         if (d + 3 > a.max_stack) {  // the rule only bites near max_stack
             wantR = apply_room(L, wantR, d + 1, a.max_stack);
             wantL = apply_room(L, wantL, d, a.max_stack);
@@ -803,11 +820,7 @@ bh_traverse_lane_kernel(TravArgs a, float *__restrict__ phi) {
     unpack2(L.AZ, zl, zr);
     float gx = a.G * (L.ax + (xl + xr)), gy = a.G * (L.ay + (yl + yr)), gz = a.G * (L.az + (zl + zr));
     if (a.pot.on) ext_acc_add(a.pot, L.px, L.py, L.pz, gx, gy, gz);
-    if (PHI) {
-        float wl, wr;
-        unpack2(W.PW, wl, wr);
-        phi[p] = W.pw + (wl + wr);
-    }
+    if (PHI) phi[p] = lane_phi(W, a.eps2);
     if (KDK) {
         const float4 vh = a.vel[p];
         a.vel[p] = make_float4(kick(vh.x, gx, a.h), kick(vh.y, gy, a.h), kick(vh.z, gz, a.h), vh.w);
@@ -1287,7 +1300,7 @@ extern "C" int gb_bh_create(gb_bh_t **out, int64_t n_max, int key_bits) {
     A((void **)&h->totals, sizeof(uint32_t) * RS_BINS);
     A((void **)&h->diag, sizeof(unsigned long long) * DIAG_COUNT);
     h->epart_cap = 4 * h->sms;
-    A((void **)&h->epart, sizeof(double2) * h->epart_cap);
+    A((void **)&h->epart, sizeof(double2) * (h->epart_cap + ENERGY_EXTRA));
     A((void **)&h->gsize, sizeof(int) * nn);
     h->groups_n = -1;
     if (!ok) {
@@ -1295,7 +1308,8 @@ extern "C" int gb_bh_create(gb_bh_t **out, int64_t n_max, int key_bits) {
         return fail(GB_ENOMEM, "gb_bh_create: device allocation failed for n_max=%lld", (long long)n_max);
     }
     if (cudaMemset(h->ticket, 0, sizeof(unsigned)) != cudaSuccess ||
-        cudaMemset(h->diag, 0, sizeof(unsigned long long) * DIAG_COUNT) != cudaSuccess) {
+        cudaMemset(h->diag, 0, sizeof(unsigned long long) * DIAG_COUNT) != cudaSuccess ||
+        cudaMemset(h->epart, 0, sizeof(double2) * (h->epart_cap + ENERGY_EXTRA)) != cudaSuccess) {
         gb_bh_destroy(h);
         return fail(GB_ECUDA, "gb_bh_create: memset failed");
     }
@@ -1372,14 +1386,16 @@ static int check_ptr(const void *p, const char *name) {
 }
 
 template <bool KDK, bool COUNT, bool PHI>
-static void launch_lane(unsigned grid, size_t smem, const TravArgs &a, float *phi, cudaStream_t s) {
-    bh_traverse_lane_kernel<KDK, COUNT, PHI><<<grid, LANE_THREADS, smem, s>>>(a, phi);
+static void launch_lane(unsigned grid, size_t smem, const TravArgs &a, float *phi, const int *parent,
+                        cudaStream_t s) {
+    bh_traverse_lane_kernel<KDK, COUNT, PHI><<<grid, LANE_THREADS, smem, s>>>(a, phi, parent);
 }
 
 template <bool KDK, bool COUNT, bool PHI>
-static void launch_warp(int tpl, unsigned grid, const TravArgs &a, float *phi, cudaStream_t s) {
-    if (tpl == 2) bh_traverse_kernel<KDK, COUNT, 2, PHI><<<grid, TRAV_WARPS * 32, 0, s>>>(a, phi);
-    else bh_traverse_kernel<KDK, COUNT, 1, PHI><<<grid, TRAV_WARPS * 32, 0, s>>>(a, phi);
+static void launch_warp(int tpl, unsigned grid, const TravArgs &a, float *phi, const int *parent,
+                        cudaStream_t s) {
+    if (tpl == 2) bh_traverse_kernel<KDK, COUNT, 2, PHI><<<grid, TRAV_WARPS * 32, 0, s>>>(a, phi, parent);
+    else bh_traverse_kernel<KDK, COUNT, 1, PHI><<<grid, TRAV_WARPS * 32, 0, s>>>(a, phi, parent);
 }
 
 // Dispatches L<KDK, COUNT, PHI>::go(args...) on run-time flags.
@@ -1399,8 +1415,8 @@ static void dispatch3(bool kdk, bool count, bool phi, Args... args) {
 }
 template <bool KDK, bool COUNT, bool PHI>
 struct LaneLaunch {
-    static void go(unsigned grid, size_t smem, const TravArgs *a, float *phi, cudaStream_t s) {
-        launch_lane<KDK, COUNT, PHI>(grid, smem, *a, phi, s);
+    static void go(unsigned grid, size_t smem, const TravArgs *a, float *phi, const int *parent, cudaStream_t s) {
+        launch_lane<KDK, COUNT, PHI>(grid, smem, *a, phi, parent, s);
     }
 };
 template <bool KDK, bool COUNT, bool PHI>
@@ -1411,8 +1427,8 @@ struct GroupLaunch {
 };
 template <bool KDK, bool COUNT, bool PHI>
 struct WarpLaunch {
-    static void go(int tpl, unsigned grid, const TravArgs *a, float *phi, cudaStream_t s) {
-        launch_warp<KDK, COUNT, PHI>(tpl, grid, *a, phi, s);
+    static void go(int tpl, unsigned grid, const TravArgs *a, float *phi, const int *parent, cudaStream_t s) {
+        launch_warp<KDK, COUNT, PHI>(tpl, grid, *a, phi, parent, s);
     }
 };
 
@@ -1468,12 +1484,12 @@ static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float *phi, float thet
     } else if (shape == 0 && max_stack <= LANE_MAX_STACK && n - 1 <= ((int64_t)1 << LANE_KBITS)) {
         const unsigned grid = (unsigned)((n + LANE_THREADS - 1) / LANE_THREADS);
         const size_t smem = sizeof(int) * (size_t)std::max(max_stack, 1) * LANE_THREADS;
-        dispatch3<LaneLaunch>(kdk, count, phi != nullptr, grid, smem, &a, phi, s);
+        dispatch3<LaneLaunch>(kdk, count, phi != nullptr, grid, smem, &a, phi, (const int *)h->parent, s);
     } else {
         const int tpl = shape == 2 ? 2 : 1;
         const int64_t warps = (n + 32 * tpl - 1) / (32 * tpl);
         const unsigned grid = (unsigned)((warps + TRAV_WARPS - 1) / TRAV_WARPS);
-        dispatch3<WarpLaunch>(kdk, count, phi != nullptr, tpl, grid, &a, phi, s);
+        dispatch3<WarpLaunch>(kdk, count, phi != nullptr, tpl, grid, &a, phi, (const int *)h->parent, s);
     }
     GB_CUDA_TRY(cudaGetLastError());
     mark(h, slot, 5, s);
@@ -1676,7 +1692,7 @@ extern "C" int gb_bh_energy(gb_bh_t *h, const float *xm, const float *vel, const
     if (!out3) return fail(GB_EINVAL, "out3 is NULL");
     GB_TRY(launch_energy((const float4 *)xm, (const float4 *)vel, phi, n, G, h->epart, h->epart_cap, out3,
                          (cudaStream_t)stream));
-    h->launches += 2;
+    h->launches += 1;
     return GB_OK;
 }
 

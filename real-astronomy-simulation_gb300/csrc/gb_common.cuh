@@ -49,8 +49,14 @@ int num_sms();
 int read_diag(unsigned long long *dev, gb_diag_t *out, int reset);
 
 // FP64 energies into out3 (KE, PE = -1/2 G sum m phi, total) from n float4
-// records and the potential sums phi: per-block partials into epart (at most
-// epart_cap blocks), then one block adds them in block order (two launches).
+// records and the potential sums phi, in one launch: per-block partials into
+// epart (at most epart_cap blocks), and the last block to finish adds them
+// in block order.  epart holds epart_cap + ENERGY_EXTRA double2: the partials,
+// then an arrival ticket (zero between calls; set to zero at allocation),
+// then a device copy of out3.  out3 in host memory (pinned or pageable):
+// the kernel writes the device copy, which is copied to out3, and the call
+// waits for stream s.
+constexpr int ENERGY_EXTRA = 3;
 int launch_energy(const float4 *xm, const float4 *vel, const float *phi, int64_t n, float G, double2 *epart,
                   int epart_cap, double *out3, cudaStream_t s);
 

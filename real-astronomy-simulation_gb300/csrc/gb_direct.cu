@@ -444,8 +444,11 @@ __device__ __forceinline__ double warp_sum_d(double v) {
     return v;
 }
 
-__global__ void energy_partial_kernel(const float4 *__restrict__ xm, const float4 *__restrict__ vel,
-                                      const float *__restrict__ phi, int64_t n, double2 *out) {
+// One launch: every block writes its partial, the block that arrives last
+// (ticket) adds the partials in block order; it leaves the ticket at zero.
+__global__ void energy_kernel(const float4 *__restrict__ xm, const float4 *__restrict__ vel,
+                              const float *__restrict__ phi, int64_t n, double2 *part, unsigned *ticket, double G,
+                              double *out3) {
     double ke = 0.0, w = 0.0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
@@ -456,6 +459,7 @@ __global__ void energy_partial_kernel(const float4 *__restrict__ xm, const float
         w += m * (double)phi[i];
     }
     __shared__ double sk[32], sw[32];
+    __shared__ bool last;
     ke = warp_sum_d(ke);
     w = warp_sum_d(w);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -467,29 +471,50 @@ __global__ void energy_partial_kernel(const float4 *__restrict__ xm, const float
         w = lane < nw ? sw[lane] : 0.0;
         ke = warp_sum_d(ke);
         w = warp_sum_d(w);
-        if (lane == 0) out[blockIdx.x] = make_double2(ke, w);
+        if (lane == 0) {
+            part[blockIdx.x] = make_double2(ke, w);
+            __threadfence();  // the partial is visible before the ticket counts it
+            last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+        }
     }
-}
-
-__global__ void energy_final_kernel(const double2 *__restrict__ part, int nb, double G, double *out3) {
-    double ke = 0.0, w = 0.0;
-    for (int b = threadIdx.x; b < nb; b += 32) { ke += part[b].x; w += part[b].y; }
+    __syncthreads();
+    if (!last || wid != 0) return;
+    __threadfence();
+    ke = 0.0;
+    w = 0.0;
+    for (int b = lane; b < (int)gridDim.x; b += 32) {
+        const double2 pb = __ldcg(part + b);
+        ke += pb.x;
+        w += pb.y;
+    }
     ke = warp_sum_d(ke);
     w = warp_sum_d(w);
-    if (threadIdx.x == 0) {
+    if (lane == 0) {
         const double pe = -0.5 * G * w;
         out3[0] = ke;
         out3[1] = pe;
         out3[2] = ke + pe;
+        *ticket = 0u;
     }
 }
 
 int launch_energy(const float4 *xm, const float4 *vel, const float *phi, int64_t n, float G, double2 *epart,
                   int epart_cap, double *out3, cudaStream_t s) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, out3) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(GB_EINVAL, "out3 is not a valid pointer");
+    }
+    const bool host = at.type == cudaMemoryTypeHost || at.type == cudaMemoryTypeUnregistered;
+    double *dst = host ? reinterpret_cast<double *>(epart + epart_cap + 1) : out3;
+    unsigned *ticket = reinterpret_cast<unsigned *>(epart + epart_cap);
     const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(epart_cap, (n + 255) / 256));
-    energy_partial_kernel<<<nb, 256, 0, s>>>(xm, vel, phi, n, epart);
-    energy_final_kernel<<<1, 32, 0, s>>>(epart, nb, (double)G, out3);
+    energy_kernel<<<nb, 256, 0, s>>>(xm, vel, phi, n, epart, ticket, (double)G, dst);
     GB_CUDA_TRY(cudaGetLastError());
+    if (host) {
+        GB_CUDA_TRY(cudaMemcpyAsync(out3, dst, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+        GB_CUDA_TRY(cudaStreamSynchronize(s));
+    }
     return GB_OK;
 }
 
@@ -683,8 +708,10 @@ extern "C" int gb_direct_create(gb_direct_t **out, int64_t n_max) {
     if (st == GB_OK && cudaMalloc(&h->phi, sizeof(float) * n_max) != cudaSuccess)
         st = fail(GB_ENOMEM, "phi scratch");
     h->epart_cap = 4 * h->sms;
-    if (st == GB_OK && cudaMalloc(&h->epart, sizeof(double2) * h->epart_cap) != cudaSuccess)
+    if (st == GB_OK && cudaMalloc(&h->epart, sizeof(double2) * (h->epart_cap + ENERGY_EXTRA)) != cudaSuccess)
         st = fail(GB_ENOMEM, "energy scratch");
+    if (st == GB_OK && cudaMemset(h->epart, 0, sizeof(double2) * (h->epart_cap + ENERGY_EXTRA)) != cudaSuccess)
+        st = fail(GB_ECUDA, "energy scratch memset");
     if (st == GB_OK && cudaMalloc(&h->diag, sizeof(unsigned long long) * DIAG_COUNT) != cudaSuccess)
         st = fail(GB_ENOMEM, "diag");
     if (st == GB_OK && cudaMemset(h->diag, 0, sizeof(unsigned long long) * DIAG_COUNT) != cudaSuccess)
@@ -999,7 +1026,7 @@ extern "C" int gb_energy(gb_direct_t *h, const float *xm, const float *vel, int6
     if (n > 0) GB_TRY(gb_direct_phi(h, xm, h->phi, n, eps2, 0, stream));
     GB_TRY(launch_energy((const float4 *)xm, (const float4 *)vel, h->phi, n, G, h->epart, h->epart_cap, out3,
                          (cudaStream_t)stream));
-    h->launches += 2;
+    h->launches += 1;
     return GB_OK;
 }
 
@@ -1014,7 +1041,7 @@ extern "C" int gb_energy_phi(gb_direct_t *h, const float *xm, const float *vel, 
     if (!out3) return fail(GB_EINVAL, "out3 is NULL");
     GB_TRY(launch_energy((const float4 *)xm, (const float4 *)vel, phi, n, G, h->epart, h->epart_cap, out3,
                          (cudaStream_t)stream));
-    h->launches += 2;
+    h->launches += 1;
     return GB_OK;
 }
 

@@ -145,13 +145,13 @@ class BarnesHut:
 
     def energies_from_phi(self, xm, vel, phi) -> tuple[float, float, float]:
         """(KE, PE, KE+PE) in FP64 from a tree potential phi."""
-        if self._out3 is None:
-            self._out3 = torch.zeros(3, dtype=torch.float64, device=self.device)
+        if self._out3 is None:  # pinned host memory: the call copies and waits
+            self._out3 = torch.zeros(3, dtype=torch.float64).pin_memory()
         _lib.call("gb_bh_energy", self._h, ptr(xm, "xm"), ptr(vel, "vel"),
-                  ptr(phi, "phi", rows4=False), xm.shape[0], self.G,
-                  ptr(self._out3, "out3", torch.float64, rows4=False), stream_handle(self.device))
-        e = self._out3.cpu().numpy()
-        return float(e[0]), float(e[1]), float(e[2])
+                  ptr(phi, "phi", rows4=False), xm.shape[0], self.G, self._out3.data_ptr(),
+                  stream_handle(self.device))
+        e = self._out3.tolist()
+        return e[0], e[1], e[2]
 
     def export(self, name: str) -> np.ndarray:
         """One array of the last build in the reference's layout."""

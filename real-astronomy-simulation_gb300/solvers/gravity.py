@@ -127,18 +127,30 @@ class DirectGravity:
                   stream_handle(self.device))
         return self._out3
 
+    def _host3(self):
+        """Pinned host buffer the energy calls copy their three sums into
+        (the call then waits for its stream)."""
+        if getattr(self, "_out3_host", None) is None:
+            self._out3_host = torch.zeros(3, dtype=torch.float64).pin_memory()
+        return self._out3_host
+
     def energies(self, xm, vel, G, eps2):
-        e = self.energies_async(xm, vel, G, eps2).cpu().numpy()
-        return float(e[0]), float(e[1]), float(e[2])
+        out = self._host3()
+        _lib.call("gb_energy", self._h, ptr(xm, "xm"), ptr(vel, "vel"), xm.shape[0],
+                  float(G), float(eps2), out.data_ptr(), stream_handle(self.device))
+        e = out.tolist()
+        return e[0], e[1], e[2]
 
     def energies_from_phi(self, xm, vel, phi, G):
         """(KE, PE, KE+PE) from potential sums phi the force pass already
-        produced: only the O(n) FP64 reductions run."""
+        produced: only the O(n) FP64 reductions run (one launch, a 24-byte
+        copy to pinned host memory)."""
+        out = self._host3()
         _lib.call("gb_energy_phi", self._h, ptr(xm, "xm"), ptr(vel, "vel"),
-                  ptr(phi, "phi", rows4=False), xm.shape[0], float(G),
-                  ptr(self._out3, "out3", torch.float64, rows4=False), stream_handle(self.device))
-        e = self._out3.cpu().numpy()
-        return float(e[0]), float(e[1]), float(e[2])
+                  ptr(phi, "phi", rows4=False), xm.shape[0], float(G), out.data_ptr(),
+                  stream_handle(self.device))
+        e = out.tolist()
+        return e[0], e[1], e[2]
 
     def launch_count(self) -> int:
         return int(_lib.load().gb_direct_launch_count(self._h))
