@@ -857,14 +857,18 @@ constexpr int GW_STACK = 1024;           // internal nodes per warp (the 1M disk
 constexpr int GW_LIST = 256;             // list entries per warp
 constexpr int GW_FLUSH = GW_LIST - 64;   // an iteration appends at most 64
 
+// The list holds entry pairs as {x0, x1, y0, y1} in la and {z0, z1, m0, m1}
+// in lb (two arrays: the scalar stores of 32 consecutive entries meet 2-way
+// bank conflicts, against 4-way with the two halves interleaved).
 struct GwWarp {
     int stk[GW_STACK];
-    float4 lst[GW_LIST / 2][2];  // entry pairs {x0, x1, y0, y1}, {z0, z1, m0, m1}
+    float4 la[GW_LIST / 2];
+    float4 lb[GW_LIST / 2];
 };
 
 __device__ __forceinline__ void gw_put(GwWarp &w, int j, float x, float y, float z, float m) {
-    float *a = reinterpret_cast<float *>(&w.lst[j >> 1][0]);
-    float *b = reinterpret_cast<float *>(&w.lst[j >> 1][1]);
+    float *a = reinterpret_cast<float *>(&w.la[j >> 1]);
+    float *b = reinterpret_cast<float *>(&w.lb[j >> 1]);
     const int h = j & 1;
     a[h] = x;
     a[2 + h] = y;
@@ -885,10 +889,11 @@ __device__ __forceinline__ float box_dist2(float x, float y, float z, float lx, 
 template <bool PHI>
 __device__ __forceinline__ void gw_eval(const GwWarp &w, int cnt, f2 PX, f2 PY, f2 PZ, f2 E2, f2 &AX, f2 &AY,
                                         f2 &AZ, f2 &PW) {
-    const ulonglong2 *L = reinterpret_cast<const ulonglong2 *>(&w.lst[0][0]);
+    const ulonglong2 *LA = reinterpret_cast<const ulonglong2 *>(w.la);
+    const ulonglong2 *LB = reinterpret_cast<const ulonglong2 *>(w.lb);
 #pragma unroll 4
     for (int q = 0; q < (cnt >> 1); ++q) {
-        const ulonglong2 A = L[2 * q], B = L[2 * q + 1];
+        const ulonglong2 A = LA[q], B = LB[q];
         const f2 dx = sub2(A.x, PX), dy = sub2(A.y, PY), dz = sub2(B.x, PZ);
         f2 r2 = fma2(dx, dx, E2);
         r2 = fma2(dy, dy, r2);

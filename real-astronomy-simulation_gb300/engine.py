@@ -14,11 +14,14 @@ raises GravityError when the traversal's max_stack rule dropped work or a
 position is not finite; the reference drops such work silently),
 ``bh_traversal`` (tree mode: traversal shape, default -1, the per-particle
 walk of the reference; 3 selects the group walk, see
-BarnesHut.set_traversal), ``fused_potential`` (default True: the force
-pass of the last step of every
-``step``/``run`` call, and of the priming in ``load_state``, also writes the
-potential of its positions, so ``energies()`` afterwards runs only the O(N)
-FP64 reductions instead of an O(N^2) potential pass), ``device``.
+BarnesHut.set_traversal), ``fused_potential`` (whether the force pass
+also writes the potential of its positions, so that ``energies()`` after it
+runs only the O(N) FP64 reductions instead of a potential pass of its own;
+the potential costs about a tenth of a step.  True: the last step of every
+``step``/``run`` call and the priming in ``load_state``; False: never;
+"auto" (default): the priming, and the step that ends where the cadence of
+the last two ``energies()`` calls puts the next one, as a run loop that
+prints every k steps does), ``device``.
 
 Energies (core/engine.py:119-124): the direct mode's potential is the
 potential_energy sum (core/solvers/gravity.py:39-57); the tree mode's is the
@@ -53,10 +56,12 @@ class Engine:
     def __init__(self, softening: float = 0.05, gravity_mode: str = "direct",
                  theta: float = 0.6, *, G: float = units.G, key_bits: int = 21,
                  max_stack: int = 64, plain_fp32: bool = False, symmetric: bool = True,
-                 check: bool = False, fused_potential: bool = True, bh_traversal: int = -1,
+                 check: bool = False, fused_potential="auto", bh_traversal: int = -1,
                  device=None):
         if gravity_mode not in ("direct", "bh"):
             raise ValueError(f"gravity_mode must be 'direct' or 'bh', got {gravity_mode!r}")
+        if fused_potential not in (True, False, "auto"):
+            raise ValueError(f"fused_potential must be True, False or 'auto', got {fused_potential!r}")
         self.softening = float(softening)
         self.gravity_mode = gravity_mode
         self.theta = float(theta)
@@ -66,7 +71,9 @@ class Engine:
         self.plain_fp32 = bool(plain_fp32)
         self.symmetric = bool(symmetric)
         self.check = bool(check)
-        self.fused_potential = bool(fused_potential)
+        self.fused_potential = fused_potential
+        self._e_steps: list = []     # step counts of the last energies() calls
+        self.potential_passes = 0    # potential passes energies() had to run itself
         self.bh_traversal = int(bh_traversal)
         self.phi = None          # potential sums (no G) of the current positions, when valid
         self._phi_valid = False
@@ -198,7 +205,7 @@ class Engine:
         self._phi_valid = False
         if self.n == 0:
             return
-        phi = self.phi if self.fused_potential else None
+        phi = self.phi if self.fused_potential in (True, "auto") else None
         with torch.cuda.device(self.device):
             if self._bh is not None:
                 self._bh.compute(self.xm, self.a4, phi=phi)
@@ -207,6 +214,15 @@ class Engine:
             else:
                 self._direct.acc(self.xm, self.a4, self.G, self.eps2, plain=self.plain_fp32)
         self._phi_valid = phi is not None
+
+    def _fuse_at(self, end_step: int) -> bool:
+        """Whether the run ending at end_step writes the potential."""
+        if self.fused_potential in (True, False):
+            return self.fused_potential
+        if len(self._e_steps) < 2:
+            return False
+        last, k = self._e_steps[-1], self._e_steps[-1] - self._e_steps[-2]
+        return k > 0 and end_step > last and (end_step - last) % k == 0
 
     def step(self, dt: float) -> None:
         """One KDK step (core/engine.py:108-116); kick and drift are fused
@@ -219,7 +235,7 @@ class Engine:
             return
         if self.n > 0:
             self._phi_valid = False
-            phi = self.phi if self.fused_potential else None
+            phi = self.phi if self._fuse_at(self.step_count + nsteps) else None
             with torch.cuda.device(self.device):
                 if self._bh is not None:
                     self._bh.kdk(self.xm, self.v4, self.a4, dt, nsteps, phi=phi)
@@ -242,7 +258,10 @@ class Engine:
         with torch.cuda.device(self.device):
             if exact:
                 return self._direct_solver().energies(self.xm, self.v4, self.G, self.eps2)
+            if not self._e_steps or self._e_steps[-1] != self.step_count:
+                self._e_steps = (self._e_steps + [self.step_count])[-2:]
             if not self._phi_valid:
+                self.potential_passes += 1
                 if self._bh is not None:
                     self._bh.compute(self.xm, torch.empty_like(self.a4), phi=self.phi)
                 else:

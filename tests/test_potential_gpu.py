@@ -281,3 +281,37 @@ def test_engine_energies_after_a_step(cuda_dev, orc, mode):
         assert abs(eng.energies()[1] - pe2) < tol * abs(pe2)
     for a, b in zip(res[True], res[False]):
         np.testing.assert_allclose(a, b, rtol=1e-6)
+
+
+@pytest.mark.parametrize("mode", ["direct", "bh"])
+def test_engine_auto_potential_follows_the_print_cadence(cuda_dev, mode):
+    """fused_potential="auto" (the default): a run loop that calls energies()
+    every 5 steps pays a potential pass of its own for the first two calls
+    only; from the third on, the step that ends at the predicted call writes
+    the potential.  Trajectories equal the always-fused Engine's bit for bit
+    and the energies agree with it (the fused and the separate potential
+    differ by FP32 rounding order)."""
+    pkg, _, _, ic = _mods()
+    if mode == "direct":
+        pos, vel, mass = ic.plummer(3000, seed=8)
+        kw = dict(softening=0.01, G=1.0)
+        dt = 1e-3
+    else:
+        pos, vel, mass = ic.exponential_disk(20000, seed=8)
+        kw = dict(theta=0.5, softening=0.05, key_bits=10)
+        dt = 1e-4
+    pos, vel, mass = _f32(pos), _f32(vel), _f32(mass)
+    out = {}
+    for fused in ("auto", True):
+        eng = pkg.Engine(gravity_mode=mode, fused_potential=fused, device=cuda_dev, **kw)
+        eng.load_state(pkg.State.from_arrays(pos, vel, mass))
+        es = []
+        for k in range(1, 31):
+            eng.step(dt)
+            if k % 5 == 0:
+                es.append(eng.energies())
+        out[fused] = (np.array(es), eng.to_state(), eng.potential_passes)
+    assert out["auto"][2] == 2 and out[True][2] == 0
+    np.testing.assert_array_equal(out["auto"][1].pos, out[True][1].pos)
+    np.testing.assert_array_equal(out["auto"][1].vel, out[True][1].vel)
+    np.testing.assert_allclose(out["auto"][0], out[True][0], rtol=2e-6 if mode == "direct" else 1e-5)

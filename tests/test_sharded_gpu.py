@@ -61,7 +61,7 @@ def test_slices_match_oracle_and_whole_call(cuda_dev, orc, n, world, variant):
     sample = np.random.default_rng(n).choice(n, min(n, 2048), replace=False)
     ref = orc.direct_acc(pos, mass, 1.0, 1e-4, sample)
     assert _rel(a[sample], ref).max() < MAX_TOL
-    assert _rel(a, whole[:, :3].double().cpu().numpy()).max() < 1e-6
+    assert _rel(a, whole[:, :3].double().cpu().numpy()).max() < 5e-6
     ref_phi = orc.phi_targets(pos, mass, 1e-4, sample)
     got_phi = phi.double().cpu().numpy()[sample]
     assert (np.abs(got_phi - ref_phi) / np.abs(ref_phi)).max() < MAX_TOL
