@@ -78,11 +78,15 @@ def test_range_flags_and_errors(cuda_dev, orc):
     base = torch.ones((1000, 4), device=cuda_dev)
     acc = base.clone()
     g.acc_range(xm, n, 1000, 1000, acc, 1.0, 1e-4, accumulate=True)
+    fresh = torch.zeros_like(base)
+    g.acc_range(xm, n, 1000, 1000, fresh, 1.0, 1e-4)
     plain = torch.zeros_like(base)
     g.acc_range(xm, n, 1000, 1000, plain, 1.0, 1e-4, plain=True)
     torch.cuda.synchronize()
     ref = orc.direct_acc(pos, mass, 1.0, 1e-4, np.arange(1000, 2000))
-    assert _rel(acc[:, :3].double().cpu().numpy() - 1.0, ref).max() < MAX_TOL
+    assert _rel(fresh[:, :3].double().cpu().numpy(), ref).max() < MAX_TOL
+    # GB_ACCUMULATE adds the same sums to what acc held (one FP32 add).
+    assert torch.equal(acc[:, :3], base[:, :3] + fresh[:, :3])
     assert _rel(plain[:, :3].double().cpu().numpy(), ref).max() < 1e-4  # plain FP32 sums
     for t0, nt in ((-1, 10), (2990, 11), (0, n + 1)):
         with pytest.raises(lib.GravityError) as e:
