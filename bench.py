@@ -443,7 +443,13 @@ def bench_group_walk(args, dev, rank, world, dist, flush, hbm, src):
     out["roofline"] = {"kernel": "bh_group_kernel", "bound": "hbm", "achieved": achieved, "peak": hbm,
                        "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured"
                        else "fallback 6800 GB/s", "unit": "GB/s", "frac": achieved / hbm,
-                       "algorithmic_bytes_per_launch": bytes_launch, "launch_ms": trav_ms}
+                       "algorithmic_bytes_per_launch": bytes_launch, "launch_ms": trav_ms, "traffic": None}
+    note = "bh_group_walk_1M_disk.md"
+    if BH_N == 1_000_000 and BH_BITS == 10 and _profile_current(note, "gb_bh.cu"):
+        out["roofline"]["traffic"] = _profiled_traffic(note)
+        out["roofline"]["traffic_source"] = f"ncu dram bytes of one launch on this workload (profiles/{note})"
+    else:
+        out["roofline"]["traffic_source"] = f"none: profiles/{note} was captured on another revision of csrc/gb_bh.cu"
     # FP32 work: 20 flop per monopole term (list entry x target), 10 per
     # box-acceptance test (two per record).
     out["work_per_step"] = {"node_reads": work["warp_node_reads"], "groups": work["warp_root_reads"],
