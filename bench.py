@@ -1113,21 +1113,41 @@ def bench_scaling(dev, sizes=(10_000, 100_000, 1_000_000, 4_000_000, 16_000_000)
         ref = grav.acc_fp64_targets(xm, targets, units.G, BH_EPS * BH_EPS)
         got = a4[torch.as_tensor(targets, device=dev), :3].double().cpu().numpy()
         rel = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
-        for _ in range(3):
-            bh.kdk(xm, v4, a4, BH_DT, 1)
         reps = 10 if n <= 4_000_000 else 3
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        s.record()
-        bh.kdk(xm, v4, a4, BH_DT, reps)
-        e.record()
-        torch.cuda.synchronize()
-        ms = s.elapsed_time(e) / reps
+
+        def timed_steps():
+            for _ in range(3):
+                bh.kdk(xm, v4, a4, BH_DT, 1)
+            torch.cuda.synchronize()
+            s.record()
+            bh.kdk(xm, v4, a4, BH_DT, reps)
+            e.record()
+            torch.cuda.synchronize()
+            return s.elapsed_time(e) / reps
+
+        ms = timed_steps()
         d = bh.diag(reset=True)
-        rows.append({"n": n, "bh_step_ms": ms, "particle_steps_per_s": n / ms * 1e3,
-                     "force_error_median": float(np.median(rel)), "p99": float(np.percentile(rel, 99)),
-                     "max": float(rel.max()),
-                     "stack_drops": d["stack_drops"], "bad_tree": d["bad_tree"]})
+        row = {"n": n, "bh_step_ms": ms, "particle_steps_per_s": n / ms * 1e3,
+               "force_error_median": float(np.median(rel)), "p99": float(np.percentile(rel, 99)),
+               "max": float(rel.max()), "stack_drops": d["stack_drops"], "bad_tree": d["bad_tree"]}
+        # The opt-in group walk on the same state: step time and its force
+        # error on the same targets (against FP64 sums of the same positions).
+        bh.set_traversal(3)
+        p0 = xm.clone()
+        a3 = torch.zeros_like(xm)
+        bh.compute(p0, a3)
+        ref3 = grav.acc_fp64_targets(p0, targets, units.G, BH_EPS * BH_EPS)
+        got3 = a3[torch.as_tensor(targets, device=dev), :3].double().cpu().numpy()
+        rel3 = np.linalg.norm(got3 - ref3, axis=1) / np.linalg.norm(ref3, axis=1)
+        ms3 = timed_steps()
+        d3 = bh.diag(reset=True)
+        row["group_walk"] = {"bh_step_ms": ms3, "particle_steps_per_s": n / ms3 * 1e3,
+                             "force_error_median": float(np.median(rel3)), "p99": float(np.percentile(rel3, 99)),
+                             "max": float(rel3.max()), "stack_overflow": d3["stack_overflow"],
+                             "bad_tree": d3["bad_tree"]}
+        rows.append(row)
+        del p0, a3
         bh.close()
         if n == 1_000_000:
             g = grav.DirectGravity(n, dev)

@@ -510,3 +510,37 @@ def test_engine_group_walk_option(cuda_dev, orc):
     torch.cuda.synchronize()
     assert torch.equal(eng.xm, xm) and torch.equal(eng.v4, v4) and torch.equal(eng.a4, a4)
     b.close()
+
+
+@pytest.mark.parametrize("case", ["b21", "b10", "dup"])
+def test_group_walk_golden_inputs(cuda_dev, orc, case):
+    """The group walk on the reference's fixture inputs (1,200 particles at
+    21- and 10-bit keys; 500 particles with duplicated positions, whose
+    equal keys exercise the index tie-break): accelerations and potentials
+    against the oracle's FP64 group walk on the oracle's tree, whose
+    topology the fixtures pin."""
+    _, bhmod, _, _ = _mods()
+    g = load_golden("bh")
+    if case == "dup":
+        pos, mass, bits, theta = g["dup_pos"], g["dup_mass"], 10, 0.7
+    else:
+        pos, mass, bits, theta = g["pos"], g["mass"], int(case[1:]), float(g["theta"])
+    pos, mass = _f32(pos), _f32(mass)
+    n = pos.shape[0]
+    soft = float(g["softening"])
+    b = bhmod.BarnesHut(n, theta=theta, softening=soft, key_bits=bits, G=float(g["G"]), device=cuda_dev)
+    b.set_traversal(3)
+    xm = _xm(pos, mass, cuda_dev)
+    acc = torch.zeros_like(xm)
+    phi = torch.zeros(n, device=cuda_dev)
+    b.compute(xm, acc, phi=phi)
+    torch.cuda.synchronize()
+    t = orc.bh_tree(pos, mass, bits=bits)
+    ref_acc, ref_phi = orc.group_walk(pos, t, theta, soft * soft, float(g["G"]))
+    _check_acc(acc[:, :3].double().cpu().numpy(), ref_acc)
+    got = phi.double().cpu().numpy()
+    rel = np.abs(got - ref_phi) / np.maximum(np.abs(ref_phi), 1e-300)
+    assert np.median(rel) < 1e-5 and rel.max() < 1e-2, rel.max()
+    d = b.diag()
+    assert d["stack_overflow"] == 0 and d["bad_tree"] == 0
+    b.close()
