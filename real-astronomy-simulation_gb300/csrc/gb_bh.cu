@@ -852,7 +852,7 @@ bh_traverse_lane_kernel(TravArgs a, float *__restrict__ phi, const int *__restri
 // not bit-identical to the other shapes; the max_stack rule does not apply.
 // A push that would overflow the warp's stack takes the child as a monopole
 // instead and counts it in stack_overflow.
-constexpr int GW_WARPS = 4;
+constexpr int GW_WARPS = 2;
 constexpr int GW_STACK = 640;            // internal nodes per warp (the 1M disk peaks near 310)
 constexpr int GW_LIST = 256;             // list entries per warp
 constexpr int GW_FLUSH = GW_LIST - 64;   // an iteration appends at most 64
@@ -1055,10 +1055,11 @@ __device__ __forceinline__ void gw_group(GwWarp &w, const TravArgs &a, float *__
 
 // Warp w walks the groups whose first leaf lies in [32 w, 32 w + 32) (gsize
 // from the Karras kernel), one after the other.
-// 8 resident CTAs per SM (64 registers, 26 KB of shared memory each): 7.8%
-// less time than 6 on the 1M disk, measured.
+// 32 resident warps per SM (64 registers, 13 KB of shared memory per CTA of
+// 2 warps): 7.8% less time than 24 warps on the 1M disk; CTAs of 2 warps
+// against 4: 1.3% less (a CTA retires when its slowest warp is done).
 template <bool KDK, bool COUNT, bool PHI>
-__global__ void __launch_bounds__(GW_WARPS * 32, 8)
+__global__ void __launch_bounds__(GW_WARPS * 32, 16)
 bh_group_kernel(TravArgs a, const int *__restrict__ gsize, float *__restrict__ phi) {
     __shared__ GwWarp sw[GW_WARPS];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
