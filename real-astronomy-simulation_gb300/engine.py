@@ -120,6 +120,7 @@ class Engine:
         self.n = state.n
         self.time = state.time
         self.step_count = state.step
+        self._e_steps = []  # the energies() cadence restarts with a new state
         self.seed = state.seed
         self.meta = dict(state.meta)
         self._ptype = state.ptype.copy()
@@ -182,6 +183,7 @@ class Engine:
         self.n = n
         self.time = float(time)
         self.step_count = int(step)
+        self._e_steps = []
         self.seed = int(seed)
         self.meta = dict(meta or {})
         self._ptype = np.zeros(n, np.int32) if ptype is None else np.asarray(ptype, np.int32).copy()
