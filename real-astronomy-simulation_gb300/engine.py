@@ -7,7 +7,8 @@ float4 records and every force evaluation running in the sm_103a CUDA
 library.  Extra keyword arguments: ``G`` (default core/units.py:21),
 ``key_bits`` (Morton key width of the tree path; the reference uses 21),
 ``max_stack`` (traversal stack rule, reference default 64), ``plain_fp32``
-(disable Kahan accumulation), ``symmetric`` (direct sum: evaluate each
+(disable Kahan accumulation; ``precision="fp32"`` says the same,
+``precision="fp32-kahan"`` the default), ``symmetric`` (direct sum: evaluate each
 unordered pair once and update both particles, default; False runs one pass
 per target), ``check`` (tree mode: every step waits for the device and
 raises GravityError when the traversal's max_stack rule dropped work or a
@@ -57,11 +58,15 @@ class Engine:
                  theta: float = 0.6, *, G: float = units.G, key_bits: int = 21,
                  max_stack: int = 64, plain_fp32: bool = False, symmetric: bool = True,
                  check: bool = False, fused_potential="auto", bh_traversal: int = -1,
-                 device=None):
+                 precision: str | None = None, device=None):
         if gravity_mode not in ("direct", "bh"):
             raise ValueError(f"gravity_mode must be 'direct' or 'bh', got {gravity_mode!r}")
         if fused_potential not in (True, False, "auto"):
             raise ValueError(f"fused_potential must be True, False or 'auto', got {fused_potential!r}")
+        if precision is not None:
+            if precision not in ("fp32-kahan", "fp32"):
+                raise ValueError(f"precision must be 'fp32-kahan' or 'fp32', got {precision!r}")
+            plain_fp32 = precision == "fp32"
         self.softening = float(softening)
         self.gravity_mode = gravity_mode
         self.theta = float(theta)

@@ -169,3 +169,12 @@ def test_noalloc_rejects_bad_arguments_without_gpu(lib):
     with pytest.raises(pkg.GravityError, match="outside") as e:
         lib_mod.call("gb_direct_acc_noalloc", fake, fake, 65537, 1.0, 1e-4, 0, None)
     assert e.value.status == lib_mod.GB_EINVAL
+
+
+def test_engine_rejects_bad_options_before_touching_the_gpu():
+    """Engine's option checks run on the host: precision, fused_potential
+    and gravity_mode values outside the documented sets raise ValueError."""
+    pkg = importlib.import_module(PKG_NAME)
+    for kw in ({"precision": "fp16"}, {"fused_potential": "sometimes"}, {"gravity_mode": "fmm"}):
+        with pytest.raises(ValueError):
+            pkg.Engine(**kw)
