@@ -525,6 +525,40 @@ def cpu_bh_step(budget_s: float = 20.0):
             "seconds": {"build": t_build, "traverse": t_trav, "kick": t_kick}}
 
 
+def bench_sharded_bh(args, dev, rank, world, dist):
+    """The tree path with the tree replicated and the targets split across
+    the ranks (ShardedBarnesHut) on the headline workload: every rank kicks,
+    drifts and builds the whole tree, walks its slice of the key order, and
+    one all-reduce of the accelerations (16 B per particle) joins the slices.
+    Total work fixed as ranks are added (strong scaling)."""
+    sh = importlib.import_module(PKG + ".sharded")
+    ic = importlib.import_module(PKG + ".ic")
+    units = importlib.import_module(PKG + ".units")
+    pos, vel, mass = ic.exponential_disk(BH_N, seed=0)
+    s = sh.ShardedBarnesHut(pos, vel, mass, theta=BH_THETA, softening=BH_EPS, G=units.G, key_bits=BH_BITS,
+                            device=dev)
+    s.run(BH_DT, args.warmup)
+    steps = max(1, args.steps)
+    st, en = _events(1)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    st[0].record()
+    s.run(BH_DT, steps)
+    en[0].record()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = max_over_ranks(st[0].elapsed_time(en[0]), dist, dev)
+    s.close()
+    return {"workload": f"LBVH Barnes-Hut KDK, exponential disk N={BH_N}, theta {BH_THETA}, replicated tree, "
+                        f"key-order targets split over {world} rank(s)",
+            "value": BH_N * steps / (ms / 1e3), "unit": "particle-steps/s", "n_ranks": world,
+            "scaling": "strong", "ms_per_step": ms / steps, "steps": steps,
+            "allreduce_bytes_per_step": 16 * BH_N,
+            "path": "ShardedBarnesHut: gb_kick/gb_drift, gb_bh_build, gb_bh_accel_range, all-reduce, gb_kick"}
+
+
 # ------------------------------------------------------------- secondary
 def bench_sharded_direct(args, dev, rank, world, dist, n=262_144, dt=5e-4):
     """Direct N^2 with the targets split across the ranks (ShardedDirect):
@@ -1269,6 +1303,7 @@ def main(argv=None):
         line["group_walk"] = res["group_walk"]
     if not args.no_secondary:
         line["sharded_direct"] = bench_sharded_direct(args, dev, rank, world, dist)
+        line["sharded_bh"] = bench_sharded_bh(args, dev, rank, world, dist)
     if rank == 0 and world == 1:
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_bh_step()

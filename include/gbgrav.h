@@ -223,6 +223,21 @@ int gb_bh_accel_phi(gb_bh_t *h, float *acc, float *phi, float theta,
                     float eps2, float G, int max_stack, int flags,
                     void *stream);
 
+/* gb_bh_accel (or, with phi not NULL, gb_bh_accel_phi) for the targets at
+ * key-order positions s0 .. s0 + ns - 1 of the last build only: each one's
+ * acceleration is written to acc at its particle index (the other records
+ * of acc are left as they are), with exactly the node visits of the full
+ * call, so the values are bit-identical to it.  In the group walk (traversal
+ * shape 3) the range covers the groups whose first leaf lies in it.  A rank
+ * that owns one slice of the key order after a replicated build runs this on
+ * a zeroed acc; an all-reduce (sum) of the ranks' acc then gives every
+ * particle its acceleration exactly, each sum having one non-zero term.
+ * Flags: GB_ACCUMULATE, GB_CHECK.  One slice of the traversal loop over all
+ * particles of core/solvers/barnes_hut.py:180-217, 257-259. */
+int gb_bh_accel_range(gb_bh_t *h, float *acc, float *phi, int64_t s0,
+                      int64_t ns, float theta, float eps2, float G,
+                      int max_stack, int flags, void *stream);
+
 /* build + accel: BarnesHut.compute (core/solvers/barnes_hut.py:242-259). */
 int gb_bh_compute(gb_bh_t *h, const float *xm, float *acc, int64_t n,
                   float theta, float eps2, float G, int max_stack, int flags,

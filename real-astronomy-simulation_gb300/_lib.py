@@ -98,6 +98,7 @@ SIGNATURES = {
     "gb_bh_compute": (I32, [P, P, P, I64, F32, F32, F32, I32, I32, P]),
     "gb_bh_kdk": (I32, [P, P, P, P, I64, F32, F32, F32, F32, I64, I32, P]),
     "gb_bh_accel_phi": (I32, [P, P, P, F32, F32, F32, I32, I32, P]),
+    "gb_bh_accel_range": (I32, [P, P, P, I64, I64, F32, F32, F32, I32, I32, P]),
     "gb_bh_kdk_phi": (I32, [P, P, P, P, P, I64, F32, F32, F32, F32, I64, I32, P]),
     "gb_bh_energy": (I32, [P, P, P, P, I64, F32, P, P]),
     "gb_bh_export": (I32, [P, I32, P, P]),

@@ -379,6 +379,7 @@ struct TravArgs {
     float4 *acc;
     float4 *vel;
     int n;
+    int s0, s1;  // targets: key-order (sorted) indices s0 .. s1 - 1 (0 .. n - 1 but for ranges)
     float theta2, eps2, G, h;
     int max_stack;
     int accumulate;
@@ -508,8 +509,8 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32)
 bh_traverse_kernel(TravArgs a, float *__restrict__ phi, const int *__restrict__ parent) {
     __shared__ int4 stk[TRAV_WARPS][TRAV_STACK];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int wbase = (blockIdx.x * TRAV_WARPS + wid) * (32 * TPL);
-    if (wbase >= a.n) return;  // whole warp out of range
+    const int wbase = a.s0 + (blockIdx.x * TRAV_WARPS + wid) * (32 * TPL);
+    if (wbase >= a.s1) return;  // whole warp out of range
     const int n = a.n;
     int s[TPL];
     bool valid[TPL];
@@ -518,7 +519,7 @@ bh_traverse_kernel(TravArgs a, float *__restrict__ phi, const int *__restrict__ 
 #pragma unroll
     for (int q = 0; q < TPL; ++q) {
         s[q] = wbase + 32 * q + lane;
-        valid[q] = s[q] < n;
+        valid[q] = s[q] < a.s1;
         L[q].px = L[q].py = L[q].pz = 0.f;
         W[q].pm = 0.f;
         if (valid[q]) {
@@ -711,8 +712,8 @@ bh_traverse_lane_kernel(TravArgs a, float *__restrict__ phi, const int *__restri
     extern __shared__ int lstk[];  // [max_stack][LANE_THREADS]
     const int tid = threadIdx.x;
     const int n = a.n;
-    const int s = blockIdx.x * LANE_THREADS + tid;
-    const bool valid = s < n;
+    const int s = a.s0 + blockIdx.x * LANE_THREADS + tid;
+    const bool valid = s < a.s1;
     Lane L;
     LanePhi W;
     W.pw = 0.f;
@@ -1064,10 +1065,11 @@ bh_group_kernel(TravArgs a, const int *__restrict__ gsize, float *__restrict__ p
     __shared__ GwWarp sw[GW_WARPS];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     GwWarp &w = sw[wid];
-    const int c0 = (blockIdx.x * GW_WARPS + wid) * 32;
-    if (c0 >= a.n) return;  // whole warp out of range
+    // Groups whose first leaf lies in [s0, s1) (a group may end past s1).
+    const int c0 = a.s0 + (blockIdx.x * GW_WARPS + wid) * 32;
+    if (c0 >= a.s1) return;  // whole warp out of range
     const int n = a.n;
-    int gs = (c0 + lane < n) ? __ldg(gsize + c0 + lane) : 0;
+    int gs = (c0 + lane < a.s1) ? __ldg(gsize + c0 + lane) : 0;
     if (n == 1 && lane == 0) gs = 1;  // a single particle: no internal node, one group
     unsigned starts = __ballot_sync(0xffffffffu, gs > 0 && gs <= GW_GROUP);
     unsigned reads = 0, evals = 0, overflow = 0, bad = 0, ngroups = 0;
@@ -1443,10 +1445,15 @@ struct WarpLaunch {
 // The traversal of the last build: accelerations into acc (KDK: the
 // closing kick into vel too) and, when phi is not NULL, the tree potential
 // sums into phi.
+// Targets: key-order indices [s0, s1) (s1 < 0: all n).
 static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float *phi, float theta, float eps2, float G, float dt,
-                    int max_stack, int flags, bool kdk, cudaStream_t s, int slot, const ExtPot &pot = ExtPot{}) {
+                    int max_stack, int flags, bool kdk, cudaStream_t s, int slot, const ExtPot &pot = ExtPot{},
+                    int64_t s0 = 0, int64_t s1 = -1) {
     const int64_t n = h->n;
     if (n <= 0) return GB_OK;
+    if (s1 < 0) s1 = n;
+    if (s1 <= s0) return GB_OK;
+    const int64_t nt = s1 - s0;
     TravArgs a;
     a.leaf = h->leaf;
     a.inode = h->inode;
@@ -1455,6 +1462,8 @@ static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float *phi, float thet
     a.acc = acc;
     a.vel = vel;
     a.n = (int)n;
+    a.s0 = (int)s0;
+    a.s1 = (int)s1;
     a.theta2 = theta * theta;
     a.eps2 = eps2;
     a.G = G;
@@ -1469,7 +1478,7 @@ static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float *phi, float thet
     // warp-coherent against 5.84 ms per lane; 10k: 0.24 against 0.18 ms).
     const int shape = h->tpl >= 0 ? h->tpl : (n < LANE_AUTO_N ? 0 : 1);
     if (shape == 3) {
-        const int64_t warps = (n + 31) / 32;
+        const int64_t warps = (nt + 31) / 32;
         const unsigned grid = (unsigned)((warps + GW_WARPS - 1) / GW_WARPS);
         if (h->groups_n != n) {
             // Built in another traversal mode: mark the groups from the
@@ -1490,12 +1499,12 @@ static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float *phi, float thet
         }
         dispatch3<GroupLaunch>(kdk, count, phi != nullptr, grid, &a, (const int *)h->gsize, phi, s);
     } else if (shape == 0 && max_stack <= LANE_MAX_STACK && n - 1 <= ((int64_t)1 << LANE_KBITS)) {
-        const unsigned grid = (unsigned)((n + LANE_THREADS - 1) / LANE_THREADS);
+        const unsigned grid = (unsigned)((nt + LANE_THREADS - 1) / LANE_THREADS);
         const size_t smem = sizeof(int) * (size_t)std::max(max_stack, 1) * LANE_THREADS;
         dispatch3<LaneLaunch>(kdk, count, phi != nullptr, grid, smem, &a, phi, (const int *)h->parent, s);
     } else {
         const int tpl = shape == 2 ? 2 : 1;
-        const int64_t warps = (n + 32 * tpl - 1) / (32 * tpl);
+        const int64_t warps = (nt + 32 * tpl - 1) / (32 * tpl);
         const unsigned grid = (unsigned)((warps + TRAV_WARPS - 1) / TRAV_WARPS);
         dispatch3<WarpLaunch>(kdk, count, phi != nullptr, tpl, grid, &a, phi, (const int *)h->parent, s);
     }
@@ -1556,6 +1565,24 @@ extern "C" int gb_bh_accel(gb_bh_t *h, float *acc, float theta, float eps2, floa
     GB_TRY(traverse(h, (float4 *)acc, nullptr, nullptr, theta, eps2, G, 0.f, max_stack, flags, false,
                     (cudaStream_t)stream, h->pending_slot));
     if ((flags & GB_CHECK) || h->check) return check_failures(h, (cudaStream_t)stream, "gb_bh_accel");
+    return GB_OK;
+}
+
+extern "C" int gb_bh_accel_range(gb_bh_t *h, float *acc, float *phi, int64_t s0, int64_t ns, float theta,
+                                 float eps2, float G, int max_stack, int flags, void *stream) {
+    if (!h) return fail(GB_EINVAL, "handle is NULL");
+    if (h->n < 0) return fail(GB_ENOTREADY, "gb_bh_accel_range before gb_bh_build");
+    if (s0 < 0 || ns < 0 || s0 > h->n || ns > h->n - s0)
+        return fail(GB_EINVAL, "target range [%lld, %lld) outside the %lld particles of the last build",
+                    (long long)s0, (long long)(s0 + ns), (long long)h->n);
+    if (flags & ~(GB_ACCUMULATE | GB_CHECK))
+        return fail(GB_EINVAL, "gb_bh_accel_range: flags 0x%x: only GB_ACCUMULATE and GB_CHECK apply", flags);
+    if (ns == 0) return GB_OK;
+    GB_TRY(check_ptr(acc, "acc"));
+    GB_TRY(check_params(theta, eps2, max_stack));
+    GB_TRY(traverse(h, (float4 *)acc, nullptr, phi, theta, eps2, G, 0.f, max_stack, flags, false,
+                    (cudaStream_t)stream, h->pending_slot, ExtPot{}, s0, s0 + ns));
+    if ((flags & GB_CHECK) || h->check) return check_failures(h, (cudaStream_t)stream, "gb_bh_accel_range");
     return GB_OK;
 }
 

@@ -90,6 +90,17 @@ class BarnesHut:
                       self.theta, self.eps2, self.G, self.max_stack, flags, stream_handle(self.device))
         return acc
 
+    def accel_range(self, acc: torch.Tensor, s0: int, ns: int, accumulate: bool = False,
+                    phi=None) -> torch.Tensor:
+        """Tree accelerations of the last build for the targets at key-order
+        positions s0 .. s0 + ns - 1 only, written at their particle indices
+        of acc (and phi); bit-identical to those of accel()."""
+        flags = _lib.GB_ACCUMULATE if accumulate else 0
+        _lib.call("gb_bh_accel_range", self._h, ptr(acc, "acc"),
+                  None if phi is None else ptr(phi, "phi", rows4=False), int(s0), int(ns),
+                  self.theta, self.eps2, self.G, self.max_stack, flags, stream_handle(self.device))
+        return acc
+
     def compute(self, *args, accumulate: bool = False, count_work: bool = False,
                 check: bool = False, phi=None):
         """acc <- tree accelerations (core/solvers/barnes_hut.py:242-259).

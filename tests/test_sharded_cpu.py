@@ -131,3 +131,85 @@ def test_shard_range_tiles_the_system():
             assert seen == list(range(n))
     with pytest.raises(ValueError):
         sh.shard_range(10, 2, 2)
+
+
+# ------------------------------------------------------------------- tree
+class OracleTreeOps(OracleOps):
+    """The tree step's device work in FP64 on the CPU: the oracle's tree
+    (keys, order, topology, summaries) and its per-particle traversal for
+    the targets of one slice of the key order."""
+
+    def __init__(self, theta, softening, G, bits):
+        super().__init__(G, softening * softening)
+        self.theta, self.bits = theta, bits
+
+    def tree_acc(self, x, n, s0, ns, a, phi=None):
+        a.zero_()
+        if phi is not None:
+            phi.zero_()
+        if ns == 0:
+            return
+        xs = x[:n].numpy()
+        t = self.orc.bh_tree(xs[:, :3], xs[:, 3], self.bits)
+        sel = np.asarray(t["order"][s0:s0 + ns], dtype=np.int64)
+        args = (xs[:, :3], t["order"], t["com"], t["nmass"], t["nmin"], t["nmax"], t["left"], t["right"],
+                self.theta, self.eps2)
+        acc, _ = self.orc.traverse(*args, self.G, 64, sel)
+        a[torch.as_tensor(sel), :3] = torch.from_numpy(acc)
+        if phi is not None:
+            p, _ = self.orc.traverse_phi(*args, 64, sel)
+            phi[torch.as_tensor(sel)] = torch.from_numpy(p)
+
+
+TREE = dict(theta=0.5, softening=0.05, G=1.0, bits=10)
+
+
+def _tree_worker(rank, world, port, out_dir, n):
+    sys.path.insert(0, ROOT)
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        sh = importlib.import_module(PKG_NAME + ".sharded")
+        pos, vel, mass = _system(n)
+        s = sh.ShardedBarnesHut(pos, vel, mass, theta=TREE["theta"], softening=TREE["softening"],
+                                G=TREE["G"], key_bits=TREE["bits"], ops=OracleTreeOps(**TREE))
+        s.run(DT, STEPS)
+        p, v, a = s.gather_state()
+        np.savez(os.path.join(out_dir, f"tree{rank}.npz"), p=p, v=v, a=a, e=np.array(s.energies()),
+                 s0=s.s0, ns=s.ns)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_tree_two_ranks_equal_one_rank(tmp_path):
+    """ShardedBarnesHut over two gloo ranks (replicated tree, key-order
+    slices, one all-reduce of the accelerations per step) equals the one-rank
+    run bit for bit, and both equal the
+    oracle's own BH KDK loop; energies agree to FP64 rounding."""
+    world, n = 2, 700
+    mp.spawn(_tree_worker, args=(world, _free_port(), str(tmp_path), n), nprocs=world, join=True)
+    sh = importlib.import_module(PKG_NAME + ".sharded")
+    pos, vel, mass = _system(n)
+    one = sh.ShardedBarnesHut(pos, vel, mass, theta=TREE["theta"], softening=TREE["softening"], G=TREE["G"],
+                              key_bits=TREE["bits"], ops=OracleTreeOps(**TREE))
+    one.run(DT, STEPS)
+    p1, v1, a1 = one.gather_state()
+    e1 = np.array(one.energies())
+    r = [np.load(tmp_path / f"tree{k}.npz") for k in range(world)]
+    assert [int(x["s0"]) for x in r] == [0, 350] and [int(x["ns"]) for x in r] == [350, 350]
+    for x in r:
+        assert np.array_equal(x["p"], p1) and np.array_equal(x["v"], v1) and np.array_equal(x["a"], a1)
+        # The oracle's FP64 energy sums are OpenMP reductions: their order
+        # follows the thread count of each process.
+        assert np.allclose(x["e"], e1, rtol=1e-13, atol=0)
+    from oracle import oracle
+
+    p, v = pos.copy(), vel.copy()
+    a, _, _ = oracle.bh_compute(p, mass, TREE["theta"], TREE["softening"], TREE["G"], bits=TREE["bits"])
+    for _ in range(STEPS):
+        v = v + a * (0.5 * DT)
+        p = p + v * DT
+        a, _, _ = oracle.bh_compute(p, mass, TREE["theta"], TREE["softening"], TREE["G"], bits=TREE["bits"])
+        v = v + a * (0.5 * DT)
+    assert np.array_equal(p1, p) and np.array_equal(v1, v) and np.array_equal(a1, a)

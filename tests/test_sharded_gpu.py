@@ -119,3 +119,68 @@ def test_sharded_stepper_one_rank_matches_oracle(cuda_dev, orc):
     pe_ref = orc.potential_energy(p, mass, 1.0, 1e-4)
     assert abs(ke - ke_ref) < 1e-5 * abs(ke_ref) and abs(pe - pe_ref) < 1e-5 * abs(pe_ref)
     s.close()
+
+
+# ------------------------------------------------------------------- tree
+@pytest.mark.parametrize("tpl", [-1, 0, 1, 2, 3])
+def test_tree_slices_equal_whole_traversal(cuda_dev, tpl):
+    """gb_bh_accel_range over the key-order slices of 3 ranks, each into a
+    zeroed array, summed: equal to one gb_bh_accel (and its potentials) bit
+    for bit in every traversal shape; slices that are not warp-aligned
+    included."""
+    _, ic, sh, lib = _mods()
+    bhmod = importlib.import_module(PKG_NAME + ".solvers.barnes_hut")
+    n = 30001
+    pos, _, mass = ic.exponential_disk(n, seed=21)
+    xm = torch.tensor(np.column_stack((pos, mass)), dtype=torch.float32, device=cuda_dev)
+    b = bhmod.BarnesHut(n, theta=0.5, softening=0.05, key_bits=10, device=cuda_dev)
+    b.set_traversal(tpl)
+    b.build(xm)
+    whole = torch.zeros_like(xm)
+    phi_whole = torch.zeros(n, device=cuda_dev)
+    b.accel(whole, phi=phi_whole)
+    total = torch.zeros_like(xm)
+    phi_total = torch.zeros(n, device=cuda_dev)
+    for r in range(3):
+        s0, ns, _ = sh.shard_range(n, r, 3)
+        part = torch.zeros_like(xm)
+        phi_part = torch.zeros(n, device=cuda_dev)
+        b.accel_range(part, s0, ns, phi=phi_part)
+        total += part
+        phi_total += phi_part
+    torch.cuda.synchronize()
+    assert torch.equal(total, whole) and torch.equal(phi_total, phi_whole)
+    with pytest.raises(lib.GravityError) as e:
+        b.accel_range(total, n - 5, 10)
+    assert e.value.status == lib.GB_EINVAL
+    b.close()
+
+
+def test_tree_sharded_stepper_one_rank_equals_fused_kdk(cuda_dev):
+    """ShardedBarnesHut on one rank (kick, drift, replicated build, the
+    range traversal over all targets, kick) follows gb_bh_kdk's fused step
+    bit for bit; its energies equal the tree handle's."""
+    _, ic, sh, _ = _mods()
+    bhmod = importlib.import_module(PKG_NAME + ".solvers.barnes_hut")
+    n, steps, dt = 20000, 4, 1e-4
+    pos, vel, mass = ic.exponential_disk(n, seed=22)
+    pos, vel, mass = _f32(pos), _f32(vel), _f32(mass)
+    s = sh.ShardedBarnesHut(pos, vel, mass, theta=0.5, softening=0.05, key_bits=10, device=cuda_dev)
+    s.run(dt, steps)
+    p, v, a = s.gather_state()
+    b = bhmod.BarnesHut(n, theta=0.5, softening=0.05, key_bits=10, device=cuda_dev)
+    xm = torch.tensor(np.column_stack((pos, mass)), dtype=torch.float32, device=cuda_dev)
+    v4 = torch.zeros_like(xm)
+    v4[:, :3] = torch.tensor(vel, dtype=torch.float32, device=cuda_dev)
+    a4 = torch.zeros_like(xm)
+    b.compute(xm, a4)
+    phi = torch.zeros(n, device=cuda_dev)
+    b.kdk(xm, v4, a4, dt, steps, phi=phi)
+    assert np.array_equal(p, xm[:, :3].double().cpu().numpy())
+    assert np.array_equal(v, v4[:, :3].double().cpu().numpy())
+    assert np.array_equal(a, a4[:, :3].double().cpu().numpy())
+    e = s.energies()
+    e_ref = b.energies_from_phi(xm, v4, phi)
+    assert e == e_ref
+    s.close()
+    b.close()
