@@ -379,7 +379,6 @@ struct TravArgs {
     float4 *acc;
     float4 *vel;
     int n;
-    int s0, s1;  // targets: key-order (sorted) indices s0 .. s1 - 1 (0 .. n - 1 but for ranges)
     float theta2, eps2, G, h;
     int max_stack;
     int accumulate;
@@ -506,11 +505,11 @@ __device__ __forceinline__ bool apply_room(Lane &L, bool open, int sp, int max_s
 // instructions per node expansion, measured).
 template <bool KDK, bool COUNT, int TPL, bool PHI>
 __global__ void __launch_bounds__(TRAV_WARPS * 32)
-bh_traverse_kernel(TravArgs a, float *__restrict__ phi, const int *__restrict__ parent) {
+bh_traverse_kernel(TravArgs a, float *__restrict__ phi, const int *__restrict__ parent, int s0, int s1) {
     __shared__ int4 stk[TRAV_WARPS][TRAV_STACK];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int wbase = a.s0 + (blockIdx.x * TRAV_WARPS + wid) * (32 * TPL);
-    if (wbase >= a.s1) return;  // whole warp out of range
+    const int wbase = s0 + (blockIdx.x * TRAV_WARPS + wid) * (32 * TPL);
+    if (wbase >= s1) return;  // whole warp out of range
     const int n = a.n;
     int s[TPL];
     bool valid[TPL];
@@ -519,7 +518,7 @@ bh_traverse_kernel(TravArgs a, float *__restrict__ phi, const int *__restrict__ 
 #pragma unroll
     for (int q = 0; q < TPL; ++q) {
         s[q] = wbase + 32 * q + lane;
-        valid[q] = s[q] < a.s1;
+        valid[q] = s[q] < s1;
         L[q].px = L[q].py = L[q].pz = 0.f;
         W[q].pm = 0.f;
         if (valid[q]) {
@@ -708,12 +707,12 @@ constexpr int64_t LANE_AUTO_N = 131072;
 
 template <bool KDK, bool COUNT, bool PHI>
 __global__ void __launch_bounds__(LANE_THREADS)
-bh_traverse_lane_kernel(TravArgs a, float *__restrict__ phi, const int *__restrict__ parent) {
+bh_traverse_lane_kernel(TravArgs a, float *__restrict__ phi, const int *__restrict__ parent, int s0, int s1) {
     extern __shared__ int lstk[];  // [max_stack][LANE_THREADS]
     const int tid = threadIdx.x;
     const int n = a.n;
-    const int s = a.s0 + blockIdx.x * LANE_THREADS + tid;
-    const bool valid = s < a.s1;
+    const int s = s0 + blockIdx.x * LANE_THREADS + tid;
+    const bool valid = s < s1;
     Lane L;
     LanePhi W;
     W.pw = 0.f;
@@ -1061,15 +1060,15 @@ __device__ __forceinline__ void gw_group(GwWarp &w, const TravArgs &a, float *__
 // against 4: 1.3% less (a CTA retires when its slowest warp is done).
 template <bool KDK, bool COUNT, bool PHI>
 __global__ void __launch_bounds__(GW_WARPS * 32, 16)
-bh_group_kernel(TravArgs a, const int *__restrict__ gsize, float *__restrict__ phi) {
+bh_group_kernel(TravArgs a, const int *__restrict__ gsize, float *__restrict__ phi, int s0, int s1) {
     __shared__ GwWarp sw[GW_WARPS];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     GwWarp &w = sw[wid];
     // Groups whose first leaf lies in [s0, s1) (a group may end past s1).
-    const int c0 = a.s0 + (blockIdx.x * GW_WARPS + wid) * 32;
-    if (c0 >= a.s1) return;  // whole warp out of range
+    const int c0 = s0 + (blockIdx.x * GW_WARPS + wid) * 32;
+    if (c0 >= s1) return;  // whole warp out of range
     const int n = a.n;
-    int gs = (c0 + lane < a.s1) ? __ldg(gsize + c0 + lane) : 0;
+    int gs = (c0 + lane < s1) ? __ldg(gsize + c0 + lane) : 0;
     if (n == 1 && lane == 0) gs = 1;  // a single particle: no internal node, one group
     unsigned starts = __ballot_sync(0xffffffffu, gs > 0 && gs <= GW_GROUP);
     unsigned reads = 0, evals = 0, overflow = 0, bad = 0, ngroups = 0;
@@ -1396,16 +1395,16 @@ static int check_ptr(const void *p, const char *name) {
 }
 
 template <bool KDK, bool COUNT, bool PHI>
-static void launch_lane(unsigned grid, size_t smem, const TravArgs &a, float *phi, const int *parent,
+static void launch_lane(unsigned grid, size_t smem, const TravArgs &a, float *phi, const int *parent, int2 r,
                         cudaStream_t s) {
-    bh_traverse_lane_kernel<KDK, COUNT, PHI><<<grid, LANE_THREADS, smem, s>>>(a, phi, parent);
+    bh_traverse_lane_kernel<KDK, COUNT, PHI><<<grid, LANE_THREADS, smem, s>>>(a, phi, parent, r.x, r.y);
 }
 
 template <bool KDK, bool COUNT, bool PHI>
-static void launch_warp(int tpl, unsigned grid, const TravArgs &a, float *phi, const int *parent,
+static void launch_warp(int tpl, unsigned grid, const TravArgs &a, float *phi, const int *parent, int2 r,
                         cudaStream_t s) {
-    if (tpl == 2) bh_traverse_kernel<KDK, COUNT, 2, PHI><<<grid, TRAV_WARPS * 32, 0, s>>>(a, phi, parent);
-    else bh_traverse_kernel<KDK, COUNT, 1, PHI><<<grid, TRAV_WARPS * 32, 0, s>>>(a, phi, parent);
+    if (tpl == 2) bh_traverse_kernel<KDK, COUNT, 2, PHI><<<grid, TRAV_WARPS * 32, 0, s>>>(a, phi, parent, r.x, r.y);
+    else bh_traverse_kernel<KDK, COUNT, 1, PHI><<<grid, TRAV_WARPS * 32, 0, s>>>(a, phi, parent, r.x, r.y);
 }
 
 // Dispatches L<KDK, COUNT, PHI>::go(args...) on run-time flags.
@@ -1425,20 +1424,22 @@ static void dispatch3(bool kdk, bool count, bool phi, Args... args) {
 }
 template <bool KDK, bool COUNT, bool PHI>
 struct LaneLaunch {
-    static void go(unsigned grid, size_t smem, const TravArgs *a, float *phi, const int *parent, cudaStream_t s) {
-        launch_lane<KDK, COUNT, PHI>(grid, smem, *a, phi, parent, s);
+    static void go(unsigned grid, size_t smem, const TravArgs *a, float *phi, const int *parent, int2 r,
+                   cudaStream_t s) {
+        launch_lane<KDK, COUNT, PHI>(grid, smem, *a, phi, parent, r, s);
     }
 };
 template <bool KDK, bool COUNT, bool PHI>
 struct GroupLaunch {
-    static void go(unsigned grid, const TravArgs *a, const int *gsize, float *phi, cudaStream_t s) {
-        bh_group_kernel<KDK, COUNT, PHI><<<grid, GW_WARPS * 32, 0, s>>>(*a, gsize, phi);
+    static void go(unsigned grid, const TravArgs *a, const int *gsize, float *phi, int2 r, cudaStream_t s) {
+        bh_group_kernel<KDK, COUNT, PHI><<<grid, GW_WARPS * 32, 0, s>>>(*a, gsize, phi, r.x, r.y);
     }
 };
 template <bool KDK, bool COUNT, bool PHI>
 struct WarpLaunch {
-    static void go(int tpl, unsigned grid, const TravArgs *a, float *phi, const int *parent, cudaStream_t s) {
-        launch_warp<KDK, COUNT, PHI>(tpl, grid, *a, phi, parent, s);
+    static void go(int tpl, unsigned grid, const TravArgs *a, float *phi, const int *parent, int2 r,
+                   cudaStream_t s) {
+        launch_warp<KDK, COUNT, PHI>(tpl, grid, *a, phi, parent, r, s);
     }
 };
 
@@ -1454,6 +1455,7 @@ static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float *phi, float thet
     if (s1 < 0) s1 = n;
     if (s1 <= s0) return GB_OK;
     const int64_t nt = s1 - s0;
+    const int2 range = make_int2((int)s0, (int)s1);  // key-order targets [s0, s1)
     TravArgs a;
     a.leaf = h->leaf;
     a.inode = h->inode;
@@ -1462,8 +1464,6 @@ static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float *phi, float thet
     a.acc = acc;
     a.vel = vel;
     a.n = (int)n;
-    a.s0 = (int)s0;
-    a.s1 = (int)s1;
     a.theta2 = theta * theta;
     a.eps2 = eps2;
     a.G = G;
@@ -1497,16 +1497,16 @@ static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float *phi, float thet
             h->launches += 1;
             h->groups_n = n;
         }
-        dispatch3<GroupLaunch>(kdk, count, phi != nullptr, grid, &a, (const int *)h->gsize, phi, s);
+        dispatch3<GroupLaunch>(kdk, count, phi != nullptr, grid, &a, (const int *)h->gsize, phi, range, s);
     } else if (shape == 0 && max_stack <= LANE_MAX_STACK && n - 1 <= ((int64_t)1 << LANE_KBITS)) {
         const unsigned grid = (unsigned)((nt + LANE_THREADS - 1) / LANE_THREADS);
         const size_t smem = sizeof(int) * (size_t)std::max(max_stack, 1) * LANE_THREADS;
-        dispatch3<LaneLaunch>(kdk, count, phi != nullptr, grid, smem, &a, phi, (const int *)h->parent, s);
+        dispatch3<LaneLaunch>(kdk, count, phi != nullptr, grid, smem, &a, phi, (const int *)h->parent, range, s);
     } else {
         const int tpl = shape == 2 ? 2 : 1;
         const int64_t warps = (nt + 32 * tpl - 1) / (32 * tpl);
         const unsigned grid = (unsigned)((warps + TRAV_WARPS - 1) / TRAV_WARPS);
-        dispatch3<WarpLaunch>(kdk, count, phi != nullptr, tpl, grid, &a, phi, (const int *)h->parent, s);
+        dispatch3<WarpLaunch>(kdk, count, phi != nullptr, tpl, grid, &a, phi, (const int *)h->parent, range, s);
     }
     GB_CUDA_TRY(cudaGetLastError());
     mark(h, slot, 5, s);
