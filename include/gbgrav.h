@@ -55,6 +55,8 @@ typedef struct gb_diag {
     uint64_t warp_root_reads;   /* 32-byte root records read (per warp) */
     uint64_t lane_interactions; /* monopole terms summed (per particle) */
     uint64_t lane_tests;        /* acceptance tests evaluated (per particle) */
+    uint64_t wait_timeouts;     /* bounded device waits that gave up (the sort's
+                                   look-back; never expected): GB_ETIMEOUT */
 } gb_diag_t;
 
 const char *gb_last_error_string(void);
@@ -208,8 +210,9 @@ int gb_bh_build(gb_bh_t *h, const float *xm, int64_t n, void *stream);
  * waits for its stream and fails when failure counters grew since the last
  * checked call on the handle (or the last diag reset): GB_ESTACK for pushes
  * dropped by the max_stack rule or lost to the traversal stack's capacity,
- * GB_EINVAL for non-finite positions or an inconsistent tree.  The results
- * are written either way. */
+ * GB_EINVAL for non-finite positions or an inconsistent tree, GB_ETIMEOUT
+ * when a bounded wait of the build's radix sort expired (never expected).
+ * The results are written either way. */
 int gb_bh_accel(gb_bh_t *h, float *acc, float theta, float eps2, float G,
                 int max_stack, int flags, void *stream);
 
@@ -276,8 +279,8 @@ int gb_bh_set_graph(gb_bh_t *h, int on);
 
 /* Failure checks on every tree call of the handle (on = 1), as the GB_CHECK
  * flag gives one call: gb_bh_accel, gb_bh_accel_ext, gb_bh_compute and
- * gb_bh_kdk wait for their stream and return GB_ESTACK / GB_EINVAL when
- * failure counters grew.  Off (0) by default: the calls stay asynchronous.
+ * gb_bh_kdk wait for their stream and return GB_ESTACK / GB_EINVAL /
+ * GB_ETIMEOUT when failure counters grew.  Off (0) by default: the calls stay asynchronous.
  * No reference counterpart (its stack rule drops work silently,
  * core/solvers/barnes_hut.py:212). */
 int gb_bh_set_check(gb_bh_t *h, int on);
@@ -491,13 +494,24 @@ int64_t gb_grid_max_cells(gb_grid_t *h);
  * leaves gsort, cell_start and the geometry unchanged, as the reference
  * does.  When info is not NULL the call waits for the stream and fills it
  * (the reference's return value ngas and its nx, ny, nz, lo, inv_cell), and
- * a non-finite gas position or smoothing length returns GB_EINVAL. */
+ * a non-finite gas position or smoothing length returns GB_EINVAL (an
+ * expired bounded wait of the radix sort, never expected, GB_ETIMEOUT). */
 int gb_grid_rebuild(gb_grid_t *h, const float *xm, const float *hsml,
                     const int32_t *is_star, int32_t *gsort, int32_t *cell_start,
                     gb_grid_info_t *info, void *stream);
 
 /* Kernels launched through this handle (measurement support). */
 uint64_t gb_grid_launch_count(gb_grid_t *h);
+
+/* Test support for the bounded waits: runs the radix sort's look-back of
+ * one 256-thread CTA for tile 1 of a fresh two-tile status array.
+ * publish_first = 1: tile 0's prefix is published first (digit d's count =
+ * d), so excl_out[d] = d and the call returns GB_OK; 0: nothing publishes
+ * tile 0, every wait gives up after spin_limit polls (1 .. 2^20), the
+ * call returns GB_ETIMEOUT and *timeouts_out = 256.  Synchronous.  No
+ * reference counterpart. */
+int gb_sort_wait_probe(int spin_limit, int publish_first, uint32_t *excl_out,
+                       uint64_t *timeouts_out);
 
 /* ------------------------------------------------------------ calibration */
 /* Launches an FP32 FMA-throughput kernel (packed = 1: .f32x2 form) on

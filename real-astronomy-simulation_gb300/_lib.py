@@ -48,7 +48,8 @@ class Diag(ctypes.Structure):
     _fields_ = [("stack_drops", ctypes.c_uint64), ("stack_overflow", ctypes.c_uint64),
                 ("nonfinite", ctypes.c_uint64), ("bad_tree", ctypes.c_uint64),
                 ("warp_node_reads", ctypes.c_uint64), ("warp_root_reads", ctypes.c_uint64),
-                ("lane_interactions", ctypes.c_uint64), ("lane_tests", ctypes.c_uint64)]
+                ("lane_interactions", ctypes.c_uint64), ("lane_tests", ctypes.c_uint64),
+                ("wait_timeouts", ctypes.c_uint64)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
@@ -123,6 +124,7 @@ SIGNATURES = {
     "gb_bh_accel_ext": (I32, [P, P, F32, F32, F32, I32, P, I32, P]),
     "gb_bh_set_graph": (I32, [P, I32]),
     "gb_bh_set_check": (I32, [P, I32]),
+    "gb_sort_wait_probe": (I32, [I32, I32, P, P]),
     "gb_kick": (I32, [P, P, I64, F32, P]),
     "gb_drift": (I32, [P, P, I64, F32, P]),
     "gb_grid_create": (I32, [ctypes.POINTER(P), I64, F64]),

@@ -1172,8 +1172,7 @@ struct gb_bh {
     void *keys[2];
     uint32_t *vals[2];
     int cur;  // which buffer holds the sorted result
-    uint32_t *hist;
-    int64_t hist_cap;
+    uint32_t *sort_scratch;  // radix_scratch_size(n_max) words
     float4 *bbox_part;
     int bbox_blocks;
     unsigned *ticket;
@@ -1186,7 +1185,6 @@ struct gb_bh {
     float4 *bmin, *bmax;
     float4 *inode;
     float4 *root;
-    uint32_t *totals;
     unsigned long long *diag;
     // Stage timing (gb_bh_timing): events recorded on the launch stream at
     // stage boundaries, GB_BH_STAGES + 1 per step, reused cyclically.
@@ -1222,7 +1220,7 @@ struct gb_bh {
     // Failure checks (GB_CHECK, gb_bh_set_check): the failure counters as
     // read by the last checked call (or zero after a diag reset).
     int check;
-    unsigned long long seen[4];
+    unsigned long long seen[DIAG_COUNT];  // failure counters at the last checked call
 };
 
 static void mark(gb_bh_t *h, int step_slot, int stage, cudaStream_t s) {
@@ -1234,9 +1232,9 @@ static size_t key_size(int bits) { return bits <= 10 ? sizeof(uint32_t) : sizeof
 
 extern "C" int gb_bh_destroy(gb_bh_t *h) {
     if (!h) return GB_OK;
-    void *ptrs[] = {h->keys[0], h->keys[1], h->vals[0], h->vals[1], h->hist, h->bbox_part, h->ticket,
+    void *ptrs[] = {h->keys[0], h->keys[1], h->vals[0], h->vals[1], h->sort_scratch, h->bbox_part, h->ticket,
                     h->prm, h->leaf, h->child, h->parent, h->arrivals, h->sums, h->bmin, h->bmax,
-                    h->inode, h->root, h->totals, h->diag, h->epart, h->gsize};
+                    h->inode, h->root, h->diag, h->epart, h->gsize};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &g : h->gexec)
@@ -1253,7 +1251,7 @@ extern "C" int gb_bh_destroy(gb_bh_t *h) {
 extern "C" int gb_bh_create(gb_bh_t **out, int64_t n_max, int key_bits) {
     if (!out) return fail(GB_EINVAL, "out is NULL");
     *out = nullptr;
-    if (n_max < 1 || n_max > ((int64_t)1 << 30)) return fail(GB_EINVAL, "n_max=%lld out of range", (long long)n_max);
+    if (n_max < 1 || n_max > RS_MAX_N) return fail(GB_EINVAL, "n_max=%lld out of range", (long long)n_max);
     if (key_bits != 10 && key_bits != 21) return fail(GB_EINVAL, "key_bits must be 10 or 21 (got %d)", key_bits);
     gb_bh_t *h = new gb_bh();
     GB_CUDA_TRY(cudaGetDevice(&h->device));
@@ -1282,8 +1280,6 @@ extern "C" int gb_bh_create(gb_bh_t **out, int64_t n_max, int key_bits) {
     h->n = -1;
     h->cur = 0;
     const int64_t nn = n_max, ni = std::max<int64_t>(n_max - 1, 1), nodes = 2 * n_max;
-    const int64_t nb = (n_max + RS_TILE - 1) / RS_TILE;
-    h->hist_cap = (int64_t)RS_BINS * nb;
     h->bbox_blocks = std::max(1, std::min(h->sms * 4, (int)((n_max + BBOX_THREADS - 1) / BBOX_THREADS)));
     bool ok = true;
     auto A = [&](void **p, size_t bytes) {
@@ -1293,7 +1289,7 @@ extern "C" int gb_bh_create(gb_bh_t **out, int64_t n_max, int key_bits) {
     A(&h->keys[1], key_size(key_bits) * nn);
     A((void **)&h->vals[0], sizeof(uint32_t) * nn);
     A((void **)&h->vals[1], sizeof(uint32_t) * nn);
-    A((void **)&h->hist, sizeof(uint32_t) * h->hist_cap);
+    A((void **)&h->sort_scratch, sizeof(uint32_t) * radix_scratch_size(n_max));
     A((void **)&h->bbox_part, sizeof(float4) * 2 * h->bbox_blocks);
     A((void **)&h->ticket, sizeof(unsigned));
     A((void **)&h->prm, sizeof(BHParams));
@@ -1306,7 +1302,6 @@ extern "C" int gb_bh_create(gb_bh_t **out, int64_t n_max, int key_bits) {
     A((void **)&h->bmax, sizeof(float4) * ni);
     A((void **)&h->inode, sizeof(float4) * 3 * ni);
     A((void **)&h->root, sizeof(float4) * 2);
-    A((void **)&h->totals, sizeof(uint32_t) * RS_BINS);
     A((void **)&h->diag, sizeof(unsigned long long) * DIAG_COUNT);
     h->epart_cap = 4 * h->sms;
     A((void **)&h->epart, sizeof(double2) * (h->epart_cap + ENERGY_EXTRA));
@@ -1345,7 +1340,7 @@ static int build_impl(gb_bh_t *h, float4 *xm, float4 *vel, const float4 *acc, in
     const int passes = (3 * BITS + 7) / 8;
     KeyT *kk[2] = {k0, k1};
     uint32_t *vv[2] = {v0, v1};
-    h->cur = radix_sort_pairs<KeyT>(kk, vv, n, passes, h->hist, h->totals, h->diag, s);
+    h->cur = radix_sort_pairs<KeyT>(kk, vv, n, passes, h->sort_scratch, h->diag, s);
     k0 = kk[h->cur];
     v0 = vv[h->cur];
     mark(h, slot, 2, s);
@@ -1364,7 +1359,7 @@ static int build_impl(gb_bh_t *h, float4 *xm, float4 *vel, const float4 *acc, in
     }
     GB_CUDA_TRY(cudaGetLastError());
     mark(h, slot, 4, s);
-    h->launches += 6 + 3 * passes - (n >= 2 ? 0 : 1);
+    h->launches += 5 + 1 + passes - (n >= 2 ? 0 : 1);
     h->n = n;
     return GB_OK;
 }
@@ -1515,15 +1510,16 @@ static int traverse(gb_bh_t *h, float4 *acc, float4 *vel, float *phi, float thet
 }
 
 // Synchronises `s` and compares the failure counters (stack drops, stack
-// overflow, non-finite positions, bad tree) with the values the last check
-// saw: anything counted since then fails the call.  Non-finite positions
-// and index guards give GB_EINVAL, dropped or overflowed pushes GB_ESTACK.
+// overflow, non-finite positions, bad tree, expired waits) with the values
+// the last check saw: anything counted since then fails the call.
+// Non-finite positions and index guards give GB_EINVAL, an expired wait
+// GB_ETIMEOUT, dropped or overflowed pushes GB_ESTACK.
 static int check_failures(gb_bh_t *h, cudaStream_t s, const char *call) {
-    unsigned long long d[4];
+    unsigned long long d[DIAG_COUNT];
     GB_CUDA_TRY(cudaMemcpyAsync(d, h->diag, sizeof(d), cudaMemcpyDeviceToHost, s));
     GB_CUDA_TRY(cudaStreamSynchronize(s));
-    unsigned long long inc[4];
-    for (int k = 0; k < 4; ++k) {
+    unsigned long long inc[DIAG_COUNT];
+    for (int k = 0; k < DIAG_COUNT; ++k) {
         inc[k] = d[k] - h->seen[k];
         h->seen[k] = d[k];
     }
@@ -1531,6 +1527,9 @@ static int check_failures(gb_bh_t *h, cudaStream_t s, const char *call) {
         return fail(GB_EINVAL, "%s: %llu non-finite particle positions", call, inc[DIAG_NONFINITE]);
     if (inc[DIAG_BAD_TREE])
         return fail(GB_EINVAL, "%s: inconsistent tree (%llu index guards taken)", call, inc[DIAG_BAD_TREE]);
+    if (inc[DIAG_WAIT_TIMEOUT])
+        return fail(GB_ETIMEOUT, "%s: %llu bounded device waits expired (radix sort look-back)", call,
+                    inc[DIAG_WAIT_TIMEOUT]);
     if (inc[DIAG_STACK_DROPS] || inc[DIAG_STACK_OVERFLOW])
         return fail(GB_ESTACK, "%s: the max_stack rule dropped %llu pushes; %llu overflowed the traversal stack",
                     call, inc[DIAG_STACK_DROPS], inc[DIAG_STACK_OVERFLOW]);
@@ -1729,6 +1728,51 @@ extern "C" int gb_bh_energy(gb_bh_t *h, const float *xm, const float *vel, const
                          (cudaStream_t)stream));
     h->launches += 1;
     return GB_OK;
+}
+
+// One CTA runs the radix sort's look-back for tile 1 of a two-tile status
+// array.  publish_first = 1: each thread first publishes tile 0's prefix
+// (its digit d as the count), so the look-back returns d; 0: tile 0 never
+// publishes and every wait runs out after spin_limit polls.
+__global__ void sort_wait_probe_kernel(uint32_t *status, int spin_limit, int publish_first, uint32_t *excl,
+                                       unsigned long long *diag) {
+    const int d = threadIdx.x;
+    if (publish_first) st_relaxed_gpu(status + d, RS_PRE | (uint32_t)d);
+    excl[d] = rs_lookback(status, 1, d, 1u, spin_limit, diag);
+}
+
+extern "C" int gb_sort_wait_probe(int spin_limit, int publish_first, uint32_t *excl_out, uint64_t *timeouts_out) {
+    if (spin_limit < 1 || spin_limit > RS_SPIN_LIMIT)
+        return fail(GB_EINVAL, "spin_limit must be in [1, %d] (got %d)", RS_SPIN_LIMIT, spin_limit);
+    if (!excl_out || !timeouts_out) return fail(GB_EINVAL, "NULL argument");
+    uint32_t *status = nullptr, *excl = nullptr;
+    unsigned long long *diag = nullptr;
+    int rc = GB_OK;
+    if (cudaMalloc(&status, sizeof(uint32_t) * 2 * RS_BINS) != cudaSuccess ||
+        cudaMalloc(&excl, sizeof(uint32_t) * RS_BINS) != cudaSuccess ||
+        cudaMalloc(&diag, sizeof(unsigned long long) * DIAG_COUNT) != cudaSuccess) {
+        rc = fail(GB_ENOMEM, "gb_sort_wait_probe: device allocation failed");
+    }
+    if (rc == GB_OK && (cudaMemset(status, 0, sizeof(uint32_t) * 2 * RS_BINS) != cudaSuccess ||
+                        cudaMemset(diag, 0, sizeof(unsigned long long) * DIAG_COUNT) != cudaSuccess))
+        rc = fail(GB_ECUDA, "gb_sort_wait_probe: memset failed");
+    if (rc == GB_OK) {
+        sort_wait_probe_kernel<<<1, RS_BINS>>>(status, spin_limit, publish_first ? 1 : 0, excl, diag);
+        unsigned long long d[DIAG_COUNT];
+        if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
+            cudaMemcpy(excl_out, excl, sizeof(uint32_t) * RS_BINS, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(d, diag, sizeof(d), cudaMemcpyDeviceToHost) != cudaSuccess) {
+            rc = fail(GB_ECUDA, "gb_sort_wait_probe: %s", cudaGetErrorString(cudaGetLastError()));
+        } else {
+            *timeouts_out = (uint64_t)d[DIAG_WAIT_TIMEOUT];
+            if (d[DIAG_WAIT_TIMEOUT])
+                rc = fail(GB_ETIMEOUT, "gb_sort_wait_probe: %llu waits expired", d[DIAG_WAIT_TIMEOUT]);
+        }
+    }
+    if (status) cudaFree(status);
+    if (excl) cudaFree(excl);
+    if (diag) cudaFree(diag);
+    return rc;
 }
 
 extern "C" int gb_bh_set_check(gb_bh_t *h, int on) {

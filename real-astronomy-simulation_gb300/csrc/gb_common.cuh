@@ -40,7 +40,8 @@ enum DiagIndex {
     DIAG_ROOT_READS = 5,
     DIAG_INTERACTIONS = 6,
     DIAG_TESTS = 7,
-    DIAG_COUNT = 8
+    DIAG_WAIT_TIMEOUT = 8,    // bounded device waits that gave up (never expected)
+    DIAG_COUNT = 9
 };
 
 int num_sms();

@@ -241,7 +241,8 @@ struct gb_grid {
     long long max_cells;
     double min_radius;
     int passes, red_blocks;
-    uint32_t *keys[2], *vals[2], *hist, *totals;
+    uint32_t *keys[2], *vals[2], *sort_scratch;
+    unsigned long long timeouts_seen;  // DIAG_WAIT_TIMEOUT at the last rebuild with info
     GridPart *part;
     unsigned *ticket;
     GridGeom *geom;
@@ -251,7 +252,7 @@ struct gb_grid {
 
 extern "C" int gb_grid_destroy(gb_grid_t *h) {
     if (!h) return GB_OK;
-    void *ptrs[] = {h->keys[0], h->keys[1], h->vals[0], h->vals[1], h->hist, h->totals, h->part, h->ticket,
+    void *ptrs[] = {h->keys[0], h->keys[1], h->vals[0], h->vals[1], h->sort_scratch, h->part, h->ticket,
                     h->geom, h->diag};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -282,8 +283,7 @@ extern "C" int gb_grid_create(gb_grid_t **out, int64_t n, double min_radius) {
     A((void **)&h->keys[1], sizeof(uint32_t) * nn);
     A((void **)&h->vals[0], sizeof(uint32_t) * nn);
     A((void **)&h->vals[1], sizeof(uint32_t) * nn);
-    A((void **)&h->hist, sizeof(uint32_t) * radix_hist_size(nn));
-    A((void **)&h->totals, sizeof(uint32_t) * RS_BINS);
+    A((void **)&h->sort_scratch, sizeof(uint32_t) * radix_scratch_size(nn));
     A((void **)&h->part, sizeof(GridPart) * h->red_blocks);
     A((void **)&h->ticket, sizeof(unsigned));
     A((void **)&h->geom, sizeof(GridGeom));
@@ -322,12 +322,12 @@ extern "C" int gb_grid_rebuild(gb_grid_t *h, const float *xm, const float *hsml,
         const unsigned g = (unsigned)((n + GRID_THREADS - 1) / GRID_THREADS);
         grid_key_kernel<<<g, GRID_THREADS, 0, s>>>((const float4 *)xm, is_star, n, h->geom, h->keys[0],
                                                    h->vals[0]);
-        const int cur = radix_sort_pairs<uint32_t>(h->keys, h->vals, n, h->passes, h->hist, h->totals, h->diag, s);
+        const int cur = radix_sort_pairs<uint32_t>(h->keys, h->vals, n, h->passes, h->sort_scratch, h->diag, s);
         grid_gsort_kernel<<<g, GRID_THREADS, 0, s>>>(h->vals[cur], n, h->geom, gsort);
         const unsigned gc = (unsigned)((h->max_cells + 1 + GRID_THREADS - 1) / GRID_THREADS);
         grid_start_kernel<<<gc, GRID_THREADS, 0, s>>>(h->keys[cur], h->geom, h->max_cells, cell_start);
         GB_CUDA_TRY(cudaGetLastError());
-        h->launches += 4 + 3 * h->passes;
+        h->launches += 4 + 1 + h->passes;
     }
     if (info) {
         GridGeom g;
@@ -345,6 +345,11 @@ extern "C" int gb_grid_rebuild(gb_grid_t *h, const float *xm, const float *hsml,
         info->inv_cell = g.inv_cell;
         if (g.status == 1) return fail(GB_EINVAL, "gb_grid_rebuild: non-finite gas position or smoothing length");
         if (g.status == 2) return fail(GB_EINVAL, "gb_grid_rebuild: cell growth did not converge");
+        unsigned long long to = 0;
+        GB_CUDA_TRY(cudaMemcpy(&to, h->diag + DIAG_WAIT_TIMEOUT, sizeof(to), cudaMemcpyDeviceToHost));
+        const unsigned long long inc = to - h->timeouts_seen;
+        h->timeouts_seen = to;
+        if (inc) return fail(GB_ETIMEOUT, "gb_grid_rebuild: %llu bounded device waits expired (radix sort)", inc);
     }
     return GB_OK;
 }

@@ -63,6 +63,7 @@ int read_diag(unsigned long long *dev, gb_diag_t *out, int reset) {
     out->warp_root_reads = d[DIAG_ROOT_READS];
     out->lane_interactions = d[DIAG_INTERACTIONS];
     out->lane_tests = d[DIAG_TESTS];
+    out->wait_timeouts = d[DIAG_WAIT_TIMEOUT];
     if (reset) GB_CUDA_TRY(cudaMemset(dev, 0, sizeof(d)));
     return GB_OK;
 }

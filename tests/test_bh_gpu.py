@@ -142,10 +142,10 @@ def test_small_sizes(cuda_dev, orc, n, tpl):
     _check_acc(a, ref)
 
 
-@pytest.mark.parametrize("n", [2, 4095, 4096, 4097, 32767, 32768, 32769, 40000])
+@pytest.mark.parametrize("n", [2, 2047, 2048, 2049, 4095, 4096, 4097, 32767, 32768, 32769, 40000])
 @pytest.mark.parametrize("bits", [21, 10])
 def test_sort_sizes_at_tile_edges(cuda_dev, orc, n, bits):
-    """Keys, order and topology at the radix sort's tile edges (4,096 keys
+    """Keys, order and topology at the radix sort's tile edges (2,048 keys
     per CTA) against numpy's stable argsort; duplicate positions exercise
     the stable order of equal keys."""
     _, bhmod, ic, _ = _mods()
@@ -165,6 +165,50 @@ def test_sort_sizes_at_tile_edges(cuda_dev, orc, n, bits):
         np.testing.assert_array_equal(t["parent"], parent)
     assert b.diag()["bad_tree"] == 0
     b.close()
+
+
+@pytest.mark.parametrize("bits", [21, 10])
+def test_sort_many_tiles(cuda_dev, orc, bits):
+    """3M keys: 1,465 tiles, more than the CTAs resident at once, so tiles
+    look back across CTAs that started in later waves.  Keys and order
+    against numpy's stable argsort; no look-back wait runs out."""
+    _, bhmod, ic, _ = _mods()
+    n = 3_000_000
+    pos, _, mass = ic.exponential_disk(n, seed=11)
+    pos, mass = _f32(pos), _f32(mass)
+    pos[1000:1300] = pos[5]  # a run of equal keys spanning tiles
+    b = bhmod.BarnesHut(n, theta=0.5, softening=0.05, key_bits=bits, device=cuda_dev)
+    b.build(_xm(pos, mass, cuda_dev))
+    codes = orc.morton_codes(pos, bits)
+    order = np.argsort(codes, kind="stable")
+    np.testing.assert_array_equal(b.export("order"), order)
+    np.testing.assert_array_equal(b.export("code"), codes[order])
+    d = b.diag()
+    assert d["wait_timeouts"] == 0 and d["bad_tree"] == 0
+    b.close()
+
+
+def test_sort_wait_probe_times_out_and_reports(cuda_dev):
+    """The sort's look-back waits are bounded: with tile 0 never published,
+    every one of the 256 waits gives up after its poll limit, the call
+    returns GB_ETIMEOUT and the context stays usable; with tile 0 published
+    first, the look-back returns tile 0's counts."""
+    import ctypes
+
+    lib_mod = importlib.import_module(PKG_NAME + "._lib")
+    lib = lib_mod.load()
+    excl = (ctypes.c_uint32 * 256)()
+    timeouts = ctypes.c_uint64(7)
+    rc = lib.gb_sort_wait_probe(1000, 1, excl, ctypes.byref(timeouts))
+    assert rc == lib_mod.GB_OK
+    assert list(excl) == list(range(256)) and timeouts.value == 0
+    rc = lib.gb_sort_wait_probe(1000, 0, excl, ctypes.byref(timeouts))
+    assert rc == lib_mod.GB_ETIMEOUT
+    assert timeouts.value == 256
+    assert lib.gb_sort_wait_probe(0, 0, excl, ctypes.byref(timeouts)) == lib_mod.GB_EINVAL
+    # The context still works.
+    x = torch.arange(8, dtype=torch.float32, device=cuda_dev)
+    assert float((x * 2).sum()) == 56.0
 
 
 def _boundary_positions(n, bits, seed):
