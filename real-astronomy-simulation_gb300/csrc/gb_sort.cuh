@@ -283,7 +283,7 @@ static int radix_sort_pairs(KeyT *k[2], uint32_t *v[2], int64_t n, int passes, u
     uint32_t *status[2] = {counters + RS_COUNTERS, counters + RS_COUNTERS + (int64_t)nb * RS_BINS};
     cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * ((int64_t)RS_MAX_PASSES * RS_BINS + RS_COUNTERS + (int64_t)nb * RS_BINS),
                     s);
-    const int hb = (int)std::min<int64_t>((n + RS_THREADS - 1) / RS_THREADS, 2048);
+    const int hb = (int)std::min<int64_t>((n + RS_THREADS - 1) / RS_THREADS, 4 * (int64_t)num_sms());
     rs_histogram_kernel<KeyT><<<hb, RS_THREADS, 0, s>>>(k[0], n, passes, counts);
     int cur = 0;
     for (int p = 0; p < passes; ++p) {
