@@ -295,11 +295,11 @@ def bench_bh(args, dev, rank, world, dist):
                        "algorithmic_bytes_per_launch": bytes_launch,
                        "launch_ms": trav_ms}
     traffic = _profiled_traffic("bh_traverse_1M_disk.md")
-    if traffic is not None and not _profile_current("bh_traverse_1M_disk.md", "gb_bh.cu"):
+    if traffic is not None and not _profile_current("bh_traverse_1M_disk.md", "gb_bh_traverse.cuh"):
         # The capture measured another revision of the kernel source: its
         # figures are not this kernel's.
         res["roofline"]["traffic_source"] = ("none: profiles/bh_traverse_1M_disk.md was captured on "
-                                             "another revision of csrc/gb_bh.cu")
+                                             "another revision of csrc/gb_bh_traverse.cuh")
         traffic = None
     if traffic is not None and BH_N == 1_000_000 and BH_BITS == 10:
         res["roofline"]["traffic"] = traffic
@@ -445,11 +445,11 @@ def bench_group_walk(args, dev, rank, world, dist, flush, hbm, src):
                        else "fallback 6800 GB/s", "unit": "GB/s", "frac": achieved / hbm,
                        "algorithmic_bytes_per_launch": bytes_launch, "launch_ms": trav_ms, "traffic": None}
     note = "bh_group_walk_1M_disk.md"
-    if BH_N == 1_000_000 and BH_BITS == 10 and _profile_current(note, "gb_bh.cu"):
+    if BH_N == 1_000_000 and BH_BITS == 10 and _profile_current(note, "gb_bh_traverse.cuh"):
         out["roofline"]["traffic"] = _profiled_traffic(note)
         out["roofline"]["traffic_source"] = f"ncu dram bytes of one launch on this workload (profiles/{note})"
     else:
-        out["roofline"]["traffic_source"] = f"none: profiles/{note} was captured on another revision of csrc/gb_bh.cu"
+        out["roofline"]["traffic_source"] = f"none: profiles/{note} was captured on another revision of csrc/gb_bh_traverse.cuh"
     # FP32 work: 20 flop per monopole term (list entry x target), 10 per
     # box-acceptance test (two per record).
     out["work_per_step"] = {"node_reads": work["warp_node_reads"], "groups": work["warp_root_reads"],
