@@ -190,10 +190,10 @@ uint64_t gb_direct_launch_count(gb_direct_t *h);
 /* ----------------------------------------------------- LBVH Barnes-Hut */
 typedef struct gb_bh gb_bh_t;
 
-/* Allocates tree scratch for up to n_max particles with key_bits bits per
- * axis (21: the reference's 63-bit keys, core/solvers/barnes_hut.py:38; 10:
- * 30-bit keys).  Replaces BarnesHut.__init__ (core/solvers/barnes_hut.py:
- * 223-240). */
+/* Allocates tree scratch for up to n_max particles (1 .. 2^30 - 1) with
+ * key_bits bits per axis (21: the reference's 63-bit keys,
+ * core/solvers/barnes_hut.py:38; 10: 30-bit keys).  Replaces
+ * BarnesHut.__init__ (core/solvers/barnes_hut.py:223-240). */
 int gb_bh_create(gb_bh_t **out, int64_t n_max, int key_bits);
 int gb_bh_destroy(gb_bh_t *h);
 
