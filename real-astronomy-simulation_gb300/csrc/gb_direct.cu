@@ -65,24 +65,20 @@ __device__ __forceinline__ float4 load_target(const DirectArgs &a, int64_t i) {
 // Force kernel for MODE_ACC / MODE_KDK.  NP packed target pairs per lane.
 // The inner loop takes two sources per iteration into two accumulator sets
 // (independent dependency chains for the scheduler); the Kahan running sums
-// live in shared memory between source chunks, which keeps registers for
-// the interleave.  One pair per lane (NP = 1) fits 64 registers: 32
-// resident warps/SM.
-template <int NP, int WARPS, int MODE, bool KAHAN, bool PHI>
+// stay in registers.  FINE: units of SCALAR_UNIT sources (up to WARPS of
+// them staged per shared-memory batch) instead of WARPS * 32, so short CTA
+// runs split the work evenly (as in the scalar kernel).
+template <int NP, int WARPS, int MODE, bool KAHAN, bool FINE, bool PHI>
 __global__ void __launch_bounds__(WARPS * 32, NP == 1 ? 1024 / (WARPS * 32) : 1)
 direct_force_kernel(DirectArgs a) {
     constexpr int K = 2 * NP;
     constexpr int TILE = 32 * K;
     constexpr int ST = WARPS * TILE;
     constexpr int JU = WARPS * 32;
-    constexpr int T = WARPS * 32;
-    constexpr int NV = PHI ? 8 : 6;  // per pair: S{x,y,z}, C{x,y,z} (+ S, C of the potential)
-    __shared__ ulonglong2 src[2 * JU];
-    __shared__ f2 kah[NV * NP][T];
+    __shared__ ulonglong2 src[2 * JU];  // per source {(x, x), (y, y)}, {(z, z), (m, m)}
 
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    const int tid = threadIdx.x;
     const int64_t c = blockIdx.x;
     const int64_t u_begin = unit_begin(a.U, a.P, c);
     const int64_t u_end = unit_begin(a.U, a.P, c + 1);
@@ -98,6 +94,7 @@ direct_force_kernel(DirectArgs a) {
         const int64_t tbase = st * ST + wib * TILE + lane;
 
         f2 X[NP], Y[NP], Z[NP];
+        f2 SX[NP], SY[NP], SZ[NP], CX[NP], CY[NP], CZ[NP], SW[NP], CW[NP];
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
             const float4 t0 = load_target<MODE>(a, tbase + (2 * p) * 32);
@@ -105,24 +102,34 @@ direct_force_kernel(DirectArgs a) {
             X[p] = pack2(t0.x, t1.x);
             Y[p] = pack2(t0.y, t1.y);
             Z[p] = pack2(t0.z, t1.z);
+            SX[p] = SY[p] = SZ[p] = CX[p] = CY[p] = CZ[p] = SW[p] = CW[p] = 0ull;
         }
-#pragma unroll
-        for (int v = 0; v < NV * NP; ++v) kah[v][tid] = 0ull;
 
-        for (; u < run_end; ++u) {
-            const int64_t ju = u - st * a.num_ju;
-            const float4 s4 = load_particle<MODE>(a, ju * JU + threadIdx.x);
-            __syncthreads();  // previous chunk fully consumed
+        while (u < run_end) {
+            const int64_t jc = u - st * a.num_ju;
+            int cnt = 1;
+            float4 s4;
+            if (FINE) {
+                // Stage up to WARPS units (SCALAR_UNIT sources each) at once.
+                cnt = (int)min((int64_t)WARPS, run_end - u);
+                s4 = (int)threadIdx.x < cnt * SCALAR_UNIT ? load_particle<MODE>(a, jc * SCALAR_UNIT + threadIdx.x)
+                                                          : make_float4(0.f, 0.f, 0.f, 0.f);
+            } else {
+                s4 = load_particle<MODE>(a, jc * JU + threadIdx.x);
+            }
+            __syncthreads();  // previous batch fully consumed
             src[2 * threadIdx.x] = make_ulonglong2(pack2(s4.x, s4.x), pack2(s4.y, s4.y));
             src[2 * threadIdx.x + 1] = make_ulonglong2(pack2(s4.z, s4.z), pack2(s4.w, s4.w));
             __syncthreads();
+            u += cnt;
+            const int nsrc = FINE ? cnt * SCALAR_UNIT : JU;
 
             f2 AX[2][NP], AY[2][NP], AZ[2][NP], AW[2][NP];
 #pragma unroll
             for (int p = 0; p < NP; ++p)
                 AX[0][p] = AY[0][p] = AZ[0][p] = AX[1][p] = AY[1][p] = AZ[1][p] = AW[0][p] = AW[1][p] = 0ull;
 #pragma unroll 2
-            for (int jj = 0; jj < JU; jj += 2) {
+            for (int jj = 0; jj < nsrc; jj += 2) {
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const ulonglong2 A = src[2 * (jj + h)];
@@ -151,30 +158,19 @@ direct_force_kernel(DirectArgs a) {
                 const f2 ax = add2(AX[0][p], AX[1][p]);
                 const f2 ay = add2(AY[0][p], AY[1][p]);
                 const f2 az = add2(AZ[0][p], AZ[1][p]);
-                f2 sx = kah[6 * p][tid], sy = kah[6 * p + 1][tid], sz = kah[6 * p + 2][tid];
                 if (KAHAN) {
-                    f2 cx = kah[6 * p + 3][tid], cy = kah[6 * p + 4][tid], cz = kah[6 * p + 5][tid];
-                    kahan_add2(sx, cx, ax);
-                    kahan_add2(sy, cy, ay);
-                    kahan_add2(sz, cz, az);
-                    kah[6 * p + 3][tid] = cx;
-                    kah[6 * p + 4][tid] = cy;
-                    kah[6 * p + 5][tid] = cz;
+                    kahan_add2(SX[p], CX[p], ax);
+                    kahan_add2(SY[p], CY[p], ay);
+                    kahan_add2(SZ[p], CZ[p], az);
                 } else {
-                    sx = add2(sx, ax);
-                    sy = add2(sy, ay);
-                    sz = add2(sz, az);
+                    SX[p] = add2(SX[p], ax);
+                    SY[p] = add2(SY[p], ay);
+                    SZ[p] = add2(SZ[p], az);
                 }
-                kah[6 * p][tid] = sx;
-                kah[6 * p + 1][tid] = sy;
-                kah[6 * p + 2][tid] = sz;
                 if (PHI) {
                     const f2 aw = add2(AW[0][p], AW[1][p]);
-                    f2 sw = kah[6 * NP + 2 * p][tid], cw = kah[6 * NP + 2 * p + 1][tid];
-                    if (KAHAN) kahan_add2(sw, cw, aw);
-                    else sw = add2(sw, aw);
-                    kah[6 * NP + 2 * p][tid] = sw;
-                    kah[6 * NP + 2 * p + 1][tid] = cw;
+                    if (KAHAN) kahan_add2(SW[p], CW[p], aw);
+                    else SW[p] = add2(SW[p], aw);
                 }
             }
         }
@@ -182,18 +178,15 @@ direct_force_kernel(DirectArgs a) {
         const int64_t slot = (c * a.smax + (st - st0)) * ST + wib * TILE + lane;
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
-            float hx0, hx1, hy0, hy1, hz0, hz1, cx0, cx1, cy0, cy1, cz0, cz1;
-            unpack2(kah[6 * p][tid], hx0, hx1);
-            unpack2(kah[6 * p + 1][tid], hy0, hy1);
-            unpack2(kah[6 * p + 2][tid], hz0, hz1);
-            unpack2(kah[6 * p + 3][tid], cx0, cx1);
-            unpack2(kah[6 * p + 4][tid], cy0, cy1);
-            unpack2(kah[6 * p + 5][tid], cz0, cz1);
-            float hw0 = 0.f, hw1 = 0.f, cw0 = 0.f, cw1 = 0.f;
-            if (PHI) {
-                unpack2(kah[6 * NP + 2 * p][tid], hw0, hw1);
-                unpack2(kah[6 * NP + 2 * p + 1][tid], cw0, cw1);
-            }
+            float hx0, hx1, hy0, hy1, hz0, hz1, cx0, cx1, cy0, cy1, cz0, cz1, hw0, hw1, cw0, cw1;
+            unpack2(SX[p], hx0, hx1);
+            unpack2(SY[p], hy0, hy1);
+            unpack2(SZ[p], hz0, hz1);
+            unpack2(CX[p], cx0, cx1);
+            unpack2(CY[p], cy0, cy1);
+            unpack2(CZ[p], cz0, cz1);
+            unpack2(SW[p], hw0, hw1);
+            unpack2(CW[p], cw0, cw1);
             const int64_t s0 = slot + (2 * p) * 32, s1 = s0 + 32;
             a.part[2 * s0] = make_float4(hx0, hy0, hz0, hw0);
             a.part[2 * s0 + 1] = make_float4(-cx0, -cy0, -cz0, -cw0);
@@ -584,11 +577,22 @@ static void launch_scalar(int mode, bool kahan, bool phi, dim3 grid, const Direc
     }
 }
 
-template <int NP, int WARPS, int MODE, bool PHI>
+template <int NP, int WARPS, int MODE, bool FINE, bool PHI>
 static void launch_packed_m(bool kahan, dim3 grid, const DirectArgs &a, cudaStream_t s) {
     const dim3 block(WARPS * 32);
-    if (kahan) direct_force_kernel<NP, WARPS, MODE, true, PHI><<<grid, block, 0, s>>>(a);
-    else direct_force_kernel<NP, WARPS, MODE, false, PHI><<<grid, block, 0, s>>>(a);
+    if (kahan) direct_force_kernel<NP, WARPS, MODE, true, FINE, PHI><<<grid, block, 0, s>>>(a);
+    else direct_force_kernel<NP, WARPS, MODE, false, FINE, PHI><<<grid, block, 0, s>>>(a);
+}
+
+template <int NP, int WARPS, bool FINE>
+static void launch_packed(int mode, bool kahan, bool phi, dim3 grid, const DirectArgs &a, cudaStream_t s) {
+    if (mode == MODE_ACC) {
+        if (phi) launch_packed_m<NP, WARPS, MODE_ACC, FINE, true>(kahan, grid, a, s);
+        else launch_packed_m<NP, WARPS, MODE_ACC, FINE, false>(kahan, grid, a, s);
+    } else {
+        if (phi) launch_packed_m<NP, WARPS, MODE_KDK, FINE, true>(kahan, grid, a, s);
+        else launch_packed_m<NP, WARPS, MODE_KDK, FINE, false>(kahan, grid, a, s);
+    }
 }
 
 // phi: the pass also sums the potential (PHI kernels).
@@ -601,13 +605,8 @@ static cudaError_t launch_force(int mode, bool kahan, bool phi, const DirectPlan
         else launch_scalar<NP, WARPS, false>(mode, kahan, phi, grid, a, s);
         return cudaGetLastError();
     }
-    if (mode == MODE_ACC) {
-        if (phi) launch_packed_m<NP, WARPS, MODE_ACC, true>(kahan, grid, a, s);
-        else launch_packed_m<NP, WARPS, MODE_ACC, false>(kahan, grid, a, s);
-    } else {
-        if (phi) launch_packed_m<NP, WARPS, MODE_KDK, true>(kahan, grid, a, s);
-        else launch_packed_m<NP, WARPS, MODE_KDK, false>(kahan, grid, a, s);
-    }
+    if (fine) launch_packed<NP, WARPS, true>(mode, kahan, phi, grid, a, s);
+    else launch_packed<NP, WARPS, false>(mode, kahan, phi, grid, a, s);
     return cudaGetLastError();
 }
 
@@ -620,10 +619,10 @@ static KernelPtr force_kernel_ptr(int np, int warps, int packed) {
         if (np == 2 && warps == 4) return (KernelPtr)direct_force_scalar_kernel<2, 4, MODE_KDK, true, false, false>;
         return (KernelPtr)direct_force_scalar_kernel<2, 8, MODE_KDK, true, false, false>;
     }
-    if (np == 1 && warps == 4) return (KernelPtr)direct_force_kernel<1, 4, MODE_KDK, true, false>;
-    if (np == 1 && warps == 8) return (KernelPtr)direct_force_kernel<1, 8, MODE_KDK, true, false>;
-    if (np == 2 && warps == 4) return (KernelPtr)direct_force_kernel<2, 4, MODE_KDK, true, false>;
-    return (KernelPtr)direct_force_kernel<2, 8, MODE_KDK, true, false>;
+    if (np == 1 && warps == 4) return (KernelPtr)direct_force_kernel<1, 4, MODE_KDK, true, false, false>;
+    if (np == 1 && warps == 8) return (KernelPtr)direct_force_kernel<1, 8, MODE_KDK, true, false, false>;
+    if (np == 2 && warps == 4) return (KernelPtr)direct_force_kernel<2, 4, MODE_KDK, true, false, false>;
+    return (KernelPtr)direct_force_kernel<2, 8, MODE_KDK, true, false, false>;
 }
 
 }  // namespace gb
@@ -772,7 +771,7 @@ static int run_direct(gb_direct_t *h, int mode, const float4 *xm, float4 *vel, f
     DirectPlan pl;
     const int np = mode == MODE_PHI ? 1 : h->np;
     const int64_t ctas = grid_ctas(h, h->np, h->warps, packed);
-    const bool fine = mode != MODE_PHI && !packed && use_fine_units(n, np, h->warps, ctas, nt);
+    const bool fine = mode != MODE_PHI && use_fine_units(n, np, h->warps, ctas, nt);
     make_plan(n, np, h->warps, ctas, &pl, fine ? SCALAR_UNIT : 0, nt);
     if (plan_partials(pl) > h->part_cap) return fail(GB_EINVAL, "scratch too small for n=%lld", (long long)n);
     if (pl.P > h->st0_cap) return fail(GB_EINVAL, "%lld CTAs exceed the handle's table", (long long)pl.P);
