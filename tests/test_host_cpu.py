@@ -113,6 +113,29 @@ def test_grid_info_struct_layout():
     assert lib_mod.GridInfo.lo.offset == 32 and lib_mod.GridInfo.inv_cell.offset == 64
 
 
+def test_diag_struct_layout():
+    """gb_diag_t: nine uint64 counters, wait_timeouts last."""
+    lib_mod = importlib.import_module(PKG_NAME + "._lib")
+    assert ctypes.sizeof(lib_mod.Diag) == 72
+    assert lib_mod.Diag.wait_timeouts.offset == 64
+    assert "wait_timeouts" in lib_mod.Diag().as_dict()
+
+
+def test_sort_wait_probe_rejects_bad_arguments_without_gpu(lib):
+    """gb_sort_wait_probe checks its poll limit and pointers before any CUDA
+    call."""
+    lib_mod = importlib.import_module(PKG_NAME + "._lib")
+    pkg = importlib.import_module(PKG_NAME)
+    excl = (ctypes.c_uint32 * 256)()
+    cnt = ctypes.c_uint64()
+    for limit in (0, -5, (1 << 20) + 1):
+        with pytest.raises(pkg.GravityError, match="spin_limit") as e:
+            lib_mod.call("gb_sort_wait_probe", limit, 0, excl, ctypes.byref(cnt))
+        assert e.value.status == lib_mod.GB_EINVAL
+    with pytest.raises(pkg.GravityError, match="NULL"):
+        lib_mod.call("gb_sort_wait_probe", 10, 0, None, ctypes.byref(cnt))
+
+
 def test_state_npz_roundtrip(tmp_path):
     st_mod = importlib.import_module(PKG_NAME + ".state")
     rng = np.random.default_rng(3)
